@@ -1,0 +1,370 @@
+"""CPU restatement (numpy + the C kernels of ``oracle/vgfill.c``) of the
+reference's gridded-interpolation step engine.
+
+TEST INFRASTRUCTURE ONLY. This module is the oracle that the CUDA path is
+checked against and the CPU baseline that ``bench.py`` times beside it; the
+product package never imports it.
+
+It follows the reference's algorithm step for step, including its loop
+structure (a Python loop over cells calling ``np.matmul(pinv, rhs)``), so its
+timing is a fair stand-in for the reference's own CPU path:
+
+- ``parse_vg_str``          cyth/interpmthds.pyx:174-184 (split rules, max(1e-5, r))
+- ``check_full_nuggetness`` misc.py:1074-1105
+- ``get_dists_arr``         interp/steps.py:73-86 over cyth/interpmthds.pyx:123-143
+- ``get_svars_arr``         interp/steps.py:88-138 over cyth/interpmthds.pyx:146-226
+- ``get_2d_arr_subset``     interp/steps.py:140-168 over cyth/interpmthds.pyx:229-248
+- ``get_vars_arr_subset``   interp/steps.py:170-243
+- ``get_interp``            interp/steps.py:245-401
+- ``fill_krig_idw_dst_data`` interp/steps.py:403-435
+- ``mod_min_max``           interp/steps.py:466-476
+- ``interp_steps``          interp/steps.py:478-835 (neighbour method 'all')
+- ``get_grps_in_time``      interp/grps.py:57-101 (without pandas)
+- ``ret_mp_idxs``           misc.py:601-613
+
+Parity status: pinned against fixtures generated by running the reference's
+own code (tests/golden/make_golden.py); see tests/test_oracle_golden.py.
+"""
+import ctypes
+
+import numpy as np
+
+from . import build as _build
+
+MODEL_CODES = {
+    "Rng": 0, "Nug": 1, "Sph": 2, "Exp": 3, "Lin": 4, "Gau": 5, "Pow": 6, "Hol": 7,
+}
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def parse_vg_str(vg_str):
+    """Components ``[(code, sill, range)]`` of a variogram string.
+
+    Same split rules as ``fill_vg_var_arr`` (cyth/interpmthds.pyx:174-184):
+    split on '+', strip, split on ' ' into sill and 'Name(range', then on '('
+    and ')'. The range is clamped to ``max(1e-5, range)``. An unknown model
+    name raises (the reference's C++ map would return a null function).
+    """
+    comps = []
+    for part in str(vg_str).encode().split(b"+"):
+        part = part.strip()
+        sill_s, vg_s = part.split(b" ")
+        vg_s, range_s = vg_s.split(b"(")
+        range_s = range_s.split(b")")[0]
+        name = vg_s.decode()
+        if name not in MODEL_CODES:
+            raise KeyError(f"unknown variogram model {name!r}")
+        comps.append((MODEL_CODES[name], float(sill_s), max(1e-5, float(range_s))))
+    return comps
+
+
+def check_full_nuggetness(in_model, min_vg_val):
+    """misc.py:1074-1105. True when the total sill or the largest range is
+    <= min_vg_val. (The reference's second test compares the whole
+    sub-model string with 'Nug', which never matches.)"""
+    in_model = str(in_model)
+    nuggetness = False
+    if in_model == "nan":
+        return nuggetness
+    models = in_model.split("+")
+    sill = 0.0
+    rng = 0.0
+    for submodel in models:
+        submodel = submodel.strip()
+        sill += float(submodel.split("(")[0].strip()[:-3].strip())
+        rng = max(rng, float(submodel.split("(")[1].split(")")[0]))
+    if np.any(np.array([sill, rng]) <= min_vg_val):
+        nuggetness = True
+    if (len(models) == 1) and models[0] == "Nug":
+        nuggetness = True
+    return nuggetness
+
+
+def get_dists_arr(x1s, y1s, x2s, y2s):
+    x1s, y1s, x2s, y2s = (np.ascontiguousarray(a, dtype=np.float64)
+                          for a in (x1s, y1s, x2s, y2s))
+    out = np.full((x1s.size, x2s.size), np.nan)
+    _build.lib().orc_fill_dists_2d_mat(
+        _ptr(x1s), _ptr(y1s), x1s.size, _ptr(x2s), _ptr(y2s), x2s.size, _ptr(out))
+    return out
+
+
+def fill_vg_var_arr(dists, covar_flag, diag_mat_flag, vg_str, min_vg_val):
+    dists = np.ascontiguousarray(dists, dtype=np.float64)
+    comps = parse_vg_str(vg_str)
+    codes = np.array([c[0] for c in comps], dtype=np.int32)
+    sills = np.array([c[1] for c in comps], dtype=np.float64)
+    ranges = np.array([c[2] for c in comps], dtype=np.float64)
+    out = np.full_like(dists, np.nan)
+    _build.lib().orc_fill_vg_var_arr(
+        _ptr(dists), dists.shape[0], dists.shape[1], _ptr(out), int(covar_flag),
+        int(diag_mat_flag), len(comps), _ptr(codes), _ptr(sills), _ptr(ranges),
+        float(min_vg_val))
+    return out
+
+
+def get_svars_arr(dists_arr, vgs, interp_types, diag_mat_flag, min_vg_val):
+    var_flag = any(t in interp_types for t in ("OK", "EDK"))
+    covar_flag = "SK" in interp_types
+    out = {}
+    for vg in vgs:
+        assert vg != "nan"
+        if var_flag:
+            out[(vg, 0)] = fill_vg_var_arr(dists_arr, 0, diag_mat_flag, vg, min_vg_val)
+        if covar_flag:
+            out[(vg, 1)] = fill_vg_var_arr(dists_arr, 1, diag_mat_flag, vg, min_vg_val)
+    return out
+
+
+def get_2d_arr_subset(arr, row_idxs, col_idxs, rows_add_rc=0, cols_add_rc=0):
+    row_idxs = np.ascontiguousarray(row_idxs, dtype=np.int64)
+    col_idxs = np.ascontiguousarray(col_idxs, dtype=np.int64)
+    arr = np.ascontiguousarray(arr, dtype=np.float64)
+    sub = np.full((row_idxs.size + rows_add_rc, col_idxs.size + cols_add_rc), np.nan)
+    _build.lib().orc_copy_2d_arr_at_idxs(
+        _ptr(arr), arr.shape[1], _ptr(row_idxs), row_idxs.size, _ptr(col_idxs),
+        col_idxs.size, _ptr(sub), sub.shape[1])
+    return sub
+
+
+def get_vars_arr_subset(model, interp_type, ref_drfts, rr_all, dr_all,
+                        ref_ref_sub_idxs, time_neb_idxs_grp, dst_drfts):
+    if interp_type == "OK":
+        add_rc, covar_flag = 1, 0
+    elif interp_type == "SK":
+        add_rc, covar_flag = 0, 1
+    elif interp_type == "EDK":
+        add_rc, covar_flag = 1 + ref_drfts.shape[1], 0
+    else:
+        raise NotImplementedError(interp_type)
+    rr = get_2d_arr_subset(rr_all[(model, covar_flag)], ref_ref_sub_idxs,
+                           ref_ref_sub_idxs, add_rc, add_rc)
+    dr = get_2d_arr_subset(dr_all[(model, covar_flag)], time_neb_idxs_grp,
+                           ref_ref_sub_idxs, 0, add_rc)
+    n = ref_ref_sub_idxs.size
+    if interp_type == "OK":
+        rr[n, :n] = 1.0
+        rr[:, n] = 1.0
+        rr[n, n] = 0.0
+        dr[:, n] = 1.0
+    elif interp_type == "EDK":
+        rr[n, :n] = 1.0
+        rr[:n, n] = 1.0
+        dr[:, n] = 1.0
+        rr[n:, n:] = 0.0
+        for k in range(ref_drfts.shape[1]):
+            rr[n + 1 + k, :n] = ref_drfts[:, k]
+            rr[:n, n + 1 + k] = ref_drfts[:, k]
+            dr[:, n + 1 + k] = dst_drfts[k, :]
+    return rr, dr
+
+
+def fill_krig_idw_dst_data(n_refs, n_dsts, inv, dr_sub, dists_sub, ref_data, j,
+                           dst_data, est_vars):
+    for i in range(n_dsts):
+        lmds = np.matmul(inv, dr_sub[i])
+        if not np.isclose(lmds[:n_refs].sum(), 1.0):
+            dst_data[j, i] = ref_data[j, np.argmin(dists_sub[i])]
+            if est_vars is not None:
+                est_vars[j, i] = 0.0
+        else:
+            dst_data[j, i] = (lmds[:n_refs] * ref_data[j]).sum()
+            if est_vars is not None:
+                est_vars[j, i] = (lmds * dr_sub[i]).sum() + lmds[n_refs]
+
+
+def get_interp(ref_data, interp_type, ref_drfts, dst_drfts, idw_exp, models,
+               interp_steps_flags, nuggetness_flags, sub_time_steps,
+               prblm_time_steps, dists_sub, rr_all, dr_all, ref_ref_sub_idxs,
+               time_neb_idxs_grp, *, est_vars_flag, intrp_dtype=np.float32):
+    """interp/steps.py:245-401. ``dists_sub`` is modified in place by IDW,
+    as in the reference."""
+    n_dsts = dists_sub.shape[0]
+    n_refs = ref_data.shape[1]
+    n_time = ref_data.shape[0]
+    dst_data = np.full((n_time, n_dsts), np.nan)
+    est_vars = (np.full((n_time, n_dsts), np.nan, dtype=intrp_dtype)
+                if (est_vars_flag and interp_type == "OK") else None)
+    ref_means = ref_data.mean(axis=1)
+    if n_refs == 1:
+        for j in range(n_time):
+            dst_data[j, :] = ref_data[j, :]
+    elif interp_type == "NNB":
+        for i in range(n_dsts):
+            k = np.argmin(dists_sub[i])
+            for j in range(n_time):
+                dst_data[j, i] = ref_data[j, k]
+    elif interp_type == "IDW":
+        wts = np.full(n_refs, np.nan)
+        flags = np.ascontiguousarray(interp_steps_flags, dtype=np.uint8)
+        rd = np.ascontiguousarray(ref_data, dtype=np.float64)
+        rm = np.ascontiguousarray(ref_means, dtype=np.float64)
+        assert dists_sub.flags.c_contiguous
+        bad = _build.lib().orc_idw_group(
+            _ptr(dists_sub), n_dsts, n_refs, _ptr(rd), n_time, _ptr(flags),
+            _ptr(rm), float(idw_exp), _ptr(wts), _ptr(dst_data))
+        assert bad < 0, "IDW weight sum below 1e-14"
+    elif interp_type in ("OK", "SK", "EDK"):
+        old_model = ""
+        last_failed = False
+        inv = None
+        dr_sub = None
+        for j in np.argsort(models):
+            model = models[j]
+            if (not interp_steps_flags[j]) or nuggetness_flags[j]:
+                dst_data[j, :] = ref_means[j]
+                if est_vars is not None:
+                    est_vars[j, :] = 0.0
+                continue
+            if model == "nan":
+                raise ValueError("NaN VG!")
+            if model != old_model:
+                rr_sub, dr_sub = get_vars_arr_subset(
+                    model, interp_type, ref_drfts, rr_all, dr_all,
+                    ref_ref_sub_idxs, time_neb_idxs_grp, dst_drfts)
+                old_model = model
+                try:
+                    inv = np.linalg.pinv(rr_sub)
+                    last_failed = False
+                except Exception:
+                    last_failed = True
+                    if sub_time_steps[j] not in prblm_time_steps:
+                        prblm_time_steps.append(sub_time_steps[j])
+                    inv = np.nan
+            if last_failed:
+                for i in range(n_dsts):
+                    dst_data[j, i] = ref_data[j, np.argmin(dists_sub[i])]
+                if est_vars is not None:
+                    est_vars[j, :] = 0.0
+            else:
+                fill_krig_idw_dst_data(n_refs, n_dsts, inv, dr_sub, dists_sub,
+                                       ref_data, j, dst_data, est_vars)
+    else:
+        raise NotImplementedError(interp_type)
+    return dst_data, est_vars
+
+
+def mod_min_max(fld, min_var_cut, max_var_cut):
+    """interp/steps.py:466-476 (in place; NaN stays NaN)."""
+    with np.errstate(invalid="ignore"):
+        if min_var_cut is not None:
+            fld[fld < min_var_cut] = min_var_cut
+        if max_var_cut is not None:
+            fld[fld > max_var_cut] = max_var_cut
+
+
+def get_grps_in_time(data):
+    """interp/grps.py:57-101 without pandas: steps with the same set of
+    non-NaN stations, in order of first appearance.
+    Returns [(station_idxs, step_mask)]."""
+    avail = np.isfinite(data)
+    keys = [avail[i].tobytes() for i in range(data.shape[0])]
+    grps = []
+    seen = {}
+    for i, k in enumerate(keys):
+        if k in seen:
+            continue
+        mask = np.array([kk == k for kk in keys])
+        seen[k] = True
+        grps.append((np.where(avail[i])[0], mask))
+    return grps
+
+
+def interp_args_for(methods, est_vars):
+    """The (type, fig_dir, label[, idw_exp]) list of interp/prepare.py:638-695
+    for a list of methods like ['OK', 'SK', 'EDK', ('IDW', 2.0), 'NNB']."""
+    args = []
+    for t in ("OK", "SK", "EDK"):
+        if t in methods:
+            args.append((t, None, t))
+    idw = [m[1] for m in methods if isinstance(m, tuple) and m[0] == "IDW"]
+    for i, e in enumerate(idw):
+        args.append(("IDW", None, f"IDW_{i:03d}", float(e)))
+    if "NNB" in methods:
+        args.append(("NNB", None, "NNB"))
+    if est_vars:
+        args.append(("EST_VARS_OK", None, "EST_VARS_OK"))
+    return args
+
+
+def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *,
+                 est_vars=False, stn_drifts=None, cell_drifts=None,
+                 min_var_thr=0.0, min_var_cut=None, max_var_cut=None,
+                 min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None):
+    """interp/steps.py:478-835 for neighbour method 'all' and one grid chunk.
+
+    data [T, N] (NaN = station missing), vgs [T] strings (or None when no
+    kriging is asked for), stn_drifts [N, k], cell_drifts [k, C].
+    Returns ({label: [T, C] fields}, problem time steps).
+    """
+    data = np.asarray(data, dtype=np.float64)
+    n_steps = data.shape[0]
+    n_cells = cell_x.size
+    if time_steps is None:
+        time_steps = np.arange(n_steps)
+    interp_types = [a[0] for a in interp_args]
+    interp_labels = [a[2] for a in interp_args]
+    krg = any(t in interp_types for t in ("OK", "SK", "EDK"))
+    if krg:
+        vgs = np.asarray(vgs, dtype=object)
+        assert np.all(vgs != "nan")
+        uniq_vgs = list(dict.fromkeys(vgs.tolist()))
+        dr = get_dists_arr(stn_x, stn_y, stn_x, stn_y)
+        rr_all = get_svars_arr(dr, uniq_vgs, interp_types, 1, min_vg_val)
+    dd = get_dists_arr(cell_x, cell_y, stn_x, stn_y)
+    if krg:
+        dr_all = get_svars_arr(dd, uniq_vgs, interp_types, 0, min_vg_val)
+    else:
+        rr_all = dr_all = None
+    flds = {lab: np.full((n_steps, n_cells), np.nan, dtype=intrp_dtype)
+            for lab in interp_labels}
+    prblm = []
+    all_cells = np.arange(n_cells)
+    for stn_idxs, step_mask in get_grps_in_time(data):
+        sub_time_steps = time_steps[step_mask]
+        if not stn_idxs.size:
+            for s in sub_time_steps:
+                if s not in prblm:
+                    prblm.append(s)
+            continue
+        vals = data[step_mask][:, stn_idxs]
+        drifts = stn_drifts[stn_idxs, :] if "EDK" in interp_types else None
+        if krg:
+            models = vgs[step_mask]
+            nug = np.array([check_full_nuggetness(m, min_vg_val) for m in models])
+        else:
+            models = nug = None
+        time_idxs = np.where(step_mask)[0]
+        # neighbour method 'all': one cell group holding every cell, every
+        # station of the group is a neighbour.
+        sub_ref_data = vals.copy("c")
+        dists_sub = get_2d_arr_subset(dd, all_cells, stn_idxs, 0, 0)
+        flags = np.array([np.any(sub_ref_data[j] >= min_var_thr)
+                          for j in range(sub_ref_data.shape[0])])
+        sub_dst_drifts = cell_drifts[:, all_cells] if "EDK" in interp_types else None
+        for i, t in enumerate(interp_types):
+            if interp_labels[i] == "EST_VARS_OK":
+                continue
+            idw_exp = interp_args[i][3] if t == "IDW" else 5
+            vals_i, ev = get_interp(
+                sub_ref_data, t, drifts, sub_dst_drifts, idw_exp, models, flags,
+                nug, sub_time_steps, prblm, dists_sub, rr_all, dr_all, stn_idxs,
+                all_cells, est_vars_flag=est_vars, intrp_dtype=intrp_dtype)
+            mod_min_max(vals_i, min_var_cut, max_var_cut)
+            for j, ti in enumerate(time_idxs):
+                flds[interp_labels[i]][ti, :] = vals_i[j].astype(intrp_dtype)
+                if est_vars and t == "OK":
+                    flds["EST_VARS_OK"][ti, :] = ev[j]
+    return flds, prblm
+
+
+def ret_mp_idxs(n_vals, n_cpus):
+    """misc.py:601-613."""
+    idxs = np.linspace(0, n_vals, n_cpus + 1, endpoint=True, dtype=np.int64)
+    idxs = np.unique(idxs)
+    if idxs.shape[0] == 1:
+        idxs = np.concatenate((np.array([0]), idxs))
+    return idxs

@@ -1,0 +1,352 @@
+"""Generate golden vectors by running the REFERENCE's own code.
+
+TEST INFRASTRUCTURE. Run only where the reference tree exists::
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+It loads the unmodified reference (interp/steps.py, interp/grps.py, misc.py
+and cyth/interpmthds.pyx compiled by oracle/build_ref.py, see refharness.py)
+and writes small seeded cases to tests/golden/*.npz:
+
+- kernels.npz   fill_dists_2d_mat, fill_vg_var_arr (every model, covar and
+                diagonal flags, min_vg_val zeroing), fill_wts_and_sum,
+                get_mults_sum, copy_2d_arr_at_idxs, check_full_nuggetness
+- interp.npz    SpInterpSteps._get_interp for OK (+variance), SK, EDK (1 and 2
+                drifts), IDW (several exponents, a cell on a station), NNB,
+                one station, flags off, nugget-only variograms, mixed models
+- steps.npz     whole multi-step runs with missing stations: the reference's
+                _get_interp called per station group by the same loop as
+                interp/steps.py:673-835 (that loop needs pandas, which is not
+                installed, so its few lines of bookkeeping are restated here)
+- nebs.npz      SpInterpNeighborGrouping.get_neb_idxs_and_grps for 'nrst' and
+                'pie' (interp/grps.py:103-288, cyth sel_equidist_refs)
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+from refharness import load_reference, make_steps  # noqa: E402
+
+VG_STRS = [
+    "0.05 Nug(0.0) + 0.95 Exp(20000)",
+    "1.0 Sph(30000)",
+    "0.2 Nug(0.0) + 0.8 Gau(15000)",
+    "0.7 Lin(40000)",
+    "0.5 Pow(1.2)",
+    "1.5 Hol(25000)",
+    "0.3 Nug(0.0) + 0.4 Sph(10000) + 0.3 Exp(50000)",
+    "2.0 Rng(1.0)",
+    "1.0 Exp(0.0)",
+]
+
+
+def grid_cells(x0, y1, cs, nx, ny):
+    """Cell centres as interp/prepare.py:193-234 builds them (row-major,
+    y descending)."""
+    xs = np.linspace(x0 + 0.5 * cs, x0 + 0.5 * cs + (nx - 1) * cs, nx)
+    ys = np.linspace(y1 - 0.5 * cs, y1 - 0.5 * cs - (ny - 1) * cs, ny)
+    mx, my = np.meshgrid(xs, ys)
+    return mx.ravel(), my.ravel()
+
+
+def grf_values(rng, xs, ys, vg_str, n_steps, mean, ref):
+    """Values = mean + GRF with the covariance of ``vg_str`` (Cholesky)."""
+    d = np.hypot(xs[:, None] - xs[None], ys[:, None] - ys[None])
+    g = ref.misc.get_theo_vg_vals(vg_str, d.ravel()).reshape(d.shape)
+    sill = sum(float(p.strip().split(" ")[0]) for p in vg_str.split("+"))
+    c = sill - g
+    c[np.diag_indices_from(c)] = sill
+    ll = np.linalg.cholesky(c + 1e-10 * np.eye(c.shape[0]))
+    return mean + (ll @ rng.standard_normal((xs.size, n_steps))).T
+
+
+def kernels_case(ref, out):
+    cy = ref.cy
+    rng = np.random.default_rng(11)
+    n, c = 23, 41
+    sx, sy = rng.uniform(0, 1e5, n), rng.uniform(0, 1e5, n)
+    cx, cy_ = rng.uniform(0, 1e5, c), rng.uniform(0, 1e5, c)
+    cx[:3], cy_[:3] = sx[:3], sy[:3]  # cells on stations: zero distances
+    d_cs = np.full((c, n), np.nan)
+    cy.fill_dists_2d_mat(cx, cy_, sx, sy, d_cs)
+    d_ss = np.full((n, n), np.nan)
+    cy.fill_dists_2d_mat(sx, sy, sx, sy, d_ss)
+    out.update(k_sx=sx, k_sy=sy, k_cx=cx, k_cy=cy_, k_d_cs=d_cs, k_d_ss=d_ss)
+    out["k_vgs"] = np.array(VG_STRS)
+    for vi, vg in enumerate(VG_STRS):
+        for covar in (0, 1):
+            for mvv in (0.0, 1e-4, 0.05):
+                a = np.full_like(d_ss, np.nan)
+                cy.fill_vg_var_arr(d_ss, a, covar, 1, vg, mvv)
+                b = np.full_like(d_cs, np.nan)
+                cy.fill_vg_var_arr(d_cs, b, covar, 0, vg, mvv)
+                out[f"k_vg_ss_{vi}_{covar}_{mvv:g}"] = a
+                out[f"k_vg_cs_{vi}_{covar}_{mvv:g}"] = b
+    # IDW primitives on one row of distances
+    for e in (1.0, 2.0, 3.5):
+        dist = d_cs[5].copy() / d_cs[5].max()
+        w = np.full(n, np.nan)
+        s = cy.fill_wts_and_sum(dist, w, e)
+        z = rng.normal(size=n)
+        out[f"k_idw_w_{e:g}"] = w
+        out[f"k_idw_s_{e:g}"] = np.array(s)
+        out[f"k_idw_z_{e:g}"] = z
+        out[f"k_idw_m_{e:g}"] = np.array(cy.get_mults_sum(w, z))
+    ri = np.array([4, 0, 17, 3], dtype=np.int64)
+    ci = np.array([22, 1, 5], dtype=np.int64)
+    sub = np.full((ri.size + 2, ci.size + 1), np.nan)
+    cy.copy_2d_arr_at_idxs(d_cs, ri, ci, sub)
+    out.update(k_copy_ri=ri, k_copy_ci=ci, k_copy_sub=sub)
+    nug_cases = VG_STRS + ["1.0 Nug(0.0)", "0.00001 Exp(1000)", "1.0 Exp(0.00001)",
+                           "0.5 Nug(0.0) + 0.5 Nug(0.0)"]
+    out["k_nug_strs"] = np.array(nug_cases)
+    out["k_nug_1e-4"] = np.array(
+        [ref.misc.check_full_nuggetness(s, 1e-4) for s in nug_cases])
+    out["k_nug_0"] = np.array([ref.misc.check_full_nuggetness(s, 0.0) for s in nug_cases])
+
+
+def interp_one(ref, st, sx, sy, cx, cy, z, itype, vgs, *, idw_exp=5.0,
+               flags=None, nug=None, drifts=None, cell_drifts=None, mvv=1e-4):
+    """One _get_interp call over all stations/cells (one group)."""
+    n, c, t = sx.size, cx.size, z.shape[0]
+    d_cs = st._get_dists_arr(cx, cy, sx, sy)
+    d_ss = st._get_dists_arr(sx, sy, sx, sy)
+    uv = list(dict.fromkeys(vgs))
+    rr = st._get_svars_arr(d_ss, uv, [itype], 1) if itype in ("OK", "SK", "EDK") else None
+    dr = st._get_svars_arr(d_cs, uv, [itype], 0) if itype in ("OK", "SK", "EDK") else None
+    if flags is None:
+        flags = np.ones(t, dtype=bool)
+    if nug is None:
+        nug = np.array([ref.misc.check_full_nuggetness(v, mvv) for v in vgs])
+    prblm = []
+    est, var = st._get_interp(
+        z.copy("c"), itype, drifts, cell_drifts, idw_exp, np.array(vgs, dtype=object),
+        flags, nug, np.arange(t), prblm, d_cs.copy(), rr, dr, np.arange(n),
+        np.arange(c))
+    return est, var, prblm
+
+
+def interp_case(ref, out):
+    rng = np.random.default_rng(22)
+    n, t = 31, 5
+    sx, sy = rng.uniform(0, 1e5, n), rng.uniform(0, 1e5, n)
+    cx, cy = grid_cells(0.0, 1e5, 5000.0, 20, 20)
+    cx = cx.copy()
+    cy = cy.copy()
+    vg0 = "0.05 Nug(0.0) + 0.95 Exp(20000)"
+    z = grf_values(rng, sx, sy, vg0, t, 5.0, ref)
+    out.update(i_sx=sx, i_sy=sy, i_cx=cx, i_cy=cy, i_z=z)
+    vgs_mixed = [vg0, "1.0 Sph(30000)", vg0, "0.2 Nug(0.0) + 0.8 Gau(15000)", "1.0 Nug(0.0)"]
+    out["i_vgs_mixed"] = np.array(vgs_mixed)
+    flags = np.array([True, True, False, True, True])
+    out["i_flags"] = flags
+    st = make_steps(ref, min_vg_val=1e-4, est_vars=True)
+    for itype in ("OK", "SK"):
+        est, var, prblm = interp_one(ref, st, sx, sy, cx, cy, z, itype, vgs_mixed, flags=flags)
+        out[f"i_{itype}_est"] = est
+        if var is not None:
+            out[f"i_{itype}_var"] = var
+    # models exercising Lin / Pow / Hol / three components on OK
+    vgs_other = ["0.7 Lin(40000)", "0.5 Pow(1.2)", "1.5 Hol(25000)",
+                 "0.3 Nug(0.0) + 0.4 Sph(10000) + 0.3 Exp(50000)", vg0]
+    out["i_vgs_other"] = np.array(vgs_other)
+    est, var, _ = interp_one(ref, st, sx, sy, cx, cy, z, "OK", vgs_other)
+    out["i_OKo_est"] = est
+    out["i_OKo_var"] = var
+    # EDK with one and two drifts
+    elev = 1000 + 5e-3 * sx + 3e-3 * sy + rng.normal(0, 20, n)
+    cel = 1000 + 5e-3 * cx + 3e-3 * cy
+    for k in (1, 2):
+        sd = np.stack([elev, sx / 1e3], 1)[:, :k].copy()
+        cd = np.stack([cel, cx / 1e3], 0)[:k].copy()
+        est, _, _ = interp_one(ref, st, sx, sy, cx, cy, z + 1e-3 * elev, "EDK",
+                               vgs_mixed, flags=flags, drifts=sd, cell_drifts=cd)
+        out[f"i_EDK{k}_est"] = est
+        out[f"i_EDK{k}_sd"] = sd
+        out[f"i_EDK{k}_cd"] = cd
+    # IDW with several exponents; cell 0 moved onto station 0 -> NaN
+    cx2, cy2 = cx.copy(), cy.copy()
+    cx2[0], cy2[0] = sx[0], sy[0]
+    out.update(i_cx2=cx2, i_cy2=cy2)
+    for e in (1.0, 2.0, 3.5):
+        est, _, _ = interp_one(ref, st, sx, sy, cx2, cy2, z, "IDW", [vg0] * t,
+                               idw_exp=e, flags=flags)
+        out[f"i_IDW_{e:g}_est"] = est
+    est, _, _ = interp_one(ref, st, sx, sy, cx2, cy2, z, "NNB", [vg0] * t)
+    out["i_NNB_est"] = est
+    # a single station
+    est, var, _ = interp_one(ref, st, sx[:1], sy[:1], cx, cy, z[:, :1], "OK", [vg0] * t)
+    out["i_one_est"] = est
+    out["i_one_var"] = var
+
+
+def steps_case(ref, out, tag, *, n, t, nx, ny, cs, box, p_miss, vgs, methods,
+               seed, min_var_thr=0.0, min_var_cut=None, max_var_cut=None,
+               mvv=1e-4, edk=False):
+    """A multi-step run: per station group, the reference's _get_interp for
+    every method, clipped by _mod_min_max and cast to float32 as in
+    interp/steps.py:673-835."""
+    rng = np.random.default_rng(seed)
+    sx, sy = rng.uniform(0, box, n), rng.uniform(0, box, n)
+    cx, cy = grid_cells(0.0, box, cs, nx, ny)
+    z = grf_values(rng, sx, sy, "0.1 Nug(0.0) + 0.9 Sph(40000)", t, 3.0, ref)
+    if p_miss > 0:
+        miss = rng.uniform(size=(t, n)) < p_miss
+        z[miss] = np.nan
+        z[2, :] = np.nan            # one step without any station
+        z[3, :] = np.nan
+        z[3, 4] = 1.25              # one step with a single station
+        z[5, :] = z[4, :]           # two steps sharing a station set
+    z[1, np.isfinite(z[1])] = -1.0  # a step under min_var_thr (flags off)
+    sd = cd = None
+    if edk:
+        sd = (100 + 2e-3 * sx + rng.normal(0, 5, n))[:, None].copy()
+        cd = (100 + 2e-3 * cx)[None].copy()
+    st = make_steps(ref, min_vg_val=mvv, est_vars=True, min_var_thr=min_var_thr,
+                    min_var_cut=min_var_cut, max_var_cut=max_var_cut)
+    d_cs = st._get_dists_arr(cx, cy, sx, sy)
+    d_ss = st._get_dists_arr(sx, sy, sx, sy)
+    types = [m if isinstance(m, str) else m[0] for m in methods]
+    uv = list(dict.fromkeys(vgs))
+    rr = st._get_svars_arr(d_ss, uv, types, 1)
+    dr = st._get_svars_arr(d_cs, uv, types, 0)
+    labels = []
+    for m in methods:
+        if isinstance(m, tuple):
+            labels.append(f"IDW_{sum(1 for l in labels if l.startswith('IDW')):03d}")
+        else:
+            labels.append(m)
+    flds = {lab: np.full((t, cx.size), np.nan, dtype=np.float32) for lab in labels}
+    flds["EST_VARS_OK"] = np.full((t, cx.size), np.nan, dtype=np.float32)
+    avail = np.isfinite(z)
+    keys = [avail[i].tobytes() for i in range(t)]
+    done = set()
+    prblm = []
+    vgs_arr = np.array(vgs, dtype=object)
+    for i0 in range(t):
+        if keys[i0] in done:
+            continue
+        done.add(keys[i0])
+        mask = np.array([k == keys[i0] for k in keys])
+        stn = np.where(avail[i0])[0]
+        if not stn.size:
+            prblm.extend(np.where(mask)[0].tolist())
+            continue
+        vals = z[mask][:, stn].copy("c")
+        flags = np.array([np.any(v >= min_var_thr) for v in vals])
+        nug = np.array([ref.misc.check_full_nuggetness(v, mvv) for v in vgs_arr[mask]])
+        dsub = st._get_2d_arr_subset(d_cs, np.arange(cx.size), stn, 0, 0)
+        tid = np.where(mask)[0]
+        for m, lab in zip(methods, labels):
+            itype = m if isinstance(m, str) else m[0]
+            e = m[1] if isinstance(m, tuple) else 5
+            est, var = st._get_interp(
+                vals, itype, sd[stn] if edk else None, cd if edk else None, e,
+                vgs_arr[mask], flags, nug, tid, prblm, dsub, rr, dr, stn,
+                np.arange(cx.size))
+            st._mod_min_max(est)
+            for j, ti in enumerate(tid):
+                flds[lab][ti] = est[j].astype(np.float32)
+                if itype == "OK":
+                    flds["EST_VARS_OK"][ti] = var[j]
+    out[f"s_{tag}_sx"] = sx
+    out[f"s_{tag}_sy"] = sy
+    out[f"s_{tag}_cx"] = cx
+    out[f"s_{tag}_cy"] = cy
+    out[f"s_{tag}_z"] = z
+    out[f"s_{tag}_vgs"] = np.array(vgs)
+    out[f"s_{tag}_methods"] = np.array([m if isinstance(m, str) else f"IDW:{m[1]}"
+                                        for m in methods])
+    out[f"s_{tag}_params"] = np.array(
+        [min_var_thr, np.nan if min_var_cut is None else min_var_cut,
+         np.nan if max_var_cut is None else max_var_cut, mvv])
+    if edk:
+        out[f"s_{tag}_sd"] = sd
+        out[f"s_{tag}_cd"] = cd
+    out[f"s_{tag}_prblm"] = np.array(sorted(set(prblm)), dtype=np.int64)
+    for lab, f in flds.items():
+        out[f"s_{tag}_out_{lab}"] = f
+
+
+class _NumpyLLP64:
+    """numpy with ``uint32`` mapped to ``uint64``.
+
+    interp/grps.py:176-178 allocates ``np.uint32`` buffers for arguments that
+    cyth/interpmthds.pyx:811-823 types as ``unsigned long``. That matches on
+    the reference author's Windows (LLP64, 32-bit long) but raises a buffer
+    dtype error on Linux (LP64). Running the reference's own module with this
+    shim as its ``np`` reproduces what it computes where it works."""
+
+    def __getattr__(self, item):
+        if item == "uint32":
+            return np.uint64
+        return getattr(np, item)
+
+
+def nebs_case(ref, out):
+    ref.grps.np = _NumpyLLP64()
+    rng = np.random.default_rng(33)
+    n = 40
+    sx, sy = rng.uniform(0, 5e4, n), rng.uniform(0, 5e4, n)
+    cx, cy = grid_cells(0.0, 5e4, 2500.0, 20, 20)
+    out.update(n_sx=sx, n_sy=sy, n_cx=cx, n_cy=cy)
+    for mth, nn, npie in (("nrst", 8, 1), ("pie", 8, 4), ("pie", 12, 6)):
+        g = ref.grps.SpInterpNeighborGrouping(mth, nn, npie, cx.copy(), cy.copy(),
+                                              verbose=False)
+        idxs, grps = g.get_neb_idxs_and_grps(sx.copy(), sy.copy())
+        tag = f"{mth}_{nn}_{npie}"
+        out[f"n_{tag}_idxs"] = idxs.astype(np.int64)
+        lab = np.full(cx.size, -1, dtype=np.int64)
+        for gi, gr in enumerate(grps):
+            lab[gr] = gi
+        out[f"n_{tag}_grp"] = lab
+
+
+def main(ref_root="/root/reference"):
+    ref = load_reference(ref_root)
+    out = {}
+    kernels_case(ref, out)
+    np.savez_compressed(HERE / "kernels.npz", **out)
+    out = {}
+    interp_case(ref, out)
+    np.savez_compressed(HERE / "interp.npz", **out)
+    out = {}
+    vg_mix = ["0.05 Nug(0.0) + 0.95 Exp(20000)", "1.0 Sph(30000)",
+              "0.2 Nug(0.0) + 0.8 Gau(15000)", "1.0 Nug(0.0)"]
+    t = 12
+    vgs = [vg_mix[i % len(vg_mix)] for i in range(t)]
+    steps_case(ref, out, "okidw", n=40, t=t, nx=24, ny=18, cs=2500.0, box=6e4,
+               p_miss=0.25, vgs=vgs, seed=44,
+               methods=["OK", "SK", ("IDW", 2.0), ("IDW", 1.0), "NNB"],
+               min_var_thr=0.0, min_var_cut=0.0, max_var_cut=None)
+    steps_case(ref, out, "edk", n=35, t=t, nx=20, ny=20, cs=3000.0, box=6e4,
+               p_miss=0.2, vgs=vgs, seed=55, methods=["EDK", "OK"], edk=True,
+               min_var_thr=0.5, min_var_cut=None, max_var_cut=4.5)
+    # config-1 shapes (150 stations, 100 km box, Exp vg, all stations present)
+    # on a sub-sampled grid: every 8th row and column of the 200 x 200 grid.
+    rng = np.random.default_rng(1)
+    n1 = 150
+    sx, sy = rng.uniform(0, 1e5, n1), rng.uniform(0, 1e5, n1)
+    vg1 = "0.05 Nug(0.0) + 0.95 Exp(20000)"
+    z1 = grf_values(rng, sx, sy, vg1, 4, 5.0, ref)
+    cx, cy = grid_cells(0.0, 1e5, 500.0, 200, 200)
+    sel = (np.arange(200)[:, None] % 8 == 0) & (np.arange(200)[None] % 8 == 0)
+    cx, cy = cx[sel.ravel()].copy(), cy[sel.ravel()].copy()
+    st = make_steps(ref, min_vg_val=1e-4, est_vars=True)
+    est, var, _ = interp_one(ref, st, sx, sy, cx, cy, z1, "OK", [vg1] * 4)
+    est_idw, _, _ = interp_one(ref, st, sx, sy, cx, cy, z1, "IDW", [vg1] * 4, idw_exp=2.0)
+    out.update(c1_sx=sx, c1_sy=sy, c1_z=z1, c1_cx=cx, c1_cy=cy, c1_ok_est=est,
+               c1_ok_var=var, c1_idw_est=est_idw)
+    np.savez_compressed(HERE / "steps.npz", **out)
+    out = {}
+    nebs_case(ref, out)
+    np.savez_compressed(HERE / "nebs.npz", **out)
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

@@ -1,0 +1,111 @@
+"""Import the reference's own step engine in this container (fixture making only).
+
+TEST INFRASTRUCTURE. Used by ``make_golden.py`` to run the UNMODIFIED reference
+code (``interp/steps.py``, ``interp/grps.py``, ``interp/vgclus.py``,
+``misc.py`` and the Cython kernels of ``cyth/interpmthds.pyx``) on small
+seeded inputs. The reference tree is read only and is never present where the
+GPU tests run; the fixtures it produces are committed under ``tests/golden``.
+
+What is stubbed, and why it does not touch the numeric path:
+- ``netCDF4``, ``osgeo``, ``shapefile``, ``cftime``, ``pathos``: imported at
+  module level by ``misc.py``/``interp/steps.py`` for I/O only.
+- ``pandas``: imported by ``interp/grps.py``/``interp/vgclus.py``; the fixtures
+  call ``_get_interp`` and ``SpInterpNeighborGrouping.get_neb_idxs_and_grps``,
+  neither of which uses pandas.
+- the package ``spinterps`` is registered with ``__path__`` pointing at the
+  reference root so that the relative imports resolve without running the
+  package ``__init__`` (which pulls in matplotlib and GIS modules).
+- ``spinterps.cyth`` is the reference's ``cyth/interpmthds.pyx`` compiled by
+  ``oracle/build_ref.py`` (Cython 3, ``cpow=True``).
+"""
+import importlib
+import importlib.util
+import sys
+import types
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parents[2]
+
+
+def _stub(name, **attrs):
+    mod = types.ModuleType(name)
+    for k, v in attrs.items():
+        setattr(mod, k, v)
+    sys.modules[name] = mod
+    return mod
+
+
+def load_reference(ref_root="/root/reference"):
+    """Return a namespace with the reference's step engine and kernels."""
+    ref_root = Path(ref_root)
+    sys.path.insert(0, str(REPO))
+    from oracle import build_ref
+
+    so_dir = build_ref.build(ref_root)
+    if so_dir is None:
+        raise RuntimeError("reference tree or Cython not available")
+
+    class _Anything:
+        def __getattr__(self, item):
+            return _Anything()
+
+        def __call__(self, *a, **k):
+            return _Anything()
+
+    _stub("netCDF4", Dataset=None)
+    _stub("shapefile")
+    osgeo = _stub("osgeo")
+    osgeo.ogr = _Anything()
+    osgeo.gdal = _Anything()
+    sys.modules["osgeo.ogr"] = osgeo.ogr
+    sys.modules["osgeo.gdal"] = osgeo.gdal
+    _stub("cftime", datetime=None)
+    _stub("pathos")
+    _stub("pathos.multiprocessing", ProcessPool=None)
+    if "pandas" not in sys.modules:
+        try:
+            import pandas  # noqa: F401
+        except ImportError:
+            _stub("pandas", DataFrame=object, Series=object, Index=object)
+
+    pkg = types.ModuleType("spinterps")
+    pkg.__path__ = [str(ref_root)]
+    sys.modules["spinterps"] = pkg
+    interp_pkg = types.ModuleType("spinterps.interp")
+    interp_pkg.__path__ = [str(ref_root / "interp")]
+    sys.modules["spinterps.interp"] = interp_pkg
+
+    spec = importlib.util.spec_from_file_location(
+        "spinterps.cyth.interpmthds",
+        str(next(Path(so_dir).glob("interpmthds*.so"))))
+    cy = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(cy)
+    cyth_pkg = types.ModuleType("spinterps.cyth")
+    cyth_pkg.__path__ = []
+    for name in dir(cy):
+        if not name.startswith("__"):
+            setattr(cyth_pkg, name, getattr(cy, name))
+    sys.modules["spinterps.cyth"] = cyth_pkg
+    sys.modules["spinterps.cyth.interpmthds"] = cy
+
+    misc = importlib.import_module("spinterps.misc")
+    steps = importlib.import_module("spinterps.interp.steps")
+    grps = importlib.import_module("spinterps.interp.grps")
+    return types.SimpleNamespace(cy=cy, misc=misc, steps=steps, grps=grps)
+
+
+def make_steps(ref, *, min_vg_val, est_vars, intrp_dtype="float32",
+               min_var_thr=0.0, min_var_cut=None, max_var_cut=None):
+    """Build a ``SpInterpSteps`` without its driver (only the attributes the
+    step engine reads, ``interp/steps.py:31-58``)."""
+    import numpy as np
+
+    obj = ref.steps.SpInterpSteps.__new__(ref.steps.SpInterpSteps)
+    obj._vb = False
+    obj._min_vg_val = float(min_vg_val)
+    obj._interp_flag_est_vars = bool(est_vars)
+    obj._intrp_dtype = np.dtype(intrp_dtype)
+    obj._min_var_thr = min_var_thr
+    obj._min_var_cut = min_var_cut
+    obj._max_var_cut = max_var_cut
+    return obj

@@ -1,0 +1,167 @@
+"""Pin the oracle (oracle/port.py + oracle/vgfill.c) to the reference.
+
+The golden vectors were produced by running the reference's own code
+(tests/golden/make_golden.py). Distances, variogram fills, IDW primitives and
+gathers must match bit for bit; kriging results go through LAPACK's pinv,
+whose last bits depend on the BLAS build, so they are compared at 1e-11
+relative to the field's scale.
+"""
+import numpy as np
+import pytest
+
+from oracle import port
+
+KRIG_RTOL = 1e-11
+
+
+def _close(a, b, rtol=KRIG_RTOL):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = np.isfinite(b)
+    scale = max(np.abs(b[m]).max(), 1e-300) if m.any() else 1.0
+    err = np.abs(a[m] - b[m]).max() / scale if m.any() else 0.0
+    assert err <= rtol, err
+
+
+def test_dists_bit_exact(golden):
+    g = golden
+    d = port.get_dists_arr(g["k_cx"], g["k_cy"], g["k_sx"], g["k_sy"])
+    assert np.array_equal(d, g["k_d_cs"])
+    d = port.get_dists_arr(g["k_sx"], g["k_sy"], g["k_sx"], g["k_sy"])
+    assert np.array_equal(d, g["k_d_ss"])
+
+
+def test_vg_fill_bit_exact(golden):
+    g = golden
+    for vi, vg in enumerate(g["k_vgs"]):
+        for covar in (0, 1):
+            for mvv in (0.0, 1e-4, 0.05):
+                a = port.fill_vg_var_arr(g["k_d_ss"], covar, 1, str(vg), mvv)
+                assert np.array_equal(a, g[f"k_vg_ss_{vi}_{covar}_{mvv:g}"]), (vg, covar, mvv)
+                b = port.fill_vg_var_arr(g["k_d_cs"], covar, 0, str(vg), mvv)
+                assert np.array_equal(b, g[f"k_vg_cs_{vi}_{covar}_{mvv:g}"]), (vg, covar, mvv)
+
+
+def test_idw_primitives_and_gather(golden):
+    import ctypes
+    from oracle import build
+    lib = build.lib()
+    g = golden
+    for e in (1.0, 2.0, 3.5):
+        d = g["k_d_cs"][5].copy() / g["k_d_cs"][5].max()
+        w = np.empty_like(d)
+        s = lib.orc_fill_wts_and_sum(ctypes.c_void_p(d.ctypes.data), d.size,
+                                     ctypes.c_void_p(w.ctypes.data), e)
+        assert np.array_equal(w, g[f"k_idw_w_{e:g}"])
+        assert s == g[f"k_idw_s_{e:g}"]
+        z = g[f"k_idw_z_{e:g}"]
+        m = lib.orc_get_mults_sum(ctypes.c_void_p(w.ctypes.data),
+                                  ctypes.c_void_p(z.ctypes.data), z.size)
+        assert m == g[f"k_idw_m_{e:g}"]
+    sub = port.get_2d_arr_subset(g["k_d_cs"], g["k_copy_ri"], g["k_copy_ci"], 2, 1)
+    assert np.array_equal(np.isnan(sub), np.isnan(g["k_copy_sub"]))
+    assert np.array_equal(np.nan_to_num(sub), np.nan_to_num(g["k_copy_sub"]))
+
+
+def test_nuggetness(golden):
+    g = golden
+    for s, r4, r0 in zip(g["k_nug_strs"], g["k_nug_1e-4"], g["k_nug_0"]):
+        assert port.check_full_nuggetness(str(s), 1e-4) == bool(r4), s
+        assert port.check_full_nuggetness(str(s), 0.0) == bool(r0), s
+
+
+def _interp(g, itype, vgs, *, cx="i_cx", cy="i_cy", z=None, n=None, flags=None,
+            idw_exp=5.0, sd=None, cd=None):
+    sx, sy = g["i_sx"], g["i_sy"]
+    z = g["i_z"] if z is None else z
+    if n is not None:
+        sx, sy, z = sx[:n], sy[:n], z[:, :n]
+    cxv, cyv = g[cx], g[cy]
+    t = z.shape[0]
+    vgs = [str(v) for v in vgs]
+    krig = itype in ("OK", "SK", "EDK")
+    d_cs = port.get_dists_arr(cxv, cyv, sx, sy)
+    d_ss = port.get_dists_arr(sx, sy, sx, sy)
+    uv = list(dict.fromkeys(vgs))
+    rr = port.get_svars_arr(d_ss, uv, [itype], 1, 1e-4) if krig else None
+    dr = port.get_svars_arr(d_cs, uv, [itype], 0, 1e-4) if krig else None
+    if flags is None:
+        flags = np.ones(t, dtype=bool)
+    nug = np.array([port.check_full_nuggetness(v, 1e-4) for v in vgs])
+    return port.get_interp(z.copy("c"), itype, sd, cd, idw_exp, np.array(vgs, dtype=object),
+                           flags, nug, np.arange(t), [], d_cs.copy(), rr, dr,
+                           np.arange(sx.size), np.arange(cxv.size), est_vars_flag=True)
+
+
+def test_get_interp_ok_sk(golden):
+    g = golden
+    for itype in ("OK", "SK"):
+        est, var = _interp(g, itype, g["i_vgs_mixed"], flags=g["i_flags"])
+        _close(est, g[f"i_{itype}_est"])
+        if itype == "OK":
+            _close(var, g["i_OK_var"], 1e-6)   # float32 storage
+    est, var = _interp(g, "OK", g["i_vgs_other"])
+    _close(est, g["i_OKo_est"])
+    _close(var, g["i_OKo_var"], 1e-6)
+
+
+def test_get_interp_edk(golden):
+    g = golden
+    elev = g["i_EDK1_sd"][:, 0]
+    for k in (1, 2):
+        est, _ = _interp(g, "EDK", g["i_vgs_mixed"], z=g["i_z"] + 1e-3 * elev,
+                         flags=g["i_flags"], sd=g[f"i_EDK{k}_sd"], cd=g[f"i_EDK{k}_cd"])
+        _close(est, g[f"i_EDK{k}_est"])
+
+
+def test_get_interp_idw_nnb_one(golden):
+    g = golden
+    t = g["i_z"].shape[0]
+    vg0 = "0.05 Nug(0.0) + 0.95 Exp(20000)"
+    for e in (1.0, 2.0, 3.5):
+        est, _ = _interp(g, "IDW", [vg0] * t, cx="i_cx2", cy="i_cy2", flags=g["i_flags"],
+                         idw_exp=e)
+        assert np.isnan(est[g["i_flags"], 0]).all()
+        _close(est, g[f"i_IDW_{e:g}_est"], 1e-15)
+    est, _ = _interp(g, "NNB", [vg0] * t, cx="i_cx2", cy="i_cy2")
+    assert np.array_equal(est, g["i_NNB_est"])
+    est, var = _interp(g, "OK", [vg0] * t, n=1)
+    assert np.array_equal(est, g["i_one_est"])
+    assert np.isnan(var).all() and np.isnan(g["i_one_var"]).all()
+
+
+@pytest.mark.parametrize("tag", ["okidw", "edk"])
+def test_interp_steps(golden, tag):
+    g = golden
+    p = f"s_{tag}_"
+    methods = []
+    for m in g[p + "methods"]:
+        m = str(m)
+        methods.append(("IDW", float(m.split(":")[1])) if m.startswith("IDW:") else m)
+    thr, mn, mx, mvv = g[p + "params"]
+    args = port.interp_args_for(methods, est_vars="OK" in methods)
+    flds, prblm = port.interp_steps(
+        g[p + "sx"], g[p + "sy"], g[p + "z"], g[p + "cx"], g[p + "cy"],
+        [str(v) for v in g[p + "vgs"]], args, est_vars="OK" in methods,
+        stn_drifts=g.get(p + "sd"), cell_drifts=g.get(p + "cd"),
+        min_var_thr=thr, min_var_cut=None if np.isnan(mn) else mn,
+        max_var_cut=None if np.isnan(mx) else mx, min_vg_val=mvv)
+    assert sorted(set(prblm)) == g[p + "prblm"].tolist()
+    for lab, f in flds.items():
+        ref = g[p + "out_" + lab]
+        _close(f, ref, 1e-6)
+
+
+def test_config1_subset(golden):
+    g = golden
+    sx, sy, z = g["c1_sx"], g["c1_sy"], g["c1_z"]
+    cx, cy = g["c1_cx"], g["c1_cy"]
+    vg = "0.05 Nug(0.0) + 0.95 Exp(20000)"
+    args = port.interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
+    flds, _ = port.interp_steps(sx, sy, z, cx, cy, [vg] * z.shape[0], args, est_vars=True,
+                                min_vg_val=1e-4, intrp_dtype=np.float64)
+    _close(flds["OK"], g["c1_ok_est"])
+    _close(flds["EST_VARS_OK"], g["c1_ok_var"], 1e-6)
+    _close(flds["IDW_000"], g["c1_idw_est"], 1e-14)
