@@ -1,0 +1,246 @@
+/*
+ * spinterps_gb300 -- C ABI of the GB300 (sm_103a) gridded-interpolation path.
+ *
+ * Every entry point takes plain pointers and sizes. Arrays marked "device"
+ * are CUDA device pointers (for example torch tensors' data_ptr()); all
+ * launches go onto the caller's stream and are stream-ordered (no entry
+ * point synchronises unless stated). The caller owns every buffer,
+ * including the workspace. Every function returns an spi_status; no C++
+ * exception crosses this boundary. Not reentrant on one stream: calls that
+ * share a workspace must be ordered on one stream.
+ *
+ * Matrices are row-major and C-contiguous, like the typed memoryviews
+ * (double[:, ::1]) of the reference's Cython kernels.
+ */
+#ifndef SPINTERPS_GB300_H
+#define SPINTERPS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *spi_stream_t; /* same object as cudaStream_t */
+
+typedef enum {
+    SPI_OK = 0,
+    SPI_ERR_ARG = 1,        /* null pointer, negative size, bad flag */
+    SPI_ERR_VG = 2,         /* variogram string does not parse / unknown model */
+    SPI_ERR_CUDA = 3,       /* a CUDA launch or call failed */
+    SPI_ERR_WORKSPACE = 4,  /* caller's workspace is too small */
+    SPI_ERR_TOO_LARGE = 5   /* a size exceeds a documented maximum */
+} spi_status;
+
+/* Variogram model codes: the model names of cyth/interpmthds.pyx:86-95. */
+enum {
+    SPI_VG_RNG = 0, SPI_VG_NUG = 1, SPI_VG_SPH = 2, SPI_VG_EXP = 3,
+    SPI_VG_LIN = 4, SPI_VG_GAU = 5, SPI_VG_POW = 6, SPI_VG_HOL = 7
+};
+
+#define SPI_MAX_VG_COMP 4
+
+/* One parsed variogram string: up to SPI_MAX_VG_COMP nested components,
+ * range already clamped to max(1e-5, range). */
+typedef struct {
+    int32_t n_comp;
+    int32_t code[SPI_MAX_VG_COMP];
+    double sill[SPI_MAX_VG_COMP];
+    double range[SPI_MAX_VG_COMP];
+} spi_vg_t;
+
+/* Kriging system kinds. */
+enum { SPI_KIND_OK = 0, SPI_KIND_SK = 1, SPI_KIND_EDK = 2 };
+
+/* ---- host helpers ------------------------------------------------------ */
+
+/* Parse 's1 M1(r1) + s2 M2(r2)' with the split rules of fill_vg_var_arr
+ * (replaces the parse in cyth/interpmthds.pyx:174-184). */
+int spi_parse_vg(const char *vg_str, spi_vg_t *out);
+
+/* misc.py:1074-1105 check_full_nuggetness: *out = 1 when the total sill or
+ * the largest range is <= min_vg_val. */
+int spi_check_full_nuggetness(const char *vg_str, double min_vg_val, int32_t *out);
+
+/* Library version string. */
+const char *spi_version(void);
+
+/* ---- drop-ins for the reference's Cython kernels (all device arrays) ---- */
+
+/* Replaces fill_dists_2d_mat (cyth/interpmthds.pyx:123-143):
+ * dists[i, j] = ((x1s[i]-x2s[j])^2 + (y1s[i]-y2s[j])^2)^0.5, shape [n1, n2]. */
+int spi_fill_dists_2d_mat(const double *x1s, const double *y1s, int64_t n1,
+                          const double *x2s, const double *y2s, int64_t n2,
+                          double *dists, spi_stream_t stream);
+
+/* Replaces fill_vg_var_arr (cyth/interpmthds.pyx:146-226): out = sum over
+ * components of covar*sill + (covar ? -1 : +1)*gamma(dists); entries
+ * <= min_vg_val set to 0; with diag_mat_flag the upper triangle is
+ * computed and mirrored. vg is a HOST pointer. */
+int spi_fill_vg_var_arr(const double *dists, int64_t rows, int64_t cols,
+                        double *out, int32_t covar_flag, int32_t diag_mat_flag,
+                        const spi_vg_t *vg, double min_vg_val,
+                        spi_stream_t stream);
+
+/* Replaces copy_2d_arr_at_idxs (cyth/interpmthds.pyx:229-248):
+ * subset[i, j] = arr[row_idxs[i], col_idxs[j]], subset row stride
+ * subset_cols (the reference allocates add_rc extra columns). */
+int spi_copy_2d_arr_at_idxs(const double *arr, int64_t arr_rows, int64_t arr_cols,
+                            const int64_t *row_idxs, int64_t n_rows,
+                            const int64_t *col_idxs, int64_t n_cols,
+                            double *subset, int64_t subset_cols,
+                            spi_stream_t stream);
+
+/* ---- batched step engine ------------------------------------------------
+ *
+ * Replaces the per-group loop of SpInterpSteps._get_interp
+ * (interp/steps.py:245-435) for all time steps at once. The host groups
+ * steps into "systems": one kriging system per (station set, variogram,
+ * kind). Station sets are lists of station indices (int32, ascending),
+ * concatenated, with int64 offsets. */
+
+/* Stations, cells and drifts shared by every system (device arrays). */
+typedef struct {
+    int64_t n_stns;
+    const double *stn_x, *stn_y;   /* [n_stns] */
+    int64_t n_cells;
+    const double *cell_x, *cell_y; /* [n_cells] */
+    int32_t n_drift;               /* k for EDK, else 0 */
+    const double *stn_drift;       /* [n_stns, n_drift] or NULL */
+    const double *cell_drift;      /* [n_drift, n_cells] or NULL */
+    double min_vg_val;
+    /* FP32 double-float copies of the coordinates minus a common origin,
+     * [n][4] = (x_hi, x_lo, y_hi, y_lo), 16-byte aligned; made by
+     * spi_split_coords and required only by the precision-1 kernels. */
+    const float *stn_split, *cell_split;
+} spi_domain_t;
+
+/* out[i] = (x_hi, x_lo, y_hi, y_lo) with x_hi = (float)(x[i] - ox) and
+ * x_lo = (float)((x[i] - ox) - x_hi), likewise for y (device arrays). */
+int spi_split_coords(const double *x, const double *y, int64_t n, double ox,
+                     double oy, float *out, spi_stream_t stream);
+
+/* y[i] = (float)x[i] (device arrays). */
+int spi_to_f32(const double *x, float *y, int64_t n, spi_stream_t stream);
+
+/* A batch of kriging systems (device arrays unless noted). Every system
+ * lists the time steps that use it; step j reads its n station values at
+ * val_off[j] of the values array (gathered in the system's station order),
+ * writes output row out_row[j], and owns dual weights at the same offset. */
+typedef struct {
+    int32_t n_sys;
+    int32_t kind;                  /* SPI_KIND_* for the whole batch */
+    const int64_t *stn_off;        /* [n_sys + 1] offsets into stn_idx */
+    const int32_t *stn_idx;        /* station indices of every system */
+    const spi_vg_t *vg;            /* [n_sys] */
+    const int64_t *mat_off;        /* [n_sys] offset (doubles) of each n x n
+                                      matrix in the matrix arenas; 32-aligned */
+    const int64_t *step_off;       /* [n_sys + 1] offsets into steps */
+    const int32_t *steps;          /* step indices, grouped by system */
+    const int64_t *val_off;        /* [n_steps] offset of step j's values */
+    const int32_t *out_row;        /* [n_steps] output row of step j */
+    int32_t max_n;                 /* max stations in one system */
+} spi_systems_t;
+
+/* Maximum drifts of EDK (a = 1 + n_drift Lagrange/drift rows). */
+#define SPI_MAX_DRIFT 7
+
+/* Build each system's matrix in covariance form and factor it in FP64:
+ *   OK/EDK: A = s*11' - Gamma, s = total sill, Gamma filled exactly as
+ *           fill_vg_var_arr with covar 0 (diagonal included);
+ *   SK:     A = the covariance fill (fill_vg_var_arr with covar 1).
+ * Under sum(lambda) = 1 the OK/EDK weights of [[A, F], [F', 0]] equal those
+ * of the reference's [[Gamma, F], [F', 0]] (the Lagrange multipliers change
+ * sign). A = L L' (Cholesky), then Linv = L^-1 (lower).
+ * L is written to l_arena, Linv to linv_arena (both at mat_off).
+ * status[s] = 0, or the 1-based pivot index where A was not positive
+ * definite; cond[s] = n * A_00 * ||Linv||_F^2, an upper bound of A's
+ * 2-norm condition number within a factor n; shift[s] = s (0 for SK). */
+int spi_krige_factor(const spi_domain_t *dom, const spi_systems_t *sys,
+                     double *l_arena, double *linv_arena, int32_t *status,
+                     double *cond, double *shift, spi_stream_t stream);
+
+/* Per-system and per-step dual quantities (FP64), for systems with
+ * status 0. With F = [1 | drift] (n x a, a = 1 + n_drift; SK: a = 0):
+ *   E = Linv F, G = Linv' E = A^-1 F, S = E'E; per step j with values z:
+ *   OK/EDK: w_hat = A^-1 z - G beta, beta = S^-1 G'z
+ *   SK:     w_hat = A^-1 z, and G = A^-1 1 (one column).
+ * Outputs: w_hat (same layout as vals), beta [n_steps, SPI_MAX_DRIFT + 1],
+ * g_cols [sum over systems of n * (SPI_MAX_DRIFT + 1)] at
+ * stn_off[s] * (SPI_MAX_DRIFT + 1) (row-major n x (SPI_MAX_DRIFT + 1)),
+ * s_inv [n_sys, (SPI_MAX_DRIFT + 1)^2] and g_colsum [n_sys, SPI_MAX_DRIFT + 1]
+ * (the column sums 1'G). */
+int spi_krige_duals(const spi_domain_t *dom, const spi_systems_t *sys,
+                    const double *linv_arena, const int32_t *status,
+                    const double *vals, double *w_hat, double *beta,
+                    double *g_cols, double *s_inv, double *g_colsum,
+                    spi_stream_t stream);
+
+/* Output description of the cell kernels. */
+typedef struct {
+    int32_t out_f64;               /* 1: est/var are double, 0: float */
+    void *est;                     /* [n_out_rows, n_cells] */
+    void *var;                     /* [n_out_rows, n_cells] or NULL (OK only) */
+    int32_t clip_min_on, clip_max_on;
+    double clip_min, clip_max;     /* _mod_min_max on the estimate */
+} spi_out_t;
+
+/* Kriging estimates (and OK variances when want_var) for every cell of
+ * every step of a system batch, FP64 throughout (precision = 0) or with
+ * FP32 right-hand sides and contractions over the FP64 factorisation
+ * (precision = 1; linv32, g_cols32 and w_hat32 are then FP32 copies of
+ * the FP64 arrays, made by spi_to_f32). Per cell, with c the right-hand side in covariance form
+ * and f = [1, cell drifts]: nu = S^-1 (G'c - f), sum(lambda) = (G'c)_0 -
+ * (1'G) nu, est_j = c'w_hat_j + f'beta_j, OK variance = s sum(lambda) -
+ * |Linv c|^2 + nu (G'c)_0 - 2 nu, which is the reference's
+ * lambda'gamma + 2 mu (interp/steps.py:429-434). Cells whose weight sum
+ * fails numpy.isclose(sum(lambda), 1), and every step of a system with
+ * non-zero status, take the nearest station's value with variance 0
+ * (interp/steps.py:363-426). */
+int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
+                    const double *linv_arena, const int32_t *status,
+                    const double *shift, const double *vals,
+                    const double *w_hat, const double *beta,
+                    const double *g_cols, const double *s_inv,
+                    const double *g_colsum, const float *linv32,
+                    const float *g_cols32, const float *w_hat32,
+                    int32_t want_var, int32_t precision,
+                    const spi_out_t *out, spi_stream_t stream);
+
+/* IDW (interp/steps.py:293-313, cyth/interpmthds.pyx:784-808) for every
+ * cell of the listed steps. data [n_steps_total, n_stns] holds every
+ * station's value, NaN where missing (the reference's data_df row). For
+ * list entry k: j = steps[k] is the data row, out_row[k] the output row;
+ * flag[j] = any present value >= min_value_to_interp_thresh (else the step
+ * mean means[j] is written). Weights (d / d_ref)^-idw_exp per cell and
+ * station are shared by every step; each step is a masked contraction pair
+ * over stations, so missing stations drop out exactly. A cell on a station
+ * present at the step gets NaN, as the reference's 1/0 weight does. Steps
+ * with fewer than two stations must not be listed (the reference copies
+ * the single value; use spi_fill_rows). precision 0: FP64; 1: FP32
+ * (requires dom->stn_split / cell_split). */
+int spi_idw_cells(const spi_domain_t *dom, int32_t n_steps, const int32_t *steps,
+                  const int32_t *out_row, const double *data, const uint8_t *flag,
+                  const double *means, double idw_exp, int32_t precision,
+                  const spi_out_t *out, spi_stream_t stream);
+
+/* NNB (interp/steps.py:285-291): value of the first present station of
+ * minimum distance (np.argmin order), per cell and listed step. */
+int spi_nnb_cells(const spi_domain_t *dom, int32_t n_steps, const int32_t *steps,
+                  const int32_t *out_row, const double *data, const spi_out_t *out,
+                  spi_stream_t stream);
+
+/* Fill whole output rows with per-row constants: est[row[j], :] = v[j]
+ * (clipped like the estimates), var[row[j], :] = vv[j] when var and vv are
+ * non-NULL (NaN allowed). Used for steps the reference answers without
+ * interpolating: one station (its value), no value above the threshold or a
+ * nugget-only variogram (the step mean, variance 0). */
+int spi_fill_rows(int32_t n_rows, const int32_t *row, const double *v,
+                  const double *vv, int64_t n_cells, const spi_out_t *out,
+                  spi_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPINTERPS_GB300_H */

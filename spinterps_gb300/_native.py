@@ -1,0 +1,124 @@
+"""ctypes binding of ``include/spinterps_gb300.h`` (the C ABI).
+
+The structs below mirror the header field by field. Every call checks the
+returned ``spi_status`` and raises :class:`SpiError`. There is no fallback:
+if the CUDA library cannot be loaded, :func:`lib` raises.
+"""
+import ctypes
+import threading
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_lib" / "libspinterps_gb300.so"
+
+c_i32 = ctypes.c_int32
+c_i64 = ctypes.c_int64
+c_dbl = ctypes.c_double
+c_ptr = ctypes.c_void_p
+
+SPI_MAX_VG_COMP = 4
+SPI_MAX_DRIFT = 7
+GA = SPI_MAX_DRIFT + 1
+KIND = {"OK": 0, "SK": 1, "EDK": 2}
+
+STATUS = {
+    0: "SPI_OK",
+    1: "SPI_ERR_ARG",
+    2: "SPI_ERR_VG",
+    3: "SPI_ERR_CUDA",
+    4: "SPI_ERR_WORKSPACE",
+    5: "SPI_ERR_TOO_LARGE",
+}
+
+
+class SpiError(RuntimeError):
+    def __init__(self, fn, code):
+        super().__init__(f"{fn} returned {STATUS.get(code, code)}")
+        self.code = code
+
+
+class VgT(ctypes.Structure):
+    _fields_ = [("n_comp", c_i32), ("code", c_i32 * SPI_MAX_VG_COMP),
+                ("sill", c_dbl * SPI_MAX_VG_COMP), ("range", c_dbl * SPI_MAX_VG_COMP)]
+
+
+class DomainT(ctypes.Structure):
+    _fields_ = [("n_stns", c_i64), ("stn_x", c_ptr), ("stn_y", c_ptr),
+                ("n_cells", c_i64), ("cell_x", c_ptr), ("cell_y", c_ptr),
+                ("n_drift", c_i32), ("stn_drift", c_ptr), ("cell_drift", c_ptr),
+                ("min_vg_val", c_dbl), ("stn_split", c_ptr), ("cell_split", c_ptr)]
+
+
+class SystemsT(ctypes.Structure):
+    _fields_ = [("n_sys", c_i32), ("kind", c_i32), ("stn_off", c_ptr), ("stn_idx", c_ptr),
+                ("vg", c_ptr), ("mat_off", c_ptr), ("step_off", c_ptr), ("steps", c_ptr),
+                ("val_off", c_ptr), ("out_row", c_ptr), ("max_n", c_i32)]
+
+
+class OutT(ctypes.Structure):
+    _fields_ = [("out_f64", c_i32), ("est", c_ptr), ("var", c_ptr), ("clip_min_on", c_i32),
+                ("clip_max_on", c_i32), ("clip_min", c_dbl), ("clip_max", c_dbl)]
+
+
+_SIGS = {
+    "spi_parse_vg": [ctypes.c_char_p, ctypes.POINTER(VgT)],
+    "spi_check_full_nuggetness": [ctypes.c_char_p, c_dbl, ctypes.POINTER(c_i32)],
+    "spi_fill_dists_2d_mat": [c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr, c_ptr],
+    "spi_fill_vg_var_arr": [c_ptr, c_i64, c_i64, c_ptr, c_i32, c_i32, ctypes.POINTER(VgT),
+                            c_dbl, c_ptr],
+    "spi_copy_2d_arr_at_idxs": [c_ptr, c_i64, c_i64, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_i64,
+                                c_ptr],
+    "spi_split_coords": [c_ptr, c_ptr, c_i64, c_dbl, c_dbl, c_ptr, c_ptr],
+    "spi_to_f32": [c_ptr, c_ptr, c_i64, c_ptr],
+    "spi_krige_factor": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr, c_ptr,
+                         c_ptr, c_ptr, c_ptr, c_ptr],
+    "spi_krige_duals": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr, c_ptr,
+                        c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
+    "spi_krige_cells": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr, c_ptr, c_ptr,
+                        c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i32,
+                        c_i32, ctypes.POINTER(OutT), c_ptr],
+    "spi_idw_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_dbl,
+                      c_i32, ctypes.POINTER(OutT), c_ptr],
+    "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
+                      ctypes.POINTER(OutT), c_ptr],
+    "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
+}
+
+# every entry point the header declares (checked by the CPU tests)
+EXPORTS = sorted(list(_SIGS) + ["spi_version"])
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path=LIB_PATH):
+    """Load the shared library (no GPU needed) and bind the signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not Path(path).exists():
+            raise RuntimeError(
+                f"spinterps_gb300 CUDA library not built ({path}); run "
+                "spinterps_gb300.build.build() first -- there is no CPU fallback")
+        lib = ctypes.CDLL(str(path))
+        for name, args in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        lib.spi_version.restype = ctypes.c_char_p
+        lib.spi_version.argtypes = []
+        _lib = lib
+        return lib
+
+
+def lib():
+    return load()
+
+
+def call(name, *args):
+    """Call an entry point; raise SpiError on a non-zero status."""
+    rc = getattr(lib(), name)(*args)
+    if rc != 0:
+        raise SpiError(name, rc)
+    return rc

@@ -1,0 +1,112 @@
+// Host-side entry points of the C ABI: variogram string parsing and the
+// nugget-only check. Pure C++ (no device code); errors are status codes.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spinterps_gb300.h"
+
+namespace {
+
+bool is_space(char c) {
+  return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f';
+}
+
+std::string strip(const std::string& s) {
+  size_t b = 0, e = s.size();
+  while (b < e && is_space(s[b])) ++b;
+  while (e > b && is_space(s[e - 1])) --e;
+  return s.substr(b, e - b);
+}
+
+// Python bytes.split(sep) with a one-character separator.
+std::vector<std::string> split(const std::string& s, char sep) {
+  std::vector<std::string> out;
+  size_t start = 0;
+  for (size_t i = 0; i <= s.size(); ++i) {
+    if (i == s.size() || s[i] == sep) {
+      out.push_back(s.substr(start, i - start));
+      start = i + 1;
+    }
+  }
+  return out;
+}
+
+// Python float(): surrounding whitespace allowed, the rest must parse whole.
+bool py_float(const std::string& tok, double* out) {
+  std::string t = strip(tok);
+  if (t.empty()) return false;
+  char* end = nullptr;
+  double v = std::strtod(t.c_str(), &end);
+  if (end != t.c_str() + t.size()) return false;
+  *out = v;
+  return true;
+}
+
+int model_code(const std::string& name) {
+  static const char* names[] = {"Rng", "Nug", "Sph", "Exp", "Lin", "Gau", "Pow", "Hol"};
+  for (int i = 0; i < 8; ++i)
+    if (name == names[i]) return i;
+  return -1;
+}
+
+}  // namespace
+
+// cyth/interpmthds.pyx:174-184: split on '+', strip, split on ' ' into
+// exactly (sill, 'Name(range'), split on '(' into exactly (Name, 'range)'),
+// range = part before ')', clamped to max(1e-5, range).
+extern "C" int spi_parse_vg(const char* vg_str, spi_vg_t* out) {
+  if (!vg_str || !out) return SPI_ERR_ARG;
+  std::memset(out, 0, sizeof(*out));
+  std::vector<std::string> parts = split(std::string(vg_str), '+');
+  if (parts.size() > SPI_MAX_VG_COMP) return SPI_ERR_TOO_LARGE;
+  int k = 0;
+  for (const std::string& raw : parts) {
+    std::string p = strip(raw);
+    std::vector<std::string> a = split(p, ' ');
+    if (a.size() != 2) return SPI_ERR_VG;
+    std::vector<std::string> b = split(a[1], '(');
+    if (b.size() != 2) return SPI_ERR_VG;
+    std::string rs = split(b[1], ')')[0];
+    int code = model_code(b[0]);
+    if (code < 0) return SPI_ERR_VG;
+    double sill, rng;
+    if (!py_float(a[0], &sill) || !py_float(rs, &rng)) return SPI_ERR_VG;
+    out->code[k] = code;
+    out->sill[k] = sill;
+    out->range[k] = std::fmax(1e-5, rng);
+    if (std::isnan(rng)) out->range[k] = 1e-5;  // Python max(1e-5, nan) is 1e-5
+    ++k;
+  }
+  out->n_comp = k;
+  return SPI_OK;
+}
+
+// misc.py:1074-1105.
+extern "C" int spi_check_full_nuggetness(const char* vg_str, double min_vg_val, int32_t* out) {
+  if (!vg_str || !out) return SPI_ERR_ARG;
+  std::string in(vg_str);
+  *out = 0;
+  if (in == "nan") return SPI_OK;
+  std::vector<std::string> models = split(in, '+');
+  double sill = 0.0, rng = 0.0;
+  for (const std::string& raw : models) {
+    std::string sub = strip(raw);
+    std::string head = strip(split(sub, '(')[0]);
+    if (head.size() < 3) return SPI_ERR_VG;
+    double s;
+    if (!py_float(head.substr(0, head.size() - 3), &s)) return SPI_ERR_VG;
+    sill += s;
+    std::vector<std::string> b = split(sub, '(');
+    if (b.size() < 2) return SPI_ERR_VG;
+    double r;
+    if (!py_float(split(b[1], ')')[0], &r)) return SPI_ERR_VG;
+    rng = std::fmax(rng, r);
+  }
+  if (sill <= min_vg_val || rng <= min_vg_val) *out = 1;
+  return SPI_OK;
+}
+
+extern "C" const char* spi_version(void) { return "spinterps_gb300 0.1 (sm_103a)"; }

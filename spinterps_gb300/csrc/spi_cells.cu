@@ -1,0 +1,418 @@
+// Kriging over all cells of all steps of a system batch.
+//
+// Replaces interp/steps.py:403-435 (_fill_krig_idw_dst_data: a Python loop
+// over cells doing lambda = pinv @ rhs per cell and step) together with the
+// cell x station variogram matrix it reads (interp/steps.py:639-650,
+// cyth/interpmthds.pyx:146-226): here the right-hand sides of a tile of
+// cells are generated in shared memory from coordinates (fused distance +
+// variogram) and contracted against
+//   - the system's dual columns G (Lagrange / drift rows, sum check),
+//   - Linv (OK variance |Linv c|^2, triangular),
+//   - the per-step dual weights w_hat (estimates of every step at once),
+// all through one shared-memory-tiled contraction routine. The estimate
+// of step j is c'w_hat_j + f'beta_j (dual form: 2n FLOP per cell-step
+// instead of the reference's 2m^2), the variance costs n^2 FLOP per
+// cell and is shared by every step of the system.
+//
+// precision 0: everything in FP64 (the plain path).
+// precision 1: right-hand sides generated in FP32 from double-float
+// coordinates (differences accurate relative to the distance itself),
+// contractions in FP32 against FP32 copies of the FP64 factor and duals,
+// FP64 epilogue.
+#include "spi_common.cuh"
+#include "spi_contract.cuh"
+
+namespace spi {
+
+constexpr int GA = SPI_MAX_DRIFT + 1;
+
+struct CellsArgs {
+  spi_domain_t dom;
+  spi_systems_t sys;
+  const int32_t* status;
+  const double* shift;
+  const double* vals;
+  const double* beta;
+  const double* s_inv;
+  const double* g_colsum;
+  int want_var;
+  spi_out_t out;
+};
+
+// Exact (FP64, reference-ordered) nearest station of a cell among a
+// system's stations: first index of the minimum distance, as np.argmin.
+__device__ int nnb_f64_warp(const spi_domain_t& dom, const int32_t* idx, int n, double cx,
+                            double cy) {
+  const int lane = threadIdx.x & 31;
+  double best = __longlong_as_double(0x7ff0000000000000LL);
+  int bj = 0x7fffffff;
+  for (int j = lane; j < n; j += 32) {
+    int st = idx[j];
+    double d = dist_f64(cx, cy, dom.stn_x[st], dom.stn_y[st]);
+    if (d < best) {
+      best = d;
+      bj = j;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+    if (ob < best || (ob == best && oj < bj)) {
+      best = ob;
+      bj = oj;
+    }
+  }
+  return bj == 0x7fffffff ? 0 : bj;
+}
+
+template <typename T, int TC, typename OutT>
+__global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __restrict__ linv,
+                                                   const T* __restrict__ gcols,
+                                                   const T* __restrict__ what, int npad) {
+  constexpr int CPT = TC / 16;
+  const int s = blockIdx.y;
+  const int64_t C = A.dom.n_cells;
+  const int64_t c0 = (int64_t)blockIdx.x * TC;
+  if (c0 >= C) return;
+  const int64_t soff = A.sys.stn_off[s];
+  const int n = (int)(A.sys.stn_off[s + 1] - soff);
+  const int32_t* idx = A.sys.stn_idx + soff;
+  const int sk = A.sys.kind == SPI_KIND_SK;
+  const int a = sk ? 1 : 1 + A.dom.n_drift;
+  const int tid = threadIdx.x;
+  const int64_t st0 = A.sys.step_off[s], st1 = A.sys.step_off[s + 1];
+  const int nsteps = (int)(st1 - st0);
+  const bool failed = A.status[s] != 0;
+
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* cvT = reinterpret_cast<T*>(smraw);                       // [npad][TC]
+  T* Bs = cvT + (int64_t)npad * TC;                            // [KC][BSTR]
+  double* qc = reinterpret_cast<double*>(Bs + KC * BSTR);      // [TC][GA]
+  double* cvar = qc + TC * GA;                                 // [TC]
+  double* suml = cvar + TC;                                    // [TC]
+  double* red = suml + TC;                                     // [16][TC]
+  int* nnb = reinterpret_cast<int*>(red + 16 * TC);            // [TC]
+  int* okf = nnb + TC;                                         // [TC]
+  const T** vptr = reinterpret_cast<const T**>(okf + TC);      // [VB]
+  __shared__ int any_bad;
+
+  const spi_vg_t vg = A.sys.vg[s];
+  const double sh = A.shift[s];
+  if (tid == 0) any_bad = failed ? 1 : 0;
+
+  if (!failed) {
+    // ---- 1. right-hand sides, cell-contiguous: cvT[j][cell] ----
+    {
+      const int cell = tid % TC, jg = tid / TC, njg = CT / TC;
+      const int64_t gc = c0 + cell;
+      const bool live = gc < C;
+      if constexpr (sizeof(T) == 8) {
+        const double cx = live ? A.dom.cell_x[gc] : 0.0, cy = live ? A.dom.cell_y[gc] : 0.0;
+        for (int j = jg; j < npad; j += njg) {
+          double v = 0.0;
+          if (live && j < n) {
+            int st = idx[j];
+            double d = dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
+            double g = vg_fill_f64(vg, d, sk, A.dom.min_vg_val);
+            v = sk ? g : __dsub_rn(sh, g);
+          }
+          cvT[(int64_t)j * TC + cell] = (T)v;
+        }
+      } else {
+        const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float mvv = (float)A.dom.min_vg_val;
+        const float shf = (float)sh;
+        float rr[SPI_MAX_VG_COMP], ss[SPI_MAX_VG_COMP];
+        for (int c = 0; c < vg.n_comp; ++c) {
+          rr[c] = (float)vg.range[c];
+          ss[c] = (float)vg.sill[c];
+        }
+        const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
+        for (int j = jg; j < npad; j += njg) {
+          float v = 0.f;
+          if (live && j < n) {
+            const float4 sp = sp4[idx[j]];
+            // double-float difference: accurate relative to the distance
+            float dx = (cp.x - sp.x) + (cp.y - sp.y);
+            float dy = (cp.z - sp.z) + (cp.w - sp.w);
+            float d = sqrtf(dx * dx + dy * dy);
+            float g = 0.f;
+            for (int c = 0; c < vg.n_comp; ++c) {
+              float gv = vg_eval_f32(vg.code[c], d, rr[c], ss[c]);
+              g += sk ? (ss[c] - gv) : gv;
+            }
+            if (g <= mvv) g = 0.f;
+            v = sk ? g : shf - g;
+          }
+          cvT[(int64_t)j * TC + cell] = (T)v;
+        }
+      }
+    }
+    // ---- 2. dual columns: qc[cell][k] = G_k' c ----
+    for (int v = tid; v < VB; v += CT) vptr[v] = (v < a) ? gcols + (soff * GA) + (int64_t)v * n : nullptr;
+    {
+      T acc[CPT][4];
+      tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, a, n, n, acc);
+      const int cg = tid % 16, rg = tid / 16;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          int k = rg * 4 + r;
+          if (k < GA) qc[(cg * CPT + c) * GA + k] = (double)acc[c][r];
+        }
+    }
+    // ---- 3. OK variance: |Linv c|^2, triangular blocks of VB rows ----
+    double yy_part[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) yy_part[c] = 0.0;
+    if (A.want_var) {
+      const T* L = linv + A.sys.mat_off[s];
+      for (int r0 = 0; r0 < n; r0 += VB) {
+        __syncthreads();
+        for (int v = tid; v < VB; v += CT) vptr[v] = (r0 + v < n) ? L + (int64_t)(r0 + v) * n : nullptr;
+        T acc[CPT][4];
+        tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, min(VB, n - r0), min(n, r0 + VB), n, acc);
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+          T q = T(0);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) q += acc[c][r] * acc[c][r];
+          yy_part[c] += (double)q;
+        }
+      }
+    }
+    __syncthreads();
+    {
+      const int cg = tid % 16, rg = tid / 16;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) red[rg * TC + cg * CPT + c] = yy_part[c];
+    }
+    __syncthreads();
+    // ---- 4. per cell: nu, sum(lambda), variance ----
+    for (int cell = tid; cell < TC; cell += CT) {
+      const int64_t gc = c0 + cell;
+      double yy = 0.0;
+      for (int g = 0; g < 16; ++g) yy += red[g * TC + cell];
+      double q[GA], nu[GA];
+      for (int k = 0; k < GA; ++k) q[k] = qc[cell * GA + k];
+      double sl;
+      double vv = 0.0;
+      if (sk) {
+        sl = q[0];
+      } else {
+        const double* Si = A.s_inv + (int64_t)s * GA * GA;
+        double f[GA];
+        f[0] = 1.0;
+        for (int k = 1; k < a; ++k)
+          f[k] = gc < C ? A.dom.cell_drift[(int64_t)(k - 1) * C + gc] : 0.0;
+        for (int k = 0; k < a; ++k) {
+          double t = 0.0;
+          for (int l = 0; l < a; ++l) t += Si[k * GA + l] * (q[l] - f[l]);
+          nu[k] = t;
+        }
+        sl = q[0];
+        for (int k = 0; k < a; ++k) sl -= A.g_colsum[(int64_t)s * GA + k] * nu[k];
+        vv = sh * sl - yy + nu[0] * q[0] - 2.0 * nu[0];
+      }
+      int ok = isclose_one(sl) ? 1 : 0;
+      okf[cell] = ok;
+      suml[cell] = sl;
+      cvar[cell] = ok ? vv : 0.0;
+      if (!ok && gc < C) atomicOr(&any_bad, 1);
+    }
+  } else {
+    for (int cell = tid; cell < TC; cell += CT) {
+      okf[cell] = 0;
+      cvar[cell] = 0.0;
+    }
+  }
+  __syncthreads();
+  // ---- 5. nearest station, only for cells that fall back ----
+  if (any_bad) {
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int cell = warp; cell < TC; cell += CT / 32) {
+      const int64_t gc = c0 + cell;
+      if (gc >= C || okf[cell]) continue;
+      int j = nnb_f64_warp(A.dom, idx, n, A.dom.cell_x[gc], A.dom.cell_y[gc]);
+      if (lane == 0) nnb[cell] = j;
+    }
+  }
+  __syncthreads();
+  // ---- 6. estimates of every step, VB steps per block ----
+  const bool var_out = A.want_var && A.out.var != nullptr && !sk;
+  OutT* est_out = reinterpret_cast<OutT*>(A.out.est);
+  OutT* var_outp = reinterpret_cast<OutT*>(A.out.var);
+  for (int v0 = 0; v0 < nsteps; v0 += VB) {
+    const int nv = min(VB, nsteps - v0);
+    __syncthreads();
+    for (int v = tid; v < VB; v += CT)
+      vptr[v] = (v < nv && !failed) ? what + A.sys.val_off[A.sys.steps[st0 + v0 + v]] : nullptr;
+    T acc[CPT][4];
+    if (!failed) {
+      tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, nv, n, n, acc);
+    } else {
+#pragma unroll
+      for (int c = 0; c < CPT; ++c)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[c][r] = T(0);
+    }
+    const int cg = tid % 16, rg = tid / 16;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int v = rg * 4 + r;
+      if (v >= nv) continue;
+      const int j = A.sys.steps[st0 + v0 + v];
+      const int64_t row = A.sys.out_row[j];
+      const int64_t vo = A.sys.val_off[j];
+      const double* bt = A.beta + (int64_t)j * GA;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        const int cell = cg * CPT + c;
+        const int64_t gc = c0 + cell;
+        if (gc >= C) continue;
+        double e;
+        if (okf[cell]) {
+          e = (double)acc[c][r];
+          if (!sk) {
+            e += bt[0];
+            for (int k = 1; k < a; ++k) e += bt[k] * A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
+          }
+        } else {
+          e = A.vals[vo + nnb[cell]];
+        }
+        e = clip_est(e, A.out);
+        est_out[row * C + gc] = cast_out<OutT>(e);
+        if (var_out) var_outp[row * C + gc] = cast_out<OutT>(cvar[cell]);
+      }
+    }
+  }
+}
+
+template <typename T, int TC>
+static size_t cells_smem(int npad) {
+  return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * sizeof(T) +
+         (size_t)TC * GA * 8 + (size_t)TC * 8 * 2 + (size_t)16 * TC * 8 + (size_t)TC * 4 * 2 +
+         (size_t)VB * sizeof(void*) + 16;
+}
+
+template <typename T, int TC, typename OutT>
+static int launch_cells(const CellsArgs& A, const T* linv, const T* gcols, const T* what,
+                        cudaStream_t st) {
+  int npad = (A.sys.max_n + KC - 1) / KC * KC;
+  if (npad < KC) npad = KC;
+  size_t smem = cells_smem<T, TC>(npad);
+  auto kern = k_krige_cells<T, TC, OutT>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return SPI_ERR_CUDA;
+  int64_t tiles = (A.dom.n_cells + TC - 1) / TC;
+  if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
+  dim3 grid((unsigned)tiles, (unsigned)A.sys.n_sys);
+  kern<<<grid, CT, smem, st>>>(A, linv, gcols, what, npad);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+// Largest cell tile whose shared memory fits.
+template <typename T>
+static int pick_tc(int max_n) {
+  int npad = (max_n + KC - 1) / KC * KC;
+  const size_t cap = 225 * 1024;
+  if (sizeof(T) == 4 && cells_smem<T, 64>(npad) <= cap) return 64;
+  if (cells_smem<T, 32>(npad) <= cap) return 32;
+  if (cells_smem<T, 16>(npad) <= cap) return 16;
+  return 0;
+}
+
+template <typename T, typename OutT>
+static int dispatch_cells(const CellsArgs& A, const T* linv, const T* gcols, const T* what,
+                          cudaStream_t st) {
+  int tc = pick_tc<T>(A.sys.max_n);
+  if (tc == 64) return launch_cells<T, 64, OutT>(A, linv, gcols, what, st);
+  if (tc == 32) return launch_cells<T, 32, OutT>(A, linv, gcols, what, st);
+  if (tc == 16) return launch_cells<T, 16, OutT>(A, linv, gcols, what, st);
+  return SPI_ERR_TOO_LARGE;
+}
+
+__global__ void k_to_f32(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+}  // namespace spi
+
+using namespace spi;
+
+extern "C" int spi_to_f32(const double* x, float* y, int64_t n, spi_stream_t stream) {
+  if (n < 0) return SPI_ERR_ARG;
+  if (n == 0) return SPI_OK;
+  if (!x || !y) return SPI_ERR_ARG;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  k_to_f32<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(x, y, n);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys,
+                               const double* linv_arena, const int32_t* status,
+                               const double* shift, const double* vals, const double* w_hat,
+                               const double* beta, const double* g_cols, const double* s_inv,
+                               const double* g_colsum, const float* linv32,
+                               const float* g_cols32, const float* w_hat32, int32_t want_var,
+                               int32_t precision, const spi_out_t* out, spi_stream_t stream) {
+  if (!dom || !sys || !out) return SPI_ERR_ARG;
+  if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
+  if (dom->n_drift < 0 || dom->n_drift > SPI_MAX_DRIFT) return SPI_ERR_TOO_LARGE;
+  if (sys->n_sys == 0 || dom->n_cells == 0) return SPI_OK;
+  if (!status || !shift || !vals || !beta || !s_inv || !g_colsum || !out->est) return SPI_ERR_ARG;
+  if (precision == 0 && (!linv_arena || !w_hat || !g_cols)) return SPI_ERR_ARG;
+  if (precision == 1 && (!linv32 || !w_hat32 || !g_cols32)) return SPI_ERR_ARG;
+  if (precision != 0 && precision != 1) return SPI_ERR_ARG;
+  CellsArgs A;
+  A.dom = *dom;
+  A.sys = *sys;
+  A.status = status;
+  A.shift = shift;
+  A.vals = vals;
+  A.beta = beta;
+  A.s_inv = s_inv;
+  A.g_colsum = g_colsum;
+  A.want_var = want_var ? 1 : 0;
+  A.out = *out;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == 0) {
+    return out->out_f64 ? dispatch_cells<double, double>(A, linv_arena, g_cols, w_hat, st)
+                        : dispatch_cells<double, float>(A, linv_arena, g_cols, w_hat, st);
+  }
+  return out->out_f64 ? dispatch_cells<float, double>(A, linv32, g_cols32, w_hat32, st)
+                      : dispatch_cells<float, float>(A, linv32, g_cols32, w_hat32, st);
+}
+
+namespace spi {
+__global__ void k_split_coords(const double* __restrict__ x, const double* __restrict__ y,
+                               int64_t n, double ox, double oy, float4* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double dx = x[i] - ox, dy = y[i] - oy;
+    float xh = (float)dx, yh = (float)dy;
+    out[i] = make_float4(xh, (float)(dx - (double)xh), yh, (float)(dy - (double)yh));
+  }
+}
+}  // namespace spi
+
+extern "C" int spi_split_coords(const double* x, const double* y, int64_t n, double ox,
+                                double oy, float* out, spi_stream_t stream) {
+  if (n < 0) return SPI_ERR_ARG;
+  if (n == 0) return SPI_OK;
+  if (!x || !y || !out || (reinterpret_cast<uintptr_t>(out) & 15)) return SPI_ERR_ARG;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  spi::k_split_coords<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+      x, y, n, ox, oy, reinterpret_cast<float4*>(out));
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}

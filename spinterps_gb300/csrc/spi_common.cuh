@@ -1,0 +1,136 @@
+// Shared device helpers of the spinterps_gb300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "spinterps_gb300.h"
+
+#define SPI_PI 3.14159265358979323846
+
+namespace spi {
+
+constexpr int kSmSlack = 1;
+
+// Distance of cyth/interpmthds.pyx:30-35 / 140: ((x1-x2)^2 + (y1-y2)^2)^0.5,
+// every operation separately rounded (no FMA) and the square root
+// correctly rounded. The reference's glibc pow(x, 0.5) is within 0.52 ulp of
+// the true root, so it agrees with this except for ~0.1% of inputs, where
+// the two differ by one ulp.
+__device__ __forceinline__ double dist_f64(double x1, double y1, double x2, double y2) {
+  double dx = __dsub_rn(x1, x2);
+  double dy = __dsub_rn(y1, y2);
+  return __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+}
+
+// Variogram models of cyth/interpmthds.pyx:38-84 in FP64, same operation
+// order, separately rounded.
+__device__ __forceinline__ double vg_eval_f64(int code, double h, double r, double s) {
+  switch (code) {
+    case SPI_VG_RNG:
+      return h;
+    case SPI_VG_NUG:
+      return s;
+    case SPI_VG_SPH: {
+      if (h >= r) return s;
+      double a = __ddiv_rn(__dmul_rn(1.5, h), r);
+      double b = __ddiv_rn(__dmul_rn(__dmul_rn(h, h), h), __dmul_rn(2.0, __dmul_rn(__dmul_rn(r, r), r)));
+      return __dmul_rn(s, __dsub_rn(a, b));
+    }
+    case SPI_VG_EXP:
+      return __dmul_rn(s, __dsub_rn(1.0, exp(__ddiv_rn(__dmul_rn(-3.0, h), r))));
+    case SPI_VG_LIN:
+      if (h > r) return s;
+      return __dmul_rn(s, __ddiv_rn(h, r));
+    case SPI_VG_GAU:
+      return __dmul_rn(s, __dsub_rn(1.0, exp(__dmul_rn(-3.0, __ddiv_rn(__dmul_rn(h, h), __dmul_rn(r, r))))));
+    case SPI_VG_POW:
+      return __dmul_rn(s, pow(h, r));
+    case SPI_VG_HOL: {
+      if (h == 0.0) return 0.0;
+      double a = __ddiv_rn(__dmul_rn(SPI_PI, h), r);
+      return __dmul_rn(s, __dsub_rn(1.0, __ddiv_rn(sin(a), a)));
+    }
+    default:
+      return __longlong_as_double(0x7ff8000000000000LL);
+  }
+}
+
+// The same models in FP32 for the split-precision path.
+__device__ __forceinline__ float vg_eval_f32(int code, float h, float r, float s) {
+  switch (code) {
+    case SPI_VG_RNG:
+      return h;
+    case SPI_VG_NUG:
+      return s;
+    case SPI_VG_SPH: {
+      if (h >= r) return s;
+      float t = h / r;
+      return s * (1.5f * t - 0.5f * t * t * t);
+    }
+    case SPI_VG_EXP:
+      return s * (1.0f - expf(-3.0f * h / r));
+    case SPI_VG_LIN:
+      return h > r ? s : s * (h / r);
+    case SPI_VG_GAU: {
+      float t = h / r;
+      return s * (1.0f - expf(-3.0f * t * t));
+    }
+    case SPI_VG_POW:
+      return s * powf(h, r);
+    case SPI_VG_HOL: {
+      if (h == 0.0f) return 0.0f;
+      float a = (float)SPI_PI * h / r;
+      return s * (1.0f - sinf(a) / a);
+    }
+    default:
+      return __int_as_float(0x7fc00000);
+  }
+}
+
+// One entry of fill_vg_var_arr (cyth/interpmthds.pyx:186-217) at distance h:
+// accumulate every component in order from 0.0, then zero entries
+// <= min_vg_val.
+__device__ __forceinline__ double vg_fill_f64(const spi_vg_t &vg, double h, int covar,
+                                              double min_vg_val) {
+  double acc = 0.0;
+  for (int c = 0; c < vg.n_comp; ++c) {
+    double g = vg_eval_f64(vg.code[c], h, vg.range[c], vg.sill[c]);
+    double t = covar ? __dsub_rn(vg.sill[c], g) : g;
+    acc = __dadd_rn(acc, t);
+  }
+  return acc <= min_vg_val ? 0.0 : acc;
+}
+
+__device__ __forceinline__ double total_sill(const spi_vg_t &vg) {
+  double s = 0.0;
+  for (int c = 0; c < vg.n_comp; ++c) s += vg.sill[c];
+  return s;
+}
+
+// numpy.isclose(a, 1.0) with its defaults (rtol 1e-5, atol 1e-8).
+__device__ __forceinline__ bool isclose_one(double a) {
+  return fabs(a - 1.0) <= (1e-8 + 1e-5 * 1.0);
+}
+
+template <typename T>
+__device__ __forceinline__ T cast_out(double v);
+template <>
+__device__ __forceinline__ double cast_out<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float cast_out<float>(double v) { return (float)v; }
+
+__device__ __forceinline__ double clip_est(double v, const spi_out_t &o) {
+  if (o.clip_min_on && v < o.clip_min) v = o.clip_min;
+  if (o.clip_max_on && v > o.clip_max) v = o.clip_max;
+  return v;
+}
+
+}  // namespace spi
+
+// Launch check used by every entry point.
+#define SPI_LAUNCH_CHECK()                                      \
+  do {                                                          \
+    cudaError_t _e = cudaGetLastError();                        \
+    if (_e != cudaSuccess) return SPI_ERR_CUDA;                 \
+  } while (0)

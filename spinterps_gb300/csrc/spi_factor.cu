@@ -1,0 +1,494 @@
+// FP64 build + factorisation of every kriging system of a batch, and the
+// per-step dual weights.
+//
+// Replaces, for all systems at once, what interp/steps.py:170-243 (LHS
+// assembly from the precomputed cell/station variogram matrices) and
+// interp/steps.py:350-352 (numpy.linalg.pinv of the LHS) do per group:
+// the LHS is built straight from station coordinates (fused distance +
+// variogram, never materialising the N x N matrix of every variogram), put
+// in covariance form A = s*11' - Gamma, and factored A = L L' in FP64. The
+// Lagrange / drift rows are handled by a Schur complement S = F'A^-1 F.
+//
+// GB300's FP64 pipe is narrow (about 2 DFMA per SM per clock), so these
+// kernels are FP64-issue bound, not memory bound: one CTA per system, tiles
+// staged in shared memory, and every operand read from L2 at most once per
+// 32-wide block of FMAs.
+#include "spi_common.cuh"
+
+namespace spi {
+
+constexpr int NB = 32;        // panel width of the blocked factorisations
+constexpr int FT = 256;       // threads per factor CTA
+constexpr int GA = SPI_MAX_DRIFT + 1;
+
+struct SysView {
+  int64_t off;
+  int n;
+  const int32_t* idx;
+  int64_t moff;
+};
+
+__device__ __forceinline__ SysView sys_view(const spi_systems_t& sys, int s) {
+  SysView v;
+  v.off = sys.stn_off[s];
+  v.n = (int)(sys.stn_off[s + 1] - v.off);
+  v.idx = sys.stn_idx + v.off;
+  v.moff = sys.mat_off[s];
+  return v;
+}
+
+// A[i, j] for i >= j. The reference fills the upper triangle of the full
+// station matrix from dists[lo, hi] and mirrors it (cyth/interpmthds.pyx:
+// 196-226); with ascending station lists the entry (i, j), i > j, is the
+// mirror of (j, i), whose distance is dist(stn[j], stn[i]).
+__global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restrict__ l_arena,
+                            double* __restrict__ shift_out) {
+  const int s = blockIdx.y;
+  SysView v = sys_view(sys, s);
+  const spi_vg_t vg = sys.vg[s];
+  const int sk = sys.kind == SPI_KIND_SK;
+  const double sh = sk ? 0.0 : total_sill(vg);
+  if (blockIdx.x == 0 && threadIdx.x == 0) shift_out[s] = sh;
+  double* A = l_arena + v.moff;
+  const int64_t nn = (int64_t)v.n * v.n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / v.n), j = (int)(e - (int64_t)i * v.n);
+    if (j > i) {
+      A[e] = 0.0;
+      continue;
+    }
+    int si = v.idx[i], sj = v.idx[j];
+    double d = dist_f64(dom.stn_x[sj], dom.stn_y[sj], dom.stn_x[si], dom.stn_y[si]);
+    double g = vg_fill_f64(vg, d, sk, dom.min_vg_val);
+    A[e] = sk ? g : __dsub_rn(sh, g);
+  }
+}
+
+// Right-looking blocked Cholesky, in place on the lower triangle.
+__global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, double* __restrict__ l_arena,
+                                            int32_t* __restrict__ status) {
+  const int s = blockIdx.x;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  double* A = l_arena + v.moff;
+  __shared__ double D[NB][NB + 1];
+  __shared__ double Pi[64][NB + 1];
+  __shared__ double Pj[64][NB + 1];
+  __shared__ int fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) fail = 0;
+  __syncthreads();
+  for (int k0 = 0; k0 < n; k0 += NB) {
+    const int nb = min(NB, n - k0);
+    for (int e = tid; e < NB * NB; e += FT) {
+      int r = e / NB, c = e % NB;
+      D[r][c] = (r < nb && c <= r) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int j = 0; j < nb; ++j) {
+        double djj = D[j][j];
+        if (!(djj > 0.0)) {  // not positive, or NaN
+          if (lane == 0) fail = k0 + j + 1;
+          break;
+        }
+        double ljj = sqrt(djj);
+        __syncwarp();
+        if (lane == j) D[j][j] = ljj;
+        if (lane > j && lane < nb) D[lane][j] = D[lane][j] / ljj;
+        __syncwarp();
+        if (lane > j && lane < nb) {
+          double lij = D[lane][j];
+          for (int c = j + 1; c <= lane; ++c) D[lane][c] -= lij * D[c][j];
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    if (fail) break;
+    for (int e = tid; e < nb * nb; e += FT) {
+      int r = e / nb, c = e % nb;
+      if (c <= r) A[(int64_t)(k0 + r) * n + k0 + c] = D[r][c];
+    }
+    // panel: rows below the diagonal block, A21 <- A21 L11^-T
+    for (int r = k0 + nb + tid; r < n; r += FT) {
+      double x[NB];
+      double* row = A + (int64_t)r * n + k0;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) x[j] = (j < nb) ? row[j] : 0.0;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        if (j < nb) {
+          double t = x[j];
+#pragma unroll
+          for (int c = 0; c < NB; ++c)
+            if (c < j) t -= x[c] * D[j][c];
+          x[j] = t / D[j][j];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        if (j < nb) row[j] = x[j];
+    }
+    __syncthreads();
+    // trailing update of the lower triangle: A22 -= L21 L21'
+    const int r0 = k0 + nb;
+    const int m = n - r0;
+    if (m <= 0) continue;
+    const int nt = (m + 63) / 64;
+    for (int ti = 0; ti < nt; ++ti) {
+      for (int tj = 0; tj <= ti; ++tj) {
+        for (int e = tid; e < 64 * NB; e += FT) {
+          int r = e / NB, c = e % NB;
+          int gi = r0 + ti * 64 + r, gj = r0 + tj * 64 + r;
+          Pi[r][c] = (gi < n && c < nb) ? A[(int64_t)gi * n + k0 + c] : 0.0;
+          Pj[r][c] = (gj < n && c < nb) ? A[(int64_t)gj * n + k0 + c] : 0.0;
+        }
+        __syncthreads();
+        const int rr = (tid / 16) * 4, cc = (tid % 16) * 4;
+        double acc[4][4] = {};
+#pragma unroll 4
+        for (int c = 0; c < NB; ++c) {
+          double a[4], b[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            a[q] = Pi[rr + q][c];
+            b[q] = Pj[cc + q][c];
+          }
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] += a[p] * b[q];
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          int gi = r0 + ti * 64 + rr + p;
+          if (gi >= n) continue;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            int gj = r0 + tj * 64 + cc + q;
+            if (gj <= gi) A[(int64_t)gi * n + gj] -= acc[p][q];
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) status[s] = fail;
+}
+
+// Linv = L^-1 by block rows: X_II = inv(L_II), X_IJ = -X_II sum_K L_IK X_KJ.
+__global__ __launch_bounds__(FT) void k_trinv(spi_systems_t sys, const double* __restrict__ l_arena,
+                                             double* __restrict__ x_arena,
+                                             const int32_t* __restrict__ status,
+                                             double* __restrict__ cond) {
+  const int s = blockIdx.x;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  const double* L = l_arena + v.moff;
+  double* X = x_arena + v.moff;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (status[s] != 0) {
+    if (tid == 0) cond[s] = __longlong_as_double(0x7ff0000000000000LL);
+    return;
+  }
+  __shared__ double Ld[NB][NB + 1];
+  __shared__ double Xd[NB][NB + 1];
+  __shared__ double T[3][NB][NB + 1];
+  __shared__ double red[FT / 32];
+  double frob = 0.0;
+  const int nblk = (n + NB - 1) / NB;
+  for (int I = 0; I < nblk; ++I) {
+    const int i0 = I * NB, nb = min(NB, n - i0);
+    for (int e = tid; e < NB * NB; e += FT) {
+      int r = e / NB, c = e % NB;
+      Ld[r][c] = (r < nb && c <= r) ? L[(int64_t)(i0 + r) * n + i0 + c] : 0.0;
+    }
+    __syncthreads();
+    if (warp == 0 && lane < nb) {
+      const int j = lane;
+      for (int i = 0; i < nb; ++i) {
+        double val = 0.0;
+        if (i >= j) {
+          double t = (i == j) ? 1.0 : 0.0;
+          for (int c = j; c < i; ++c) t -= Ld[i][c] * Xd[c][j];
+          val = t / Ld[i][i];
+        }
+        Xd[i][j] = val;
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < nb * nb; e += FT) {
+      int r = e / nb, c = e % nb;
+      double xv = (c <= r) ? Xd[r][c] : 0.0;
+      X[(int64_t)(i0 + r) * n + i0 + c] = xv;
+      frob += xv * xv;
+    }
+    // off-diagonal blocks, 3 column blocks at a time
+    for (int J0 = 0; J0 < I; J0 += 3) {
+      const int nj = min(3, I - J0);
+      for (int e = tid; e < nj * NB * NB; e += FT) {
+        int jj = e / (NB * NB), rem = e % (NB * NB), r = rem / NB, c = rem % NB;
+        double t = 0.0;
+        if (r < nb) {
+          const int J = J0 + jj;
+          const double* lrow = L + (int64_t)(i0 + r) * n;
+          for (int k = J * NB; k < i0; ++k) t += lrow[k] * X[(int64_t)k * n + J * NB + c];
+        }
+        T[jj][r][c] = t;
+      }
+      __syncthreads();
+      for (int e = tid; e < nj * NB * NB; e += FT) {
+        int jj = e / (NB * NB), rem = e % (NB * NB), r = rem / NB, c = rem % NB;
+        if (r < nb) {
+          double t = 0.0;
+          for (int q = 0; q <= r; ++q) t += Xd[r][q] * T[jj][q][c];
+          double xv = -t;
+          X[(int64_t)(i0 + r) * n + (J0 + jj) * NB + c] = xv;
+          frob += xv * xv;
+        }
+      }
+      __syncthreads();
+    }
+    // zero the upper part of this block row (kept clean for contractions)
+    for (int e = tid; e < nb * (n - i0 - nb); e += FT) {
+      int r = e / (n - i0 - nb), c = e % (n - i0 - nb);
+      X[(int64_t)(i0 + r) * n + i0 + nb + c] = 0.0;
+    }
+    __syncthreads();
+  }
+  for (int o = 16; o > 0; o >>= 1) frob += __shfl_xor_sync(0xffffffffu, frob, o);
+  if (lane == 0) red[warp] = frob;
+  __syncthreads();
+  if (tid == 0) {
+    double f = 0.0;
+    for (int w = 0; w < FT / 32; ++w) f += red[w];
+    double a00 = L[0] * L[0];
+    cond[s] = (double)n * a00 * f;
+  }
+}
+
+// y = X x (X lower, row-major n x n): warp per row, lanes along the row.
+__device__ void matvec_lower(const double* __restrict__ X, int n, const double* __restrict__ x,
+                             double* __restrict__ y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = warp; i < n; i += nw) {
+    const double* row = X + (int64_t)i * n;
+    double t = 0.0;
+    for (int j = lane; j <= i; j += 32) t += row[j] * x[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) y[i] = t;
+  }
+}
+
+// y = X' q: thread per column, coalesced along rows.
+__device__ void matvec_lower_t(const double* __restrict__ X, int n, const double* __restrict__ q,
+                               double* __restrict__ y) {
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double t = 0.0;
+    for (int i = j; i < n; ++i) t += X[(int64_t)i * n + j] * q[i];
+    y[j] = t;
+  }
+}
+
+__device__ double block_dot(const double* __restrict__ a, const double* __restrict__ b, int n,
+                            double* red) {
+  double t = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) t += a[i] * b[i];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = t;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += red[w];
+  __syncthreads();
+  return r;
+}
+
+// Per-system G, S^-1, 1'G and per-step dual weights. Dynamic shared
+// memory: 3 vectors of n doubles.
+__global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sys,
+                                             const double* __restrict__ x_arena,
+                                             const int32_t* __restrict__ status,
+                                             const double* __restrict__ vals,
+                                             double* __restrict__ w_hat,
+                                             double* __restrict__ beta,
+                                             double* __restrict__ g_cols,
+                                             double* __restrict__ s_inv,
+                                             double* __restrict__ g_colsum) {
+  const int s = blockIdx.x;
+  if (status[s] != 0) return;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  const double* X = x_arena + v.moff;
+  extern __shared__ double sm[];
+  double* va = sm;
+  double* vb = sm + n;
+  double* vz = sm + 2 * n;
+  __shared__ double red[FT / 32];
+  __shared__ double S[GA][GA];
+  __shared__ double Si[GA][GA];
+  __shared__ double hb[GA];
+  const int sk = sys.kind == SPI_KIND_SK;
+  const int a = sk ? 1 : 1 + dom.n_drift;
+  double* G = g_cols + v.off * GA;  // column k at G + k * n
+  // G_k = Linv' (Linv F_k)
+  for (int k = 0; k < a; ++k) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      va[i] = (k == 0) ? 1.0 : dom.stn_drift[(int64_t)v.idx[i] * dom.n_drift + (k - 1)];
+    __syncthreads();
+    matvec_lower(X, n, va, vb);
+    __syncthreads();
+    matvec_lower_t(X, n, vb, G + (int64_t)k * n);
+    __syncthreads();
+  }
+  // S = F'G, 1'G
+  for (int k = 0; k < a; ++k) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      va[i] = (k == 0) ? 1.0 : dom.stn_drift[(int64_t)v.idx[i] * dom.n_drift + (k - 1)];
+    __syncthreads();
+    for (int l = 0; l < a; ++l) {
+      double d = block_dot(va, G + (int64_t)l * n, n, red);
+      if (threadIdx.x == 0) S[k][l] = d;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // Gauss-Jordan with partial pivoting on the small a x a Schur complement
+    double M[GA][2 * GA];
+    for (int i = 0; i < a; ++i)
+      for (int j = 0; j < 2 * a; ++j) M[i][j] = (j < a) ? S[i][j] : (j - a == i ? 1.0 : 0.0);
+    for (int c = 0; c < a; ++c) {
+      int p = c;
+      for (int r = c + 1; r < a; ++r)
+        if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+      if (p != c)
+        for (int j = 0; j < 2 * a; ++j) {
+          double t = M[c][j];
+          M[c][j] = M[p][j];
+          M[p][j] = t;
+        }
+      double piv = M[c][c];
+      for (int j = 0; j < 2 * a; ++j) M[c][j] /= piv;
+      for (int r = 0; r < a; ++r)
+        if (r != c) {
+          double f = M[r][c];
+          for (int j = 0; j < 2 * a; ++j) M[r][j] -= f * M[c][j];
+        }
+    }
+    for (int i = 0; i < GA; ++i)
+      for (int j = 0; j < GA; ++j) {
+        double val = (i < a && j < a) ? M[i][a + j] : 0.0;
+        Si[i][j] = val;
+        s_inv[(int64_t)s * GA * GA + i * GA + j] = val;
+      }
+  }
+  __syncthreads();
+  for (int k = 0; k < GA; ++k) {
+    double cs = 0.0;
+    if (k < a) {
+      for (int i = 0; i < n; ++i) cs += G[(int64_t)k * n + i];
+    }
+    if (threadIdx.x == 0) g_colsum[(int64_t)s * GA + k] = cs;
+  }
+  // per step
+  for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1]; ++si) {
+    const int j = sys.steps[si];
+    const int64_t vo = sys.val_off[j];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) vz[i] = vals[vo + i];
+    __syncthreads();
+    if (!sk) {
+      for (int k = 0; k < a; ++k) {
+        double d = block_dot(G + (int64_t)k * n, vz, n, red);
+        if (threadIdx.x == 0) hb[k] = d;
+      }
+      __syncthreads();
+    }
+    matvec_lower(X, n, vz, va);
+    __syncthreads();
+    matvec_lower_t(X, n, va, vb);
+    __syncthreads();
+    if (!sk) {
+      double bt[GA];
+      for (int k = 0; k < GA; ++k) {
+        double t = 0.0;
+        for (int l = 0; l < a; ++l) t += Si[k][l] * hb[l];
+        bt[k] = (k < a) ? t : 0.0;
+      }
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double w = vb[i];
+        for (int k = 0; k < a; ++k) w -= G[(int64_t)k * n + i] * bt[k];
+        w_hat[vo + i] = w;
+      }
+      if (threadIdx.x < GA) beta[(int64_t)j * GA + threadIdx.x] = bt[threadIdx.x];
+    } else {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) w_hat[vo + i] = vb[i];
+      if (threadIdx.x < GA) beta[(int64_t)j * GA + threadIdx.x] = 0.0;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace spi
+
+using namespace spi;
+
+static int check_sys(const spi_domain_t* dom, const spi_systems_t* sys) {
+  if (!dom || !sys) return SPI_ERR_ARG;
+  if (sys->n_sys < 0 || sys->max_n < 0) return SPI_ERR_ARG;
+  if (sys->kind < SPI_KIND_OK || sys->kind > SPI_KIND_EDK) return SPI_ERR_ARG;
+  if (dom->n_drift < 0 || dom->n_drift > SPI_MAX_DRIFT) return SPI_ERR_TOO_LARGE;
+  if (sys->kind == SPI_KIND_EDK && dom->n_drift > 0 && (!dom->stn_drift || !dom->cell_drift))
+    return SPI_ERR_ARG;
+  if (sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
+  return SPI_OK;
+}
+
+extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sys,
+                                double* l_arena, double* linv_arena, int32_t* status,
+                                double* cond, double* shift, spi_stream_t stream) {
+  int rc = check_sys(dom, sys);
+  if (rc) return rc;
+  if (sys->n_sys == 0) return SPI_OK;
+  if (!l_arena || !linv_arena || !status || !cond || !shift) return SPI_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  spi_domain_t d = *dom;
+  spi_systems_t sy = *sys;
+  int64_t nn = (int64_t)sys->max_n * sys->max_n;
+  int gx = (int)((nn + 255) / 256);
+  if (gx > 64) gx = 64;
+  if (gx < 1) gx = 1;
+  k_build_sys<<<dim3(gx, sys->n_sys), 256, 0, st>>>(d, sy, l_arena, shift);
+  SPI_LAUNCH_CHECK();
+  k_chol<<<sys->n_sys, FT, 0, st>>>(sy, l_arena, status);
+  SPI_LAUNCH_CHECK();
+  k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, l_arena, linv_arena, status, cond);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys,
+                               const double* linv_arena, const int32_t* status,
+                               const double* vals, double* w_hat, double* beta,
+                               double* g_cols, double* s_inv, double* g_colsum,
+                               spi_stream_t stream) {
+  int rc = check_sys(dom, sys);
+  if (rc) return rc;
+  if (sys->n_sys == 0) return SPI_OK;
+  if (!linv_arena || !status || !vals || !w_hat || !beta || !g_cols || !s_inv || !g_colsum)
+    return SPI_ERR_ARG;
+  size_t smem = (size_t)3 * sys->max_n * sizeof(double);
+  if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(k_duals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return SPI_ERR_CUDA;
+  }
+  k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, linv_arena, status, vals,
+                                                          w_hat, beta, g_cols, s_inv, g_colsum);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}

@@ -1,0 +1,493 @@
+"""Host side of the GB300 step engine: the reference's SpInterpSteps, batched.
+
+Mirrors ``interp/steps.py`` of spinterps:
+
+- :class:`SpInterpSteps` keeps the reference's method names for the
+  materialising kernels (``_get_dists_arr`` 73-86, ``_get_svars_arr``
+  88-138, ``_get_2d_arr_subset`` 140-168), computed on the GPU through the
+  C ABI.
+- :func:`interp_steps` replaces ``_get_all_interp_outputs`` (478-835) with
+  its per-group ``_get_interp`` calls (245-401) for neighbour method 'all':
+  it takes the same inputs (station coordinates, the station x step value
+  matrix with NaN for missing, cell coordinates, drifts, one variogram
+  string per step, the interp_args list of interp/prepare.py:638-695) and
+  returns the same fields ({label: [steps, cells]}, float32 by default) plus
+  the problem steps. All steps go to the GPU at once: steps are grouped into
+  kriging systems (station set x variogram), every system is built and
+  factored in FP64 in one launch, and one launch writes every cell of every
+  step of every system.
+
+Reference behaviours kept (file:line):
+- steps without stations: outputs stay NaN, step reported as a problem
+  step (673-690);
+- one station: its value everywhere, OK variance NaN (282-283);
+- no value >= min_value_to_interp_thresh, or a nugget-only variogram
+  (misc.py:1074-1105): the step mean, variance 0 (325-331; IDW 311-313);
+- the isclose(sum(lambda), 1) check with nearest-station fallback (418-426);
+- the OK variance lambda'gamma + 2 mu (429-434);
+- estimates clipped to [min_var_cut, max_var_cut] (466-476), fields cast to
+  float32 (interp/prepare.py:42).
+"""
+import ctypes
+from collections import OrderedDict
+
+import numpy as np
+import torch
+
+from . import _native as nat
+
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
+def _require_cuda(device):
+    if not torch.cuda.is_available():
+        raise RuntimeError("spinterps_gb300 needs a CUDA GPU; there is no CPU fallback")
+    dev = torch.device(device)
+    if dev.type != "cuda":
+        raise ValueError("device must be a CUDA device")
+    nat.lib()
+    return dev
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+_VG_CACHE = {}
+_NUG_CACHE = {}
+
+
+def parse_vg(vg_str):
+    """Parse a variogram string with the reference's rules (C ABI)."""
+    v = _VG_CACHE.get(vg_str)
+    if v is None:
+        v = nat.VgT()
+        nat.call("spi_parse_vg", str(vg_str).encode(), ctypes.byref(v))
+        _VG_CACHE[vg_str] = v
+    return v
+
+
+def check_full_nuggetness(vg_str, min_vg_val):
+    key = (vg_str, float(min_vg_val))
+    r = _NUG_CACHE.get(key)
+    if r is None:
+        out = nat.c_i32(0)
+        nat.call("spi_check_full_nuggetness", str(vg_str).encode(), float(min_vg_val),
+                 ctypes.byref(out))
+        r = bool(out.value)
+        _NUG_CACHE[key] = r
+    return r
+
+
+def _vg_tensor(vgs, dev):
+    arr = (nat.VgT * len(vgs))(*vgs)
+    raw = bytes(arr)
+    return torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(dev)
+
+
+def _as_dev(x, dev, dtype=torch.float64):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x)).to(device=dev, dtype=dtype)
+
+
+class SpInterpSteps:
+    """GPU versions of the reference step engine's materialising kernels.
+
+    Inputs may be numpy arrays (results come back as numpy) or CUDA tensors
+    (results stay on the device).
+    """
+
+    def __init__(self, min_vg_val=0.0, device="cuda"):
+        self._min_vg_val = float(min_vg_val)
+        self._dev = _require_cuda(device)
+
+    def _io(self, *arrs):
+        host = not isinstance(arrs[0], torch.Tensor)
+        return host, [_as_dev(a, self._dev) for a in arrs]
+
+    @staticmethod
+    def _back(t, host):
+        if host:
+            return t.cpu().numpy()
+        return t
+
+    def _get_dists_arr(self, x1s, y1s, x2s, y2s):
+        host, (x1, y1, x2, y2) = self._io(x1s, y1s, x2s, y2s)
+        assert x1.ndim == y1.ndim == x2.ndim == y2.ndim == 1
+        assert x1.numel() == y1.numel() and x2.numel() == y2.numel()
+        out = torch.full((x1.numel(), x2.numel()), float("nan"), dtype=torch.float64,
+                         device=self._dev)
+        nat.call("spi_fill_dists_2d_mat", _ptr(x1), _ptr(y1), x1.numel(), _ptr(x2), _ptr(y2),
+                 x2.numel(), _ptr(out), _stream())
+        return self._back(out, host)
+
+    def _get_svars_arr(self, dists_arr, vgs, interp_types, diag_mat_flag):
+        assert isinstance(interp_types, (list, tuple))
+        host, (d,) = self._io(dists_arr)
+        var_flag = any(t in interp_types for t in ("OK", "EDK"))
+        covar_flag = "SK" in interp_types
+        out = {}
+        for vg in vgs:
+            assert vg != "nan"
+            for flag, on in ((0, var_flag), (1, covar_flag)):
+                if not on:
+                    continue
+                a = torch.full_like(d, float("nan"))
+                v = parse_vg(vg)
+                nat.call("spi_fill_vg_var_arr", _ptr(d), d.shape[0], d.shape[1], _ptr(a), flag,
+                         int(diag_mat_flag), ctypes.byref(v), self._min_vg_val, _stream())
+                out[(vg, flag)] = self._back(a, host)
+        return out
+
+    def _get_2d_arr_subset(self, arr, row_idxs, col_idxs, rows_add_rc=0, cols_add_rc=0):
+        host, (a,) = self._io(arr)
+        ri = _as_dev(row_idxs, self._dev, torch.int64)
+        ci = _as_dev(col_idxs, self._dev, torch.int64)
+        assert a.ndim == 2 and ri.ndim == 1 and ci.ndim == 1
+        assert a.numel() and ri.numel() and ci.numel()
+        assert int(ri.min()) >= 0 and int(ri.max()) < a.shape[0]
+        assert int(ci.min()) >= 0 and int(ci.max()) < a.shape[1]
+        sub = torch.full((ri.numel() + rows_add_rc, ci.numel() + cols_add_rc), float("nan"),
+                         dtype=torch.float64, device=self._dev)
+        nat.call("spi_copy_2d_arr_at_idxs", _ptr(a), a.shape[0], a.shape[1], _ptr(ri),
+                 ri.numel(), _ptr(ci), ci.numel(), _ptr(sub), sub.shape[1], _stream())
+        return self._back(sub, host)
+
+
+class _Domain:
+    """Device copies of the coordinates/drifts and the spi_domain_t."""
+
+    def __init__(self, dev, stn_x, stn_y, cell_x, cell_y, stn_drifts, cell_drifts,
+                 min_vg_val, precision):
+        self.sx = _as_dev(stn_x, dev)
+        self.sy = _as_dev(stn_y, dev)
+        self.cx = _as_dev(cell_x, dev)
+        self.cy = _as_dev(cell_y, dev)
+        self.N = self.sx.numel()
+        self.C = self.cx.numel()
+        self.sd = self.cd = None
+        k = 0
+        if stn_drifts is not None:
+            self.sd = _as_dev(np.asarray(stn_drifts).reshape(self.N, -1), dev)
+            self.cd = _as_dev(np.asarray(cell_drifts).reshape(-1, self.C), dev)
+            k = self.sd.shape[1]
+            if k > nat.SPI_MAX_DRIFT:
+                raise ValueError(f"at most {nat.SPI_MAX_DRIFT} drifts")
+        self.ssplit = self.csplit = None
+        if precision == 1:
+            ox = float(min(self.sx.min().item(), self.cx.min().item()))
+            oy = float(min(self.sy.min().item(), self.cy.min().item()))
+            self.ssplit = torch.empty((self.N, 4), dtype=torch.float32, device=dev)
+            self.csplit = torch.empty((self.C, 4), dtype=torch.float32, device=dev)
+            nat.call("spi_split_coords", _ptr(self.sx), _ptr(self.sy), self.N, ox, oy,
+                     _ptr(self.ssplit), _stream())
+            nat.call("spi_split_coords", _ptr(self.cx), _ptr(self.cy), self.C, ox, oy,
+                     _ptr(self.csplit), _stream())
+        self.st = nat.DomainT(self.N, _ptr(self.sx), _ptr(self.sy), self.C, _ptr(self.cx),
+                              _ptr(self.cy), k, _ptr(self.sd), _ptr(self.cd), float(min_vg_val),
+                              _ptr(self.ssplit), _ptr(self.csplit))
+
+
+def _out_struct(est, var, min_var_cut, max_var_cut):
+    return nat.OutT(1 if est.dtype == torch.float64 else 0, _ptr(est), _ptr(var),
+                    0 if min_var_cut is None else 1, 0 if max_var_cut is None else 1,
+                    0.0 if min_var_cut is None else float(min_var_cut),
+                    0.0 if max_var_cut is None else float(max_var_cut))
+
+
+def _align(x, a=32):
+    return (x + a - 1) // a * a
+
+
+class _KrigeBatch:
+    """One chunk of kriging systems: device descriptors and workspaces."""
+
+    def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision):
+        self.ch = ch
+        self.kind = kind
+        self.precision = precision
+        ns = np.array([len(systems[i][0]) for i in ch], dtype=np.int64)
+        stn_off = np.concatenate([[0], np.cumsum(ns)]).astype(np.int64)
+        stn_idx = np.concatenate([systems[i][0] for i in ch]).astype(np.int32)
+        sizes = np.array([_align(n * n) for n in ns], dtype=np.int64)
+        mat_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        self.arena = int(sizes.sum())
+        steps_l = [systems[i][2] for i in ch]
+        step_off = np.concatenate([[0], np.cumsum([len(x) for x in steps_l])]).astype(np.int64)
+        steps = np.concatenate([np.asarray(x, dtype=np.int32) for x in steps_l])
+        vals_l, off = [], 0
+        for i, sl in zip(ch, steps_l):
+            idx = systems[i][0]
+            for j in sl:
+                val_off[j] = off
+                vals_l.append(data[j, idx])
+                off += len(idx)
+        self.steps_l = steps_l
+        self.vals = torch.as_tensor(np.concatenate(vals_l), device=dev)
+        self.vgt = _vg_tensor([parse_vg(systems[i][1]) for i in ch], dev)
+        self.t = [torch.as_tensor(a, device=dev) for a in
+                  (stn_off, stn_idx, mat_off, step_off, steps, val_off.copy())]
+        self.out_row = torch.as_tensor(np.arange(T, dtype=np.int32), device=dev)
+        t = self.t
+        self.sy = nat.SystemsT(len(ch), nat.KIND[kind], _ptr(t[0]), _ptr(t[1]), _ptr(self.vgt),
+                               _ptr(t[2]), _ptr(t[3]), _ptr(t[4]), _ptr(t[5]),
+                               _ptr(self.out_row), int(ns.max()))
+        n_sys = len(ch)
+        self.L = torch.empty(self.arena, dtype=torch.float64, device=dev)
+        self.X = torch.empty(self.arena, dtype=torch.float64, device=dev)
+        self.status = torch.empty(n_sys, dtype=torch.int32, device=dev)
+        self.cond = torch.empty(n_sys, dtype=torch.float64, device=dev)
+        self.shift = torch.empty(n_sys, dtype=torch.float64, device=dev)
+        self.g_cols = torch.zeros(int(stn_off[-1]) * nat.GA, dtype=torch.float64, device=dev)
+        self.s_inv = torch.zeros(n_sys * nat.GA * nat.GA, dtype=torch.float64, device=dev)
+        self.g_colsum = torch.zeros(n_sys * nat.GA, dtype=torch.float64, device=dev)
+        self.w_hat = torch.zeros_like(self.vals)
+        self.beta = beta
+        self.X32 = self.g32 = self.w32 = None
+        if precision == 1:
+            self.X32 = torch.empty(self.arena, dtype=torch.float32, device=dev)
+            self.g32 = torch.empty(self.g_cols.numel(), dtype=torch.float32, device=dev)
+            self.w32 = torch.empty(self.w_hat.numel(), dtype=torch.float32, device=dev)
+        # algorithmic FLOP of the cell kernel: per (system, cell) the
+        # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
+        self.n = ns
+        self.n_steps = np.array([len(x) for x in steps_l], dtype=np.int64)
+
+    def cell_flops(self, C, want_var, a):
+        per = 2 * self.n * a + 2 * self.n * self.n_steps
+        if want_var:
+            per = per + self.n * (self.n + 1)
+        return float(per.sum()) * C
+
+    def run(self, dom, out, want_var, ev=None):
+        s = _stream()
+        nat.call("spi_krige_factor", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.L),
+                 _ptr(self.X), _ptr(self.status), _ptr(self.cond), _ptr(self.shift), s)
+        nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.X),
+                 _ptr(self.status), _ptr(self.vals), _ptr(self.w_hat), _ptr(self.beta),
+                 _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum), s)
+        if self.precision == 1:
+            nat.call("spi_to_f32", _ptr(self.X), _ptr(self.X32), self.arena, s)
+            nat.call("spi_to_f32", _ptr(self.g_cols), _ptr(self.g32), self.g_cols.numel(), s)
+            nat.call("spi_to_f32", _ptr(self.w_hat), _ptr(self.w32), self.w_hat.numel(), s)
+        if ev is not None:
+            ev[0].record()
+        nat.call("spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.X),
+                 _ptr(self.status), _ptr(self.shift), _ptr(self.vals), _ptr(self.w_hat),
+                 _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum),
+                 _ptr(self.X32), _ptr(self.g32), _ptr(self.w32), 1 if want_var else 0,
+                 self.precision, ctypes.byref(out), s)
+        if ev is not None:
+            ev[1].record()
+
+
+def _chunk_systems(systems, precision, arena_budget):
+    order = sorted(range(len(systems)), key=lambda i: -len(systems[i][0]))
+    chunks, cur, cur_bytes = [], [], 0
+    for i in order:
+        n = len(systems[i][0])
+        b = _align(n * n) * 8 * (3 if precision == 1 else 2)
+        if cur and (cur_bytes + b > arena_budget or len(cur) >= 65535):
+            chunks.append(cur)
+            cur, cur_bytes = [], 0
+        cur.append(i)
+        cur_bytes += b
+    if cur:
+        chunks.append(cur)
+    return chunks
+
+
+class InterpPlan:
+    """All host-side work of one interpolation job, done once: step
+    grouping, flags, nugget checks, kriging systems, value gathering and
+    the uploads. :meth:`execute` then runs only GPU work (factorisations,
+    duals, cell kernels, IDW / NNB, row fills) on the current stream, from
+    device-resident inputs into device-resident fields."""
+
+    def __init__(self, stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *,
+                 est_vars=False, stn_drifts=None, cell_drifts=None, min_var_thr=0.0,
+                 min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
+                 time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30):
+        dev = self.dev = _require_cuda(device)
+        prec = self.prec = PRECISION[precision]
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        T, N = data.shape
+        self.T = T
+        C = self.C = int(np.asarray(cell_x).size)
+        if time_steps is None:
+            time_steps = np.arange(T)
+        types = self.types = [a[0] for a in interp_args]
+        labels = self.labels = [a[2] for a in interp_args]
+        self.interp_args = interp_args
+        self.min_var_cut, self.max_var_cut = min_var_cut, max_var_cut
+        tdt = torch.float64 if np.dtype(intrp_dtype) == np.float64 else torch.float32
+        self.flds = OrderedDict((lab, torch.full((T, C), float("nan"), dtype=tdt, device=dev))
+                                for lab in labels)
+        avail = np.isfinite(data)
+        n_av = avail.sum(1)
+        means = np.full(T, np.nan)
+        for j in np.where(n_av > 0)[0]:
+            means[j] = data[j, avail[j]].mean()   # numpy's pairwise mean, as the reference
+        flags = ((data >= min_var_thr) & avail).any(1)
+        self.prblm = [time_steps[j] for j in np.where(n_av == 0)[0]]
+        self.single = np.where(n_av == 1)[0]
+        self.single_val = np.array([data[j, avail[j]][0] for j in self.single], dtype=np.float64)
+        multi = self.multi = np.where(n_av >= 2)[0]
+        self.dom = _Domain(dev, stn_x, stn_y, cell_x, cell_y,
+                           stn_drifts if "EDK" in types else None,
+                           cell_drifts if "EDK" in types else None, min_vg_val, prec)
+        self.krig = []
+        krig = [t for t in ("OK", "SK", "EDK") if t in types]
+        if krig:
+            vgs = np.asarray(vgs, dtype=object)
+            assert np.all(vgs != "nan"), "NaN VGs not allowed!"
+            nug = np.array([check_full_nuggetness(v, min_vg_val) for v in vgs])
+            packed = np.packbits(avail, axis=1)
+            _, grp = np.unique(packed, axis=0, return_inverse=True)
+            grp = grp.ravel()
+            for kind in krig:
+                est = self.flds[kind]
+                var = self.flds["EST_VARS_OK"] if (kind == "OK" and est_vars) else None
+                out = _out_struct(est, var, min_var_cut, max_var_cut)
+                mean_steps = [j for j in multi if (not flags[j]) or nug[j]]
+                systems = OrderedDict()
+                for j in multi:
+                    if (not flags[j]) or nug[j]:
+                        continue
+                    key = (int(grp[j]), vgs[j])
+                    if key not in systems:
+                        systems[key] = (np.where(avail[j])[0], vgs[j], [])
+                    systems[key][2].append(int(j))
+                systems = list(systems.values())
+                val_off = np.zeros(T, dtype=np.int64)
+                beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
+                batches = [_KrigeBatch(dev, self.dom, kind, systems, ch, data, T, val_off, beta,
+                                       prec)
+                           for ch in _chunk_systems(systems, prec, arena_budget)]
+                fills = (
+                    _fill_args(dev, self.single, self.single_val,
+                               None if var is None else np.full(self.single.size, np.nan)),
+                    _fill_args(dev, mean_steps, means[mean_steps], np.zeros(len(mean_steps))))
+                a = 1 if kind == "SK" else 1 + self.dom.st.n_drift
+                self.krig.append((kind, out, var is not None, batches, fills, a))
+        self.idw = []
+        if any(t in ("IDW", "NNB") for t in types):
+            self.data_d = torch.as_tensor(data, device=dev)
+            self.steps_t = torch.as_tensor(multi.astype(np.int32), device=dev)
+            self.flag_t = torch.as_tensor(flags.astype(np.uint8), device=dev)
+            self.mean_t = torch.as_tensor(np.nan_to_num(means), device=dev)
+            n_present = n_av[multi].astype(np.float64)
+            for i, t in enumerate(types):
+                if t not in ("IDW", "NNB"):
+                    continue
+                out = _out_struct(self.flds[labels[i]], None, min_var_cut, max_var_cut)
+                fill = _fill_args(dev, self.single, self.single_val, None)
+                p = float(interp_args[i][3]) if t == "IDW" else 0.0
+                self.idw.append((t, out, fill, p))
+            self.idw_flops = 4.0 * N * len(multi) * C
+        self.info = {"failed_steps": {}, "cond": {}}
+
+    def execute(self, timing=False):
+        """Run the whole job on the GPU (current stream). With ``timing``,
+        returns per-stage CUDA-event pairs (kernel timing without syncs)."""
+        C = self.C
+        evs = {"krige_cells": [], "idw": []}
+        s = _stream()
+        for kind, out, want_var, batches, fills, a in self.krig:
+            for f in fills:
+                _fill_run(f, C, out, s)
+            for b in batches:
+                ev = None
+                if timing:
+                    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                    evs["krige_cells"].append((ev, b.cell_flops(C, want_var, a)))
+                b.run(self.dom, out, want_var, ev)
+        for t, out, fill, p in self.idw:
+            _fill_run(fill, C, out, s)
+            if not len(self.multi):
+                continue
+            ev = None
+            if timing:
+                ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                ev[0].record()
+            if t == "IDW":
+                nat.call("spi_idw_cells", ctypes.byref(self.dom.st), len(self.multi),
+                         _ptr(self.steps_t), _ptr(self.steps_t), _ptr(self.data_d),
+                         _ptr(self.flag_t), _ptr(self.mean_t), p, self.prec, ctypes.byref(out),
+                         s)
+            else:
+                nat.call("spi_nnb_cells", ctypes.byref(self.dom.st), len(self.multi),
+                         _ptr(self.steps_t), _ptr(self.steps_t), _ptr(self.data_d),
+                         ctypes.byref(out), s)
+            if timing:
+                ev[1].record()
+                evs["idw"].append((ev, self.idw_flops))
+        return evs
+
+    def collect_info(self):
+        for kind, out, want_var, batches, fills, a in self.krig:
+            failed, cond = [], {}
+            for b in batches:
+                st = b.status.cpu().numpy()
+                cn = b.cond.cpu().numpy()
+                for k, sl in enumerate(b.steps_l):
+                    for j in sl:
+                        cond[int(j)] = float(cn[k])
+                        if st[k] != 0:
+                            failed.append(int(j))
+            self.info["failed_steps"][kind] = sorted(failed)
+            self.info["cond"][kind] = cond
+        return self.info
+
+    def fields(self, numpy=True):
+        torch.cuda.current_stream().synchronize()
+        if numpy:
+            return OrderedDict((k, v.cpu().numpy()) for k, v in self.flds.items())
+        return self.flds
+
+
+def _fill_args(dev, rows, vals, vvals):
+    if not len(rows):
+        return None
+    r = torch.as_tensor(np.asarray(rows, dtype=np.int32), device=dev)
+    v = torch.as_tensor(np.asarray(vals, dtype=np.float64), device=dev)
+    vv = None if vvals is None else torch.as_tensor(np.asarray(vvals, dtype=np.float64),
+                                                    device=dev)
+    return (len(rows), r, v, vv)
+
+
+def _fill_run(f, C, out, s):
+    if f is None:
+        return
+    n, r, v, vv = f
+    nat.call("spi_fill_rows", n, _ptr(r), _ptr(v), _ptr(vv), C, ctypes.byref(out), s)
+
+
+def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_vars=False,
+                 stn_drifts=None, cell_drifts=None, min_var_thr=0.0, min_var_cut=None,
+                 max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
+                 precision="fp64", device="cuda", return_numpy=True, return_info=False,
+                 arena_budget=8 << 30):
+    """Interpolate every step onto every cell on the GPU.
+
+    Same inputs and outputs as the reference step engine for one grid chunk
+    (see the module docstring). ``precision`` is "fp64" (plain FP64) or
+    "mixed" (FP32 right-hand sides and contractions over the FP64
+    factorisation). Returns ``(fields, problem_steps)``, plus an info dict
+    (failed systems, condition estimates) when ``return_info``.
+    """
+    plan = InterpPlan(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, est_vars=est_vars,
+                      stn_drifts=stn_drifts, cell_drifts=cell_drifts, min_var_thr=min_var_thr,
+                      min_var_cut=min_var_cut, max_var_cut=max_var_cut, min_vg_val=min_vg_val,
+                      intrp_dtype=intrp_dtype, time_steps=time_steps, precision=precision,
+                      device=device, arena_budget=arena_budget)
+    plan.execute()
+    flds = plan.fields(numpy=return_numpy)
+    if return_info:
+        return flds, plan.prblm, plan.collect_info()
+    return flds, plan.prblm

@@ -1,0 +1,133 @@
+"""The C ABI library: loads without a GPU, exports every declared symbol,
+its ctypes mirror matches the C layout, and its host-side parsers follow
+the reference's rules (checked against the oracle and the golden vectors)."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import port
+from spinterps_gb300 import _native as nat
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        txt = h.read_text()
+        names.update(re.findall(r"^(?:int|const char \*)\s*(spi_\w+)\s*\(", txt, re.M))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = nat.load()
+    decl = declared_symbols()
+    assert decl, "no declarations found"
+    for name in decl:
+        assert hasattr(lib, name), name
+    assert sorted(decl) == nat.EXPORTS
+    assert lib.spi_version().startswith(b"spinterps_gb300")
+
+
+def test_struct_layout_matches_header(tmp_path):
+    src = tmp_path / "layout.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "spinterps_gb300.h"
+#define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  printf("spi_vg_t %zu\nspi_domain_t %zu\nspi_systems_t %zu\nspi_out_t %zu\n",
+         sizeof(spi_vg_t), sizeof(spi_domain_t), sizeof(spi_systems_t), sizeof(spi_out_t));
+  P(spi_vg_t, sill) P(spi_vg_t, range) P(spi_domain_t, n_drift) P(spi_domain_t, min_vg_val)
+  P(spi_domain_t, stn_split) P(spi_domain_t, cell_split) P(spi_systems_t, max_n)
+  P(spi_systems_t, out_row) P(spi_out_t, clip_min) P(spi_out_t, clip_max)
+  return 0;
+}''')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.rsplit(" ", 1) for l in subprocess.run(
+        [str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    assert int(got["spi_vg_t"]) == ctypes.sizeof(nat.VgT)
+    assert int(got["spi_domain_t"]) == ctypes.sizeof(nat.DomainT)
+    assert int(got["spi_systems_t"]) == ctypes.sizeof(nat.SystemsT)
+    assert int(got["spi_out_t"]) == ctypes.sizeof(nat.OutT)
+    assert int(got["spi_vg_t.sill"]) == nat.VgT.sill.offset
+    assert int(got["spi_vg_t.range"]) == nat.VgT.range.offset
+    assert int(got["spi_domain_t.n_drift"]) == nat.DomainT.n_drift.offset
+    assert int(got["spi_domain_t.min_vg_val"]) == nat.DomainT.min_vg_val.offset
+    assert int(got["spi_domain_t.stn_split"]) == nat.DomainT.stn_split.offset
+    assert int(got["spi_domain_t.cell_split"]) == nat.DomainT.cell_split.offset
+    assert int(got["spi_systems_t.max_n"]) == nat.SystemsT.max_n.offset
+    assert int(got["spi_systems_t.out_row"]) == nat.SystemsT.out_row.offset
+    assert int(got["spi_out_t.clip_min"]) == nat.OutT.clip_min.offset
+    assert int(got["spi_out_t.clip_max"]) == nat.OutT.clip_max.offset
+
+
+def _parse(s):
+    v = nat.VgT()
+    rc = nat.lib().spi_parse_vg(s.encode(), ctypes.byref(v))
+    return rc, v
+
+
+def test_parse_vg_matches_reference_rules(golden):
+    for s in list(golden["k_vgs"]) + ["1.0 Nug(0.0)", "0.3 Gau(-5)", "2 Exp(1e5)",
+                                      " 0.5 Sph(300) +0.5 Exp(10) "]:
+        s = str(s)
+        rc, v = _parse(s)
+        assert rc == 0, s
+        ref = port.parse_vg_str(s)
+        assert v.n_comp == len(ref)
+        for k, (code, sill, rng) in enumerate(ref):
+            assert v.code[k] == code and v.sill[k] == sill and v.range[k] == rng, s
+
+
+@pytest.mark.parametrize("bad", ["1.0 Foo(3)", "1.0  Exp(3)", "1.0 Exp3", "Exp(3)",
+                                 "1.0 Exp(3) + ", "x Exp(3)", "1.0 Exp(1e+5)"])
+def test_parse_vg_rejects_what_the_reference_rejects(bad):
+    rc, _ = _parse(bad)
+    assert rc == 2  # SPI_ERR_VG
+    with pytest.raises(Exception):
+        port.parse_vg_str(bad)
+
+
+def test_parse_vg_too_many_components():
+    rc, _ = _parse(" + ".join(["0.1 Exp(10)"] * 5))
+    assert rc == 5  # SPI_ERR_TOO_LARGE
+
+
+def test_nuggetness_matches_reference(golden):
+    for s, r4, r0 in zip(golden["k_nug_strs"], golden["k_nug_1e-4"], golden["k_nug_0"]):
+        for mvv, r in ((1e-4, r4), (0.0, r0)):
+            out = nat.c_i32(-1)
+            assert nat.lib().spi_check_full_nuggetness(str(s).encode(), mvv, ctypes.byref(out)) == 0
+            assert bool(out.value) == bool(r), (s, mvv)
+
+
+def test_null_and_size_errors_without_gpu():
+    lib = nat.lib()
+    assert lib.spi_fill_dists_2d_mat(None, None, -1, None, None, 3, None, None) == 1
+    assert lib.spi_fill_dists_2d_mat(None, None, 0, None, None, 0, None, None) == 0
+    assert lib.spi_parse_vg(None, None) == 1
+    out = nat.OutT()
+    assert lib.spi_fill_rows(-1, None, None, None, 10, ctypes.byref(out), None) == 1
+    dom = nat.DomainT()
+    dom.n_drift = 99
+    sy = nat.SystemsT()
+    sy.n_sys = 1
+    assert lib.spi_krige_factor(ctypes.byref(dom), ctypes.byref(sy), None, None, None, None,
+                                None, None) == 5
+
+
+def test_host_mirror_has_no_cpu_fallback():
+    import torch
+    import spinterps_gb300 as spi
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        spi.interp_steps(np.zeros(3), np.zeros(3), np.zeros((1, 3)), np.zeros(2), np.zeros(2),
+                         ["1.0 Exp(10)"], [("OK", None, "OK")])

@@ -1,0 +1,231 @@
+"""Parity of the CUDA path (through the C ABI) with the reference.
+
+Golden vectors come from the reference's own code (tests/golden); larger
+cases are checked against the oracle (oracle/port.py, pinned to the same
+vectors). Tolerances, relative to the largest magnitude of the field:
+  FP64 path  1e-9  (spec bar for the plain FP64 GPU path)
+  mixed path 1e-5  (spec bar for split-precision FP32)
+  float32 output fields: 2e-6 (one float32 rounding of either side)
+Distances are the correctly rounded root; the reference's glibc pow(x, 0.5)
+differs from it by one ulp on ~0.1% of inputs.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import port  # noqa: E402
+
+FP64_TOL = 1e-9
+MIXED_TOL = 1e-5
+F32_TOL = 2e-6
+
+
+def _spi():
+    import spinterps_gb300 as spi
+    return spi
+
+
+def _err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    nan_a, nan_b = np.isnan(a), np.isnan(b)
+    assert np.array_equal(nan_a, nan_b), (nan_a.sum(), nan_b.sum())
+    m = ~nan_b
+    if not m.any():
+        return 0.0
+    scale = max(np.abs(b[m]).max(), 1e-300)
+    return float(np.abs(a[m] - b[m]).max() / scale)
+
+
+def test_dists_drop_in(golden):
+    spi = _spi()
+    st = spi.SpInterpSteps(min_vg_val=1e-4)
+    g = golden
+    d = st._get_dists_arr(g["k_cx"], g["k_cy"], g["k_sx"], g["k_sy"])
+    ref = g["k_d_cs"]
+    ulp = np.abs(d - ref) / np.spacing(np.maximum(ref, 1e-300))
+    assert (ulp <= 1).all()
+    assert (d == ref).mean() > 0.98
+    assert (d[:3, :3].diagonal() == 0).all()
+
+
+def test_vg_fill_drop_in(golden):
+    spi = _spi()
+    st = spi.SpInterpSteps(min_vg_val=0.0)
+    g = golden
+    for vi, vg in enumerate(g["k_vgs"]):
+        vg = str(vg)
+        for covar in (0, 1):
+            for mvv in (0.0, 1e-4, 0.05):
+                st._min_vg_val = mvv
+                types = ["SK"] if covar else ["OK"]
+                a = st._get_svars_arr(g["k_d_ss"], [vg], types, 1)[(vg, covar)]
+                b = st._get_svars_arr(g["k_d_cs"], [vg], types, 0)[(vg, covar)]
+                for got, key in ((a, f"k_vg_ss_{vi}_{covar}_{mvv:g}"),
+                                 (b, f"k_vg_cs_{vi}_{covar}_{mvv:g}")):
+                    ref = g[key]
+                    # values within the zeroing threshold may flip by one ulp
+                    near = np.abs(ref - mvv) <= 1e-12 * max(1.0, abs(mvv))
+                    diff = np.abs(got - ref)
+                    scale = max(np.abs(ref).max(), 1e-300)
+                    assert (diff[~near] <= 1e-13 * scale).all(), (vg, covar, mvv)
+
+
+def test_copy_subset_drop_in(golden):
+    spi = _spi()
+    st = spi.SpInterpSteps()
+    g = golden
+    sub = st._get_2d_arr_subset(g["k_d_cs"], g["k_copy_ri"], g["k_copy_ci"], 2, 1)
+    ref = g["k_copy_sub"]
+    assert np.array_equal(np.isnan(sub), np.isnan(ref))
+    assert np.array_equal(np.nan_to_num(sub), np.nan_to_num(ref))
+
+
+def _one_group(g, methods, vgs, *, cx="i_cx", cy="i_cy", z=None, n=None, sd=None, cd=None,
+               precision="fp64"):
+    """Run interp_steps on the fixture's single station group with every
+    step flagged for interpolation (the fixture passed its flags directly to
+    _get_interp; callers compare the steps whose flag was on)."""
+    spi = _spi()
+    sx, sy = g["i_sx"], g["i_sy"]
+    z = (g["i_z"] if z is None else z).copy()
+    if n is not None:
+        sx, sy, z = sx[:n], sy[:n], z[:, :n]
+    args = port.interp_args_for(methods, est_vars="OK" in methods)
+    return spi.interp_steps(sx, sy, z, g[cx], g[cy], [str(v) for v in vgs], args,
+                            est_vars="OK" in methods, stn_drifts=sd, cell_drifts=cd,
+                            min_var_thr=-np.inf, min_vg_val=1e-4, intrp_dtype=np.float64,
+                            precision=precision)[0]
+
+
+def test_ok_sk_single_group_vs_reference(golden):
+    g = golden
+    flags = g["i_flags"]
+    for itype in ("OK", "SK"):
+        got = _one_group(g, [itype], g["i_vgs_mixed"])
+        ref = g[f"i_{itype}_est"]
+        on = np.where(flags)[0]
+        assert _err(got[itype][on], ref[on]) <= FP64_TOL, itype
+        if itype == "OK":
+            assert _err(got["EST_VARS_OK"][on], g["i_OK_var"][on]) <= F32_TOL
+    got = _one_group(g, ["OK"], g["i_vgs_other"])
+    assert _err(got["OK"], g["i_OKo_est"]) <= FP64_TOL
+    assert _err(got["EST_VARS_OK"], g["i_OKo_var"]) <= F32_TOL
+
+
+def test_edk_single_group_vs_reference(golden):
+    g = golden
+    flags = g["i_flags"]
+    on = np.where(flags)[0]
+    elev = g["i_EDK1_sd"][:, 0]
+    for k in (1, 2):
+        got = _one_group(g, ["EDK"], g["i_vgs_mixed"], z=g["i_z"] + 1e-3 * elev,
+                         sd=g[f"i_EDK{k}_sd"], cd=g[f"i_EDK{k}_cd"])
+        assert _err(got["EDK"][on], g[f"i_EDK{k}_est"][on]) <= FP64_TOL, k
+
+
+def test_idw_nnb_single_group_vs_reference(golden):
+    g = golden
+    flags = g["i_flags"]
+    on = np.where(flags)[0]
+    t = g["i_z"].shape[0]
+    vg0 = "0.05 Nug(0.0) + 0.95 Exp(20000)"
+    for e in (1.0, 2.0, 3.5):
+        got = _one_group(g, [("IDW", e)], [vg0] * t, cx="i_cx2", cy="i_cy2")
+        assert _err(got["IDW_000"][on], g[f"i_IDW_{e:g}_est"][on]) <= FP64_TOL, e
+    got = _one_group(g, ["NNB"], [vg0] * t, cx="i_cx2", cy="i_cy2")
+    assert np.array_equal(got["NNB"], g["i_NNB_est"])
+    got = _one_group(g, ["OK"], [vg0] * t, n=1)
+    assert np.array_equal(got["OK"], g["i_one_est"])
+    assert np.isnan(got["EST_VARS_OK"]).all()
+
+
+@pytest.mark.parametrize("tag", ["okidw", "edk"])
+def test_multi_step_runs_vs_reference(golden, tag):
+    spi = _spi()
+    g = golden
+    p = f"s_{tag}_"
+    methods = []
+    for m in g[p + "methods"]:
+        m = str(m)
+        methods.append(("IDW", float(m.split(":")[1])) if m.startswith("IDW:") else m)
+    thr, mn, mx, mvv = g[p + "params"]
+    args = port.interp_args_for(methods, est_vars="OK" in methods)
+    for precision, tol in (("fp64", F32_TOL), ("mixed", MIXED_TOL)):
+        flds, prblm = spi.interp_steps(
+            g[p + "sx"], g[p + "sy"], g[p + "z"], g[p + "cx"], g[p + "cy"],
+            [str(v) for v in g[p + "vgs"]], args, est_vars="OK" in methods,
+            stn_drifts=g.get(p + "sd"), cell_drifts=g.get(p + "cd"), min_var_thr=thr,
+            min_var_cut=None if np.isnan(mn) else mn, max_var_cut=None if np.isnan(mx) else mx,
+            min_vg_val=mvv, precision=precision)
+        assert sorted(set(prblm)) == g[p + "prblm"].tolist()
+        for lab, f in flds.items():
+            assert f.dtype == np.float32
+            e = _err(f, g[p + "out_" + lab])
+            assert e <= tol, (precision, lab, e)
+
+
+def test_config1_subset_vs_reference(golden):
+    spi = _spi()
+    g = golden
+    vg = "0.05 Nug(0.0) + 0.95 Exp(20000)"
+    args = port.interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
+    for precision, tol, vtol in (("fp64", FP64_TOL, F32_TOL), ("mixed", MIXED_TOL, MIXED_TOL)):
+        flds, _ = spi.interp_steps(g["c1_sx"], g["c1_sy"], g["c1_z"], g["c1_cx"], g["c1_cy"],
+                                   [vg] * 4, args, est_vars=True, min_vg_val=1e-4,
+                                   intrp_dtype=np.float64, precision=precision)
+        assert _err(flds["OK"], g["c1_ok_est"]) <= tol, precision
+        assert _err(flds["EST_VARS_OK"], g["c1_ok_var"]) <= vtol, precision
+        assert _err(flds["IDW_000"], g["c1_idw_est"]) <= tol, precision
+
+
+def _random_case(seed, n=120, t=6, nx=40, ny=30, p_miss=0.3, box=1.2e5):
+    rng = np.random.default_rng(seed)
+    sx, sy = rng.uniform(0, box, n), rng.uniform(0, box, n)
+    gx, gy = np.meshgrid(np.arange(nx) * (box / nx) + box / nx / 2,
+                         box - box / ny / 2 - np.arange(ny) * (box / ny))
+    z = rng.gamma(0.8, 2.0, size=(t, n)) * (rng.uniform(size=(t, n)) < 0.6)
+    z[rng.uniform(size=(t, n)) < p_miss] = np.nan
+    types = ["Sph", "Exp", "Gau"]
+    vgs = []
+    for j in range(t):
+        r = rng.uniform(10e3, 40e3)
+        s = rng.uniform(0.5, 2.0)
+        nf = rng.uniform(0, 0.2)
+        vgs.append(f"{nf * s:.5f} Nug(0.0) + {s - nf * s:.5f} {types[j % 3]}({r:.1f})")
+    elev = 500 + 4e-3 * sx + rng.normal(0, 30, n)
+    celev = 500 + 4e-3 * gx.ravel()
+    return sx, sy, z, gx.ravel(), gy.ravel(), vgs, elev[:, None], celev[None]
+
+
+def test_random_steps_vs_oracle():
+    spi = _spi()
+    sx, sy, z, cx, cy, vgs, sd, cd = _random_case(7)
+    methods = ["OK", "SK", "EDK", ("IDW", 2.0), ("IDW", 1.5), "NNB"]
+    args = port.interp_args_for(methods, est_vars=True)
+    kw = dict(est_vars=True, stn_drifts=sd, cell_drifts=cd, min_var_thr=0.1, min_vg_val=1e-4,
+              intrp_dtype=np.float64)
+    ref, rp = port.interp_steps(sx, sy, z, cx, cy, vgs, args, **kw)
+    got, gp, info = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, return_info=True, **kw)
+    assert gp == rp
+    for lab in ref:
+        assert _err(got[lab], ref[lab]) <= FP64_TOL, lab
+    mixed, _ = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, precision="mixed", **kw)
+    for lab in ref:
+        assert _err(mixed[lab], ref[lab]) <= MIXED_TOL, lab
+
+
+def test_float32_fields_and_clipping():
+    spi = _spi()
+    sx, sy, z, cx, cy, vgs, _, _ = _random_case(9, t=4)
+    args = port.interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
+    kw = dict(est_vars=True, min_var_cut=0.5, max_var_cut=3.0, min_vg_val=1e-4)
+    ref, _ = port.interp_steps(sx, sy, z, cx, cy, vgs, args, **kw)
+    got, _ = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, **kw)
+    for lab in ref:
+        assert got[lab].dtype == np.float32
+        assert _err(got[lab], ref[lab]) <= F32_TOL, lab
+    assert np.nanmin(got["OK"]) >= 0.5 and np.nanmax(got["OK"]) <= 3.0
