@@ -133,8 +133,9 @@ typedef struct {
     const int64_t *stn_off;        /* [n_sys + 1] offsets into stn_idx */
     const int32_t *stn_idx;        /* station indices of every system */
     const spi_vg_t *vg;            /* [n_sys] */
-    const int64_t *mat_off;        /* [n_sys] offset (doubles) of each n x n
-                                      matrix in the matrix arenas; 32-aligned */
+    const int64_t *mat_off;        /* [n_sys] offset (doubles) of each
+                                      system's matrix in the arenas, 32-aligned,
+                                      sized (n + SPI_MAX_DRIFT + 1)^2 */
     const int64_t *step_off;       /* [n_sys + 1] offsets into steps */
     const int32_t *steps;          /* step indices, grouped by system */
     const int64_t *val_off;        /* [n_steps] offset of step j's values */
@@ -145,35 +146,55 @@ typedef struct {
 /* Maximum drifts of EDK (a = 1 + n_drift Lagrange/drift rows). */
 #define SPI_MAX_DRIFT 7
 
-/* Build each system's matrix in covariance form and factor it in FP64:
- *   OK/EDK: A = s*11' - Gamma, s = total sill, Gamma filled exactly as
- *           fill_vg_var_arr with covar 0 (diagonal included);
- *   SK:     A = the covariance fill (fill_vg_var_arr with covar 1).
- * Under sum(lambda) = 1 the OK/EDK weights of [[A, F], [F', 0]] equal those
- * of the reference's [[Gamma, F], [F', 0]] (the Lagrange multipliers change
- * sign). A = L L' (Cholesky), then Linv = L^-1 (lower).
- * L is written to l_arena, Linv to linv_arena (both at mat_off).
- * status[s] = 0, or the 1-based pivot index where A was not positive
- * definite; cond[s] = n * A_00 * ||Linv||_F^2, an upper bound of A's
- * 2-norm condition number within a factor n; shift[s] = s (0 for SK). */
-int spi_krige_factor(const spi_domain_t *dom, const spi_systems_t *sys,
-                     double *l_arena, double *linv_arena, int32_t *status,
-                     double *cond, double *shift, spi_stream_t stream);
+/* Per-batch workspace of the kriging entry points (device arrays, caller
+ * owned). Arenas hold one matrix per system at sys->mat_off[s], sized for
+ * (n + SPI_MAX_DRIFT + 1)^2 doubles; per-system arrays have n_sys entries;
+ * w_hat has the layout of the values array; beta is [n_steps_total, GA] and
+ * g_cols [total stations * GA], GA = SPI_MAX_DRIFT + 1. The float arrays are
+ * needed only by the precision-1 cell kernel. */
+typedef struct {
+    double *l_arena;     /* Cholesky factor L; for routed systems the
+                            inverse of the reference's saddle matrix */
+    double *linv_arena;  /* Linv = L^-1 */
+    int32_t *status;     /* Cholesky: 0, or the 1-based failing pivot */
+    int32_t *route;      /* 0 Cholesky path, 1 exact-inverse path,
+                            2 singular (nearest-station fallback) */
+    double *cond;        /* n * A_00 * ||Linv||_F^2 (>= cond_2(A)) */
+    double *shift;       /* s of A = s 11' - Gamma (0 for SK) */
+    double *w_hat;       /* per-step dual weights */
+    double *beta;        /* per-step Lagrange / drift coefficients */
+    double *g_cols;      /* per-system dual columns */
+    double *s_inv;       /* per-system S^-1 [n_sys, GA * GA] */
+    double *g_colsum;    /* per-system [n_sys, GA] */
+    float *linv32, *g_cols32, *w_hat32;
+} spi_krige_ws_t;
 
-/* Per-system and per-step dual quantities (FP64), for systems with
- * status 0. With F = [1 | drift] (n x a, a = 1 + n_drift; SK: a = 0):
- *   E = Linv F, G = Linv' E = A^-1 F, S = E'E; per step j with values z:
- *   OK/EDK: w_hat = A^-1 z - G beta, beta = S^-1 G'z
- *   SK:     w_hat = A^-1 z, and G = A^-1 1 (one column).
- * Outputs: w_hat (same layout as vals), beta [n_steps, SPI_MAX_DRIFT + 1],
- * g_cols [sum over systems of n * (SPI_MAX_DRIFT + 1)] at
- * stn_off[s] * (SPI_MAX_DRIFT + 1) (row-major n x (SPI_MAX_DRIFT + 1)),
- * s_inv [n_sys, (SPI_MAX_DRIFT + 1)^2] and g_colsum [n_sys, SPI_MAX_DRIFT + 1]
- * (the column sums 1'G). */
+/* Build and factor every system of the batch in FP64.
+ * Cholesky path: A = s*11' - Gamma for OK/EDK (s = total sill, Gamma
+ * filled exactly as fill_vg_var_arr with covar 0, diagonal included), the
+ * covariance fill for SK; A = L L', Linv = L^-1. Under sum(lambda) = 1 the
+ * weights of [[A, F], [F', 0]] equal those of the reference's
+ * [[Gamma, F], [F', 0]] (Lagrange multipliers change sign).
+ * Systems whose Cholesky fails or whose cond exceeds cond_max take the
+ * exact-inverse path (route 1): the reference's own saddle matrix
+ * (interp/steps.py:170-243) is inverted in place by Gauss-Jordan with
+ * partial pivoting, i.e. numpy.linalg.pinv (interp/steps.py:351) without
+ * its 1e-15 singular-value cut-off, which is the same matrix whenever the
+ * cut-off removes nothing. An exactly singular saddle matrix gives route 2. */
+int spi_krige_factor(const spi_domain_t *dom, const spi_systems_t *sys,
+                     const spi_krige_ws_t *ws, double cond_max,
+                     spi_stream_t stream);
+
+/* Per-system and per-step dual quantities (FP64).
+ * Route 0, with F = [1 | drift] (n x a, a = 1 + n_drift; SK: a = 0):
+ *   E = Linv F, G = Linv' E = A^-1 F, S = E'E; per step with values z:
+ *   OK/EDK: w_hat = A^-1 z - G beta, beta = S^-1 G'z;  SK: w_hat = A^-1 z,
+ *   G = A^-1 1. g_colsum = 1'G.
+ * Route 1, with P the inverse saddle matrix: w = P [z; 0] split into
+ * w_hat = w[:n], beta = w[n:]; u = P [1; 0] split into g_cols column 0 =
+ * u[:n], g_colsum = u[n:]. */
 int spi_krige_duals(const spi_domain_t *dom, const spi_systems_t *sys,
-                    const double *linv_arena, const int32_t *status,
-                    const double *vals, double *w_hat, double *beta,
-                    double *g_cols, double *s_inv, double *g_colsum,
+                    const double *vals, const spi_krige_ws_t *ws,
                     spi_stream_t stream);
 
 /* Output description of the cell kernels. */
@@ -186,26 +207,26 @@ typedef struct {
 } spi_out_t;
 
 /* Kriging estimates (and OK variances when want_var) for every cell of
- * every step of a system batch, FP64 throughout (precision = 0) or with
- * FP32 right-hand sides and contractions over the FP64 factorisation
- * (precision = 1; linv32, g_cols32 and w_hat32 are then FP32 copies of
- * the FP64 arrays, made by spi_to_f32). Per cell, with c the right-hand side in covariance form
- * and f = [1, cell drifts]: nu = S^-1 (G'c - f), sum(lambda) = (G'c)_0 -
+ * every step of a system batch. precision 0: FP64 throughout; 1: FP32
+ * right-hand sides and contractions over the FP64 factorisation (uses the
+ * float copies in ws, made by spi_to_f32). route_filter: 0 all systems;
+ * 1 only route-0 systems with cond <= cond_split; 2 every other system. A
+ * mixed-precision job runs precision 1 with filter 1, then precision 0 with
+ * filter 2: ill-conditioned and routed systems are always computed in FP64
+ * (precision 1 accepts only filter 1).
+ * Route 0, per cell with c the right-hand side in covariance form and
+ * f = [1, cell drifts]: nu = S^-1 (G'c - f), sum(lambda) = (G'c)_0 -
  * (1'G) nu, est_j = c'w_hat_j + f'beta_j, OK variance = s sum(lambda) -
- * |Linv c|^2 + nu (G'c)_0 - 2 nu, which is the reference's
- * lambda'gamma + 2 mu (interp/steps.py:429-434). Cells whose weight sum
- * fails numpy.isclose(sum(lambda), 1), and every step of a system with
- * non-zero status, take the nearest station's value with variance 0
- * (interp/steps.py:363-426). */
+ * |Linv c|^2 + nu (G'c)_0 - 2 nu, i.e. the reference's lambda'gamma + 2 mu
+ * (interp/steps.py:429-434). Route 1, with r = [gamma, f]: est_j = r'w_j,
+ * sum(lambda) = r'u, variance lambda'r + lambda_n with lambda = P r (the
+ * reference's primal formula). Cells failing numpy.isclose(sum(lambda), 1),
+ * and every cell of a route-2 system, take the nearest station's value
+ * with variance 0 (interp/steps.py:363-426). */
 int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
-                    const double *linv_arena, const int32_t *status,
-                    const double *shift, const double *vals,
-                    const double *w_hat, const double *beta,
-                    const double *g_cols, const double *s_inv,
-                    const double *g_colsum, const float *linv32,
-                    const float *g_cols32, const float *w_hat32,
-                    int32_t want_var, int32_t precision,
-                    const spi_out_t *out, spi_stream_t stream);
+                    const double *vals, const spi_krige_ws_t *ws,
+                    int32_t want_var, int32_t precision, int32_t route_filter,
+                    double cond_split, const spi_out_t *out, spi_stream_t stream);
 
 /* IDW (interp/steps.py:293-313, cyth/interpmthds.pyx:784-808) for every
  * cell of the listed steps. data [n_steps_total, n_stns] holds every

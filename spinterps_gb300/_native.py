@@ -55,6 +55,13 @@ class SystemsT(ctypes.Structure):
                 ("val_off", c_ptr), ("out_row", c_ptr), ("max_n", c_i32)]
 
 
+class KrigeWsT(ctypes.Structure):
+    _fields_ = [("l_arena", c_ptr), ("linv_arena", c_ptr), ("status", c_ptr), ("route", c_ptr),
+                ("cond", c_ptr), ("shift", c_ptr), ("w_hat", c_ptr), ("beta", c_ptr),
+                ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr), ("linv32", c_ptr),
+                ("g_cols32", c_ptr), ("w_hat32", c_ptr)]
+
+
 class OutT(ctypes.Structure):
     _fields_ = [("out_f64", c_i32), ("est", c_ptr), ("var", c_ptr), ("clip_min_on", c_i32),
                 ("clip_max_on", c_i32), ("clip_min", c_dbl), ("clip_max", c_dbl)]
@@ -70,13 +77,13 @@ _SIGS = {
                                 c_ptr],
     "spi_split_coords": [c_ptr, c_ptr, c_i64, c_dbl, c_dbl, c_ptr, c_ptr],
     "spi_to_f32": [c_ptr, c_ptr, c_i64, c_ptr],
-    "spi_krige_factor": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr, c_ptr,
-                         c_ptr, c_ptr, c_ptr, c_ptr],
-    "spi_krige_duals": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr, c_ptr,
-                        c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
-    "spi_krige_cells": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr, c_ptr, c_ptr,
-                        c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i32,
-                        c_i32, ctypes.POINTER(OutT), c_ptr],
+    "spi_krige_factor": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
+                         ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],
+    "spi_krige_duals": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr,
+                        ctypes.POINTER(KrigeWsT), c_ptr],
+    "spi_krige_cells": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr,
+                        ctypes.POINTER(KrigeWsT), c_i32, c_i32, c_i32, c_dbl,
+                        ctypes.POINTER(OutT), c_ptr],
     "spi_idw_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_dbl,
                       c_i32, ctypes.POINTER(OutT), c_ptr],
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,

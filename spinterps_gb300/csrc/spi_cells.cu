@@ -29,13 +29,11 @@ constexpr int GA = SPI_MAX_DRIFT + 1;
 struct CellsArgs {
   spi_domain_t dom;
   spi_systems_t sys;
-  const int32_t* status;
-  const double* shift;
+  spi_krige_ws_t ws;
   const double* vals;
-  const double* beta;
-  const double* s_inv;
-  const double* g_colsum;
   int want_var;
+  int route_filter;
+  double cond_split;
   spi_out_t out;
 };
 
@@ -77,12 +75,20 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
   const int64_t soff = A.sys.stn_off[s];
   const int n = (int)(A.sys.stn_off[s + 1] - soff);
   const int32_t* idx = A.sys.stn_idx + soff;
+  const int route = A.ws.route[s];
+  {
+    // filter 1: well-conditioned Cholesky systems; filter 2: all others
+    const bool fast = route == 0 && A.ws.cond[s] <= A.cond_split;
+    if ((A.route_filter == 1 && !fast) || (A.route_filter == 2 && fast)) return;
+  }
+  const bool prim = route == 1;   // exact-inverse path: primal formulas
+  const bool failed = route == 2;
   const int sk = A.sys.kind == SPI_KIND_SK;
-  const int a = sk ? 1 : 1 + A.dom.n_drift;
+  const int a = sk ? 1 : 1 + A.dom.n_drift;   // drift / Lagrange rows (SK: the u column)
+  const int ndual = prim ? 1 : a;             // dual columns contracted per cell
   const int tid = threadIdx.x;
   const int64_t st0 = A.sys.step_off[s], st1 = A.sys.step_off[s + 1];
   const int nsteps = (int)(st1 - st0);
-  const bool failed = A.status[s] != 0;
 
   extern __shared__ __align__(16) unsigned char smraw[];
   T* cvT = reinterpret_cast<T*>(smraw);                       // [npad][TC]
@@ -97,7 +103,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
   __shared__ int any_bad;
 
   const spi_vg_t vg = A.sys.vg[s];
-  const double sh = A.shift[s];
+  // right-hand side: covariance form s - gamma on the Cholesky path, the
+  // reference's gamma itself on the exact-inverse path
+  const double sh = A.ws.shift[s];
   if (tid == 0) any_bad = failed ? 1 : 0;
 
   if (!failed) {
@@ -114,7 +122,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
             int st = idx[j];
             double d = dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
             double g = vg_fill_f64(vg, d, sk, A.dom.min_vg_val);
-            v = sk ? g : __dsub_rn(sh, g);
+            v = (sk || prim) ? g : __dsub_rn(sh, g);
           }
           cvT[(int64_t)j * TC + cell] = (T)v;
         }
@@ -150,10 +158,11 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
       }
     }
     // ---- 2. dual columns: qc[cell][k] = G_k' c ----
-    for (int v = tid; v < VB; v += CT) vptr[v] = (v < a) ? gcols + (soff * GA) + (int64_t)v * n : nullptr;
+    for (int v = tid; v < VB; v += CT)
+      vptr[v] = (v < ndual) ? gcols + (soff * GA) + (int64_t)v * n : nullptr;
     {
       T acc[CPT][4];
-      tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, a, n, n, acc);
+      tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, ndual, n, n, acc);
       const int cg = tid % 16, rg = tid / 16;
 #pragma unroll
       for (int c = 0; c < CPT; ++c)
@@ -167,7 +176,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
     double yy_part[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) yy_part[c] = 0.0;
-    if (A.want_var) {
+    if (A.want_var && !prim) {
       const T* L = linv + A.sys.mat_off[s];
       for (int r0 = 0; r0 < n; r0 += VB) {
         __syncthreads();
@@ -195,25 +204,29 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
       const int64_t gc = c0 + cell;
       double yy = 0.0;
       for (int g = 0; g < 16; ++g) yy += red[g * TC + cell];
-      double q[GA], nu[GA];
+      double q[GA], nu[GA], f[GA];
       for (int k = 0; k < GA; ++k) q[k] = qc[cell * GA + k];
+      f[0] = 1.0;
+      for (int k = 1; k < GA; ++k)
+        f[k] = (k < a && gc < C && !sk) ? A.dom.cell_drift[(int64_t)(k - 1) * C + gc] : 0.0;
       double sl;
       double vv = 0.0;
-      if (sk) {
+      if (prim) {
+        // r = [gamma, f]: sum(lambda) = r'u with u = P [1; 0]
+        sl = q[0];
+        if (!sk)
+          for (int k = 0; k < a; ++k) sl += f[k] * A.ws.g_colsum[(int64_t)s * GA + k];
+      } else if (sk) {
         sl = q[0];
       } else {
-        const double* Si = A.s_inv + (int64_t)s * GA * GA;
-        double f[GA];
-        f[0] = 1.0;
-        for (int k = 1; k < a; ++k)
-          f[k] = gc < C ? A.dom.cell_drift[(int64_t)(k - 1) * C + gc] : 0.0;
+        const double* Si = A.ws.s_inv + (int64_t)s * GA * GA;
         for (int k = 0; k < a; ++k) {
           double t = 0.0;
           for (int l = 0; l < a; ++l) t += Si[k * GA + l] * (q[l] - f[l]);
           nu[k] = t;
         }
         sl = q[0];
-        for (int k = 0; k < a; ++k) sl -= A.g_colsum[(int64_t)s * GA + k] * nu[k];
+        for (int k = 0; k < a; ++k) sl -= A.ws.g_colsum[(int64_t)s * GA + k] * nu[k];
         vv = sh * sl - yy + nu[0] * q[0] - 2.0 * nu[0];
       }
       int ok = isclose_one(sl) ? 1 : 0;
@@ -221,6 +234,33 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
       suml[cell] = sl;
       cvar[cell] = ok ? vv : 0.0;
       if (!ok && gc < C) atomicOr(&any_bad, 1);
+    }
+    // ---- 4b. exact-inverse path, OK variance of cells that pass the
+    // check: lambda = P r, var = lambda'r + lambda_n (warp per cell) ----
+    if (prim && A.want_var && !sk) {
+      __syncthreads();
+      const int warp = tid >> 5, lane = tid & 31;
+      const int m = n + a;
+      const double* P = A.ws.l_arena + A.sys.mat_off[s];
+      for (int cell = warp; cell < TC; cell += CT / 32) {
+        const int64_t gc = c0 + cell;
+        if (gc >= C || !okf[cell]) continue;
+        auto rj = [&](int j) -> double {
+          if (j < n) return (double)cvT[(int64_t)j * TC + cell];
+          int k = j - n;
+          return k == 0 ? 1.0 : A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
+        };
+        double acc = 0.0, lam_n = 0.0;
+        for (int i = 0; i < m; ++i) {
+          const double* row = P + (int64_t)i * m;
+          double t = 0.0;
+          for (int j = lane; j < m; j += 32) t += row[j] * rj(j);
+          for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+          acc += t * rj(i);
+          if (i == n) lam_n = t;
+        }
+        if (lane == 0) cvar[cell] = acc + lam_n;
+      }
     }
   } else {
     for (int cell = tid; cell < TC; cell += CT) {
@@ -266,7 +306,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
       const int j = A.sys.steps[st0 + v0 + v];
       const int64_t row = A.sys.out_row[j];
       const int64_t vo = A.sys.val_off[j];
-      const double* bt = A.beta + (int64_t)j * GA;
+      const double* bt = A.ws.beta + (int64_t)j * GA;
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
         const int cell = cg * CPT + c;
@@ -358,38 +398,41 @@ extern "C" int spi_to_f32(const double* x, float* y, int64_t n, spi_stream_t str
 }
 
 extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys,
-                               const double* linv_arena, const int32_t* status,
-                               const double* shift, const double* vals, const double* w_hat,
-                               const double* beta, const double* g_cols, const double* s_inv,
-                               const double* g_colsum, const float* linv32,
-                               const float* g_cols32, const float* w_hat32, int32_t want_var,
-                               int32_t precision, const spi_out_t* out, spi_stream_t stream) {
-  if (!dom || !sys || !out) return SPI_ERR_ARG;
+                               const double* vals, const spi_krige_ws_t* ws, int32_t want_var,
+                               int32_t precision, int32_t route_filter, double cond_split,
+                               const spi_out_t* out, spi_stream_t stream) {
+  if (!dom || !sys || !out || !ws) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (dom->n_drift < 0 || dom->n_drift > SPI_MAX_DRIFT) return SPI_ERR_TOO_LARGE;
-  if (sys->n_sys == 0 || dom->n_cells == 0) return SPI_OK;
-  if (!status || !shift || !vals || !beta || !s_inv || !g_colsum || !out->est) return SPI_ERR_ARG;
-  if (precision == 0 && (!linv_arena || !w_hat || !g_cols)) return SPI_ERR_ARG;
-  if (precision == 1 && (!linv32 || !w_hat32 || !g_cols32)) return SPI_ERR_ARG;
+  if (route_filter < 0 || route_filter > 2) return SPI_ERR_ARG;
   if (precision != 0 && precision != 1) return SPI_ERR_ARG;
+  if (sys->n_sys == 0 || dom->n_cells == 0) return SPI_OK;
+  if (!vals || !out->est || !ws->route || !ws->shift || !ws->beta || !ws->s_inv ||
+      !ws->g_colsum || !ws->l_arena || !ws->cond)
+    return SPI_ERR_ARG;
+  if (precision == 0 && (!ws->linv_arena || !ws->w_hat || !ws->g_cols)) return SPI_ERR_ARG;
+  if (precision == 1 && (!ws->linv32 || !ws->w_hat32 || !ws->g_cols32 || !dom->cell_split ||
+                         !dom->stn_split))
+    return SPI_ERR_ARG;
+  // routed systems are computed in FP64 only
+  if (precision == 1 && route_filter != 1) return SPI_ERR_ARG;
   CellsArgs A;
   A.dom = *dom;
   A.sys = *sys;
-  A.status = status;
-  A.shift = shift;
+  A.ws = *ws;
   A.vals = vals;
-  A.beta = beta;
-  A.s_inv = s_inv;
-  A.g_colsum = g_colsum;
   A.want_var = want_var ? 1 : 0;
+  A.route_filter = route_filter;
+  A.cond_split = cond_split;
   A.out = *out;
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == 0) {
-    return out->out_f64 ? dispatch_cells<double, double>(A, linv_arena, g_cols, w_hat, st)
-                        : dispatch_cells<double, float>(A, linv_arena, g_cols, w_hat, st);
+    return out->out_f64
+               ? dispatch_cells<double, double>(A, ws->linv_arena, ws->g_cols, ws->w_hat, st)
+               : dispatch_cells<double, float>(A, ws->linv_arena, ws->g_cols, ws->w_hat, st);
   }
-  return out->out_f64 ? dispatch_cells<float, double>(A, linv32, g_cols32, w_hat32, st)
-                      : dispatch_cells<float, float>(A, linv32, g_cols32, w_hat32, st);
+  return out->out_f64 ? dispatch_cells<float, double>(A, ws->linv32, ws->g_cols32, ws->w_hat32, st)
+                      : dispatch_cells<float, float>(A, ws->linv32, ws->g_cols32, ws->w_hat32, st);
 }
 
 namespace spi {

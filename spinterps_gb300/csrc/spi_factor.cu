@@ -270,6 +270,130 @@ __global__ __launch_bounds__(FT) void k_trinv(spi_systems_t sys, const double* _
   }
 }
 
+// Exact-inverse path. Systems whose Cholesky failed, or whose condition
+// estimate exceeds cond_max, get the reference's own saddle matrix
+// [[Gamma, F], [F', 0]] (interp/steps.py:170-243; SK: the covariance
+// matrix) inverted in place by Gauss-Jordan with partial pivoting (first
+// row of maximum |pivot|), columns unscrambled in reverse pivot order.
+// That is numpy.linalg.pinv (interp/steps.py:351) whenever pinv's 1e-15
+// singular-value cut-off removes nothing. Dynamic shared memory: m pivot
+// factors + m pivot indices.
+__global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
+                                          double* __restrict__ l_arena,
+                                          const int32_t* __restrict__ status,
+                                          const double* __restrict__ cond,
+                                          int32_t* __restrict__ route, double cond_max) {
+  const int s = blockIdx.x;
+  const int tid = threadIdx.x;
+  if (status[s] == 0 && cond[s] <= cond_max) {
+    if (tid == 0) route[s] = 0;
+    return;
+  }
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  const int sk = sys.kind == SPI_KIND_SK;
+  const int a = sk ? 0 : 1 + dom.n_drift;
+  const int m = n + a;
+  const spi_vg_t vg = sys.vg[s];
+  double* A = l_arena + v.moff;
+  extern __shared__ double gsm[];
+  double* f = gsm;                                   // [m]
+  int* piv = reinterpret_cast<int*>(gsm + m);        // [m]
+  __shared__ double rv[FT];
+  __shared__ int ri[FT];
+  __shared__ int fail;
+  __shared__ double dk;
+  // saddle matrix, full storage
+  for (int64_t e = tid; e < (int64_t)m * m; e += FT) {
+    int i = (int)(e / m), j = (int)(e - (int64_t)i * m);
+    double val;
+    if (i < n && j < n) {
+      int lo = min(i, j), hi = max(i, j);
+      int sl = v.idx[lo], sh = v.idx[hi];
+      double d = dist_f64(dom.stn_x[sl], dom.stn_y[sl], dom.stn_x[sh], dom.stn_y[sh]);
+      val = vg_fill_f64(vg, d, sk, dom.min_vg_val);
+    } else if (i >= n && j >= n) {
+      val = 0.0;
+    } else {
+      int st = (i < n) ? v.idx[i] : v.idx[j];
+      int k = (i < n) ? (j - n) : (i - n);
+      val = (k == 0) ? 1.0 : dom.stn_drift[(int64_t)st * dom.n_drift + (k - 1)];
+    }
+    A[e] = val;
+  }
+  if (tid == 0) fail = 0;
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    // pivot: first row of maximum |A[i][k]|, i >= k
+    double best = -1.0;
+    int bi = 0x7fffffff;
+    for (int i = k + tid; i < m; i += FT) {
+      double x = fabs(A[(int64_t)i * m + k]);
+      if (x > best || (x == best && i < bi) || isnan(x)) {
+        best = isnan(x) ? __longlong_as_double(0x7ff0000000000000LL) : x;
+        bi = i;
+      }
+    }
+    rv[tid] = best;
+    ri[tid] = bi;
+    __syncthreads();
+    for (int o = FT / 2; o > 0; o >>= 1) {
+      if (tid < o) {
+        double ob = rv[tid + o];
+        int oi = ri[tid + o];
+        if (ob > rv[tid] || (ob == rv[tid] && oi < ri[tid])) {
+          rv[tid] = ob;
+          ri[tid] = oi;
+        }
+      }
+      __syncthreads();
+    }
+    const int p = ri[0];
+    if (tid == 0) {
+      piv[k] = p;
+      if (!(rv[0] > 0.0) || isinf(rv[0])) fail = k + 1;
+    }
+    __syncthreads();
+    if (fail) break;
+    if (p != k)
+      for (int j = tid; j < m; j += FT) {
+        double t = A[(int64_t)k * m + j];
+        A[(int64_t)k * m + j] = A[(int64_t)p * m + j];
+        A[(int64_t)p * m + j] = t;
+      }
+    __syncthreads();
+    if (tid == 0) dk = A[(int64_t)k * m + k];
+    __syncthreads();
+    const double dd = dk;
+    for (int j = tid; j < m; j += FT) {
+      double x = (j == k) ? 1.0 : A[(int64_t)k * m + j];
+      A[(int64_t)k * m + j] = x / dd;
+    }
+    for (int i = tid; i < m; i += FT) f[i] = (i == k) ? 0.0 : A[(int64_t)i * m + k];
+    __syncthreads();
+    for (int64_t e = tid; e < (int64_t)m * m; e += FT) {
+      int i = (int)(e / m), j = (int)(e - (int64_t)i * m);
+      if (i == k) continue;
+      double base = (j == k) ? 0.0 : A[e];
+      A[e] = base - f[i] * A[(int64_t)k * m + j];
+    }
+    __syncthreads();
+  }
+  if (!fail) {
+    for (int k = m - 1; k >= 0; --k) {
+      const int p = piv[k];
+      if (p != k)
+        for (int i = tid; i < m; i += FT) {
+          double t = A[(int64_t)i * m + k];
+          A[(int64_t)i * m + k] = A[(int64_t)i * m + p];
+          A[(int64_t)i * m + p] = t;
+        }
+      __syncthreads();
+    }
+  }
+  if (tid == 0) route[s] = fail ? 2 : 1;
+}
+
 // y = X x (X lower, row-major n x n): warp per row, lanes along the row.
 __device__ void matvec_lower(const double* __restrict__ X, int n, const double* __restrict__ x,
                              double* __restrict__ y) {
@@ -308,33 +432,67 @@ __device__ double block_dot(const double* __restrict__ a, const double* __restri
   return r;
 }
 
-// Per-system G, S^-1, 1'G and per-step dual weights. Dynamic shared
-// memory: 3 vectors of n doubles.
+// y = P[:, :n] x for the m x m row-major P (warp per row).
+__device__ void matvec_rows(const double* __restrict__ P, int m, int n,
+                            const double* __restrict__ x, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = warp; i < m; i += nw) {
+    const double* row = P + (int64_t)i * m;
+    double t = 0.0;
+    for (int j = lane; j < n; j += 32) t += row[j] * x[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) y[i] = t;
+  }
+}
+
+// Per-system G, S^-1, 1'G and per-step dual weights (route 0), or the
+// split dual vectors of the inverse saddle matrix (route 1). Dynamic shared
+// memory: 3 vectors of n + GA doubles.
 __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sys,
-                                             const double* __restrict__ x_arena,
-                                             const int32_t* __restrict__ status,
-                                             const double* __restrict__ vals,
-                                             double* __restrict__ w_hat,
-                                             double* __restrict__ beta,
-                                             double* __restrict__ g_cols,
-                                             double* __restrict__ s_inv,
-                                             double* __restrict__ g_colsum) {
+                                             spi_krige_ws_t ws,
+                                             const double* __restrict__ vals) {
   const int s = blockIdx.x;
-  if (status[s] != 0) return;
+  const int route = ws.route[s];
+  if (route == 2) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
-  const double* X = x_arena + v.moff;
+  const double* X = ws.linv_arena + v.moff;
   extern __shared__ double sm[];
   double* va = sm;
-  double* vb = sm + n;
-  double* vz = sm + 2 * n;
+  double* vb = sm + (n + GA);
+  double* vz = sm + 2 * (n + GA);
   __shared__ double red[FT / 32];
   __shared__ double S[GA][GA];
   __shared__ double Si[GA][GA];
   __shared__ double hb[GA];
   const int sk = sys.kind == SPI_KIND_SK;
   const int a = sk ? 1 : 1 + dom.n_drift;
-  double* G = g_cols + v.off * GA;  // column k at G + k * n
+  double* G = ws.g_cols + v.off * GA;  // column k at G + k * n
+  if (route == 1) {
+    const int ar = sk ? 0 : a;
+    const int m = n + ar;
+    const double* P = ws.l_arena + v.moff;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) va[i] = 1.0;
+    __syncthreads();
+    matvec_rows(P, m, n, va, vb);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) G[i] = vb[i];
+    if (threadIdx.x < GA)
+      ws.g_colsum[(int64_t)s * GA + threadIdx.x] = (threadIdx.x < ar) ? vb[n + threadIdx.x] : 0.0;
+    for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1]; ++si) {
+      const int j = sys.steps[si];
+      const int64_t vo = sys.val_off[j];
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) vz[i] = vals[vo + i];
+      __syncthreads();
+      matvec_rows(P, m, n, vz, vb);
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) ws.w_hat[vo + i] = vb[i];
+      if (threadIdx.x < GA)
+        ws.beta[(int64_t)j * GA + threadIdx.x] = (threadIdx.x < ar) ? vb[n + threadIdx.x] : 0.0;
+    }
+    return;
+  }
   // G_k = Linv' (Linv F_k)
   for (int k = 0; k < a; ++k) {
     for (int i = threadIdx.x; i < n; i += blockDim.x)
@@ -345,7 +503,7 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
     matvec_lower_t(X, n, vb, G + (int64_t)k * n);
     __syncthreads();
   }
-  // S = F'G, 1'G
+  // S = F'G
   for (int k = 0; k < a; ++k) {
     for (int i = threadIdx.x; i < n; i += blockDim.x)
       va[i] = (k == 0) ? 1.0 : dom.stn_drift[(int64_t)v.idx[i] * dom.n_drift + (k - 1)];
@@ -383,21 +541,24 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
       for (int j = 0; j < GA; ++j) {
         double val = (i < a && j < a) ? M[i][a + j] : 0.0;
         Si[i][j] = val;
-        s_inv[(int64_t)s * GA * GA + i * GA + j] = val;
+        ws.s_inv[(int64_t)s * GA * GA + i * GA + j] = val;
       }
   }
   __syncthreads();
   for (int k = 0; k < GA; ++k) {
     double cs = 0.0;
     if (k < a) {
-      for (int i = 0; i < n; ++i) cs += G[(int64_t)k * n + i];
+      for (int i = threadIdx.x; i < n; i += blockDim.x) va[i] = 1.0;
+      __syncthreads();
+      cs = block_dot(va, G + (int64_t)k * n, n, red);
     }
-    if (threadIdx.x == 0) g_colsum[(int64_t)s * GA + k] = cs;
+    if (threadIdx.x == 0) ws.g_colsum[(int64_t)s * GA + k] = cs;
   }
   // per step
   for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1]; ++si) {
     const int j = sys.steps[si];
     const int64_t vo = sys.val_off[j];
+    __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) vz[i] = vals[vo + i];
     __syncthreads();
     if (!sk) {
@@ -421,14 +582,13 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double w = vb[i];
         for (int k = 0; k < a; ++k) w -= G[(int64_t)k * n + i] * bt[k];
-        w_hat[vo + i] = w;
+        ws.w_hat[vo + i] = w;
       }
-      if (threadIdx.x < GA) beta[(int64_t)j * GA + threadIdx.x] = bt[threadIdx.x];
+      if (threadIdx.x < GA) ws.beta[(int64_t)j * GA + threadIdx.x] = bt[threadIdx.x];
     } else {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) w_hat[vo + i] = vb[i];
-      if (threadIdx.x < GA) beta[(int64_t)j * GA + threadIdx.x] = 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) ws.w_hat[vo + i] = vb[i];
+      if (threadIdx.x < GA) ws.beta[(int64_t)j * GA + threadIdx.x] = 0.0;
     }
-    __syncthreads();
   }
 }
 
@@ -447,13 +607,20 @@ static int check_sys(const spi_domain_t* dom, const spi_systems_t* sys) {
   return SPI_OK;
 }
 
+static int check_ws(const spi_krige_ws_t* ws) {
+  if (!ws || !ws->l_arena || !ws->linv_arena || !ws->status || !ws->route || !ws->cond ||
+      !ws->shift || !ws->w_hat || !ws->beta || !ws->g_cols || !ws->s_inv || !ws->g_colsum)
+    return SPI_ERR_ARG;
+  return SPI_OK;
+}
+
 extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sys,
-                                double* l_arena, double* linv_arena, int32_t* status,
-                                double* cond, double* shift, spi_stream_t stream) {
+                                const spi_krige_ws_t* ws, double cond_max,
+                                spi_stream_t stream) {
   int rc = check_sys(dom, sys);
   if (rc) return rc;
   if (sys->n_sys == 0) return SPI_OK;
-  if (!l_arena || !linv_arena || !status || !cond || !shift) return SPI_ERR_ARG;
+  if ((rc = check_ws(ws))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   spi_domain_t d = *dom;
   spi_systems_t sy = *sys;
@@ -461,34 +628,40 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   int gx = (int)((nn + 255) / 256);
   if (gx > 64) gx = 64;
   if (gx < 1) gx = 1;
-  k_build_sys<<<dim3(gx, sys->n_sys), 256, 0, st>>>(d, sy, l_arena, shift);
+  k_build_sys<<<dim3(gx, sys->n_sys), 256, 0, st>>>(d, sy, ws->l_arena, ws->shift);
   SPI_LAUNCH_CHECK();
-  k_chol<<<sys->n_sys, FT, 0, st>>>(sy, l_arena, status);
+  k_chol<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status);
   SPI_LAUNCH_CHECK();
-  k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, l_arena, linv_arena, status, cond);
+  k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->linv_arena, ws->status, ws->cond);
+  SPI_LAUNCH_CHECK();
+  size_t gsm = (size_t)(sys->max_n + GA) * (sizeof(double) + sizeof(int));
+  if (gsm > 200 * 1024) return SPI_ERR_TOO_LARGE;
+  if (gsm > 48 * 1024 &&
+      cudaFuncSetAttribute(k_gj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm) !=
+          cudaSuccess)
+    return SPI_ERR_CUDA;
+  k_gj<<<sys->n_sys, FT, gsm, st>>>(d, sy, ws->l_arena, ws->status, ws->cond, ws->route,
+                                    cond_max);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }
 
 extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys,
-                               const double* linv_arena, const int32_t* status,
-                               const double* vals, double* w_hat, double* beta,
-                               double* g_cols, double* s_inv, double* g_colsum,
+                               const double* vals, const spi_krige_ws_t* ws,
                                spi_stream_t stream) {
   int rc = check_sys(dom, sys);
   if (rc) return rc;
   if (sys->n_sys == 0) return SPI_OK;
-  if (!linv_arena || !status || !vals || !w_hat || !beta || !g_cols || !s_inv || !g_colsum)
-    return SPI_ERR_ARG;
-  size_t smem = (size_t)3 * sys->max_n * sizeof(double);
+  if ((rc = check_ws(ws))) return rc;
+  if (!vals) return SPI_ERR_ARG;
+  size_t smem = (size_t)3 * (sys->max_n + GA) * sizeof(double);
   if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(k_duals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return SPI_ERR_CUDA;
   }
-  k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, linv_arena, status, vals,
-                                                          w_hat, beta, g_cols, s_inv, g_colsum);
+  k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

@@ -214,7 +214,7 @@ class _KrigeBatch:
         ns = np.array([len(systems[i][0]) for i in ch], dtype=np.int64)
         stn_off = np.concatenate([[0], np.cumsum(ns)]).astype(np.int64)
         stn_idx = np.concatenate([systems[i][0] for i in ch]).astype(np.int32)
-        sizes = np.array([_align(n * n) for n in ns], dtype=np.int64)
+        sizes = np.array([_align((n + nat.GA) * (n + nat.GA)) for n in ns], dtype=np.int64)
         mat_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
         self.arena = int(sizes.sum())
         steps_l = [systems[i][2] for i in ch]
@@ -241,6 +241,7 @@ class _KrigeBatch:
         self.L = torch.empty(self.arena, dtype=torch.float64, device=dev)
         self.X = torch.empty(self.arena, dtype=torch.float64, device=dev)
         self.status = torch.empty(n_sys, dtype=torch.int32, device=dev)
+        self.route = torch.empty(n_sys, dtype=torch.int32, device=dev)
         self.cond = torch.empty(n_sys, dtype=torch.float64, device=dev)
         self.shift = torch.empty(n_sys, dtype=torch.float64, device=dev)
         self.g_cols = torch.zeros(int(stn_off[-1]) * nat.GA, dtype=torch.float64, device=dev)
@@ -253,6 +254,11 @@ class _KrigeBatch:
             self.X32 = torch.empty(self.arena, dtype=torch.float32, device=dev)
             self.g32 = torch.empty(self.g_cols.numel(), dtype=torch.float32, device=dev)
             self.w32 = torch.empty(self.w_hat.numel(), dtype=torch.float32, device=dev)
+        self.ws = nat.KrigeWsT(_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
+                               _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat),
+                               _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv),
+                               _ptr(self.g_colsum), _ptr(self.X32), _ptr(self.g32),
+                               _ptr(self.w32))
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
         self.n = ns
@@ -264,24 +270,24 @@ class _KrigeBatch:
             per = per + self.n * (self.n + 1)
         return float(per.sum()) * C
 
-    def run(self, dom, out, want_var, ev=None):
+    def run(self, dom, out, want_var, cond_max, cond_split, ev=None):
         s = _stream()
-        nat.call("spi_krige_factor", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.L),
-                 _ptr(self.X), _ptr(self.status), _ptr(self.cond), _ptr(self.shift), s)
-        nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.X),
-                 _ptr(self.status), _ptr(self.vals), _ptr(self.w_hat), _ptr(self.beta),
-                 _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum), s)
+        ws = ctypes.byref(self.ws)
+        nat.call("spi_krige_factor", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
+                 float(cond_max), s)
+        nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
+                 ws, s)
         if self.precision == 1:
             nat.call("spi_to_f32", _ptr(self.X), _ptr(self.X32), self.arena, s)
             nat.call("spi_to_f32", _ptr(self.g_cols), _ptr(self.g32), self.g_cols.numel(), s)
             nat.call("spi_to_f32", _ptr(self.w_hat), _ptr(self.w32), self.w_hat.numel(), s)
         if ev is not None:
             ev[0].record()
-        nat.call("spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.X),
-                 _ptr(self.status), _ptr(self.shift), _ptr(self.vals), _ptr(self.w_hat),
-                 _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum),
-                 _ptr(self.X32), _ptr(self.g32), _ptr(self.w32), 1 if want_var else 0,
-                 self.precision, ctypes.byref(out), s)
+        passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
+        for prec, filt in passes:
+            nat.call("spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy),
+                     _ptr(self.vals), ws, 1 if want_var else 0, prec, filt, float(cond_split),
+                     ctypes.byref(out), s)
         if ev is not None:
             ev[1].record()
 
@@ -291,7 +297,7 @@ def _chunk_systems(systems, precision, arena_budget):
     chunks, cur, cur_bytes = [], [], 0
     for i in order:
         n = len(systems[i][0])
-        b = _align(n * n) * 8 * (3 if precision == 1 else 2)
+        b = _align((n + nat.GA) ** 2) * 8 * (3 if precision == 1 else 2)
         if cur and (cur_bytes + b > arena_budget or len(cur) >= 65535):
             chunks.append(cur)
             cur, cur_bytes = [], 0
@@ -312,8 +318,10 @@ class InterpPlan:
     def __init__(self, stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *,
                  est_vars=False, stn_drifts=None, cell_drifts=None, min_var_thr=0.0,
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
-                 time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30):
+                 time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
+                 cond_max=1e12, cond_split=1e8):
         dev = self.dev = _require_cuda(device)
+        self.cond_max, self.cond_split = cond_max, cond_split
         prec = self.prec = PRECISION[precision]
         data = np.ascontiguousarray(data, dtype=np.float64)
         T, N = data.shape
@@ -406,7 +414,7 @@ class InterpPlan:
                 if timing:
                     ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                     evs["krige_cells"].append((ev, b.cell_flops(C, want_var, a)))
-                b.run(self.dom, out, want_var, ev)
+                b.run(self.dom, out, want_var, self.cond_max, self.cond_split, ev)
         for t, out, fill, p in self.idw:
             _fill_run(fill, C, out, s)
             if not len(self.multi):
@@ -431,16 +439,19 @@ class InterpPlan:
 
     def collect_info(self):
         for kind, out, want_var, batches, fills, a in self.krig:
-            failed, cond = [], {}
+            failed, routed, cond = [], [], {}
             for b in batches:
-                st = b.status.cpu().numpy()
+                rt = b.route.cpu().numpy()
                 cn = b.cond.cpu().numpy()
                 for k, sl in enumerate(b.steps_l):
                     for j in sl:
                         cond[int(j)] = float(cn[k])
-                        if st[k] != 0:
+                        if rt[k] == 2:
                             failed.append(int(j))
+                        elif rt[k] == 1:
+                            routed.append(int(j))
             self.info["failed_steps"][kind] = sorted(failed)
+            self.info.setdefault("exact_inverse_steps", {})[kind] = sorted(routed)
             self.info["cond"][kind] = cond
         return self.info
 
@@ -472,7 +483,7 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  stn_drifts=None, cell_drifts=None, min_var_thr=0.0, min_var_cut=None,
                  max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
-                 arena_budget=8 << 30):
+                 arena_budget=8 << 30, cond_max=1e12, cond_split=1e8):
     """Interpolate every step onto every cell on the GPU.
 
     Same inputs and outputs as the reference step engine for one grid chunk
@@ -485,7 +496,8 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                       stn_drifts=stn_drifts, cell_drifts=cell_drifts, min_var_thr=min_var_thr,
                       min_var_cut=min_var_cut, max_var_cut=max_var_cut, min_vg_val=min_vg_val,
                       intrp_dtype=intrp_dtype, time_steps=time_steps, precision=precision,
-                      device=device, arena_budget=arena_budget)
+                      device=device, arena_budget=arena_budget, cond_max=cond_max,
+                      cond_split=cond_split)
     plan.execute()
     flds = plan.fields(numpy=return_numpy)
     if return_info:

@@ -119,8 +119,15 @@ def test_null_and_size_errors_without_gpu():
     dom.n_drift = 99
     sy = nat.SystemsT()
     sy.n_sys = 1
-    assert lib.spi_krige_factor(ctypes.byref(dom), ctypes.byref(sy), None, None, None, None,
-                                None, None) == 5
+    ws = nat.KrigeWsT()
+    assert lib.spi_krige_factor(ctypes.byref(dom), ctypes.byref(sy), ctypes.byref(ws), 1e12,
+                                None) == 5
+    dom.n_drift = 0
+    assert lib.spi_krige_factor(ctypes.byref(dom), ctypes.byref(sy), ctypes.byref(ws), 1e12,
+                                None) == 1  # null workspace arrays
+    dom.n_cells = 10
+    assert lib.spi_krige_cells(ctypes.byref(dom), ctypes.byref(sy), None, ctypes.byref(ws), 1,
+                               1, 2, 1e8, ctypes.byref(out), None) == 1
 
 
 def test_host_mirror_has_no_cpu_fallback():
