@@ -84,7 +84,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
   const bool prim = route == 1;   // exact-inverse path: primal formulas
   const bool failed = route == 2;
   const int sk = A.sys.kind == SPI_KIND_SK;
-  const int a = sk ? 1 : 1 + A.dom.n_drift;   // drift / Lagrange rows (SK: the u column)
+  // Lagrange / drift rows; on the Cholesky path SK contracts one dual
+  // column (u = A^-1 1) in the same slot
+  const int a = sk ? 1 : extra_rows(A.sys.kind, A.dom.n_drift);
   const int ndual = prim ? 1 : a;             // dual columns contracted per cell
   const int tid = threadIdx.x;
   const int64_t st0 = A.sys.step_off[s], st1 = A.sys.step_off[s + 1];
@@ -101,12 +103,16 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
   int* okf = nnb + TC;                                         // [TC]
   const T** vptr = reinterpret_cast<const T**>(okf + TC);      // [VB]
   __shared__ int any_bad;
+  __shared__ int any_ok;
 
   const spi_vg_t vg = A.sys.vg[s];
   // right-hand side: covariance form s - gamma on the Cholesky path, the
   // reference's gamma itself on the exact-inverse path
   const double sh = A.ws.shift[s];
-  if (tid == 0) any_bad = failed ? 1 : 0;
+  if (tid == 0) {
+    any_bad = failed ? 1 : 0;
+    any_ok = 0;
+  }
 
   if (!failed) {
     // ---- 1. right-hand sides, cell-contiguous: cvT[j][cell] ----
@@ -123,6 +129,10 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
             double d = dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
             double g = vg_fill_f64(vg, d, sk, A.dom.min_vg_val);
             v = (sk || prim) ? g : __dsub_rn(sh, g);
+          }
+          if (prim && live && j >= n && j < n + a) {
+            const int k = j - n;  // r = [gamma, 1, drifts] rows of the saddle system
+            v = (k == 0) ? 1.0 : A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
           }
           cvT[(int64_t)j * TC + cell] = (T)v;
         }
@@ -234,32 +244,44 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
       suml[cell] = sl;
       cvar[cell] = ok ? vv : 0.0;
       if (!ok && gc < C) atomicOr(&any_bad, 1);
+      if (ok && gc < C) atomicOr(&any_ok, 1);
     }
-    // ---- 4b. exact-inverse path, OK variance of cells that pass the
-    // check: lambda = P r, var = lambda'r + lambda_n (warp per cell) ----
-    if (prim && A.want_var && !sk) {
-      __syncthreads();
-      const int warp = tid >> 5, lane = tid & 31;
+    // ---- 4b. exact-inverse path, OK variance of the cells that pass the
+    // check: lambda = P r, var = lambda'r + lambda_n, through the same tiled
+    // contraction over P's rows; skipped when no cell of the tile passes ----
+    __syncthreads();
+    if (prim && A.want_var && !sk && any_ok) {
       const int m = n + a;
-      const double* P = A.ws.l_arena + A.sys.mat_off[s];
-      for (int cell = warp; cell < TC; cell += CT / 32) {
-        const int64_t gc = c0 + cell;
-        if (gc >= C || !okf[cell]) continue;
-        auto rj = [&](int j) -> double {
-          if (j < n) return (double)cvT[(int64_t)j * TC + cell];
-          int k = j - n;
-          return k == 0 ? 1.0 : A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
-        };
-        double acc = 0.0, lam_n = 0.0;
-        for (int i = 0; i < m; ++i) {
-          const double* row = P + (int64_t)i * m;
-          double t = 0.0;
-          for (int j = lane; j < m; j += 32) t += row[j] * rj(j);
-          for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-          acc += t * rj(i);
-          if (i == n) lam_n = t;
+      const T* P = reinterpret_cast<const T*>(A.ws.l_arena) + A.sys.mat_off[s];
+      double vpart[CPT];
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) vpart[c] = 0.0;
+      const int cg = tid % 16, rg = tid / 16;
+      for (int r0 = 0; r0 < m; r0 += VB) {
+        __syncthreads();
+        for (int v = tid; v < VB; v += CT) vptr[v] = (r0 + v < m) ? P + (int64_t)(r0 + v) * m : nullptr;
+        T acc[CPT][4];
+        tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, min(VB, m - r0), m, m, acc);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int row = r0 + rg * 4 + r;
+          if (row >= m) continue;
+#pragma unroll
+          for (int c = 0; c < CPT; ++c) {
+            const int cell = cg * CPT + c;
+            vpart[c] += (double)acc[c][r] * (double)cvT[(int64_t)row * TC + cell];
+            if (row == n) vpart[c] += (double)acc[c][r];
+          }
         }
-        if (lane == 0) cvar[cell] = acc + lam_n;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) red[rg * TC + cg * CPT + c] = vpart[c];
+      __syncthreads();
+      for (int cell = tid; cell < TC; cell += CT) {
+        double vv = 0.0;
+        for (int g = 0; g < 16; ++g) vv += red[g * TC + cell];
+        if (okf[cell]) cvar[cell] = vv;
       }
     }
   } else {
@@ -340,8 +362,7 @@ static size_t cells_smem(int npad) {
 template <typename T, int TC, typename OutT>
 static int launch_cells(const CellsArgs& A, const T* linv, const T* gcols, const T* what,
                         cudaStream_t st) {
-  int npad = (A.sys.max_n + KC - 1) / KC * KC;
-  if (npad < KC) npad = KC;
+  int npad = (A.sys.max_n + GA + KC - 1) / KC * KC;
   size_t smem = cells_smem<T, TC>(npad);
   auto kern = k_krige_cells<T, TC, OutT>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -358,7 +379,7 @@ static int launch_cells(const CellsArgs& A, const T* linv, const T* gcols, const
 // Largest cell tile whose shared memory fits.
 template <typename T>
 static int pick_tc(int max_n) {
-  int npad = (max_n + KC - 1) / KC * KC;
+  int npad = (max_n + GA + KC - 1) / KC * KC;
   const size_t cap = 225 * 1024;
   if (sizeof(T) == 4 && cells_smem<T, 64>(npad) <= cap) return 64;
   if (cells_smem<T, 32>(npad) <= cap) return 32;

@@ -108,6 +108,13 @@ __device__ __forceinline__ double total_sill(const spi_vg_t &vg) {
   return s;
 }
 
+// Lagrange / drift rows appended to a system of the given kind: OK 1 (the
+// unbiasedness row), EDK 1 + k (plus one row per drift), SK none
+// (interp/steps.py:180-219).
+__host__ __device__ __forceinline__ int extra_rows(int kind, int n_drift) {
+  return kind == SPI_KIND_OK ? 1 : (kind == SPI_KIND_EDK ? 1 + n_drift : 0);
+}
+
 // numpy.isclose(a, 1.0) with its defaults (rtol 1e-5, atol 1e-8).
 __device__ __forceinline__ bool isclose_one(double a) {
   return fabs(a - 1.0) <= (1e-8 + 1e-5 * 1.0);

@@ -292,7 +292,7 @@ __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
   SysView v = sys_view(sys, s);
   const int n = v.n;
   const int sk = sys.kind == SPI_KIND_SK;
-  const int a = sk ? 0 : 1 + dom.n_drift;
+  const int a = extra_rows(sys.kind, dom.n_drift);
   const int m = n + a;
   const spi_vg_t vg = sys.vg[s];
   double* A = l_arena + v.moff;
@@ -466,7 +466,7 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
   __shared__ double Si[GA][GA];
   __shared__ double hb[GA];
   const int sk = sys.kind == SPI_KIND_SK;
-  const int a = sk ? 1 : 1 + dom.n_drift;
+  const int a = sk ? 1 : extra_rows(sys.kind, dom.n_drift);
   double* G = ws.g_cols + v.off * GA;  // column k at G + k * n
   if (route == 1) {
     const int ar = sk ? 0 : a;

@@ -319,7 +319,7 @@ class InterpPlan:
                  est_vars=False, stn_drifts=None, cell_drifts=None, min_var_thr=0.0,
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
-                 cond_max=1e12, cond_split=1e8):
+                 cond_max=1e13, cond_split=1e7):
         dev = self.dev = _require_cuda(device)
         self.cond_max, self.cond_split = cond_max, cond_split
         prec = self.prec = PRECISION[precision]
@@ -381,7 +381,7 @@ class InterpPlan:
                     _fill_args(dev, self.single, self.single_val,
                                None if var is None else np.full(self.single.size, np.nan)),
                     _fill_args(dev, mean_steps, means[mean_steps], np.zeros(len(mean_steps))))
-                a = 1 if kind == "SK" else 1 + self.dom.st.n_drift
+                a = 1 + self.dom.st.n_drift if kind == "EDK" else 1
                 self.krig.append((kind, out, var is not None, batches, fills, a))
         self.idw = []
         if any(t in ("IDW", "NNB") for t in types):
@@ -483,7 +483,7 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  stn_drifts=None, cell_drifts=None, min_var_thr=0.0, min_var_cut=None,
                  max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
-                 arena_budget=8 << 30, cond_max=1e12, cond_split=1e8):
+                 arena_budget=8 << 30, cond_max=1e13, cond_split=1e7):
     """Interpolate every step onto every cell on the GPU.
 
     Same inputs and outputs as the reference step engine for one grid chunk
