@@ -150,8 +150,7 @@ typedef struct {
  * owned). Arenas hold one matrix per system at sys->mat_off[s], sized for
  * (n + SPI_MAX_DRIFT + 1)^2 doubles; per-system arrays have n_sys entries;
  * w_hat has the layout of the values array; beta is [n_steps_total, GA] and
- * g_cols [total stations * GA], GA = SPI_MAX_DRIFT + 1. The float arrays are
- * needed only by the precision-1 cell kernel. */
+ * g_cols [total stations * GA], GA = SPI_MAX_DRIFT + 1. */
 typedef struct {
     double *l_arena;     /* Cholesky factor L; for routed systems the
                             inverse of the reference's saddle matrix */
@@ -166,7 +165,6 @@ typedef struct {
     double *g_cols;      /* per-system dual columns */
     double *s_inv;       /* per-system S^-1 [n_sys, GA * GA] */
     double *g_colsum;    /* per-system [n_sys, GA] */
-    float *linv32, *g_cols32, *w_hat32;
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -208,8 +206,8 @@ typedef struct {
 
 /* Kriging estimates (and OK variances when want_var) for every cell of
  * every step of a system batch. precision 0: FP64 throughout; 1: FP32
- * right-hand sides and contractions over the FP64 factorisation (uses the
- * float copies in ws, made by spi_to_f32). route_filter: 0 all systems;
+ * right-hand sides, split-FP32 contractions against the FP64 factor and
+ * duals (hi/lo pairs, FP64 accumulation every 64 terms). route_filter: 0 all systems;
  * 1 only route-0 systems with cond <= cond_split; 2 every other system. A
  * mixed-precision job runs precision 1 with filter 1, then precision 0 with
  * filter 2: ill-conditioned and routed systems are always computed in FP64

@@ -58,8 +58,7 @@ class SystemsT(ctypes.Structure):
 class KrigeWsT(ctypes.Structure):
     _fields_ = [("l_arena", c_ptr), ("linv_arena", c_ptr), ("status", c_ptr), ("route", c_ptr),
                 ("cond", c_ptr), ("shift", c_ptr), ("w_hat", c_ptr), ("beta", c_ptr),
-                ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr), ("linv32", c_ptr),
-                ("g_cols32", c_ptr), ("w_hat32", c_ptr)]
+                ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr)]
 
 
 class OutT(ctypes.Structure):

@@ -17,8 +17,8 @@
 // precision 0: everything in FP64 (the plain path).
 // precision 1: right-hand sides generated in FP32 from double-float
 // coordinates (differences accurate relative to the distance itself),
-// contractions in FP32 against FP32 copies of the FP64 factor and duals,
-// FP64 epilogue.
+// contracted in split FP32 (each FP64 factor / dual value as an FP32 hi/lo
+// pair, FP32 partial sums flushed to FP64 every 64 terms), FP64 epilogue.
 #include "spi_common.cuh"
 #include "spi_contract.cuh"
 
@@ -64,9 +64,10 @@ __device__ int nnb_f64_warp(const spi_domain_t& dom, const int32_t* idx, int n, 
 }
 
 template <typename T, int TC, typename OutT>
-__global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __restrict__ linv,
-                                                   const T* __restrict__ gcols,
-                                                   const T* __restrict__ what, int npad) {
+__global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
+  const double* __restrict__ linv = A.ws.linv_arena;
+  const double* __restrict__ gcols = A.ws.g_cols;
+  const double* __restrict__ what = A.ws.w_hat;
   constexpr int CPT = TC / 16;
   const int s = blockIdx.y;
   const int64_t C = A.dom.n_cells;
@@ -94,14 +95,14 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
 
   extern __shared__ __align__(16) unsigned char smraw[];
   T* cvT = reinterpret_cast<T*>(smraw);                       // [npad][TC]
-  T* Bs = cvT + (int64_t)npad * TC;                            // [KC][BSTR]
-  double* qc = reinterpret_cast<double*>(Bs + KC * BSTR);      // [TC][GA]
+  T* Bs = cvT + (int64_t)npad * TC;                            // KC * BSTR doubles
+  double* qc = reinterpret_cast<double*>(Bs) + KC * BSTR;      // [TC][GA]
   double* cvar = qc + TC * GA;                                 // [TC]
   double* suml = cvar + TC;                                    // [TC]
   double* red = suml + TC;                                     // [16][TC]
   int* nnb = reinterpret_cast<int*>(red + 16 * TC);            // [TC]
   int* okf = nnb + TC;                                         // [TC]
-  const T** vptr = reinterpret_cast<const T**>(okf + TC);      // [VB]
+  const double** vptr = reinterpret_cast<const double**>(okf + TC);  // [VB]
   __shared__ int any_bad;
   __shared__ int any_ok;
 
@@ -171,8 +172,8 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
     for (int v = tid; v < VB; v += CT)
       vptr[v] = (v < ndual) ? gcols + (soff * GA) + (int64_t)v * n : nullptr;
     {
-      T acc[CPT][4];
-      tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, ndual, n, n, acc);
+      double acc[CPT][4];
+      tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, ndual, n, n, acc);
       const int cg = tid % 16, rg = tid / 16;
 #pragma unroll
       for (int c = 0; c < CPT; ++c)
@@ -187,18 +188,18 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
 #pragma unroll
     for (int c = 0; c < CPT; ++c) yy_part[c] = 0.0;
     if (A.want_var && !prim) {
-      const T* L = linv + A.sys.mat_off[s];
+      const double* L = linv + A.sys.mat_off[s];
       for (int r0 = 0; r0 < n; r0 += VB) {
         __syncthreads();
         for (int v = tid; v < VB; v += CT) vptr[v] = (r0 + v < n) ? L + (int64_t)(r0 + v) * n : nullptr;
-        T acc[CPT][4];
-        tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, min(VB, n - r0), min(n, r0 + VB), n, acc);
+        double acc[CPT][4];
+        tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, min(VB, n - r0), min(n, r0 + VB), n, acc);
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
-          T q = T(0);
+          double q = 0.0;
 #pragma unroll
           for (int r = 0; r < 4; ++r) q += acc[c][r] * acc[c][r];
-          yy_part[c] += (double)q;
+          yy_part[c] += q;
         }
       }
     }
@@ -252,7 +253,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
     __syncthreads();
     if (prim && A.want_var && !sk && any_ok) {
       const int m = n + a;
-      const T* P = reinterpret_cast<const T*>(A.ws.l_arena) + A.sys.mat_off[s];
+      const double* P = A.ws.l_arena + A.sys.mat_off[s];
       double vpart[CPT];
 #pragma unroll
       for (int c = 0; c < CPT; ++c) vpart[c] = 0.0;
@@ -260,8 +261,8 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
       for (int r0 = 0; r0 < m; r0 += VB) {
         __syncthreads();
         for (int v = tid; v < VB; v += CT) vptr[v] = (r0 + v < m) ? P + (int64_t)(r0 + v) * m : nullptr;
-        T acc[CPT][4];
-        tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, min(VB, m - r0), m, m, acc);
+        double acc[CPT][4];
+        tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, min(VB, m - r0), m, m, acc);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = r0 + rg * 4 + r;
@@ -311,14 +312,14 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
     __syncthreads();
     for (int v = tid; v < VB; v += CT)
       vptr[v] = (v < nv && !failed) ? what + A.sys.val_off[A.sys.steps[st0 + v0 + v]] : nullptr;
-    T acc[CPT][4];
+    double acc[CPT][4];
     if (!failed) {
-      tile_contract<T, TC>(cvT, Bs, PtrLoader<T>{vptr, nullptr}, nv, n, n, acc);
+      tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, nv, n, n, acc);
     } else {
 #pragma unroll
       for (int c = 0; c < CPT; ++c)
 #pragma unroll
-        for (int r = 0; r < 4; ++r) acc[c][r] = T(0);
+        for (int r = 0; r < 4; ++r) acc[c][r] = 0.0;
     }
     const int cg = tid % 16, rg = tid / 16;
 #pragma unroll
@@ -354,14 +355,13 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, const T* __rest
 
 template <typename T, int TC>
 static size_t cells_smem(int npad) {
-  return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * sizeof(T) +
+  return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * 8 +
          (size_t)TC * GA * 8 + (size_t)TC * 8 * 2 + (size_t)16 * TC * 8 + (size_t)TC * 4 * 2 +
          (size_t)VB * sizeof(void*) + 16;
 }
 
 template <typename T, int TC, typename OutT>
-static int launch_cells(const CellsArgs& A, const T* linv, const T* gcols, const T* what,
-                        cudaStream_t st) {
+static int launch_cells(const CellsArgs& A, cudaStream_t st) {
   int npad = (A.sys.max_n + GA + KC - 1) / KC * KC;
   size_t smem = cells_smem<T, TC>(npad);
   auto kern = k_krige_cells<T, TC, OutT>;
@@ -371,7 +371,7 @@ static int launch_cells(const CellsArgs& A, const T* linv, const T* gcols, const
   int64_t tiles = (A.dom.n_cells + TC - 1) / TC;
   if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
   dim3 grid((unsigned)tiles, (unsigned)A.sys.n_sys);
-  kern<<<grid, CT, smem, st>>>(A, linv, gcols, what, npad);
+  kern<<<grid, CT, smem, st>>>(A, npad);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }
@@ -388,12 +388,11 @@ static int pick_tc(int max_n) {
 }
 
 template <typename T, typename OutT>
-static int dispatch_cells(const CellsArgs& A, const T* linv, const T* gcols, const T* what,
-                          cudaStream_t st) {
+static int dispatch_cells(const CellsArgs& A, cudaStream_t st) {
   int tc = pick_tc<T>(A.sys.max_n);
-  if (tc == 64) return launch_cells<T, 64, OutT>(A, linv, gcols, what, st);
-  if (tc == 32) return launch_cells<T, 32, OutT>(A, linv, gcols, what, st);
-  if (tc == 16) return launch_cells<T, 16, OutT>(A, linv, gcols, what, st);
+  if (tc == 64) return launch_cells<T, 64, OutT>(A, st);
+  if (tc == 32) return launch_cells<T, 32, OutT>(A, st);
+  if (tc == 16) return launch_cells<T, 16, OutT>(A, st);
   return SPI_ERR_TOO_LARGE;
 }
 
@@ -431,10 +430,8 @@ extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys
   if (!vals || !out->est || !ws->route || !ws->shift || !ws->beta || !ws->s_inv ||
       !ws->g_colsum || !ws->l_arena || !ws->cond)
     return SPI_ERR_ARG;
-  if (precision == 0 && (!ws->linv_arena || !ws->w_hat || !ws->g_cols)) return SPI_ERR_ARG;
-  if (precision == 1 && (!ws->linv32 || !ws->w_hat32 || !ws->g_cols32 || !dom->cell_split ||
-                         !dom->stn_split))
-    return SPI_ERR_ARG;
+  if (!ws->linv_arena || !ws->w_hat || !ws->g_cols) return SPI_ERR_ARG;
+  if (precision == 1 && (!dom->cell_split || !dom->stn_split)) return SPI_ERR_ARG;
   // routed systems are computed in FP64 only
   if (precision == 1 && route_filter != 1) return SPI_ERR_ARG;
   CellsArgs A;
@@ -447,13 +444,9 @@ extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys
   A.cond_split = cond_split;
   A.out = *out;
   cudaStream_t st = (cudaStream_t)stream;
-  if (precision == 0) {
-    return out->out_f64
-               ? dispatch_cells<double, double>(A, ws->linv_arena, ws->g_cols, ws->w_hat, st)
-               : dispatch_cells<double, float>(A, ws->linv_arena, ws->g_cols, ws->w_hat, st);
-  }
-  return out->out_f64 ? dispatch_cells<float, double>(A, ws->linv32, ws->g_cols32, ws->w_hat32, st)
-                      : dispatch_cells<float, float>(A, ws->linv32, ws->g_cols32, ws->w_hat32, st);
+  if (precision == 0)
+    return out->out_f64 ? dispatch_cells<double, double>(A, st) : dispatch_cells<double, float>(A, st);
+  return out->out_f64 ? dispatch_cells<float, double>(A, st) : dispatch_cells<float, float>(A, st);
 }
 
 namespace spi {

@@ -33,17 +33,16 @@ struct IdwArgs {
 };
 
 // B loader: vector 2k = masked values of step k, 2k+1 = its mask.
-template <typename T>
 struct MaskLoader {
   const double* data;
   const int32_t* steps;
   int64_t n_stns;
   int v0;
-  __device__ __forceinline__ T operator()(int v, int j) const {
+  __device__ __forceinline__ double operator()(int v, int j) const {
     const int k = (v0 + v) >> 1;
     double x = data[(int64_t)steps[k] * n_stns + j];
     bool have = !isnan(x);
-    return (v & 1) ? (have ? T(1) : T(0)) : (have ? (T)x : T(0));
+    return (v & 1) ? (have ? 1.0 : 0.0) : (have ? x : 0.0);
   }
 };
 
@@ -57,8 +56,8 @@ __global__ __launch_bounds__(CT) void k_idw(IdwArgs A, int npad) {
   const int tid = threadIdx.x;
   extern __shared__ __align__(16) unsigned char smraw[];
   T* W = reinterpret_cast<T*>(smraw);                          // [npad][TC]
-  T* Bs = W + (int64_t)npad * TC;                              // [KC][BSTR]
-  double* dref = reinterpret_cast<double*>(Bs + KC * BSTR);    // [TC]
+  T* Bs = W + (int64_t)npad * TC;                              // KC * BSTR doubles
+  double* dref = reinterpret_cast<double*>(Bs) + KC * BSTR;    // [TC]
   double* red = dref + TC;                                     // [CT]
   int* onst = reinterpret_cast<int*>(red + CT);                // [TC]
   int* redi = onst + TC;                                       // [CT]
@@ -140,8 +139,8 @@ __global__ __launch_bounds__(CT) void k_idw(IdwArgs A, int npad) {
   const int cg = tid % 16, rg = tid / 16;
   for (int k0 = 0; k0 < A.n_steps; k0 += VB / 2) {
     const int nk = min(VB / 2, A.n_steps - k0);
-    T acc[CPT][4];
-    tile_contract<T, TC>(W, Bs, MaskLoader<T>{A.data, A.steps, N, 2 * k0}, 2 * nk, (int)N,
+    double acc[CPT][4];
+    tile_contract<T, TC>(W, Bs, MaskLoader{A.data, A.steps, N, 2 * k0}, 2 * nk, (int)N,
                          (int)N, acc);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -162,7 +161,7 @@ __global__ __launch_bounds__(CT) void k_idw(IdwArgs A, int npad) {
           if (o >= 0 && !isnan(A.data[(int64_t)j * N + o])) {
             e = __longlong_as_double(0x7ff8000000000000LL);
           } else {
-            e = (double)acc[c][2 * h] / (double)acc[c][2 * h + 1];
+            e = acc[c][2 * h] / acc[c][2 * h + 1];
           }
         }
         e = clip_est(e, A.out);
@@ -233,7 +232,7 @@ __global__ void k_fill_rows(int32_t n_rows, const int32_t* __restrict__ row,
 
 template <typename T, int TC>
 static size_t idw_smem(int npad) {
-  return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * sizeof(T) + (size_t)TC * 8 +
+  return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * 8 + (size_t)TC * 8 +
          (size_t)CT * 8 + (size_t)TC * 4 + (size_t)CT * 4 + 16;
 }
 

@@ -249,16 +249,10 @@ class _KrigeBatch:
         self.g_colsum = torch.zeros(n_sys * nat.GA, dtype=torch.float64, device=dev)
         self.w_hat = torch.zeros_like(self.vals)
         self.beta = beta
-        self.X32 = self.g32 = self.w32 = None
-        if precision == 1:
-            self.X32 = torch.empty(self.arena, dtype=torch.float32, device=dev)
-            self.g32 = torch.empty(self.g_cols.numel(), dtype=torch.float32, device=dev)
-            self.w32 = torch.empty(self.w_hat.numel(), dtype=torch.float32, device=dev)
         self.ws = nat.KrigeWsT(_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
                                _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat),
                                _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv),
-                               _ptr(self.g_colsum), _ptr(self.X32), _ptr(self.g32),
-                               _ptr(self.w32))
+                               _ptr(self.g_colsum))
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
         self.n = ns
@@ -277,10 +271,6 @@ class _KrigeBatch:
                  float(cond_max), s)
         nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
                  ws, s)
-        if self.precision == 1:
-            nat.call("spi_to_f32", _ptr(self.X), _ptr(self.X32), self.arena, s)
-            nat.call("spi_to_f32", _ptr(self.g_cols), _ptr(self.g32), self.g_cols.numel(), s)
-            nat.call("spi_to_f32", _ptr(self.w_hat), _ptr(self.w32), self.w_hat.numel(), s)
         if ev is not None:
             ev[0].record()
         passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
@@ -297,7 +287,7 @@ def _chunk_systems(systems, precision, arena_budget):
     chunks, cur, cur_bytes = [], [], 0
     for i in order:
         n = len(systems[i][0])
-        b = _align((n + nat.GA) ** 2) * 8 * (3 if precision == 1 else 2)
+        b = _align((n + nat.GA) ** 2) * 8 * 2
         if cur and (cur_bytes + b > arena_budget or len(cur) >= 65535):
             chunks.append(cur)
             cur, cur_bytes = [], 0
