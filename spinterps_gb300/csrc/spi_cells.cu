@@ -156,13 +156,15 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
             float dx = (cp.x - sp.x) + (cp.y - sp.y);
             float dy = (cp.z - sp.z) + (cp.w - sp.w);
             float d = sqrtf(dx * dx + dy * dy);
-            float g = 0.f;
-            for (int c = 0; c < vg.n_comp; ++c) {
-              float gv = vg_eval_f32(vg.code[c], d, rr[c], ss[c]);
-              g += sk ? (ss[c] - gv) : gv;
-            }
-            if (g <= mvv) g = 0.f;
-            v = sk ? g : shf - g;
+            // covariance directly (no s - gamma cancellation); the
+            // reference's zeroing of gamma <= min_vg_val (OK/EDK) or of
+            // the covariance <= min_vg_val (SK) applied to it
+            float cdir = 0.f;
+            for (int c = 0; c < vg.n_comp; ++c) cdir += cov_eval_f32(vg.code[c], d, rr[c], ss[c]);
+            if (sk)
+              v = cdir <= mvv ? 0.f : cdir;
+            else
+              v = (shf - cdir <= mvv) ? shf : cdir;
           }
           cvT[(int64_t)j * TC + cell] = (T)v;
         }

@@ -88,6 +88,42 @@ __device__ __forceinline__ float vg_eval_f32(int code, float h, float r, float s
   }
 }
 
+// Covariance contribution s - gamma(h) of one component, written so that
+// it is computed without cancellation (s * rho(h)), for the FP32 path:
+// Exp s e^{-3h/r}, Gau s e^{-3h^2/r^2}, Sph s (1-t)^2 (1 + t/2) for
+// t = h/r < 1, Lin s (1 - t), Hol s sin(a)/a, Nug 0 (its gamma is s at every
+// h, h = 0 included), Pow s (1 - h^r), Rng s - h.
+__device__ __forceinline__ float cov_eval_f32(int code, float h, float r, float s) {
+  switch (code) {
+    case SPI_VG_RNG:
+      return s - h;
+    case SPI_VG_NUG:
+      return 0.0f;
+    case SPI_VG_SPH: {
+      if (h >= r) return 0.0f;
+      float t = h / r, u = 1.0f - t;
+      return s * (u * u) * (1.0f + 0.5f * t);
+    }
+    case SPI_VG_EXP:
+      return s * expf(-3.0f * h / r);
+    case SPI_VG_LIN:
+      return h > r ? 0.0f : s * (1.0f - h / r);
+    case SPI_VG_GAU: {
+      float t = h / r;
+      return s * expf(-3.0f * t * t);
+    }
+    case SPI_VG_POW:
+      return s * (1.0f - powf(h, r));
+    case SPI_VG_HOL: {
+      if (h == 0.0f) return s;
+      float a = (float)SPI_PI * h / r;
+      return s * (sinf(a) / a);
+    }
+    default:
+      return __int_as_float(0x7fc00000);
+  }
+}
+
 // One entry of fill_vg_var_arr (cyth/interpmthds.pyx:186-217) at distance h:
 // accumulate every component in order from 0.0, then zero entries
 // <= min_vg_val.
