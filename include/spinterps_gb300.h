@@ -120,8 +120,9 @@ typedef struct {
 int spi_split_coords(const double *x, const double *y, int64_t n, double ox,
                      double oy, float *out, spi_stream_t stream);
 
-/* y[i] = (float)x[i] (device arrays). */
-int spi_to_f32(const double *x, float *y, int64_t n, spi_stream_t stream);
+/* hi[i] = (float)x[i], lo[i] = (float)(x[i] - hi[i]) (device arrays): the
+ * FP32 pair of the split-precision contractions, made once per system. */
+int spi_split_f64(const double *x, float *hi, float *lo, int64_t n, spi_stream_t stream);
 
 /* A batch of kriging systems (device arrays unless noted). Every system
  * lists the time steps that use it; step j reads its n station values at
@@ -150,7 +151,9 @@ typedef struct {
  * owned). Arenas hold one matrix per system at sys->mat_off[s], sized for
  * (n + SPI_MAX_DRIFT + 1)^2 doubles; per-system arrays have n_sys entries;
  * w_hat has the layout of the values array; beta is [n_steps_total, GA] and
- * g_cols [total stations * GA], GA = SPI_MAX_DRIFT + 1. */
+ * g_cols [total stations * GA], GA = SPI_MAX_DRIFT + 1. The float arrays are
+ * FP32 (hi, lo) pairs of linv_arena, g_cols and w_hat (spi_split_f64),
+ * read by the precision-1 cell kernel only. */
 typedef struct {
     double *l_arena;     /* Cholesky factor L; for routed systems the
                             inverse of the reference's saddle matrix */
@@ -165,6 +168,7 @@ typedef struct {
     double *g_cols;      /* per-system dual columns */
     double *s_inv;       /* per-system S^-1 [n_sys, GA * GA] */
     double *g_colsum;    /* per-system [n_sys, GA] */
+    float *linv_hi, *linv_lo, *g_hi, *g_lo, *w_hi, *w_lo;
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -206,8 +210,9 @@ typedef struct {
 
 /* Kriging estimates (and OK variances when want_var) for every cell of
  * every step of a system batch. precision 0: FP64 throughout; 1: FP32
- * right-hand sides, split-FP32 contractions against the FP64 factor and
- * duals (hi/lo pairs, FP64 accumulation every 64 terms). route_filter: 0 all systems;
+ * right-hand sides, split-FP32 contractions against the FP32 (hi, lo)
+ * pairs of the FP64 factor and duals in ws (FP64 accumulation every 64
+ * terms). route_filter: 0 all systems;
  * 1 only route-0 systems with cond <= cond_split; 2 every other system. A
  * mixed-precision job runs precision 1 with filter 1, then precision 0 with
  * filter 2: ill-conditioned and routed systems are always computed in FP64
@@ -236,12 +241,15 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
  * over stations, so missing stations drop out exactly. A cell on a station
  * present at the step gets NaN, as the reference's 1/0 weight does. Steps
  * with fewer than two stations must not be listed (the reference copies
- * the single value; use spi_fill_rows). precision 0: FP64; 1: FP32
- * (requires dom->stn_split / cell_split). */
+ * the single value; use spi_fill_rows). precision 0: FP64; 1: FP32 weights
+ * contracted against the FP32 (hi, lo) pair of data (data_hi / data_lo,
+ * from spi_split_f64; NaN stays NaN in hi) with FP64 accumulation; requires
+ * dom->stn_split / cell_split. */
 int spi_idw_cells(const spi_domain_t *dom, int32_t n_steps, const int32_t *steps,
-                  const int32_t *out_row, const double *data, const uint8_t *flag,
-                  const double *means, double idw_exp, int32_t precision,
-                  const spi_out_t *out, spi_stream_t stream);
+                  const int32_t *out_row, const double *data, const float *data_hi,
+                  const float *data_lo, const uint8_t *flag, const double *means,
+                  double idw_exp, int32_t precision, const spi_out_t *out,
+                  spi_stream_t stream);
 
 /* NNB (interp/steps.py:285-291): value of the first present station of
  * minimum distance (np.argmin order), per cell and listed step. */

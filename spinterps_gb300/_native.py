@@ -58,7 +58,9 @@ class SystemsT(ctypes.Structure):
 class KrigeWsT(ctypes.Structure):
     _fields_ = [("l_arena", c_ptr), ("linv_arena", c_ptr), ("status", c_ptr), ("route", c_ptr),
                 ("cond", c_ptr), ("shift", c_ptr), ("w_hat", c_ptr), ("beta", c_ptr),
-                ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr)]
+                ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr), ("linv_hi", c_ptr),
+                ("linv_lo", c_ptr), ("g_hi", c_ptr), ("g_lo", c_ptr), ("w_hi", c_ptr),
+                ("w_lo", c_ptr)]
 
 
 class OutT(ctypes.Structure):
@@ -75,7 +77,7 @@ _SIGS = {
     "spi_copy_2d_arr_at_idxs": [c_ptr, c_i64, c_i64, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_i64,
                                 c_ptr],
     "spi_split_coords": [c_ptr, c_ptr, c_i64, c_dbl, c_dbl, c_ptr, c_ptr],
-    "spi_to_f32": [c_ptr, c_ptr, c_i64, c_ptr],
+    "spi_split_f64": [c_ptr, c_ptr, c_ptr, c_i64, c_ptr],
     "spi_krige_factor": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],
     "spi_krige_duals": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr,
@@ -83,8 +85,8 @@ _SIGS = {
     "spi_krige_cells": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr,
                         ctypes.POINTER(KrigeWsT), c_i32, c_i32, c_i32, c_dbl,
                         ctypes.POINTER(OutT), c_ptr],
-    "spi_idw_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_dbl,
-                      c_i32, ctypes.POINTER(OutT), c_ptr],
+    "spi_idw_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                      c_ptr, c_dbl, c_i32, ctypes.POINTER(OutT), c_ptr],
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],

@@ -63,19 +63,26 @@ __device__ int nnb_f64_warp(const spi_domain_t& dom, const int32_t* idx, int n, 
   return bj == 0x7fffffff ? 0 : bj;
 }
 
+template <typename T, int TC, bool W>
+__device__ __forceinline__ void contract(const T* cvT, T* Bs, const double* const* vp64,
+                                         const float* const* vph, const float* const* vpl,
+                                         int nv, int jmax, int nload,
+                                         double (&out)[Layout<TC, W>::CPT][Layout<TC, W>::VPT]) {
+  if constexpr (sizeof(T) == 8)
+    tile_contract<T, TC, W>(cvT, Bs, PtrLoader64{vp64}, nv, jmax, nload, out);
+  else
+    tile_contract<T, TC, W>(cvT, Bs, PtrLoader32{vph, vpl}, nv, jmax, nload, out);
+}
+
 template <typename T, int TC, typename OutT>
 __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
-  const double* __restrict__ linv = A.ws.linv_arena;
-  const double* __restrict__ gcols = A.ws.g_cols;
-  const double* __restrict__ what = A.ws.w_hat;
-  constexpr int CPT = TC / 16;
+  using WL = Layout<TC, true>;
+  using NL = Layout<TC, false>;
+  constexpr int CPT = WL::CPT;
   const int s = blockIdx.y;
   const int64_t C = A.dom.n_cells;
   const int64_t c0 = (int64_t)blockIdx.x * TC;
   if (c0 >= C) return;
-  const int64_t soff = A.sys.stn_off[s];
-  const int n = (int)(A.sys.stn_off[s + 1] - soff);
-  const int32_t* idx = A.sys.stn_idx + soff;
   const int route = A.ws.route[s];
   {
     // filter 1: well-conditioned Cholesky systems; filter 2: all others
@@ -84,6 +91,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   }
   const bool prim = route == 1;   // exact-inverse path: primal formulas
   const bool failed = route == 2;
+  const int64_t soff = A.sys.stn_off[s];
+  const int n = (int)(A.sys.stn_off[s + 1] - soff);
+  const int32_t* idx = A.sys.stn_idx + soff;
   const int sk = A.sys.kind == SPI_KIND_SK;
   // Lagrange / drift rows; on the Cholesky path SK contracts one dual
   // column (u = A^-1 1) in the same slot
@@ -92,19 +102,29 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   const int tid = threadIdx.x;
   const int64_t st0 = A.sys.step_off[s], st1 = A.sys.step_off[s + 1];
   const int nsteps = (int)(st1 - st0);
+  const int64_t moff = A.sys.mat_off[s];
 
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* cvT = reinterpret_cast<T*>(smraw);                       // [npad][TC]
-  T* Bs = cvT + (int64_t)npad * TC;                            // KC * BSTR doubles
-  double* qc = reinterpret_cast<double*>(Bs) + KC * BSTR;      // [TC][GA]
-  double* cvar = qc + TC * GA;                                 // [TC]
-  double* suml = cvar + TC;                                    // [TC]
-  double* red = suml + TC;                                     // [16][TC]
-  int* nnb = reinterpret_cast<int*>(red + 16 * TC);            // [TC]
-  int* okf = nnb + TC;                                         // [TC]
-  const double** vptr = reinterpret_cast<const double**>(okf + TC);  // [VB]
+  T* cvT = reinterpret_cast<T*>(smraw);                                // [npad][TC]
+  T* Bs = cvT + (int64_t)npad * TC;                                     // KC * BSTR doubles
+  double* qc = reinterpret_cast<double*>(Bs) + KC * BSTR;               // [TC][GA]
+  double* cvar = qc + TC * GA;                                          // [TC]
+  double* red = cvar + TC;                                              // [16][TC]
+  int* nnb = reinterpret_cast<int*>(red + 16 * TC);                     // [TC]
+  int* okf = nnb + TC;                                                  // [TC]
+  const double** vp64 = reinterpret_cast<const double**>(okf + TC);    // [VB]
+  const float** vph = reinterpret_cast<const float**>(vp64 + VB);      // [VB]
+  const float** vpl = vph + VB;                                         // [VB]
   __shared__ int any_bad;
   __shared__ int any_ok;
+
+  // vector v of the next pass: FP64 base + off, or its FP32 hi / lo copies
+  auto setv = [&](int v, const double* b64, const float* bh, const float* bl, int64_t off,
+                  bool valid) {
+    vp64[v] = valid ? b64 + off : nullptr;
+    vph[v] = (valid && bh) ? bh + off : nullptr;
+    vpl[v] = (valid && bl) ? bl + off : nullptr;
+  };
 
   const spi_vg_t vg = A.sys.vg[s];
   // right-hand side: covariance form s - gamma on the Cholesky path, the
@@ -114,6 +134,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     any_bad = failed ? 1 : 0;
     any_ok = 0;
   }
+  for (int e = tid; e < TC * GA; e += CT) qc[e] = 0.0;
 
   if (!failed) {
     // ---- 1. right-hand sides, cell-contiguous: cvT[j][cell] ----
@@ -170,32 +191,32 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
         }
       }
     }
-    // ---- 2. dual columns: qc[cell][k] = G_k' c ----
-    for (int v = tid; v < VB; v += CT)
-      vptr[v] = (v < ndual) ? gcols + (soff * GA) + (int64_t)v * n : nullptr;
-    {
-      double acc[CPT][4];
-      tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, ndual, n, n, acc);
-      const int cg = tid % 16, rg = tid / 16;
-#pragma unroll
-      for (int c = 0; c < CPT; ++c)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          int k = rg * 4 + r;
-          if (k < GA) qc[(cg * CPT + c) * GA + k] = (double)acc[c][r];
-        }
+    // ---- 2. dual columns (narrow passes): qc[cell][k] = G_k' c ----
+    for (int v0 = 0; v0 < ndual; v0 += NL::NV) {
+      const int nv = min(NL::NV, ndual - v0);
+      __syncthreads();
+      for (int v = tid; v < NL::NV; v += CT) {
+        const int64_t off = soff * GA + (int64_t)(v0 + v) * n;
+        setv(v, A.ws.g_cols, A.ws.g_hi, A.ws.g_lo, off, v < nv);
+      }
+      double acc[NL::CPT][NL::VPT];
+      contract<T, TC, false>(cvT, Bs, vp64, vph, vpl, nv, n, n, acc);
+      const int cell = tid % TC, k = v0 + tid / TC;
+      if (tid / TC < nv) qc[cell * GA + k] = acc[0][0];
     }
-    // ---- 3. OK variance: |Linv c|^2, triangular blocks of VB rows ----
+    // ---- 3. OK variance |Linv c|^2, wide passes over Linv's rows
+    // (triangular: a pass of rows r0..r0+63 stops at column r0+63) ----
     double yy_part[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) yy_part[c] = 0.0;
     if (A.want_var && !prim) {
-      const double* L = linv + A.sys.mat_off[s];
       for (int r0 = 0; r0 < n; r0 += VB) {
         __syncthreads();
-        for (int v = tid; v < VB; v += CT) vptr[v] = (r0 + v < n) ? L + (int64_t)(r0 + v) * n : nullptr;
+        for (int v = tid; v < VB; v += CT)
+          setv(v, A.ws.linv_arena, A.ws.linv_hi, A.ws.linv_lo, moff + (int64_t)(r0 + v) * n,
+               r0 + v < n);
         double acc[CPT][4];
-        tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, min(VB, n - r0), min(n, r0 + VB), n, acc);
+        contract<T, TC, true>(cvT, Bs, vp64, vph, vpl, min(VB, n - r0), min(n, r0 + VB), n, acc);
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
           double q = 0.0;
@@ -244,47 +265,48 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       }
       int ok = isclose_one(sl) ? 1 : 0;
       okf[cell] = ok;
-      suml[cell] = sl;
       cvar[cell] = ok ? vv : 0.0;
       if (!ok && gc < C) atomicOr(&any_bad, 1);
       if (ok && gc < C) atomicOr(&any_ok, 1);
     }
     // ---- 4b. exact-inverse path, OK variance of the cells that pass the
-    // check: lambda = P r, var = lambda'r + lambda_n, through the same tiled
-    // contraction over P's rows; skipped when no cell of the tile passes ----
+    // check: lambda = P r, var = lambda'r + lambda_n, wide passes over P's
+    // rows; skipped when no cell of the tile passes ----
     __syncthreads();
-    if (prim && A.want_var && !sk && any_ok) {
-      const int m = n + a;
-      const double* P = A.ws.l_arena + A.sys.mat_off[s];
-      double vpart[CPT];
+    if constexpr (sizeof(T) == 8) {
+      if (prim && A.want_var && !sk && any_ok) {
+        const int m = n + a;
+        double vpart[CPT];
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) vpart[c] = 0.0;
-      const int cg = tid % 16, rg = tid / 16;
-      for (int r0 = 0; r0 < m; r0 += VB) {
-        __syncthreads();
-        for (int v = tid; v < VB; v += CT) vptr[v] = (r0 + v < m) ? P + (int64_t)(r0 + v) * m : nullptr;
-        double acc[CPT][4];
-        tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, min(VB, m - r0), m, m, acc);
+        for (int c = 0; c < CPT; ++c) vpart[c] = 0.0;
+        const int cg = tid % 16, rg = tid / 16;
+        for (int r0 = 0; r0 < m; r0 += VB) {
+          __syncthreads();
+          for (int v = tid; v < VB; v += CT)
+            setv(v, A.ws.l_arena, nullptr, nullptr, moff + (int64_t)(r0 + v) * m, r0 + v < m);
+          double acc[CPT][4];
+          contract<T, TC, true>(cvT, Bs, vp64, vph, vpl, min(VB, m - r0), m, m, acc);
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const int row = r0 + rg * 4 + r;
-          if (row >= m) continue;
+          for (int r = 0; r < 4; ++r) {
+            const int row = r0 + rg * 4 + r;
+            if (row >= m) continue;
 #pragma unroll
-          for (int c = 0; c < CPT; ++c) {
-            const int cell = cg * CPT + c;
-            vpart[c] += (double)acc[c][r] * (double)cvT[(int64_t)row * TC + cell];
-            if (row == n) vpart[c] += (double)acc[c][r];
+            for (int c = 0; c < CPT; ++c) {
+              const int cell = cg * CPT + c;
+              vpart[c] += acc[c][r] * (double)cvT[(int64_t)row * TC + cell];
+              if (row == n) vpart[c] += acc[c][r];
+            }
           }
         }
-      }
-      __syncthreads();
+        __syncthreads();
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) red[rg * TC + cg * CPT + c] = vpart[c];
-      __syncthreads();
-      for (int cell = tid; cell < TC; cell += CT) {
-        double vv = 0.0;
-        for (int g = 0; g < 16; ++g) vv += red[g * TC + cell];
-        if (okf[cell]) cvar[cell] = vv;
+        for (int c = 0; c < CPT; ++c) red[rg * TC + cg * CPT + c] = vpart[c];
+        __syncthreads();
+        for (int cell = tid; cell < TC; cell += CT) {
+          double vv = 0.0;
+          for (int g = 0; g < 16; ++g) vv += red[g * TC + cell];
+          if (okf[cell]) cvar[cell] = vv;
+        }
       }
     }
   } else {
@@ -305,61 +327,78 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     }
   }
   __syncthreads();
-  // ---- 6. estimates of every step, VB steps per block ----
+  // ---- 6. estimates of every step: wide passes of 64 steps while many
+  // remain, narrow passes for the rest ----
   const bool var_out = A.want_var && A.out.var != nullptr && !sk;
   OutT* est_out = reinterpret_cast<OutT*>(A.out.est);
   OutT* var_outp = reinterpret_cast<OutT*>(A.out.var);
-  for (int v0 = 0; v0 < nsteps; v0 += VB) {
-    const int nv = min(VB, nsteps - v0);
-    __syncthreads();
-    for (int v = tid; v < VB; v += CT)
-      vptr[v] = (v < nv && !failed) ? what + A.sys.val_off[A.sys.steps[st0 + v0 + v]] : nullptr;
-    double acc[CPT][4];
-    if (!failed) {
-      tile_contract<T, TC>(cvT, Bs, PtrLoader{vptr}, nv, n, n, acc);
-    } else {
-#pragma unroll
-      for (int c = 0; c < CPT; ++c)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) acc[c][r] = 0.0;
-    }
-    const int cg = tid % 16, rg = tid / 16;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int v = rg * 4 + r;
-      if (v >= nv) continue;
-      const int j = A.sys.steps[st0 + v0 + v];
-      const int64_t row = A.sys.out_row[j];
-      const int64_t vo = A.sys.val_off[j];
-      const double* bt = A.ws.beta + (int64_t)j * GA;
-#pragma unroll
-      for (int c = 0; c < CPT; ++c) {
-        const int cell = cg * CPT + c;
-        const int64_t gc = c0 + cell;
-        if (gc >= C) continue;
-        double e;
-        if (okf[cell]) {
-          e = (double)acc[c][r];
-          if (!sk) {
-            e += bt[0];
-            for (int k = 1; k < a; ++k) e += bt[k] * A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
-          }
-        } else {
-          e = A.vals[vo + nnb[cell]];
-        }
-        e = clip_est(e, A.out);
-        est_out[row * C + gc] = cast_out<OutT>(e);
-        if (var_out) var_outp[row * C + gc] = cast_out<OutT>(cvar[cell]);
+  auto emit = [&](int cell, int vstep, double accv) {
+    const int64_t gc = c0 + cell;
+    if (gc >= C) return;
+    const int j = A.sys.steps[st0 + vstep];
+    const int64_t row = A.sys.out_row[j];
+    double e;
+    if (okf[cell]) {
+      e = accv;
+      if (!sk) {
+        const double* bt = A.ws.beta + (int64_t)j * GA;
+        e += bt[0];
+        for (int k = 1; k < a; ++k) e += bt[k] * A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
       }
+    } else {
+      e = A.vals[A.sys.val_off[j] + nnb[cell]];
     }
+    e = clip_est(e, A.out);
+    est_out[row * C + gc] = cast_out<OutT>(e);
+    if (var_out) var_outp[row * C + gc] = cast_out<OutT>(cvar[cell]);
+  };
+  for (int v0 = 0; v0 < nsteps;) {
+    const int rem = nsteps - v0;
+    const bool wide = rem >= 32;
+    const int nv = min(wide ? VB : NL::NV, rem);
+    __syncthreads();
+    for (int v = tid; v < VB; v += CT) {
+      const bool valid = v < nv && !failed;
+      const int64_t off = valid ? A.sys.val_off[A.sys.steps[st0 + v0 + v]] : 0;
+      setv(v, A.ws.w_hat, A.ws.w_hi, A.ws.w_lo, off, valid);
+    }
+    if (wide) {
+      double acc[CPT][4];
+      if (!failed) {
+        contract<T, TC, true>(cvT, Bs, vp64, vph, vpl, nv, n, n, acc);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc[c][r] = 0.0;
+      }
+      const int cg = tid % 16, rg = tid / 16;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int vl = rg * 4 + r;
+        if (vl >= nv) continue;
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) emit(cg * CPT + c, v0 + vl, acc[c][r]);
+      }
+    } else {
+      double acc[NL::CPT][NL::VPT];
+      if (!failed) {
+        contract<T, TC, false>(cvT, Bs, vp64, vph, vpl, nv, n, n, acc);
+      } else {
+        acc[0][0] = 0.0;
+      }
+      const int vl = tid / TC;
+      if (vl < nv) emit(tid % TC, v0 + vl, acc[0][0]);
+    }
+    v0 += nv;
   }
 }
 
 template <typename T, int TC>
 static size_t cells_smem(int npad) {
   return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * 8 +
-         (size_t)TC * GA * 8 + (size_t)TC * 8 * 2 + (size_t)16 * TC * 8 + (size_t)TC * 4 * 2 +
-         (size_t)VB * sizeof(void*) + 16;
+         (size_t)TC * GA * 8 + (size_t)TC * 8 + (size_t)16 * TC * 8 + (size_t)TC * 4 * 2 +
+         (size_t)3 * VB * sizeof(void*) + 16;
 }
 
 template <typename T, int TC, typename OutT>
@@ -398,23 +437,29 @@ static int dispatch_cells(const CellsArgs& A, cudaStream_t st) {
   return SPI_ERR_TOO_LARGE;
 }
 
-__global__ void k_to_f32(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+__global__ void k_split_f64(const double* __restrict__ x, float* __restrict__ hi,
+                            float* __restrict__ lo, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = (float)x[i];
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = x[i];
+    float h = (float)v;
+    hi[i] = h;
+    lo[i] = (float)(v - (double)h);
+  }
 }
 
 }  // namespace spi
 
 using namespace spi;
 
-extern "C" int spi_to_f32(const double* x, float* y, int64_t n, spi_stream_t stream) {
+extern "C" int spi_split_f64(const double* x, float* hi, float* lo, int64_t n,
+                             spi_stream_t stream) {
   if (n < 0) return SPI_ERR_ARG;
   if (n == 0) return SPI_OK;
-  if (!x || !y) return SPI_ERR_ARG;
+  if (!x || !hi || !lo) return SPI_ERR_ARG;
   int64_t blocks = (n + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  k_to_f32<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(x, y, n);
+  k_split_f64<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(x, hi, lo, n);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }
@@ -433,7 +478,9 @@ extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys
       !ws->g_colsum || !ws->l_arena || !ws->cond)
     return SPI_ERR_ARG;
   if (!ws->linv_arena || !ws->w_hat || !ws->g_cols) return SPI_ERR_ARG;
-  if (precision == 1 && (!dom->cell_split || !dom->stn_split)) return SPI_ERR_ARG;
+  if (precision == 1 && (!dom->cell_split || !dom->stn_split || !ws->linv_hi || !ws->linv_lo ||
+                         !ws->g_hi || !ws->g_lo || !ws->w_hi || !ws->w_lo))
+    return SPI_ERR_ARG;
   // routed systems are computed in FP64 only
   if (precision == 1 && route_filter != 1) return SPI_ERR_ARG;
   CellsArgs A;

@@ -1,12 +1,22 @@
 // Shared-memory-tiled contraction used by the cell kernels.
 //
-// acc[c][r] = sum_{j < jmax} cvT[j][cg*CPT + c] * B_{rg*4 + r}[j]
-// where cvT [npad][TC] holds TC cells' right-hand sides (or weights),
-// cell-contiguous, and B_v[j] is produced by a loader functor. 256 threads:
-// thread t owns cell group cg = t % 16 (CPT = TC / 16 cells) and vector
-// group rg = t / 16 (4 vectors), so a CTA computes a TC x 64 block per
-// pass. B is staged through shared memory in KC-long chunks; each inner
-// step reads CPT + 4 values (two vector loads) for 4*CPT FMAs.
+// out[c][r] = sum_{j < jmax} cvT[j][cell(c)] * B_{vec(r)}[j]
+// cvT [npad][TC] holds TC cells' right-hand sides (or weights),
+// cell-contiguous; B_v[j] comes from a loader functor. 256 threads, in two
+// layouts:
+//   wide   (W = true):  16 cell groups x 16 vector groups, CPT = TC/16
+//                       cells x 4 vectors per thread, 64 vectors per pass;
+//   narrow (W = false): TC cell groups x 256/TC vector groups, 1 cell x 1
+//                       vector per thread, 256/TC vectors per pass (for the
+//                       few dual / step vectors, so no FMAs go to padding).
+// B is staged through shared memory in KC-long chunks.
+//
+// FP64 cvT (the plain FP64 path): FP64 B, FP64 accumulation.
+// FP32 cvT (split precision): B arrives as FP32 (hi, lo) pairs made once
+// per system from the FP64 factor / duals (b = hi + lo to 48 bits); both
+// are multiplied with a and the FP32 partial sums are flushed into FP64
+// accumulators every 2 * KC terms, so the only FP32-level error left is
+// the rounding of cvT itself.
 #pragma once
 #include "spi_common.cuh"
 
@@ -14,7 +24,7 @@ namespace spi {
 
 constexpr int CT = 256;         // threads per cell CTA
 constexpr int KC = 32;          // contraction chunk
-constexpr int VB = 64;          // vectors (columns) per contraction block
+constexpr int VB = 64;          // vectors per wide pass
 constexpr int BSTR = VB + 4;    // Bs row stride (16-byte aligned rows)
 
 template <typename T>
@@ -35,32 +45,43 @@ struct Vec4<double> {
   }
 };
 
-// Loads B_v[j] (FP64) from a table of vector base pointers (nullptr: zeros).
-struct PtrLoader {
+// Vector base pointers in shared memory (nullptr rows are never read).
+struct PtrLoader64 {
   const double* const* vptr;
   __device__ __forceinline__ double operator()(int v, int j) const { return vptr[v][j]; }
 };
+struct PtrLoader32 {
+  const float* const* hptr;
+  const float* const* lptr;
+  __device__ __forceinline__ float2 operator()(int v, int j) const {
+    return make_float2(hptr[v][j], lptr[v][j]);
+  }
+};
 
-// FP64 cvT: plain FP64 contraction.
-// FP32 cvT (split precision): each FP64 B value is staged as an FP32 pair
-// b = b_hi + b_lo (48 significant bits), both multiplied with a, and the
-// FP32 partial sums are flushed into FP64 accumulators every 2 * KC terms,
-// so the only FP32-level error left is the rounding of cvT itself.
-// Bs must hold 2 * KC * BSTR floats (= KC * BSTR doubles).
-template <typename T, int TC, typename Loader>
+template <int TC, bool W>
+struct Layout {
+  static constexpr int NCG = W ? 16 : TC;          // cell groups
+  static constexpr int CPT = TC / NCG;             // cells per thread
+  static constexpr int NVG = CT / NCG;             // vector groups
+  static constexpr int VPT = W ? 4 : 1;            // vectors per thread
+  static constexpr int NV = NVG * VPT;             // vectors per pass
+};
+
+template <typename T, int TC, bool W, typename Loader>
 __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __restrict__ Bs,
                                               const Loader& ld, int nv, int jmax, int n,
-                                              double (&out)[TC / 16][4]) {
-  constexpr int CPT = TC / 16;
-  const int tid = threadIdx.x, cg = tid % 16, rg = tid / 16;
+                                              double (&out)[Layout<TC, W>::CPT][Layout<TC, W>::VPT]) {
+  using LY = Layout<TC, W>;
+  constexpr int CPT = LY::CPT, VPT = LY::VPT, NV = LY::NV;
+  const int tid = threadIdx.x, cg = tid % LY::NCG, rg = tid / LY::NCG;
 #pragma unroll
   for (int c = 0; c < CPT; ++c)
 #pragma unroll
-    for (int r = 0; r < 4; ++r) out[c][r] = 0.0;
+    for (int r = 0; r < VPT; ++r) out[c][r] = 0.0;
   if constexpr (sizeof(T) == 8) {
     for (int k0 = 0; k0 < jmax; k0 += KC) {
       __syncthreads();
-      for (int e = tid; e < VB * KC; e += CT) {
+      for (int e = tid; e < NV * KC; e += CT) {
         int v = e / KC, jj = e % KC;
         int j = k0 + jj;
         Bs[jj * BSTR + v] = (v < nv && j < n) ? ld(v, j) : 0.0;
@@ -68,40 +89,43 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
       __syncthreads();
 #pragma unroll 8
       for (int jj = 0; jj < KC; ++jj) {
-        double a[CPT], b[4];
+        double a[CPT], b[VPT];
         const double* ap = cvT + (int64_t)(k0 + jj) * TC + cg * CPT;
 #pragma unroll
         for (int c = 0; c < CPT; ++c) a[c] = ap[c];
-        Vec4<double>::load(Bs + jj * BSTR + rg * 4, b);
+        if constexpr (VPT == 4) {
+          Vec4<double>::load(Bs + jj * BSTR + rg * 4, b);
+        } else {
+          b[0] = Bs[jj * BSTR + rg];
+        }
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
 #pragma unroll
-          for (int r = 0; r < 4; ++r) out[c][r] += a[c] * b[r];
+          for (int r = 0; r < VPT; ++r) out[c][r] += a[c] * b[r];
       }
     }
   } else {
     float* Bh = Bs;
     float* Bl = Bs + KC * BSTR;
-    float acc[CPT][4];
+    float acc[CPT][VPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
 #pragma unroll
-      for (int r = 0; r < 4; ++r) acc[c][r] = 0.f;
+      for (int r = 0; r < VPT; ++r) acc[c][r] = 0.f;
     int chunk = 0;
     for (int k0 = 0; k0 < jmax; k0 += KC, ++chunk) {
       __syncthreads();
-      for (int e = tid; e < VB * KC; e += CT) {
+      for (int e = tid; e < NV * KC; e += CT) {
         int v = e / KC, jj = e % KC;
         int j = k0 + jj;
-        double x = (v < nv && j < n) ? ld(v, j) : 0.0;
-        float h = (float)x;
-        Bh[jj * BSTR + v] = h;
-        Bl[jj * BSTR + v] = (float)(x - (double)h);
+        float2 x = (v < nv && j < n) ? ld(v, j) : make_float2(0.f, 0.f);
+        Bh[jj * BSTR + v] = x.x;
+        Bl[jj * BSTR + v] = x.y;
       }
       __syncthreads();
 #pragma unroll 8
       for (int jj = 0; jj < KC; ++jj) {
-        float a[CPT], bh[4], bl[4];
+        float a[CPT], bh[VPT], bl[VPT];
         const float* ap = cvT + (int64_t)(k0 + jj) * TC + cg * CPT;
         if constexpr (CPT == 4) {
           Vec4<float>::load(ap, a);
@@ -109,12 +133,17 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
 #pragma unroll
           for (int c = 0; c < CPT; ++c) a[c] = ap[c];
         }
-        Vec4<float>::load(Bh + jj * BSTR + rg * 4, bh);
-        Vec4<float>::load(Bl + jj * BSTR + rg * 4, bl);
+        if constexpr (VPT == 4) {
+          Vec4<float>::load(Bh + jj * BSTR + rg * 4, bh);
+          Vec4<float>::load(Bl + jj * BSTR + rg * 4, bl);
+        } else {
+          bh[0] = Bh[jj * BSTR + rg];
+          bl[0] = Bl[jj * BSTR + rg];
+        }
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
 #pragma unroll
-          for (int r = 0; r < 4; ++r) {
+          for (int r = 0; r < VPT; ++r) {
             acc[c][r] = fmaf(a[c], bh[r], acc[c][r]);
             acc[c][r] = fmaf(a[c], bl[r], acc[c][r]);
           }
@@ -123,7 +152,7 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
 #pragma unroll
-          for (int r = 0; r < 4; ++r) {
+          for (int r = 0; r < VPT; ++r) {
             out[c][r] += (double)acc[c][r];
             acc[c][r] = 0.f;
           }
@@ -132,7 +161,7 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
 #pragma unroll
-      for (int r = 0; r < 4; ++r) out[c][r] += (double)acc[c][r];
+      for (int r = 0; r < VPT; ++r) out[c][r] += (double)acc[c][r];
   }
 }
 

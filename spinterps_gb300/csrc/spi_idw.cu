@@ -26,14 +26,16 @@ struct IdwArgs {
   const int32_t* steps;
   const int32_t* out_row;
   const double* data;    // [T, N], NaN = missing
+  const float* data_hi;  // FP32 (hi, lo) pair of data (precision 1)
+  const float* data_lo;
   const uint8_t* flag;   // [T]
   const double* means;   // [T]
   double p;
   spi_out_t out;
 };
 
-// B loader: vector 2k = masked values of step k, 2k+1 = its mask.
-struct MaskLoader {
+// B loaders: vector 2k = masked values of step k, 2k+1 = its mask.
+struct MaskLoader64 {
   const double* data;
   const int32_t* steps;
   int64_t n_stns;
@@ -43,6 +45,21 @@ struct MaskLoader {
     double x = data[(int64_t)steps[k] * n_stns + j];
     bool have = !isnan(x);
     return (v & 1) ? (have ? 1.0 : 0.0) : (have ? x : 0.0);
+  }
+};
+struct MaskLoader32 {
+  const float* hi;
+  const float* lo;
+  const int32_t* steps;
+  int64_t n_stns;
+  int v0;
+  __device__ __forceinline__ float2 operator()(int v, int j) const {
+    const int k = (v0 + v) >> 1;
+    const int64_t e = (int64_t)steps[k] * n_stns + j;
+    float h = hi[e];
+    bool have = !isnan(h);
+    if (v & 1) return make_float2(have ? 1.f : 0.f, 0.f);
+    return have ? make_float2(h, lo[e]) : make_float2(0.f, 0.f);
   }
 };
 
@@ -140,8 +157,12 @@ __global__ __launch_bounds__(CT) void k_idw(IdwArgs A, int npad) {
   for (int k0 = 0; k0 < A.n_steps; k0 += VB / 2) {
     const int nk = min(VB / 2, A.n_steps - k0);
     double acc[CPT][4];
-    tile_contract<T, TC>(W, Bs, MaskLoader{A.data, A.steps, N, 2 * k0}, 2 * nk, (int)N,
-                         (int)N, acc);
+    if constexpr (sizeof(T) == 8)
+      tile_contract<T, TC, true>(W, Bs, MaskLoader64{A.data, A.steps, N, 2 * k0}, 2 * nk,
+                                 (int)N, (int)N, acc);
+    else
+      tile_contract<T, TC, true>(W, Bs, MaskLoader32{A.data_hi, A.data_lo, A.steps, N, 2 * k0},
+                                 2 * nk, (int)N, (int)N, acc);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int k = rg * 2 + h;
@@ -280,19 +301,23 @@ static int idw_args(IdwArgs& A, const spi_domain_t* dom, int32_t n_steps, const 
 }
 
 extern "C" int spi_idw_cells(const spi_domain_t* dom, int32_t n_steps, const int32_t* steps,
-                             const int32_t* out_row, const double* data, const uint8_t* flag,
-                             const double* means, double idw_exp, int32_t precision,
-                             const spi_out_t* out, spi_stream_t stream) {
+                             const int32_t* out_row, const double* data, const float* data_hi,
+                             const float* data_lo, const uint8_t* flag, const double* means,
+                             double idw_exp, int32_t precision, const spi_out_t* out,
+                             spi_stream_t stream) {
   IdwArgs A;
   int rc = idw_args(A, dom, n_steps, steps, out_row, data, out);
   if (rc == 1) return SPI_OK;
   if (rc) return rc;
   if (!flag || !means) return SPI_ERR_ARG;
-  if (precision == 1 && (!dom->stn_split || !dom->cell_split)) return SPI_ERR_ARG;
+  if (precision == 1 && (!dom->stn_split || !dom->cell_split || !data_hi || !data_lo))
+    return SPI_ERR_ARG;
   if (precision != 0 && precision != 1) return SPI_ERR_ARG;
   A.flag = flag;
   A.means = means;
   A.p = idw_exp;
+  A.data_hi = data_hi;
+  A.data_lo = data_lo;
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == 0)
     return out->out_f64 ? dispatch_idw<double, double>(A, st) : dispatch_idw<double, float>(A, st);

@@ -249,10 +249,17 @@ class _KrigeBatch:
         self.g_colsum = torch.zeros(n_sys * nat.GA, dtype=torch.float64, device=dev)
         self.w_hat = torch.zeros_like(self.vals)
         self.beta = beta
+        self.split = None
+        if precision == 1:
+            # FP32 (hi, lo) pairs of Linv, G and w_hat for the split-precision kernel
+            self.split = [torch.empty(k, dtype=torch.float32, device=dev)
+                          for k in (self.arena, self.arena, self.g_cols.numel(),
+                                    self.g_cols.numel(), self.w_hat.numel(), self.w_hat.numel())]
         self.ws = nat.KrigeWsT(_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
                                _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat),
                                _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv),
-                               _ptr(self.g_colsum))
+                               _ptr(self.g_colsum),
+                               *[_ptr(t) for t in (self.split or [None] * 6)])
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
         self.n = ns
@@ -271,6 +278,11 @@ class _KrigeBatch:
                  float(cond_max), s)
         nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
                  ws, s)
+        if self.split is not None:
+            xh, xl, gh, gl, wh, wl = self.split
+            nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
+            nat.call("spi_split_f64", _ptr(self.g_cols), _ptr(gh), _ptr(gl), self.g_cols.numel(), s)
+            nat.call("spi_split_f64", _ptr(self.w_hat), _ptr(wh), _ptr(wl), self.w_hat.numel(), s)
         if ev is not None:
             ev[0].record()
         passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
@@ -376,6 +388,10 @@ class InterpPlan:
         self.idw = []
         if any(t in ("IDW", "NNB") for t in types):
             self.data_d = torch.as_tensor(data, device=dev)
+            self.data_hi = self.data_lo = None
+            if prec == 1:
+                self.data_hi = torch.empty(data.size, dtype=torch.float32, device=dev)
+                self.data_lo = torch.empty(data.size, dtype=torch.float32, device=dev)
             self.steps_t = torch.as_tensor(multi.astype(np.int32), device=dev)
             self.flag_t = torch.as_tensor(flags.astype(np.uint8), device=dev)
             self.mean_t = torch.as_tensor(np.nan_to_num(means), device=dev)
@@ -414,10 +430,13 @@ class InterpPlan:
                 ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                 ev[0].record()
             if t == "IDW":
+                if self.data_hi is not None:
+                    nat.call("spi_split_f64", _ptr(self.data_d), _ptr(self.data_hi),
+                             _ptr(self.data_lo), self.data_d.numel(), s)
                 nat.call("spi_idw_cells", ctypes.byref(self.dom.st), len(self.multi),
                          _ptr(self.steps_t), _ptr(self.steps_t), _ptr(self.data_d),
-                         _ptr(self.flag_t), _ptr(self.mean_t), p, self.prec, ctypes.byref(out),
-                         s)
+                         _ptr(self.data_hi), _ptr(self.data_lo), _ptr(self.flag_t),
+                         _ptr(self.mean_t), p, self.prec, ctypes.byref(out), s)
             else:
                 nat.call("spi_nnb_cells", ctypes.byref(self.dom.st), len(self.multi),
                          _ptr(self.steps_t), _ptr(self.steps_t), _ptr(self.data_d),
