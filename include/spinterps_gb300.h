@@ -266,6 +266,34 @@ int spi_fill_rows(int32_t n_rows, const int32_t *row, const double *v,
                   const double *vv, int64_t n_cells, const spi_out_t *out,
                   spi_stream_t stream);
 
+/* ---- allocation-free variant ------------------------------------------ */
+
+/* Limits of spi_krige_ok_noalloc and the size of its static scratch. */
+#define SPI_NOALLOC_MAX_STNS 512
+#define SPI_NOALLOC_MAX_STEPS 64
+#define SPI_NOALLOC_SCRATCH_BYTES 4629248  /* 4.4 MiB on every GPU that loads the library */
+
+/* No counterpart in the reference. Ordinary kriging (estimate, and the OK
+ * variance when want_var) of ONE station set, n <= SPI_NOALLOC_MAX_STNS
+ * stations and n_steps <= SPI_NOALLOC_MAX_STEPS steps, in FP64 -- the same
+ * computation as spi_krige_factor + spi_krige_duals + spi_krige_cells for a
+ * one-system batch -- for callers that cannot allocate device memory (hosts
+ * whose pool allocator owns the whole GPU and forbids cudaMalloc, services
+ * that cannot afford an allocation per call). It allocates nothing: its
+ * workspace is a static device array of SPI_NOALLOC_SCRATCH_BYTES, reserved
+ * on every GPU that loads the library until the process exits.
+ * stn_idx [n] (device): the stations' indices into dom; vals [n_steps, n]
+ * (device): their values per step; vg (host): the variogram; est / var of
+ * out: [n_steps, dom->n_cells], row j = step j. dom->n_drift is ignored.
+ * Sizes above the limits return SPI_ERR_TOO_LARGE. The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress, with
+ * that device current); make that first call before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (other
+ * streams or host threads) race and must be serialised by the caller. */
+int spi_krige_ok_noalloc(const spi_domain_t *dom, const int32_t *stn_idx, int32_t n,
+                         const spi_vg_t *vg, const double *vals, int32_t n_steps,
+                         int32_t want_var, const spi_out_t *out, spi_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

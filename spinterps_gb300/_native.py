@@ -20,6 +20,8 @@ SPI_MAX_VG_COMP = 4
 SPI_MAX_DRIFT = 7
 GA = SPI_MAX_DRIFT + 1
 KIND = {"OK": 0, "SK": 1, "EDK": 2}
+SPI_NOALLOC_MAX_STNS = 512
+SPI_NOALLOC_MAX_STEPS = 64
 
 STATUS = {
     0: "SPI_OK",
@@ -90,6 +92,8 @@ _SIGS = {
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
+    "spi_krige_ok_noalloc": [ctypes.POINTER(DomainT), c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
+                             c_i32, c_i32, ctypes.POINTER(OutT), c_ptr],
 }
 
 # every entry point the header declares (checked by the CPU tests)

@@ -138,3 +138,10 @@ def test_host_mirror_has_no_cpu_fallback():
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         spi.interp_steps(np.zeros(3), np.zeros(3), np.zeros((1, 3)), np.zeros(2), np.zeros(2),
                          ["1.0 Exp(10)"], [("OK", None, "OK")])
+
+
+def test_noalloc_limits_match_header():
+    txt = (ROOT / "include" / "spinterps_gb300.h").read_text()
+    stns = int(re.search(r"#define SPI_NOALLOC_MAX_STNS (\d+)", txt).group(1))
+    steps = int(re.search(r"#define SPI_NOALLOC_MAX_STEPS (\d+)", txt).group(1))
+    assert (stns, steps) == (nat.SPI_NOALLOC_MAX_STNS, nat.SPI_NOALLOC_MAX_STEPS)

@@ -1,0 +1,95 @@
+"""The allocation-free kriging entry point, spi_krige_ok_noalloc.
+
+It is meant for callers that cannot allocate device memory (their own pool
+allocator owns the GPU, or an allocation per call is too costly): it keeps
+its workspace in a static device array instead of a caller-provided one.
+Here it is called through the C ABI twice in a row, with different station
+sets, variograms and step counts (the second call must not see the first
+call's leftovers in the shared array), and each result is compared with the
+regular entry points (spi_krige_factor / _duals / _cells through
+interp_steps) at the FP64 parity tolerance of the other GPU tests. Sizes
+beyond its limits must be rejected before any work is launched.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-9
+
+
+def _err(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(b)
+    return float(np.abs(a[m] - b[m]).max() / np.abs(b[m]).max())
+
+
+def _case(rng, n_all, subset, n_steps):
+    z = np.full((n_steps, n_all), np.nan)
+    z[:, subset] = 3.0 + rng.normal(size=(n_steps, subset.size))
+    return z
+
+
+def test_noalloc_matches_regular_entry_points_twice():
+    import spinterps_gb300 as spi
+    from spinterps_gb300 import _native as nat
+    from spinterps_gb300.steps import _ptr, _stream, parse_vg
+
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(5)
+    n_all = 160
+    sx, sy = rng.uniform(0, 8e4, n_all), rng.uniform(0, 8e4, n_all)
+    gx, gy = np.meshgrid(np.arange(40) * 2000.0 + 1000.0, 8e4 - 1000.0 - np.arange(30) * 2000.0)
+    cx, cy = gx.ravel(), gy.ravel()
+    C = cx.size
+    t_sx, t_sy, t_cx, t_cy = (torch.as_tensor(a, device=dev) for a in (sx, sy, cx, cy))
+    dom = nat.DomainT(n_all, _ptr(t_sx), _ptr(t_sy), C, _ptr(t_cx), _ptr(t_cy), 0, None, None,
+                      1e-4, None, None)
+    calls = [
+        (np.arange(0, 120), "0.05 Nug(0.0) + 0.95 Exp(20000)", 3),
+        (np.sort(rng.choice(n_all, 150, replace=False)), "0.1 Nug(0.0) + 1.4 Sph(35000)", 5),
+    ]
+    args = [("OK", None, "OK"), ("EST_VARS_OK", None, "EST_VARS_OK")]
+    for subset, vg, n_steps in calls:
+        z = _case(rng, n_all, subset, n_steps)
+        ref, _ = spi.interp_steps(sx, sy, z, cx, cy, [vg] * n_steps, args, est_vars=True,
+                                  min_var_thr=-np.inf, min_vg_val=1e-4,
+                                  intrp_dtype=np.float64)
+        idx = torch.as_tensor(subset.astype(np.int32), device=dev)
+        vals = torch.as_tensor(np.ascontiguousarray(z[:, subset]), device=dev)
+        est = torch.full((n_steps, C), float("nan"), dtype=torch.float64, device=dev)
+        var = torch.full((n_steps, C), float("nan"), dtype=torch.float64, device=dev)
+        out = nat.OutT(1, _ptr(est), _ptr(var), 0, 0, 0.0, 0.0)
+        v = parse_vg(vg)
+        rc = nat.lib().spi_krige_ok_noalloc(ctypes.byref(dom), _ptr(idx), subset.size,
+                                            ctypes.byref(v), _ptr(vals), n_steps, 1,
+                                            ctypes.byref(out), _stream())
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert _err(est.cpu().numpy(), ref["OK"]) <= FP64_TOL
+        assert _err(var.cpu().numpy(), ref["EST_VARS_OK"]) <= FP64_TOL
+
+
+def test_noalloc_rejects_sizes_beyond_its_limits():
+    from spinterps_gb300 import _native as nat
+    from spinterps_gb300.steps import _ptr, _stream, parse_vg
+
+    dev = torch.device("cuda:0")
+    x = torch.zeros(1000, dtype=torch.float64, device=dev)
+    idx = torch.zeros(1000, dtype=torch.int32, device=dev)
+    dom = nat.DomainT(1000, _ptr(x), _ptr(x), 10, _ptr(x), _ptr(x), 0, None, None, 0.0, None,
+                      None)
+    out = nat.OutT(1, _ptr(x), None, 0, 0, 0.0, 0.0)
+    v = parse_vg("1.0 Exp(1000)")
+    lib = nat.lib()
+    too_many_stations = nat.SPI_NOALLOC_MAX_STNS + 1
+    assert lib.spi_krige_ok_noalloc(ctypes.byref(dom), _ptr(idx), too_many_stations,
+                                    ctypes.byref(v), _ptr(x), 1, 0, ctypes.byref(out),
+                                    _stream()) == 5
+    assert lib.spi_krige_ok_noalloc(ctypes.byref(dom), _ptr(idx), 10, ctypes.byref(v), _ptr(x),
+                                    nat.SPI_NOALLOC_MAX_STEPS + 1, 0, ctypes.byref(out),
+                                    _stream()) == 5
