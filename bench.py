@@ -279,7 +279,7 @@ def run_ours(args):
                          precision=args.precision, **KW)
         torch.cuda.synchronize()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_val = world * Te * C / (np.median(e2e_ms) / 1e3)
+    e2e_val = world * Te * C / (np.median(e2e_ms) / 1e3) if e2e_ms else None
     # plain FP64 GPU path on a step subset, and the mixed path's error on it
     fp64 = None
     if args.fp64_steps > 0 and rank == 0:
@@ -324,7 +324,8 @@ def run_ours(args):
                        "l2": "per-step working set (4.4 GB of fields + 1.6 GB factors) >> L2",
                        "singular_steps_nnb": failed, "exact_inverse_steps": routed},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms": float(np.median(e2e_ms))},
+                    "d2h_bytes_per_step": int(d2h),
+                    "ms": float(np.median(e2e_ms)) if e2e_ms else None},
             "gpu_launches": launches_per_exec * args.steps,
             "roofline": roofline,
             "idw_ms_per_step": idw_ms / args.steps,
