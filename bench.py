@@ -338,6 +338,22 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile_case(args):
+    """The small case that ncu full captures use: 8 steps of the workload
+    (two Exp, two Sph, four Gau from short to long range; two of them take
+    the exact-inverse path) over the first 2^17 cells, one execution."""
+    import torch
+    from spinterps_gb300.steps import InterpPlan
+    w = make_workload()
+    pick = [2, 3, 0, 7, 308, 142, 29, 271]
+    C = 1 << 17
+    plan = InterpPlan(w["sx"], w["sy"], w["z"][pick], w["cx"][:C], w["cy"][:C],
+                      [w["vgs"][j] for j in pick], interp_args(), precision=args.precision, **KW)
+    plan.execute()
+    torch.cuda.synchronize()
+    print("profile case done")
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -369,9 +385,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--fp64-steps", type=int, default=4)
     ap.add_argument("--slices", type=int, default=5)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run the small case used for ncu full captures and exit")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -109,8 +109,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   T* Bs = cvT + (int64_t)npad * TC;                                     // KC * BSTR doubles
   double* qc = reinterpret_cast<double*>(Bs) + KC * BSTR;               // [TC][GA]
   double* cvar = qc + TC * GA;                                          // [TC]
-  double* red = cvar + TC;                                              // [16][TC]
-  int* nnb = reinterpret_cast<int*>(red + 16 * TC);                     // [TC]
+  // per-cell partial sums reuse the staging buffer (free between passes)
+  double* red = reinterpret_cast<double*>(Bs);                          // [16][TC]
+  int* nnb = reinterpret_cast<int*>(cvar + TC);                         // [TC]
   int* okf = nnb + TC;                                                  // [TC]
   const double** vp64 = reinterpret_cast<const double**>(okf + TC);    // [VB]
   const float** vph = reinterpret_cast<const float**>(vp64 + VB);      // [VB]
@@ -397,7 +398,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
 template <typename T, int TC>
 static size_t cells_smem(int npad) {
   return (size_t)npad * TC * sizeof(T) + (size_t)KC * BSTR * 8 +
-         (size_t)TC * GA * 8 + (size_t)TC * 8 + (size_t)16 * TC * 8 + (size_t)TC * 4 * 2 +
+         (size_t)TC * GA * 8 + (size_t)TC * 8 + (size_t)TC * 4 * 2 +
          (size_t)3 * VB * sizeof(void*) + 16;
 }
 
@@ -421,7 +422,7 @@ static int launch_cells(const CellsArgs& A, cudaStream_t st) {
 template <typename T>
 static int pick_tc(int max_n) {
   int npad = (max_n + GA + KC - 1) / KC * KC;
-  const size_t cap = 225 * 1024;
+  const size_t cap = 227 * 1024;
   if (sizeof(T) == 4 && cells_smem<T, 64>(npad) <= cap) return 64;
   if (cells_smem<T, 32>(npad) <= cap) return 32;
   if (cells_smem<T, 16>(npad) <= cap) return 16;

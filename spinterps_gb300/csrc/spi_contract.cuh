@@ -15,8 +15,9 @@
 // FP32 cvT (split precision): B arrives as FP32 (hi, lo) pairs made once
 // per system from the FP64 factor / duals (b = hi + lo to 48 bits); both
 // are multiplied with a and the FP32 partial sums are flushed into FP64
-// accumulators every 2 * KC terms, so the only FP32-level error left is
-// the rounding of cvT itself.
+// accumulators every 4 * KC terms (GB300's FP64 pipe is ~1/64 of FP32, so
+// the flush rate is kept low), leaving the rounding of cvT and the FP32
+// summation of 128-term partials as the FP32-level errors.
 #pragma once
 #include "spi_common.cuh"
 
@@ -148,7 +149,7 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
             acc[c][r] = fmaf(a[c], bl[r], acc[c][r]);
           }
       }
-      if (chunk & 1) {
+      if ((chunk & 3) == 3) {
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
 #pragma unroll
