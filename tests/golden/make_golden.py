@@ -20,6 +20,9 @@ and writes small seeded cases to tests/golden/*.npz:
                 installed, so its few lines of bookkeeping are restated here)
 - nebs.npz      SpInterpNeighborGrouping.get_neb_idxs_and_grps for 'nrst' and
                 'pie' (interp/grps.py:103-288, cyth sel_equidist_refs)
+- fitter.npz    variograms/vgs.py Variogram: empirical variogram (pairs,
+                clipping, equal-count bins, robust estimator), the objective,
+                and whole fits with numpy's global RNG seeded
 """
 import sys
 from pathlib import Path
@@ -28,7 +31,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
-from refharness import load_reference, make_steps  # noqa: E402
+from refharness import load_reference, load_variogram, make_steps  # noqa: E402
 
 VG_STRS = [
     "0.05 Nug(0.0) + 0.95 Exp(20000)",
@@ -305,6 +308,73 @@ def nebs_case(ref, out):
         out[f"n_{tag}_grp"] = lab
 
 
+def fitter_case(ref_root, out):
+    """variograms/vgs.py: empirical variogram, objective and fit, with the
+    settings FitVariogramsSteps passes (variograms/fitvgs.py:187-206) and the
+    reference test driver's choices (test/test_fitvgs.py:125-131: mdr 0.7,
+    perm_r_list [1, 2], fit_vgs Sph/Exp, nugget 'Nug', n_best 1) and nk 50
+    (variograms/vgsinput.py:207). DE draws from numpy's global RNG (the
+    reference passes no seed), so seeding it makes the fit reproducible."""
+    vgs_mod = load_variogram(ref_root)
+    rng = np.random.default_rng(66)
+    cases = []
+    for ci, (n, vg, box) in enumerate(((40, "0.1 Nug(0.0) + 0.9 Exp(15000)", 6e4),
+                                       (90, "0.2 Nug(0.0) + 1.3 Sph(40000)", 1.2e5),
+                                       (150, "1.0 Gau(20000)", 1e5))):
+        x, y = rng.uniform(0, box, n), rng.uniform(0, box, n)
+        d = np.hypot(x[:, None] - x[None], y[:, None] - y[None])
+        # covariance of the generating model (semivariogram -> covariance)
+        comps = [(float(p.split()[0]), p.split()[1].split("(")[0], float(p.split("(")[1][:-1]))
+                 for p in (q.strip() for q in vg.split("+"))]
+        cov = np.zeros_like(d)
+        for s, name, r in comps:
+            if name == "Nug":
+                cov += s * (d == 0)
+            elif name == "Exp":
+                cov += s * np.exp(-3 * d / r)
+            elif name == "Gau":
+                cov += s * np.exp(-3 * (d / r) ** 2)
+            elif name == "Sph":
+                t = np.minimum(d / r, 1.0)
+                cov += s * (1 - 1.5 * t + 0.5 * t ** 3)
+        z = np.linalg.cholesky(cov + 1e-8 * np.eye(n)) @ rng.standard_normal(n)
+        v = vgs_mod.Variogram(x=x, y=y, z=z, mdr=0.7, nk=50, typ="var", perm_r_list=[1, 2],
+                              fil_nug_vg="Nug", ld=None, uh=None, h_itrs=100,
+                              opt_meth="L-BFGS-B", opt_iters=10000, fit_vgs=["Sph", "Exp"],
+                              n_best=1, evg_name="robust", use_wts=False, ngp=5,
+                              fit_thresh=0.01)
+        v._max_dist_est()
+        v._vg_var_raw()
+        out[f"f{ci}_x"], out[f"f{ci}_y"], out[f"f{ci}_z"] = x, y, z
+        out[f"f{ci}_h"] = v.vg_h_arr.copy()
+        out[f"f{ci}_g"] = v.vg_vg_arr.copy()
+        out[f"f{ci}_np"] = v.pairs_no.copy()
+        out[f"f{ci}_maxd"] = np.array(v.max_dist)
+        # objective at a few parameter sets
+        prm = np.array([[v.vg_h_arr[0], v.vg_vg_arr[0], 2e4, 0.7],
+                        [v.vg_h_arr[0], v.vg_vg_arr[0], 5e4, 1.2]])
+        objs = []
+        for p4 in prm:
+            objs.append(v._vg_calib(p4[2:], ("Sph", v.sph_vg)))
+            objs.append(v._vg_calib(p4[2:], ("Exp", v.exp_vg)))
+            objs.append(v._vg_calib(p4, ("Nug", v.nug_vg), ("Exp", v.exp_vg)))
+        out[f"f{ci}_prm"] = prm
+        out[f"f{ci}_obj"] = np.array(objs)
+        # a full fit with numpy's global RNG seeded
+        v2 = vgs_mod.Variogram(x=x, y=y, z=z, mdr=0.7, nk=50, typ="var", perm_r_list=[1, 2],
+                               fil_nug_vg="Nug", ld=None, uh=None, h_itrs=100,
+                               opt_meth="L-BFGS-B", opt_iters=10000, fit_vgs=["Sph", "Exp"],
+                               n_best=1, evg_name="robust", use_wts=False, ngp=5,
+                               fit_thresh=0.01)
+        np.random.seed(1000 + ci)
+        v2.fit()
+        out[f"f{ci}_vgstr"] = np.array(v2.vg_str_list)
+        out[f"f{ci}_bestobj"] = np.array(v2.n_best_objs)
+        out[f"f{ci}_bestprm"] = np.array(v2.best_vg_params[-1])
+        cases.append(ci)
+    out["f_cases"] = np.array(cases)
+
+
 def main(ref_root="/root/reference"):
     ref = load_reference(ref_root)
     out = {}
@@ -344,6 +414,9 @@ def main(ref_root="/root/reference"):
     out = {}
     nebs_case(ref, out)
     np.savez_compressed(HERE / "nebs.npz", **out)
+    out = {}
+    fitter_case(ref_root, out)
+    np.savez_compressed(HERE / "fitter.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

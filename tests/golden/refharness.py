@@ -109,3 +109,80 @@ def make_steps(ref, *, min_vg_val, est_vars, intrp_dtype="float32",
     obj._min_var_cut = min_var_cut
     obj._max_var_cut = max_var_cut
     return obj
+
+
+class _Column:
+    """Column view of the stand-in DataFrame."""
+
+    def __init__(self, frame, i):
+        self._f, self._i = frame, i
+
+    @property
+    def values(self):
+        return self._f._a[:, self._i]
+
+    def replace(self, old, new, inplace=False):
+        col = self._f._a[:, self._i]
+        col[col == old] = new
+
+
+class MiniDataFrame:
+    """The few pandas.DataFrame operations variograms/vgs.py performs
+    (construction, column views, sort_values with numpy's quicksort as pandas
+    does, column assignment, dropna, values, shape), on one float array. The
+    in-place replace through a column (vgs.py:654) takes effect, as it did in
+    the pandas 1.x releases contemporary with the reference."""
+
+    def __init__(self, data=None, columns=None):
+        import numpy as np
+        if isinstance(data, dict):
+            self._cols = list(data)
+            self._a = np.column_stack([np.asarray(data[c], dtype=float) for c in data])
+        else:
+            self._cols = list(columns)
+            self._a = np.array(data, dtype=float).reshape(-1, len(self._cols))
+
+    def __getitem__(self, k):
+        return _Column(self, self._cols.index(k))
+
+    def __setitem__(self, k, v):
+        self._a[:, self._cols.index(k)] = v
+
+    @property
+    def values(self):
+        return self._a
+
+    @property
+    def shape(self):
+        return self._a.shape
+
+    def sort_values(self, by, inplace=False):
+        import numpy as np
+        order = np.argsort(self._a[:, self._cols.index(by[0])], kind="quicksort")
+        self._a = self._a[order]
+
+    def dropna(self, inplace=False):
+        import numpy as np
+        self._a = self._a[~np.isnan(self._a).any(axis=1)]
+
+
+def load_variogram(ref_root="/root/reference"):
+    """The reference's Variogram class (variograms/vgs.py) with the stand-in
+    DataFrame in place of pandas."""
+    import importlib.util
+    ref_root = Path(ref_root)
+    pd = sys.modules.get("pandas")
+    if pd is None or not hasattr(pd, "__version__"):
+        pd = _stub("pandas")
+    saved = getattr(pd, "DataFrame", None)
+    pd.DataFrame = MiniDataFrame
+    try:
+        spec = importlib.util.spec_from_file_location(
+            "spinterps_variograms_vgs", str(ref_root / "variograms" / "vgs.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+    finally:
+        if saved is not None:
+            pd.DataFrame = saved
+    mod.DataFrame = MiniDataFrame
+    return mod
