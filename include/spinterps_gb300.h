@@ -266,6 +266,69 @@ int spi_fill_rows(int32_t n_rows, const int32_t *row, const double *v,
                   const double *vv, int64_t n_cells, const spi_out_t *out,
                   spi_stream_t stream);
 
+/* ---- variogram fitting --------------------------------------------------
+ *
+ * Replaces variograms/vgs.py (Variogram, with the settings of
+ * variograms/fitvgs.py:187-206) for a batch of steps. Points of step s are
+ * at pt_off[s] .. pt_off[s+1] of x, y, z (the stations with a value). */
+
+/* Workspace of spi_vg_empirical (device arrays): pd, pp, sd sized for all
+ * pairs of the batch (sum of n_s (n_s - 1) / 2), bcnt, bstart, bcur for all
+ * buckets (sum of bucket counts); bcnt must be zero on entry. */
+typedef struct {
+    double *pd;       /* pair distances, pair order */
+    int32_t *pp;      /* pair indices sorted by distance */
+    double *sd;       /* sorted distances */
+    int32_t *bcnt, *bstart, *bcur;
+} spi_vg_emp_ws_t;
+
+/* Empirical variograms (vgs.py:311-391, 495-520, 597-659 with a numeric
+ * mdr): all pairs i > j, sorted by distance, cut at mdr * max distance,
+ * bins of nk consecutive pairs with their mean distance, the robust
+ * (Cressie-Hawkins) estimate and the pair count. pair_off / bkt_off [n+1]
+ * are the per-step offsets of pairs and distance buckets, dmax[s] an upper
+ * bound of step s's pair distances, max_pairs / max_buckets the largest
+ * per-step counts. Outputs at bin_off[s] (room for ceil(pairs / nk) bins):
+ * bin_h, bin_g, bin_n; n_bins[s] bins used, max_dist[s] = mdr * max
+ * distance. */
+int spi_vg_empirical(int32_t n_steps, const int64_t *pt_off, const double *x, const double *y,
+                     const double *z, const int64_t *pair_off, const int64_t *bkt_off,
+                     const double *dmax, int64_t max_pairs, int64_t max_buckets, int32_t nk,
+                     double mdr, const spi_vg_emp_ws_t *ws, const int64_t *bin_off,
+                     double *bin_h, double *bin_g, double *bin_n, int32_t *n_bins,
+                     double *max_dist, spi_stream_t stream);
+
+/* One differential-evolution problem: fit n_comp nested models (codes) to
+ * step `step`'s empirical variogram. Parameters per component are (range,
+ * sill) with the bounds of vgs.py:731-753: Pow (1e-5, 2) x (1e-5, var2);
+ * the nugget placed first in a multi-model permutation fixed at (h_0,
+ * gamma_0) when fixed_first; otherwise (h_0, 1e9) x (1e-5, var2), var2 = 2 *
+ * variance of the step's values. With warm != 0 the initial population is
+ * drawn in [warm_lo, warm_hi] (unit-cube coordinates within the bounds)
+ * instead of the whole box. */
+typedef struct {
+    int32_t step;
+    int32_t n_comp;
+    int32_t code[2];
+    int32_t fixed_first;
+    int32_t warm;
+    double var2;
+    uint64_t seed;
+    double warm_lo[4], warm_hi[4];
+} spi_de_problem_t;
+
+/* Differential evolution (scipy's best1bin scheme, population 50 D^2 for D
+ * parameters, F dithered in [0.5, 1), CR 0.7) for every problem at once,
+ * minimising sum over bins (gamma - model)^2 (vgs.py:661-678, no weights);
+ * stops when std(energies) <= tol |mean(energies)| or after maxiter
+ * generations. best_x [n_prob, 4] (range, sill per component), best_f the
+ * FP64 objective at best_x, n_gen the generations used. n_comp must be 1 or
+ * 2 (NaN results otherwise, and for steps without bins). */
+int spi_vg_de(int32_t n_prob, const spi_de_problem_t *prob, const int64_t *bin_off,
+              const int32_t *n_bins, const double *bin_h, const double *bin_g,
+              int32_t maxiter, double tol, double *best_x, double *best_f, int32_t *n_gen,
+              spi_stream_t stream);
+
 /* ---- allocation-free variant ------------------------------------------ */
 
 /* Limits of spi_krige_ok_noalloc and the size of its static scratch. */

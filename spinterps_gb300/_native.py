@@ -92,6 +92,10 @@ _SIGS = {
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
+    "spi_vg_empirical": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64,
+                         c_i32, c_dbl, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
+    "spi_vg_de": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_dbl, c_ptr, c_ptr, c_ptr,
+                  c_ptr],
     "spi_krige_ok_noalloc": [ctypes.POINTER(DomainT), c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
                              c_i32, c_i32, ctypes.POINTER(OutT), c_ptr],
 }
