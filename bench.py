@@ -354,6 +354,79 @@ def run_profile_case(args):
     print("profile case done")
 
 
+def _cpu_fit_worker(args):
+    os.environ["OMP_NUM_THREADS"] = "1"
+    x, y, z, seed = args
+    from oracle import fitter
+    t0 = time.perf_counter()
+    fitter.fit(x, y, z, seed=seed)
+    return time.perf_counter() - t0
+
+
+def run_fit(args):
+    """Variogram fitting of the workload's 365 steps (the reference's fitvgs
+    settings): plain GPU fit, warm-started GPU fit, CPU oracle sample, and
+    the leave-one-out kriging RMSE of the fitted variograms."""
+    import multiprocessing as mp
+    import torch
+    from spinterps_gb300 import fitvgs, steps, warmstart
+    w = make_workload()
+    pts = fitvgs.step_points(w["sx"], w["sy"], w["z"])
+    T = len(pts)
+    cpu = None
+    if not args.no_cpu:
+        cores = os.cpu_count()
+        jobs = [(pts[k][0], pts[k][1], pts[k][2], k) for k in range(cores)]
+        ctx = mp.get_context("spawn")
+        saved = os.environ.get("OPENBLAS_NUM_THREADS")
+        os.environ["OPENBLAS_NUM_THREADS"] = "1"
+        t0 = time.perf_counter()
+        with ctx.Pool(cores) as pool:
+            secs = pool.map(_cpu_fit_worker, jobs, chunksize=1)
+        wall = time.perf_counter() - t0
+        if saved is None:
+            os.environ.pop("OPENBLAS_NUM_THREADS", None)
+        cpu = {"value": cores / wall, "unit": "fits/s", "cores": cores, "kind": "port",
+               "sample": f"{cores} steps, one per core (oracle fitter: the reference's "
+                         f"algorithm with scipy DE), median {np.median(secs):.1f} s per fit"}
+    mlp = warmstart.WarmStartMLP.load()
+    for _ in range(args.warmup):
+        fitvgs.fit_steps(None, None, None, emp=fitvgs.Empirical(None, None, None,
+                                                                points=pts[:8]).run())
+        warmstart.warm_fit_steps(None, None, None, mlp, points=pts[:8])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain, dp = fitvgs.fit_steps(None, None, None, emp=fitvgs.Empirical(
+        None, None, None, points=pts).run(), seed=1, return_details=True)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    warm, dw = warmstart.warm_fit_steps(None, None, None, mlp, points=pts, seed=1)
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    vg_p = [s[-1] if s else "1.0 Nug(0.0)" for s in plain]
+    vg_w = [s[-1] if s else "1.0 Nug(0.0)" for s in warm]
+    _, r_p = steps.krige_loo(w["sx"], w["sy"], w["z"], vg_p, min_vg_val=1e-4)
+    _, r_w = steps.krige_loo(w["sx"], w["sy"], w["z"], vg_w, min_vg_val=1e-4)
+    ok = np.isfinite(r_p) & np.isfinite(r_w)
+    line = {"metric": "variogram fits/s, learned warm start vs plain fit", "value": T / t_warm,
+            "unit": "fits/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": WORKLOAD + "_fit", "steps": T, "fitter": "mdr 0.7, nk 50, "
+                       "perm_r_list [1, 2], Sph/Exp + Nug, robust, DE tol 0.01"},
+            "plain": {"fits_per_s": T / t_plain, "de_ms": dp["_de_ms"],
+                      "de_member_evals": dp["_de_member_evals"]},
+            "warm": {"fits_per_s": T / t_warm, "de_ms": dw["_de_ms"],
+                     "de_member_evals": dw["_de_member_evals"],
+                     "fallback_steps": len(dw["_fallback_steps"]), "ms": dw["_ms"]},
+            "speedup_wall": t_plain / t_warm,
+            "speedup_de_work": dp["_de_member_evals"] / max(1, dw["_de_member_evals"]),
+            "loo_cv_rmse": {"plain": float(r_p[ok].mean()), "warm": float(r_w[ok].mean()),
+                            "ratio": float(r_w[ok].mean() / r_p[ok].mean()),
+                            "steps": int(ok.sum())},
+            "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -385,12 +458,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--fp64-steps", type=int, default=4)
     ap.add_argument("--slices", type=int, default=5)
+    ap.add_argument("--fit", action="store_true",
+                    help="variogram fitting benchmark (plain vs learned warm start)")
     ap.add_argument("--profile-case", action="store_true",
                     help="run the small case used for ncu full captures and exit")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
+    elif args.fit:
+        run_fit(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -266,6 +266,15 @@ int spi_fill_rows(int32_t n_rows, const int32_t *row, const double *v,
                   const double *vv, int64_t n_cells, const spi_out_t *out,
                   spi_stream_t stream);
 
+/* Leave-one-out cross-validation residuals of every station of every step
+ * of a factored batch (after spi_krige_factor and spi_krige_duals):
+ * resid (layout of the values array) = z_i minus the kriging estimate at
+ * station i from the other stations, in closed form, w_hat_i / (P11)_ii.
+ * Route-0 systems only (NaN elsewhere). Cross-validation itself has no
+ * counterpart in the reference's step engine; it judges fitted variograms. */
+int spi_krige_loo(const spi_domain_t *dom, const spi_systems_t *sys,
+                  const spi_krige_ws_t *ws, double *resid, spi_stream_t stream);
+
 /* ---- variogram fitting --------------------------------------------------
  *
  * Replaces variograms/vgs.py (Variogram, with the settings of
@@ -328,6 +337,42 @@ int spi_vg_de(int32_t n_prob, const spi_de_problem_t *prob, const int64_t *bin_o
               const int32_t *n_bins, const double *bin_h, const double *bin_g,
               int32_t maxiter, double tol, double *best_x, double *best_f, int32_t *n_gen,
               spi_stream_t stream);
+
+/* ---- learned warm start of the fitter ----------------------------------
+ *
+ * No counterpart in the reference: an MLP proposes each step's model
+ * permutation and parameters so that the fitter's differential evolution
+ * starts from a narrow box instead of the whole one (see spi_de_problem_t).
+ * Device arrays, FP32. Network in -> h1 -> h2 -> out, tanh hidden layers,
+ * parameters packed W1[in][h1], b1, W2[h1][h2], b2, W3[h2][out], b3
+ * (spi_mlp_n_params of them); the first n_class outputs are class logits.
+ * ws: B * (h1 + h2 + 2 * out + h2 + h1) floats. */
+
+/* Features of step s (points at pt_off[s]): semivariance in n_bins (<= 64)
+ * equal-width lag bins up to half the bounding-box diagonal, divided by the
+ * variance. feat [n_steps, n_bins]. */
+int spi_vg_features(int32_t n_steps, const int64_t *pt_off, const double *x, const double *y,
+                    const double *z, int32_t n_bins, float *feat, spi_stream_t stream);
+
+int64_t spi_mlp_n_params(int32_t in, int32_t h1, int32_t h2, int32_t out);
+
+/* O [B, out] = network(X [B, in]). */
+int spi_mlp_forward(int32_t in, int32_t h1, int32_t h2, int32_t out, int32_t n_class,
+                    const float *params, const float *X, int32_t B, float *ws, float *O,
+                    spi_stream_t stream);
+
+/* Batch loss and gradient: loss[b] (summing to the batch mean of softmax
+ * cross-entropy on the class cls[b] plus wp/2 * sum_k mask (o_k - yp_k)^2
+ * over the out - n_class regression outputs) and grad [n_params]. */
+int spi_mlp_grad(int32_t in, int32_t h1, int32_t h2, int32_t out, int32_t n_class,
+                 const float *params, const float *X, const int32_t *cls, const float *yp,
+                 const float *mask, float wp, int32_t B, float *ws, float *grad, float *loss,
+                 spi_stream_t stream);
+
+/* One Adam step (bias-corrected, step number t >= 1) over n_par parameters. */
+int spi_mlp_adam(float *params, const float *grad, float *m, float *v, int64_t n_par,
+                 float lr, float beta1, float beta2, float eps, int32_t t,
+                 spi_stream_t stream);
 
 /* ---- allocation-free variant ------------------------------------------ */
 

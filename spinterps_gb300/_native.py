@@ -92,16 +92,25 @@ _SIGS = {
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
+    "spi_krige_loo": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
+                      ctypes.POINTER(KrigeWsT), c_ptr, c_ptr],
     "spi_vg_empirical": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64,
                          c_i32, c_dbl, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
     "spi_vg_de": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_dbl, c_ptr, c_ptr, c_ptr,
                   c_ptr],
+    "spi_vg_features": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr],
+    "spi_mlp_forward": [c_i32, c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_i32, c_ptr, c_ptr,
+                        c_ptr],
+    "spi_mlp_grad": [c_i32, c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                     ctypes.c_float, c_i32, c_ptr, c_ptr, c_ptr, c_ptr],
+    "spi_mlp_adam": [c_ptr, c_ptr, c_ptr, c_ptr, c_i64, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, ctypes.c_float, c_i32, c_ptr],
     "spi_krige_ok_noalloc": [ctypes.POINTER(DomainT), c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
                              c_i32, c_i32, ctypes.POINTER(OutT), c_ptr],
 }
 
 # every entry point the header declares (checked by the CPU tests)
-EXPORTS = sorted(list(_SIGS) + ["spi_version"])
+EXPORTS = sorted(list(_SIGS) + ["spi_version", "spi_mlp_n_params"])
 
 _lib = None
 _lock = threading.Lock()
@@ -124,6 +133,8 @@ def load(path=LIB_PATH):
             fn.restype = ctypes.c_int
         lib.spi_version.restype = ctypes.c_char_p
         lib.spi_version.argtypes = []
+        lib.spi_mlp_n_params.restype = c_i64
+        lib.spi_mlp_n_params.argtypes = [c_i32, c_i32, c_i32, c_i32]
         _lib = lib
         return lib
 

@@ -592,9 +592,50 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
   }
 }
 
+// Leave-one-out cross-validation residuals of every station of every step
+// (closed form): with P11 = A^-1 - G S^-1 G' the top-left block of the
+// inverse saddle matrix, z_i - (kriged value at station i from the others)
+// = (P11 z)_i / (P11)_ii = w_hat_i / (|Linv[:, i]|^2 - g_i' S^-1 g_i).
+// Equal to solving the n leave-one-out systems of the reference's
+// formulation one by one (interp/steps.py:170-435 with station i left out)
+// whenever its pinv is the inverse. Route-0 systems only; others get NaN.
+__global__ __launch_bounds__(FT) void k_loo(spi_domain_t dom, spi_systems_t sys,
+                                           spi_krige_ws_t ws, double* __restrict__ resid) {
+  const int s = blockIdx.x;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  const bool ok = ws.route[s] == 0;
+  const int sk = sys.kind == SPI_KIND_SK;
+  const int a = sk ? 0 : extra_rows(sys.kind, dom.n_drift);
+  extern __shared__ double dg[];  // [n] diagonal of P11
+  const double* X = ws.linv_arena + v.moff;
+  const double* G = ws.g_cols + v.off * GA;
+  const double* Si = ws.s_inv + (int64_t)s * GA * GA;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double d = 0.0;
+    if (ok) {
+      for (int k = i; k < n; ++k) {
+        double x = X[(int64_t)k * n + i];
+        d += x * x;
+      }
+      for (int p = 0; p < a; ++p)
+        for (int q = 0; q < a; ++q) d -= G[(int64_t)p * n + i] * Si[p * GA + q] * G[(int64_t)q * n + i];
+    }
+    dg[i] = d;
+  }
+  __syncthreads();
+  for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1]; ++si) {
+    const int64_t vo = sys.val_off[sys.steps[si]];
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      resid[vo + i] = ok ? ws.w_hat[vo + i] / dg[i] : __longlong_as_double(0x7ff8000000000000LL);
+  }
+}
+
 }  // namespace spi
 
 using namespace spi;
+
+
 
 static int check_sys(const spi_domain_t* dom, const spi_systems_t* sys) {
   if (!dom || !sys) return SPI_ERR_ARG;
@@ -662,6 +703,24 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
       return SPI_ERR_CUDA;
   }
   k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+extern "C" int spi_krige_loo(const spi_domain_t* dom, const spi_systems_t* sys,
+                             const spi_krige_ws_t* ws, double* resid, spi_stream_t stream) {
+  int rc = check_sys(dom, sys);
+  if (rc) return rc;
+  if (sys->n_sys == 0) return SPI_OK;
+  if ((rc = check_ws(ws))) return rc;
+  if (!resid) return SPI_ERR_ARG;
+  size_t smem = (size_t)sys->max_n * sizeof(double);
+  if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_loo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return SPI_ERR_CUDA;
+  k_loo<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, resid);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

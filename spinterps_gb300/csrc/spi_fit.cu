@@ -22,6 +22,19 @@
 
 namespace spi {
 
+// x^4 rounded once, as the correctly rounded pow of the host libm that the
+// reference's ``** 4`` calls: x^2 = p + e and p^2 = hi + lo are exact
+// (Dekker's product by FMA), x^4 = hi + (lo + 2pe) with the e^2 term below
+// 2^-104 relative, and the final add rounds the exact two-term sum.
+__device__ __forceinline__ double pow4_rn(double x) {
+  const double p = __dmul_rn(x, x);
+  const double e = __fma_rn(x, x, -p);
+  const double hi = __dmul_rn(p, p);
+  double lo = __fma_rn(p, p, -hi);
+  lo = __fma_rn(__dmul_rn(2.0, p), e, lo);
+  return __dadd_rn(hi, lo);
+}
+
 // numpy's pairwise sum (the reduction numpy.sum / numpy.mean use) for
 // n <= 128 contiguous values: plain loop below 8, else 8 strided partial
 // sums combined ((r0+r1)+(r2+r3))+((r4+r5)+(r6+r7)), then the tail.
@@ -250,7 +263,7 @@ __global__ void k_vg_bins(VgEmpArgs A) {
       pair_ij(pp[a0 + k], &i, &j);
       return __dsqrt_rn(fabs(__dsub_rn(A.z[po + i], A.z[po + j])));
     });
-    double e = pow(__ddiv_rn(sq, (double)cnt), 4.0);
+    double e = pow4_rn(__ddiv_rn(sq, (double)cnt));
     e = __ddiv_rn(__ddiv_rn(e, __dadd_rn(0.457, __ddiv_rn(0.494, (double)cnt))), 2.0);
     A.bin_h[bo + m] = __ddiv_rn(h, (double)cnt);
     A.bin_g[bo + m] = e;

@@ -58,33 +58,45 @@ def perm_list(fit_vgs, perm_r_list, fil_nug_vg):
     return out
 
 
+def step_points(stn_x, stn_y, data, drop_zeros=False, min_vld_stns=1):
+    """Per step, the (x, y, z) of the stations with a value, as
+    FitVariogramsSteps selects them (variograms/fitvgs.py:149-184); steps
+    that get no variogram map to None."""
+    data = np.asarray(data, dtype=np.float64)
+    stn_x = np.asarray(stn_x, dtype=np.float64)
+    stn_y = np.asarray(stn_y, dtype=np.float64)
+    pts = []
+    for t in range(data.shape[0]):
+        idx = np.where(np.isfinite(data[t]))[0]
+        z = data[t, idx]
+        if drop_zeros:
+            keep = z != 0
+            idx, z = idx[keep], z[keep]
+        if idx.size < max(min_vld_stns, 2) or np.isclose(z.std(), 0.0):
+            pts.append(None)
+            continue
+        pts.append((stn_x[idx], stn_y[idx], z))
+    return pts
+
+
 class Empirical:
     """Device-resident empirical variograms of a batch of steps."""
 
     def __init__(self, stn_x, stn_y, data, *, nk=50, mdr=0.7, drop_zeros=False,
-                 min_vld_stns=1, device="cuda"):
+                 min_vld_stns=1, device="cuda", points=None):
         dev = self.dev = _require_cuda(device)
-        data = np.asarray(data, dtype=np.float64)
-        stn_x = np.asarray(stn_x, dtype=np.float64)
-        stn_y = np.asarray(stn_y, dtype=np.float64)
-        self.T = data.shape[0]
+        if points is None:
+            points = step_points(stn_x, stn_y, data, drop_zeros, min_vld_stns)
+        self.T = len(points)
         self.nk, self.mdr = int(nk), float(mdr)
         steps, xs, ys, zs, var2 = [], [], [], [], []
-        for t in range(self.T):
-            idx = np.where(np.isfinite(data[t]))[0]
-            if idx.size < min_vld_stns:
+        for t, p in enumerate(points):
+            if p is None:
                 continue
-            z = data[t, idx]
-            if drop_zeros:
-                keep = z != 0
-                idx, z = idx[keep], z[keep]
-                if idx.size < min_vld_stns:
-                    continue
-            if idx.size < 2 or np.isclose(z.std(), 0.0):
-                continue
+            x, y, z = (np.asarray(a, dtype=np.float64) for a in p)
             steps.append(t)
-            xs.append(stn_x[idx])
-            ys.append(stn_y[idx])
+            xs.append(x)
+            ys.append(y)
             zs.append(z)
             var2.append(2 * np.var(z))
         self.steps = np.array(steps, dtype=np.int64)
@@ -145,15 +157,18 @@ class Empirical:
 
 def fit_steps(stn_x, stn_y, data, *, nk=50, mdr=0.7, perm_r_list=(1, 2), fil_nug_vg="Nug",
               fit_vgs=("Sph", "Exp"), n_best=1, opt_iters=10000, tol=0.01, fit_thresh=0.01,
-              drop_zeros=False, min_vld_stns=1, seed=0, warm=None, device="cuda",
-              return_details=False):
+              drop_zeros=False, min_vld_stns=1, seed=0, warm=None, step_perms=None,
+              emp=None, device="cuda", return_details=False):
     """Fit every step's variogram. Returns a list (one per step) of the
     n_best variogram strings, best last (None where the reference fits
     nothing). ``warm``: optional {(step, perm tuple): (lo[4], hi[4])} initial
-    population boxes in unit-cube coordinates (the learned warm start)."""
-    emp = Empirical(stn_x, stn_y, data, nk=nk, mdr=mdr, drop_zeros=drop_zeros,
-                    min_vld_stns=min_vld_stns, device=device).run()
-    T = np.asarray(data).shape[0]
+    population boxes in unit-cube coordinates; ``step_perms``: optional
+    {step: [perm tuples]} to fit only those permutations of a step (both for
+    the learned warm start); ``emp``: an already computed Empirical."""
+    if emp is None:
+        emp = Empirical(stn_x, stn_y, data, nk=nk, mdr=mdr, drop_zeros=drop_zeros,
+                        min_vld_stns=min_vld_stns, device=device).run()
+    T = emp.T
     out = [None] * T
     details = {}
     if emp.S == 0:
@@ -161,9 +176,12 @@ def fit_steps(stn_x, stn_y, data, *, nk=50, mdr=0.7, perm_r_list=(1, 2), fil_nug
     perms = perm_list(fit_vgs, perm_r_list, fil_nug_vg)
     if any(len(o) > 2 for o in perms):
         raise ValueError("the GPU fitter fits at most two nested components (perm_r_list <= 2)")
-    probs = []
+    probs, plist = [], []
     for k in range(emp.S):
-        for pi, o in enumerate(perms):
+        sp = perms if step_perms is None else step_perms.get(int(emp.steps[k]), perms)
+        plist.append(sp)
+        for o in sp:
+            pi = perms.index(o)
             p = DeProblem()
             p.step = k
             p.n_comp = len(o)
@@ -183,18 +201,26 @@ def fit_steps(stn_x, stn_y, data, *, nk=50, mdr=0.7, perm_r_list=(1, 2), fil_nug
     best_x = torch.zeros((len(probs), 4), dtype=torch.float64, device=emp.dev)
     best_f = torch.zeros(len(probs), dtype=torch.float64, device=emp.dev)
     n_gen = torch.zeros(len(probs), dtype=torch.int32, device=emp.dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
     nat.call("spi_vg_de", len(probs), _ptr(d_prob), _ptr(emp.d_bin_off), _ptr(emp.n_bins),
              _ptr(emp.bin_h), _ptr(emp.bin_g), int(opt_iters), float(tol), _ptr(best_x),
              _ptr(best_f), _ptr(n_gen), _stream())
+    ev1.record()
     bx = best_x.cpu().numpy()
     bf = best_f.cpu().numpy()
     ng = n_gen.cpu().numpy()
+    details["_de_ms"] = ev0.elapsed_time(ev1)
+    details["_de_problems"] = len(probs)
+    details["_de_member_evals"] = int(sum(50 * (2 * p.n_comp) ** 2 * int(g_)
+                                          for p, g_ in zip(probs, ng)))
     q = 0
     for k in range(emp.S):
         tot_pts = int(emp.n_pts[k])
         min_obj = np.inf
         best_names, best_params, best_objs, skip = [], [], [], []
-        for o in perms:
+        sp = plist[k]
+        for o in sp:
             x, f = bx[q], bf[q]
             q += 1
             if o in skip:
@@ -229,8 +255,6 @@ def fit_steps(stn_x, stn_y, data, *, nk=50, mdr=0.7, perm_r_list=(1, 2), fil_nug
         out[t] = strs
         details[t] = {"aic": best_objs, "params": best_params[-1] if best_params else None,
                       "names": best_names[-1] if best_names else None,
-                      "objective": {perms[i]: float(bf[q - len(perms) + i])
-                                    for i in range(len(perms))},
-                      "generations": {perms[i]: int(ng[q - len(perms) + i])
-                                      for i in range(len(perms))}}
+                      "objective": {sp[i]: float(bf[q - len(sp) + i]) for i in range(len(sp))},
+                      "generations": {sp[i]: int(ng[q - len(sp) + i]) for i in range(len(sp))}}
     return (out, details) if return_details else out

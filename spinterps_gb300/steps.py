@@ -512,3 +512,47 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
     if return_info:
         return flds, plan.prblm, plan.collect_info()
     return flds, plan.prblm
+
+
+def krige_loo(stn_x, stn_y, data, vgs, *, min_vg_val=0.0, device="cuda", cond_max=1e13):
+    """Leave-one-out cross-validation of ordinary kriging per step.
+
+    Returns (residuals, rmse): residuals[t] is z minus the kriging estimate
+    at each present station of step t from the other stations (closed form
+    from the step's FP64 factorisation, spi_krige_loo), rmse[t] their root
+    mean square (NaN for steps with fewer than three stations, a nugget-only
+    variogram, or a system off the Cholesky path)."""
+    dev = _require_cuda(device)
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    T = data.shape[0]
+    avail = np.isfinite(data)
+    sx = np.asarray(stn_x, dtype=np.float64)
+    dom = _Domain(dev, stn_x, stn_y, sx[:1], np.asarray(stn_y, dtype=np.float64)[:1], None,
+                  None, min_vg_val, 0)
+    systems = []
+    for t in range(T):
+        idx = np.where(avail[t])[0]
+        if idx.size < 3 or check_full_nuggetness(vgs[t], min_vg_val):
+            continue
+        systems.append((idx, vgs[t], [t]))
+    res = [None] * T
+    rmse = np.full(T, np.nan)
+    val_off = np.zeros(T, dtype=np.int64)
+    beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
+    for ch in _chunk_systems(systems, 0, 8 << 30):
+        b = _KrigeBatch(dev, dom, "OK", systems, ch, data, T, val_off, beta, 0)
+        s = _stream()
+        ws = ctypes.byref(b.ws)
+        nat.call("spi_krige_factor", ctypes.byref(dom.st), ctypes.byref(b.sy), ws,
+                 float(cond_max), s)
+        nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(b.sy), _ptr(b.vals),
+                 ws, s)
+        r = torch.empty_like(b.vals)
+        nat.call("spi_krige_loo", ctypes.byref(dom.st), ctypes.byref(b.sy), ws, _ptr(r), s)
+        r = r.cpu().numpy()
+        for i in ch:
+            idx, _, (t,) = systems[i]
+            e = r[val_off[t]:val_off[t] + idx.size]
+            res[t] = e
+            rmse[t] = float(np.sqrt(np.mean(e * e)))
+    return res, rmse

@@ -19,7 +19,7 @@ def declared_symbols():
     names = set()
     for h in (ROOT / "include").glob("*.h"):
         txt = h.read_text()
-        names.update(re.findall(r"^(?:int|const char \*)\s*(spi_\w+)\s*\(", txt, re.M))
+        names.update(re.findall(r"^(?:int|int64_t|const char \*)\s*(spi_\w+)\s*\(", txt, re.M))
     return sorted(names)
 
 
