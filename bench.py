@@ -427,6 +427,88 @@ def run_fit(args):
     print(json.dumps(line))
 
 
+def run_large(args):
+    """The large hourly EDK configuration on one wave of steps: 4000
+    stations in a 500 km box, per-station missingness U(0.05, 0.5), two
+    drifts (fBm elevation, easting), a 2000 x 2000 grid at 250 m, float32
+    fields; each step's variogram from the learned warm start with cold-fit
+    fallback (timed apart). Mixed and plain FP64 paths run the same plan;
+    the line reports both, their ratio and the mixed path's error."""
+    import torch
+    from spinterps_gb300 import fitvgs, synth, warmstart
+    from spinterps_gb300.steps import InterpPlan
+    from oracle.port import interp_args_for  # the (type, dir, label) list only
+    T = args.large_steps
+    t0 = time.perf_counter()
+    w = synth.large_edk(n_steps=T)
+    t_gen = time.perf_counter() - t0
+    pts = fitvgs.step_points(w["sx"], w["sy"], w["z"])
+    mlp = warmstart.WarmStartMLP.load()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    strs, det = warmstart.warm_fit_steps(None, None, None, mlp, points=pts, seed=1)
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    vgs = [s[-1] if s else "1.0 Nug(0.0)" for s in strs]
+    iargs = interp_args_for(["EDK"], est_vars=False)
+    C = w["cx"].size
+    kw = dict(stn_drifts=w["stn_drift"], cell_drifts=w["cell_drift"], min_vg_val=1e-4,
+              intrp_dtype=np.float32, arena_budget=96 << 30)
+
+    def timed(plan, reps):
+        evs, tot = [], 0.0
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record()
+            ev = plan.execute(timing=True)
+            b.record()
+            torch.cuda.synchronize()
+            tot += a.elapsed_time(b)
+            evs.append(ev)
+        cells_ms = sum(x.elapsed_time(y) for ev in evs for (x, y), _ in ev["krige_cells"])
+        return tot / reps, cells_ms / reps
+
+    pm = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], vgs, iargs, precision="mixed",
+                    **kw)
+    pm.execute()
+    with Clocks(0) as clk:
+        ms_m, cells_m = timed(pm, args.steps)
+    info = pm.collect_info()
+    cond = np.array(list(info["cond"]["EDK"].values()))
+    fm = pm.flds["EDK"]
+    n_fast = int(np.sum(cond <= pm.cond_split))
+    del pm
+    torch.cuda.empty_cache()
+    p64 = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], vgs, iargs, precision="fp64",
+                     **kw)
+    ms_64, cells_64 = timed(p64, 1)
+    f64 = p64.flds["EDK"]
+    m = torch.isfinite(f64)
+    sc = f64[m].double().abs().max()
+    dd = (fm[m].double() - f64[m].double()).abs()
+    err = {"max": float(dd.max() / sc), "rms": float(dd.pow(2).mean().sqrt() / sc)}
+    n_av = np.isfinite(w["z"]).sum(1)
+    line = {"metric": METRIC, "value": T * C / (ms_m / 1e3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "higher_is_better": True, "dtype": "f32+f64",
+            "data": "synthetic (seeded; shapes and distributions of the reference's large hourly "
+                    "configuration)",
+            "config": {"workload": f"large_edk_4000stn_{T}of8760steps_2000x2000", "stations": 4000,
+                       "steps": T, "cells": C, "methods": ["EDK (elevation, easting)"],
+                       "stations_per_step": [int(n_av.min()), int(n_av.max())],
+                       "output": "float32", "vgs": "learned warm start, cold-fit fallback"},
+            "ms_per_execution": ms_m, "cells_kernel_ms": cells_m,
+            "fp64_path": {"value": T * C / (ms_64 / 1e3), "unit": UNIT, "ms": ms_64,
+                          "cells_kernel_ms": cells_64},
+            "mixed_over_fp64": ms_64 / ms_m, "mixed_err_vs_fp64": err,
+            "tiers": {"fp32": n_fast, "fp64": int(cond.size - n_fast),
+                      "cond_median": float(np.median(cond)), "cond_max": float(cond.max())},
+            "fit": {"seconds": t_fit, "fallback_steps": len(det["_fallback_steps"]),
+                    "de_ms": det["_de_ms"], "ms": det["_ms"]},
+            "synthesis_s": t_gen, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -463,11 +545,16 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="run the small case used for ncu full captures and exit")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--large", action="store_true",
+                    help="the large hourly EDK configuration (one wave of steps) instead")
+    ap.add_argument("--large-steps", type=int, default=152)
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
     elif args.fit:
         run_fit(args)
+    elif args.large:
+        run_large(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

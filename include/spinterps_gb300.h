@@ -338,6 +338,19 @@ int spi_vg_de(int32_t n_prob, const spi_de_problem_t *prob, const int64_t *bin_o
               int32_t maxiter, double tol, double *best_x, double *best_f, int32_t *n_gen,
               spi_stream_t stream);
 
+/* Refined proposal of each problem's permutation (one free structure: X,
+ * or Nug fixed at (h_0, gamma_0) + X; NaN for others and for steps without
+ * bins): the least-squares sill (closed form, clipped to (1e-5, var2)) at
+ * each range of a log grid over [r0 / span, r0 * span] (within (h_0,
+ * 1e9)), refined by golden section. x [n_prob, 4] in spi_vg_de's layout, f
+ * the objective there, noise the bins' scatter sum of squares
+ * nb/(nb-1) * sum((g[i+1] - g[i])^2) / 2. No counterpart in the reference:
+ * part of the learned warm start. */
+int spi_vg_refine(int32_t n_prob, const spi_de_problem_t *prob, const int64_t *bin_off,
+                  const int32_t *n_bins, const double *bin_h, const double *bin_g,
+                  const double *r0, double span, double *x, double *f, double *noise,
+                  spi_stream_t stream);
+
 /* ---- learned warm start of the fitter ----------------------------------
  *
  * No counterpart in the reference: an MLP proposes each step's model

@@ -21,47 +21,10 @@
 // pair, FP32 partial sums flushed to FP64 every 64 terms), FP64 epilogue.
 #include "spi_common.cuh"
 #include "spi_contract.cuh"
+#include "spi_rhs.cuh"
+#include "spi_cells.cuh"
 
 namespace spi {
-
-constexpr int GA = SPI_MAX_DRIFT + 1;
-
-struct CellsArgs {
-  spi_domain_t dom;
-  spi_systems_t sys;
-  spi_krige_ws_t ws;
-  const double* vals;
-  int want_var;
-  int route_filter;
-  double cond_split;
-  spi_out_t out;
-};
-
-// Exact (FP64, reference-ordered) nearest station of a cell among a
-// system's stations: first index of the minimum distance, as np.argmin.
-__device__ int nnb_f64_warp(const spi_domain_t& dom, const int32_t* idx, int n, double cx,
-                            double cy) {
-  const int lane = threadIdx.x & 31;
-  double best = __longlong_as_double(0x7ff0000000000000LL);
-  int bj = 0x7fffffff;
-  for (int j = lane; j < n; j += 32) {
-    int st = idx[j];
-    double d = dist_f64(cx, cy, dom.stn_x[st], dom.stn_y[st]);
-    if (d < best) {
-      best = d;
-      bj = j;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    double ob = __shfl_xor_sync(0xffffffffu, best, o);
-    int oj = __shfl_xor_sync(0xffffffffu, bj, o);
-    if (ob < best || (ob == best && oj < bj)) {
-      best = ob;
-      bj = oj;
-    }
-  }
-  return bj == 0x7fffffff ? 0 : bj;
-}
 
 template <typename T, int TC, bool W>
 __device__ __forceinline__ void contract(const T* cvT, T* Bs, const double* const* vp64,
@@ -98,7 +61,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   // Lagrange / drift rows; on the Cholesky path SK contracts one dual
   // column (u = A^-1 1) in the same slot
   const int a = sk ? 1 : extra_rows(A.sys.kind, A.dom.n_drift);
-  const int ndual = prim ? 1 : a;             // dual columns contracted per cell
+  // dual columns contracted per cell; the FP32 tier adds SK's |u| column
+  // (a rounding bound for its sum check)
+  const int ndual = prim ? 1 : ((sk && sizeof(T) == 4) ? 2 : a);
   const int tid = threadIdx.x;
   const int64_t st0 = A.sys.step_off[s], st1 = A.sys.step_off[s + 1];
   const int nsteps = (int)(st1 - st0);
@@ -118,6 +83,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   const float** vpl = vph + VB;                                         // [VB]
   __shared__ int any_bad;
   __shared__ int any_ok;
+  __shared__ int any_chk;
 
   // vector v of the next pass: FP64 base + off, or its FP32 hi / lo copies
   auto setv = [&](int v, const double* b64, const float* bh, const float* bl, int64_t off,
@@ -134,6 +100,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   if (tid == 0) {
     any_bad = failed ? 1 : 0;
     any_ok = 0;
+    any_chk = 0;
   }
   for (int e = tid; e < TC * GA; e += CT) qc[e] = 0.0;
 
@@ -147,12 +114,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
         const double cx = live ? A.dom.cell_x[gc] : 0.0, cy = live ? A.dom.cell_y[gc] : 0.0;
         for (int j = jg; j < npad; j += njg) {
           double v = 0.0;
-          if (live && j < n) {
-            int st = idx[j];
-            double d = dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
-            double g = vg_fill_f64(vg, d, sk, A.dom.min_vg_val);
-            v = (sk || prim) ? g : __dsub_rn(sh, g);
-          }
+          if (live && j < n) v = rhs_f64(A.dom, vg, sk, prim, sh, cx, cy, idx[j]);
           if (prim && live && j >= n && j < n + a) {
             const int k = j - n;  // r = [gamma, 1, drifts] rows of the saddle system
             v = (k == 0) ? 1.0 : A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
@@ -162,31 +124,14 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       } else {
         const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
                                : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float mvv = (float)A.dom.min_vg_val;
-        const float shf = (float)sh;
-        float rr[SPI_MAX_VG_COMP], ss[SPI_MAX_VG_COMP];
-        for (int c = 0; c < vg.n_comp; ++c) {
-          rr[c] = (float)vg.range[c];
-          ss[c] = (float)vg.sill[c];
-        }
+        RhsF32 kf;
+        kf.init(vg, sk, sh, A.dom.min_vg_val);
         const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
         for (int j = jg; j < npad; j += njg) {
           float v = 0.f;
           if (live && j < n) {
-            const float4 sp = sp4[idx[j]];
-            // double-float difference: accurate relative to the distance
-            float dx = (cp.x - sp.x) + (cp.y - sp.y);
-            float dy = (cp.z - sp.z) + (cp.w - sp.w);
-            float d = sqrtf(dx * dx + dy * dy);
-            // covariance directly (no s - gamma cancellation); the
-            // reference's zeroing of gamma <= min_vg_val (OK/EDK) or of
-            // the covariance <= min_vg_val (SK) applied to it
-            float cdir = 0.f;
-            for (int c = 0; c < vg.n_comp; ++c) cdir += cov_eval_f32(vg.code[c], d, rr[c], ss[c]);
-            if (sk)
-              v = cdir <= mvv ? 0.f : cdir;
-            else
-              v = (shf - cdir <= mvv) ? shf : cdir;
+            const int st = idx[j];
+            v = rhs_f32(A.dom, vg, kf, sk, sh, cp, sp4[st], gc, st);
           }
           cvT[(int64_t)j * TC + cell] = (T)v;
         }
@@ -265,10 +210,35 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
         vv = sh * sl - yy + nu[0] * q[0] - 2.0 * nu[0];
       }
       int ok = isclose_one(sl) ? 1 : 0;
+      // SK's sum(lambda) varies from cell to cell: where the FP32 value
+      // is within its rounding bound of the check's boundary, the FP64
+      // value decides (otherwise estimate and nearest station can swap)
+      if (sizeof(T) == 4 && sk && gc < C &&
+          near_isclose_boundary(sl, kSumLambdaRelErr * q[1])) {
+        ok = 2;
+        atomicOr(&any_chk, 1);
+      }
       okf[cell] = ok;
-      cvar[cell] = ok ? vv : 0.0;
+      cvar[cell] = ok == 1 ? vv : 0.0;
       if (!ok && gc < C) atomicOr(&any_bad, 1);
-      if (ok && gc < C) atomicOr(&any_ok, 1);
+      if (ok == 1 && gc < C) atomicOr(&any_ok, 1);
+    }
+    __syncthreads();
+    if constexpr (sizeof(T) == 4) {
+      if (any_chk) {
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int cell = warp; cell < TC; cell += CT / 32) {
+          if (okf[cell] != 2) continue;
+          const int64_t gc = c0 + cell;
+          const double sl = sk_sum_lambda_f64(A.dom, vg, idx, n, A.ws.g_cols + soff * GA,
+                                              A.dom.cell_x[gc], A.dom.cell_y[gc]);
+          if (lane == 0) {
+            const int ok = isclose_one(sl) ? 1 : 0;
+            okf[cell] = ok;
+            atomicOr(ok ? &any_ok : &any_bad, 1);
+          }
+        }
+      }
     }
     // ---- 4b. exact-inverse path, OK variance of the cells that pass the
     // check: lambda = P r, var = lambda'r + lambda_n, wide passes over P's
@@ -429,13 +399,16 @@ static int pick_tc(int max_n) {
   return 0;
 }
 
+// Systems whose right-hand-side tile does not fit in shared memory take the
+// streamed kernel (estimates only; the OK variance needs the stored tile).
 template <typename T, typename OutT>
 static int dispatch_cells(const CellsArgs& A, cudaStream_t st) {
   int tc = pick_tc<T>(A.sys.max_n);
   if (tc == 64) return launch_cells<T, 64, OutT>(A, st);
   if (tc == 32) return launch_cells<T, 32, OutT>(A, st);
   if (tc == 16) return launch_cells<T, 16, OutT>(A, st);
-  return SPI_ERR_TOO_LARGE;
+  if (A.want_var && A.sys.kind != SPI_KIND_SK) return SPI_ERR_TOO_LARGE;
+  return launch_cells_stream(A, sizeof(T) == 8 ? 0 : 1, st);
 }
 
 __global__ void k_split_f64(const double* __restrict__ x, float* __restrict__ hi,

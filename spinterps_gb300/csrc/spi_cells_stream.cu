@@ -1,0 +1,266 @@
+// Kriging estimates over all cells for systems too large for the
+// shared-memory right-hand side of k_krige_cells (n stations x a cell tile
+// beyond 227 KB: n > ~1600 in FP64, ~3500 in FP32), e.g. thousands of
+// stations with external drifts. Estimates only: the right-hand side of a
+// cell is used once per pass, so it is generated on the fly, never stored.
+//
+// Layout: one CTA = 32 cells x 8 warps. A lane owns a cell; the 8 warps
+// split the system's stations (warp w takes stations w, w + 8, ...). Each
+// lane generates its cell's entry for the warp's station (coordinates and
+// station data are warp-uniform broadcast loads) and accumulates it against
+// up to 4 vectors: the system's dual columns (Lagrange / drift rows, for
+// the sum check of interp/steps.py:419) and the steps' dual weights. The 8
+// partial sums per cell are reduced in shared memory; more steps than fit
+// in one pass regenerate the right-hand side. Precision as k_krige_cells:
+// FP64 throughout, or FP32 entries against FP32 hi/lo vector pairs with
+// FP32 partials flushed to FP64 every 128 terms.
+#include "spi_cells.cuh"
+#include "spi_rhs.cuh"
+
+namespace spi {
+
+constexpr int STC = 32;  // cells per CTA (one per lane)
+constexpr int SNW = 8;   // warps per CTA (station groups)
+constexpr int SSV = 4;   // vectors per pass
+
+template <typename T, typename OutT>
+__global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A) {
+  const int s = blockIdx.y;
+  const int64_t C = A.dom.n_cells;
+  const int64_t c0 = (int64_t)blockIdx.x * STC;
+  if (c0 >= C) return;
+  const int route = A.ws.route[s];
+  {
+    const bool fast = route == 0 && A.ws.cond[s] <= A.cond_split;
+    if ((A.route_filter == 1 && !fast) || (A.route_filter == 2 && fast)) return;
+  }
+  const bool prim = route == 1;
+  const bool failed = route == 2;
+  const int64_t soff = A.sys.stn_off[s];
+  const int n = (int)(A.sys.stn_off[s + 1] - soff);
+  const int32_t* idx = A.sys.stn_idx + soff;
+  const int sk = A.sys.kind == SPI_KIND_SK;
+  const int a = sk ? 1 : extra_rows(A.sys.kind, A.dom.n_drift);
+  const int ndual = prim ? 1 : ((sk && sizeof(T) == 4) ? 2 : a);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t st0 = A.sys.step_off[s];
+  const int nsteps = (int)(A.sys.step_off[s + 1] - st0);
+  const int nvec = ndual + nsteps;
+  const spi_vg_t vg = A.sys.vg[s];
+  const double sh = A.ws.shift[s];
+
+  __shared__ double red[SNW][SSV][STC];
+  __shared__ double vres[SSV][STC];
+  __shared__ int okf[STC], nnb[STC];
+  __shared__ const double* vp64[SSV];
+  __shared__ const float* vph[SSV];
+  __shared__ const float* vpl[SSV];
+  __shared__ int any_bad;
+  __shared__ int any_chk;
+
+  const int64_t gc = c0 + lane;
+  const bool live = gc < C;
+  OutT* est_out = reinterpret_cast<OutT*>(A.out.est);
+  auto emit = [&](int cell, int vstep, double accv) {
+    const int64_t g = c0 + cell;
+    if (g >= C) return;
+    const int j = A.sys.steps[st0 + vstep];
+    const int64_t row = A.sys.out_row[j];
+    double e;
+    if (okf[cell]) {
+      e = accv;
+      if (!sk) {
+        const double* bt = A.ws.beta + (int64_t)j * GA;
+        e += bt[0];
+        for (int k = 1; k < a; ++k) e += bt[k] * A.dom.cell_drift[(int64_t)(k - 1) * C + g];
+      }
+    } else {
+      e = A.vals[A.sys.val_off[j] + nnb[cell]];
+    }
+    est_out[row * C + g] = cast_out<OutT>(clip_est(e, A.out));
+  };
+  auto nearest = [&]() {
+    __syncthreads();
+    if (any_bad)
+      for (int cell = warp; cell < STC; cell += SNW) {
+        const int64_t g = c0 + cell;
+        if (g >= C || okf[cell]) continue;
+        const int j = nnb_f64_warp(A.dom, idx, n, A.dom.cell_x[g], A.dom.cell_y[g]);
+        if (lane == 0) nnb[cell] = j;
+      }
+    __syncthreads();
+  };
+
+  if (failed) {
+    if (tid < STC) okf[tid] = 0;
+    if (tid == 0) any_bad = 1;
+    nearest();
+    for (int e = tid; e < nsteps * STC; e += STC * SNW) emit(e % STC, e / STC, 0.0);
+    return;
+  }
+
+  double cx = 0.0, cy = 0.0;
+  float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
+  RhsF32 kf;
+  if constexpr (sizeof(T) == 8) {
+    if (live) {
+      cx = A.dom.cell_x[gc];
+      cy = A.dom.cell_y[gc];
+    }
+  } else {
+    if (live) cp = reinterpret_cast<const float4*>(A.dom.cell_split)[gc];
+    kf.init(vg, sk, sh, A.dom.min_vg_val);
+  }
+  const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
+
+  for (int v0 = 0; v0 < nvec; v0 += SSV) {
+    const int nv = min(SSV, nvec - v0);
+    __syncthreads();
+    if (tid < SSV) {
+      const int v = v0 + tid;
+      const double* p64 = nullptr;
+      const float *ph = nullptr, *pl = nullptr;
+      if (tid < nv) {
+        int64_t off;
+        if (v < ndual) {
+          off = soff * GA + (int64_t)v * n;
+          p64 = A.ws.g_cols + off;
+          if (A.ws.g_hi) ph = A.ws.g_hi + off, pl = A.ws.g_lo + off;
+        } else {
+          off = A.sys.val_off[A.sys.steps[st0 + (v - ndual)]];
+          p64 = A.ws.w_hat + off;
+          if (A.ws.w_hi) ph = A.ws.w_hi + off, pl = A.ws.w_lo + off;
+        }
+      }
+      vp64[tid] = p64;
+      vph[tid] = ph;
+      vpl[tid] = pl;
+    }
+    __syncthreads();
+    double acc[SSV];
+#pragma unroll
+    for (int v = 0; v < SSV; ++v) acc[v] = 0.0;
+    if constexpr (sizeof(T) == 8) {
+      for (int j = warp; j < n; j += SNW) {
+        const int st = idx[j];
+        const double c = live ? rhs_f64(A.dom, vg, sk, prim, sh, cx, cy, st) : 0.0;
+#pragma unroll
+        for (int v = 0; v < SSV; ++v)
+          if (v < nv) acc[v] = fma(c, vp64[v][j], acc[v]);
+      }
+    } else {
+      float ph[SSV], pl[SSV];
+#pragma unroll
+      for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
+      int cnt = 0;
+      for (int j = warp; j < n; j += SNW) {
+        const int st = idx[j];
+        const float c = live ? rhs_f32(A.dom, vg, kf, sk, sh, cp, sp4[st], gc, st) : 0.f;
+#pragma unroll
+        for (int v = 0; v < SSV; ++v)
+          if (v < nv) {
+            ph[v] = fmaf(c, vph[v][j], ph[v]);
+            pl[v] = fmaf(c, vpl[v][j], pl[v]);
+          }
+        if (++cnt == 128) {
+          cnt = 0;
+#pragma unroll
+          for (int v = 0; v < SSV; ++v) {
+            acc[v] += (double)ph[v] + (double)pl[v];
+            ph[v] = pl[v] = 0.f;
+          }
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < SSV; ++v) acc[v] += (double)ph[v] + (double)pl[v];
+    }
+#pragma unroll
+    for (int v = 0; v < SSV; ++v) red[warp][v][lane] = acc[v];
+    __syncthreads();
+    for (int e = tid; e < nv * STC; e += STC * SNW) {
+      const int v = e / STC, cell = e % STC;
+      double t = 0.0;
+#pragma unroll
+      for (int w = 0; w < SNW; ++w) t += red[w][v][cell];
+      vres[v][cell] = t;
+    }
+    __syncthreads();
+    if (v0 == 0) {
+      // the sum check of every cell, from the dual columns (all in pass 0)
+      if (tid == 0) any_bad = any_chk = 0;
+      __syncthreads();
+      if (tid < STC) {
+        const int cell = tid;
+        const int64_t g = c0 + cell;
+        double q[GA], f[GA], nu[GA];
+        for (int k = 0; k < GA; ++k) q[k] = k < ndual ? vres[k][cell] : 0.0;
+        f[0] = 1.0;
+        for (int k = 1; k < GA; ++k)
+          f[k] = (k < a && g < C && !sk) ? A.dom.cell_drift[(int64_t)(k - 1) * C + g] : 0.0;
+        double sl;
+        if (prim) {
+          sl = q[0];
+          if (!sk)
+            for (int k = 0; k < a; ++k) sl += f[k] * A.ws.g_colsum[(int64_t)s * GA + k];
+        } else if (sk) {
+          sl = q[0];
+        } else {
+          const double* Si = A.ws.s_inv + (int64_t)s * GA * GA;
+          for (int k = 0; k < a; ++k) {
+            double t = 0.0;
+            for (int l = 0; l < a; ++l) t += Si[k * GA + l] * (q[l] - f[l]);
+            nu[k] = t;
+          }
+          sl = q[0];
+          for (int k = 0; k < a; ++k) sl -= A.ws.g_colsum[(int64_t)s * GA + k] * nu[k];
+        }
+        int ok = isclose_one(sl) ? 1 : 0;
+        // SK's FP32 sum(lambda) within its rounding bound of the check's
+        // boundary: decided in FP64 (as k_krige_cells)
+        if (sizeof(T) == 4 && sk && g < C &&
+            near_isclose_boundary(sl, kSumLambdaRelErr * q[1])) {
+          ok = 2;
+          atomicOr(&any_chk, 1);
+        }
+        okf[cell] = ok;
+        if (!ok && g < C) atomicOr(&any_bad, 1);
+      }
+      __syncthreads();
+      if (any_chk)
+        for (int cell = warp; cell < STC; cell += SNW) {
+          if (okf[cell] != 2) continue;
+          const int64_t g = c0 + cell;
+          const double sl = sk_sum_lambda_f64(A.dom, vg, idx, n, A.ws.g_cols + soff * GA,
+                                              A.dom.cell_x[g], A.dom.cell_y[g]);
+          if (lane == 0) {
+            const int ok = isclose_one(sl) ? 1 : 0;
+            okf[cell] = ok;
+            if (!ok) atomicOr(&any_bad, 1);
+          }
+        }
+      nearest();
+    }
+    for (int e = tid; e < nv * STC; e += STC * SNW) {
+      const int v = v0 + e / STC, cell = e % STC;
+      if (v >= ndual) emit(cell, v - ndual, vres[e / STC][cell]);
+    }
+  }
+}
+
+int launch_cells_stream(const CellsArgs& A, int precision, cudaStream_t st) {
+  const int64_t tiles = (A.dom.n_cells + STC - 1) / STC;
+  if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
+  dim3 grid((unsigned)tiles, (unsigned)A.sys.n_sys);
+  const bool f64 = A.out.out_f64 != 0;
+  if (precision == 0) {
+    if (f64) k_krige_cells_stream<double, double><<<grid, STC * SNW, 0, st>>>(A);
+    else k_krige_cells_stream<double, float><<<grid, STC * SNW, 0, st>>>(A);
+  } else {
+    if (f64) k_krige_cells_stream<float, double><<<grid, STC * SNW, 0, st>>>(A);
+    else k_krige_cells_stream<float, float><<<grid, STC * SNW, 0, st>>>(A);
+  }
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+}  // namespace spi

@@ -156,6 +156,12 @@ __device__ __forceinline__ bool isclose_one(double a) {
   return fabs(a - 1.0) <= (1e-8 + 1e-5 * 1.0);
 }
 
+// Whether an FP32-tier sum(lambda) with rounding bound err could fall on
+// the other side of the isclose_one boundary than its FP64 value.
+__device__ __forceinline__ bool near_isclose_boundary(double a, double err) {
+  return fabs(fabs(a - 1.0) - (1e-8 + 1e-5 * 1.0)) <= err;
+}
+
 template <typename T>
 __device__ __forceinline__ T cast_out(double v);
 template <>

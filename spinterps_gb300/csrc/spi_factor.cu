@@ -503,6 +503,13 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
     matvec_lower_t(X, n, vb, G + (int64_t)k * n);
     __syncthreads();
   }
+  // SK: |u| (u = A^-1 1) as a second column. The FP32 cell kernels
+  // contract it to bound the rounding of sum(lambda) = u'c per cell
+  // (covariances are >= 0, so sum |u_i| c_i bounds sum |u_i c_i|).
+  if (sk) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) G[n + i] = fabs(G[i]);
+  }
   // S = F'G
   for (int k = 0; k < a; ++k) {
     for (int i = threadIdx.x; i < n; i += blockDim.x)

@@ -339,6 +339,167 @@ __device__ double fit_model_f64(int code, double h, double r, double s) {
   }
 }
 
+// ---- proposal refinement for the learned warm start (no counterpart in
+// the reference) ----
+// For a permutation with one free structure (X, or Nug fixed at (h_0,
+// gamma_0) + X) the sill is a linear parameter: for a fixed range its
+// least-squares value is sum(rho (g - base)) / sum(rho^2), clipped to the
+// sill bounds. The range is searched on a log grid around the proposal,
+// then refined by golden section on the best bracket.
+constexpr int RF_T = 256;
+constexpr int RF_GRID = 32;
+constexpr int RF_GOLD = 40;
+
+__device__ void block_sum3(double& a, double& b, double& c, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) {
+    red[w * 3] = a;
+    red[w * 3 + 1] = b;
+    red[w * 3 + 2] = c;
+  }
+  __syncthreads();
+  a = b = c = 0.0;
+  for (int k = 0; k < RF_T / 32; ++k) {
+    a += red[k * 3];
+    b += red[k * 3 + 1];
+    c += red[k * 3 + 2];
+  }
+}
+
+__global__ __launch_bounds__(RF_T) void k_vg_refine(int n_prob, const spi_de_problem_t* prob,
+                                                    const int64_t* bin_off, const int32_t* n_bins,
+                                                    const double* bin_h, const double* bin_g,
+                                                    const double* r0, double span, double* out_x,
+                                                    double* out_f, double* noise) {
+  const int p = blockIdx.x;
+  const spi_de_problem_t P = prob[p];
+  const int64_t off = bin_off[P.step];
+  const int nb = n_bins[P.step];
+  const double* h = bin_h + off;
+  const double* g = bin_g + off;
+  __shared__ double red[RF_T / 32 * 3];
+  const int tid = threadIdx.x;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  // bin noise: sum of squares of the scatter, from successive differences
+  double dd = 0.0, u0 = 0.0, u1 = 0.0;
+  for (int i = tid; i + 1 < nb; i += RF_T) {
+    const double t = g[i + 1] - g[i];
+    dd += t * t;
+  }
+  block_sum3(dd, u0, u1, red);
+  const bool fixed = P.fixed_first && P.n_comp == 2;
+  const bool ok = nb > 0 && (P.n_comp == 1 || fixed);
+  if (!ok) {
+    if (tid < 4) out_x[p * 4 + tid] = nan;
+    if (tid == 0) {
+      out_f[p] = nan;
+      noise[p] = nb > 2 ? 0.5 * dd * nb / (nb - 1) : 0.0;
+    }
+    return;
+  }
+  const double h0 = h[0], g0 = g[0];
+  const int code = fixed ? P.code[1] : P.code[0];
+  const double base = fixed ? g0 : 0.0;
+  const double slo = 1e-5, shi = P.var2;
+  // profile objective at log-range u: (objective, sill)
+  auto prof = [&](double u, double& sill) -> double {
+    const double r = exp(u);
+    double srr = 0.0, srg = 0.0, sgg = 0.0;
+    for (int i = tid; i < nb; i += RF_T) {
+      const double rho = code == SPI_VG_NUG ? 1.0 : fit_model_f64(code, h[i], r, 1.0);
+      const double y = g[i] - base;
+      srr += rho * rho;
+      srg += rho * y;
+      sgg += y * y;
+    }
+    block_sum3(srr, srg, sgg, red);
+    double sl = srr > 0.0 ? srg / srr : slo;
+    sl = fmin(fmax(sl, slo), shi);
+    sill = sl;
+    return sgg - 2.0 * sl * srg + sl * sl * srr;
+  };
+  double ulo = log(fmax(h0, 1e-300)), uhi = log(1e9);
+  const double uc = log(fmax(r0[p], 1e-300));
+  if (code != SPI_VG_NUG && isfinite(uc) && span > 1.0) {
+    const double ls = log(span);
+    const double a = fmax(ulo, uc - ls), b = fmin(uhi, uc + ls);
+    if (a < b) {
+      ulo = a;
+      uhi = b;
+    }
+  }
+  double best_u = ulo, best_f = 1e300, sill = slo;
+  if (code == SPI_VG_NUG) {
+    best_f = prof(ulo, sill);
+  } else {
+    int bk = 0;
+    for (int k = 0; k < RF_GRID; ++k) {
+      const double u = ulo + (uhi - ulo) * k / (RF_GRID - 1);
+      double sl;
+      const double f = prof(u, sl);
+      if (f < best_f) {
+        best_f = f;
+        bk = k;
+      }
+    }
+    // golden section on the bracket around the best grid point
+    const double step = (uhi - ulo) / (RF_GRID - 1);
+    double a = ulo + step * max(bk - 1, 0), b = ulo + step * min(bk + 1, RF_GRID - 1);
+    const double gr = 0.6180339887498949;
+    double c = b - gr * (b - a), d = a + gr * (b - a), sc, sd;
+    double fc = prof(c, sc), fd = prof(d, sd);
+    for (int it = 0; it < RF_GOLD; ++it) {
+      if (fc < fd) {
+        b = d;
+        d = c;
+        fd = fc;
+        c = b - gr * (b - a);
+        fc = prof(c, sc);
+      } else {
+        a = c;
+        c = d;
+        fc = fd;
+        d = a + gr * (b - a);
+        fd = prof(d, sd);
+      }
+    }
+    best_u = 0.5 * (a + b);
+  }
+  const double r = code == SPI_VG_NUG ? h0 : exp(best_u);
+  prof(code == SPI_VG_NUG ? ulo : best_u, sill);
+  // the objective at the result, summed directly (no expansion)
+  double f = 0.0, z0 = 0.0, z1 = 0.0;
+  for (int i = tid; i < nb; i += RF_T) {
+    const double m = base + fit_model_f64(code, h[i], r, sill);
+    const double t = g[i] - m;
+    f += t * t;
+  }
+  block_sum3(f, z0, z1, red);
+  if (tid == 0) {
+    double* x = out_x + p * 4;
+    if (fixed) {
+      x[0] = h0;
+      x[1] = g0;
+      x[2] = r;
+      x[3] = sill;
+    } else {
+      x[0] = r;
+      x[1] = sill;
+      x[2] = 0.0;
+      x[3] = 0.0;
+    }
+    out_f[p] = f;
+    noise[p] = nb > 2 ? 0.5 * dd * nb / (nb - 1) : 0.0;
+  }
+}
+
 constexpr int DE_T = 256;
 constexpr int DE_MAXNP = 800;    // 50 * 4^2
 constexpr int DE_MAXBINS = 16384;   // bins kept in shared memory (more: read from L2)
@@ -624,6 +785,20 @@ extern "C" int spi_vg_de(int32_t n_prob, const spi_de_problem_t* prob, const int
     return SPI_ERR_CUDA;
   DeArgs A{n_prob, prob, bin_off, n_bins, bin_h, bin_g, maxiter, tol, best_x, best_f, n_gen};
   k_de<<<n_prob, DE_T, smem, (cudaStream_t)stream>>>(A);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+extern "C" int spi_vg_refine(int32_t n_prob, const spi_de_problem_t* prob, const int64_t* bin_off,
+                             const int32_t* n_bins, const double* bin_h, const double* bin_g,
+                             const double* r0, double span, double* x, double* f, double* noise,
+                             spi_stream_t stream) {
+  if (n_prob < 0 || !(span >= 1.0)) return SPI_ERR_ARG;
+  if (n_prob == 0) return SPI_OK;
+  if (!prob || !bin_off || !n_bins || !bin_h || !bin_g || !r0 || !x || !f || !noise)
+    return SPI_ERR_ARG;
+  k_vg_refine<<<n_prob, RF_T, 0, (cudaStream_t)stream>>>(n_prob, prob, bin_off, n_bins, bin_h,
+                                                        bin_g, r0, span, x, f, noise);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

@@ -1,9 +1,10 @@
 """Train the fitter's warm-start network (spinterps_gb300.warmstart).
 
 Training data: Gaussian random fields on 300-1500 stations uniform in a
-250 km x 250 km box, each with a random Sph / Exp / Gau model (range
-5-100 km, sill 0.5-2) and, for half of them, a nugget of up to 30% of the
-sill. Each field is fitted by the project's own GPU fitter
+box of 100-400 km (aspect 0.5-1), each with a random Sph / Exp / Gau model
+(range 2-40% of the box, sill 0.5-2) and, for half of them, a nugget of up
+to 30% of the sill; half of the fields are then made precipitation-like
+(zero below a random 20-70% quantile, gamma amounts above it). Each field is fitted by the project's own GPU fitter
 (spinterps_gb300.fitvgs, the reference's fitvgs settings); its choice
 (permutation and parameters) is the label, its 20 lag-bin features the
 input. The network is trained by the kernels of csrc/spi_mlp.cu (FP32 Adam).
@@ -31,17 +32,20 @@ def _cov(typ, d, rng, sill):
     return sill * (1 - 1.5 * t + 0.5 * t ** 3)
 
 
-def synth_points(n_fields, seed=0, box=250e3, n_lo=300, n_hi=1500, device="cuda"):
-    """[(x, y, z)] of n_fields synthetic fields and their generating models."""
+def synth_points(n_fields, seed=0, n_lo=300, n_hi=1500, device="cuda"):
+    """[(x, y, z)] of n_fields synthetic fields and their generating models
+    (type, range, sill, nugget fraction, dry fraction or 0)."""
+    from scipy.stats import gamma, norm
     rng = np.random.default_rng(seed)
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
     pts, models = [], []
     for _ in range(n_fields):
         n = int(rng.integers(n_lo, n_hi + 1))
-        x, y = rng.uniform(0, box, n), rng.uniform(0, box, n)
+        box = rng.uniform(100e3, 400e3)
+        x, y = rng.uniform(0, box, n), rng.uniform(0, box * rng.uniform(0.5, 1.0), n)
         typ = str(rng.choice(["Sph", "Exp", "Gau"]))
-        r = rng.uniform(5e3, 100e3)
+        r = rng.uniform(0.02, 0.4) * box
         sill = rng.uniform(0.5, 2.0)
         nugf = rng.uniform(0.0, 0.3) if rng.uniform() < 0.5 else 0.0
         X = torch.as_tensor(np.stack([x, y], 1), device=device)
@@ -55,9 +59,16 @@ def synth_points(n_fields, seed=0, box=250e3, n_lo=300, n_hi=1500, device="cuda"
                 break
             except RuntimeError:
                 jitter *= 10
-        z = L @ torch.randn(n, generator=gen, device=device, dtype=torch.float64)
-        pts.append((x, y, z.cpu().numpy()))
-        models.append((typ, r, sill, nugf))
+        z = (L @ torch.randn(n, generator=gen, device=device, dtype=torch.float64)).cpu().numpy()
+        dry = 0.0
+        if rng.uniform() < 0.5:
+            # precipitation-like: dry below a quantile, gamma amounts above it
+            dry = rng.uniform(0.2, 0.7)
+            u = norm.cdf(z / np.sqrt(sill))
+            z = np.where(u > dry, gamma.ppf(np.clip((u - dry) / (1 - dry), 1e-12, 1 - 1e-12),
+                                            rng.uniform(0.5, 2.0), scale=2.0), 0.0)
+        pts.append((x, y, z))
+        models.append((typ, r, sill, nugf, dry))
     return pts, models
 
 
@@ -65,6 +76,7 @@ def make_training_set(n_fields, seed=0, chunk=200, device="cuda"):
     """Features and fitter labels of n_fields synthetic fields."""
     perms = default_perms()
     feats, cls, yp, mk = [], [], [], []
+    t0 = time.time()
     for c0 in range(0, n_fields, chunk):
         pts, _ = synth_points(min(chunk, n_fields - c0), seed=seed + c0, device=device)
         emp = Empirical(None, None, None, points=pts, device=device).run()
@@ -75,6 +87,8 @@ def make_training_set(n_fields, seed=0, chunk=200, device="cuda"):
         cls.append(c)
         yp.append(y)
         mk.append(m)
+        print(f"  fields {c0 + len(pts)}/{n_fields} fitted, {time.time() - t0:.1f}s "
+              f"(DE {det['_de_ms'] / 1e3:.1f}s)", flush=True)
     return (np.concatenate(feats), np.concatenate(cls), np.concatenate(yp),
             np.concatenate(mk))
 

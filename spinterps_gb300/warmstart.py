@@ -5,15 +5,24 @@ each model permutation's whole parameter box (variograms/vgs.py:731-764,
 ranges up to 1e9). Here a small MLP (20 -> 128 -> 128 -> logits of the
 permutations + 3 parameters, FP32, trained and evaluated by the kernels of
 csrc/spi_mlp.cu) reads 20 lag-bin features of a step's values and proposes
-the permutation the fitter would choose and its parameters. The fitter then
-fits only the ``topk`` most likely permutations, each from a narrow initial
-box around the proposal (the DE still searches the full bounds), and falls
-back to the plain cold fit of every permutation when the proposal explains
-the empirical variogram poorly (its objective above ``fallback`` times the
-bins' total sum of squares).
+the permutation the fitter would choose and its parameters. Each proposal
+is refined on the GPU (spi_vg_refine: for the proposed permutation's one
+free structure the least-squares sill is closed form at any range, so the
+range is searched within a factor ``span`` of the network's). The fitter
+then fits only the ``topk`` most likely permutations, each from a narrow
+initial box around its refined proposal (the DE still searches the full
+bounds), and falls back to the plain cold fit of every permutation when
+the refined top proposal explains the empirical variogram poorly: its
+objective (the fitter's sum of squared bin residuals) above ``fallback``
+times the bins' noise, the sum of squares that scatter alone leaves,
+estimated from successive bin differences as
+nb/(nb-1) * sum((g[i+1] - g[i])^2) / 2 (bin_noise). A correct model scores
+about 1 on that scale.
 
-Parameters are normalised as (log10(range) - 4, structured sill / variance,
-nugget / variance).
+Parameters are normalised as (log10(range / hmax), structured sill /
+variance, nugget / variance), hmax = half the diagonal of the stations'
+bounding box (the features' lag scale), so the network does not depend on
+the size of the station network's box.
 """
 import ctypes
 import time
@@ -144,9 +153,15 @@ def step_features(points, steps, device="cuda"):
     return feat.cpu().numpy()
 
 
+def lag_scale(x, y):
+    """hmax of the features: half the diagonal of the points' bounding box."""
+    x, y = np.asarray(x, dtype=np.float64), np.asarray(y, dtype=np.float64)
+    return max(0.5 * float(np.hypot(np.ptp(x), np.ptp(y))), 1e-300)
+
+
 def labels(details, points, perms):
     """Training labels from the plain fitter's choices: class = chosen
-    permutation, parameters (log10 range - 4, structured sill / var,
+    permutation, parameters (log10(range / hmax), structured sill / var,
     nugget / var) with a mask of the ones the class has. points: per-step
     (x, y, z) as fitted."""
     cls, yp, mk, keep = [], [], [], []
@@ -158,6 +173,7 @@ def labels(details, points, perms):
             continue
         z = np.asarray(points[t][2])
         var = max(np.var(z), 1e-300)
+        hmax = lag_scale(points[t][0], points[t][1])
         y = np.zeros(N_PAR)
         m = np.zeros(N_PAR)
         for k, name in enumerate(names):
@@ -165,7 +181,7 @@ def labels(details, points, perms):
             if name == "Nug":
                 y[2], m[2] = s / var, 1
             else:
-                y[0], m[0] = np.log10(max(r, 1.0)) - 4.0, 1
+                y[0], m[0] = np.log10(max(r, 1e-300) / hmax), 1
                 y[1], m[1] = s / var, 1
         cls.append(perms.index(names))
         yp.append(y)
@@ -179,94 +195,99 @@ def _unit(v, lo, hi):
     return float(np.clip((v - lo) / (hi - lo), 0.0, 1.0)) if hi > lo else 0.0
 
 
-def _model(name, h, r, s):
-    """The fitter's models (variograms/vgs.py:553-595), arg (range, sill)."""
-    if name == "Nug":
-        return np.full(h.shape, s)
-    if name == "Exp":
-        return s * (1 - np.exp(-3 * (h / r)))
-    if name == "Gau":
-        return s * (1 - np.exp(-3 * (h / r) ** 2))
-    if name == "Sph":
-        out = s * (1.5 * h / r - h ** 3 / (2 * r ** 3))
-        out[h > r] = s
-        return out
-    if name == "Lin":
-        out = s * (h / r)
-        out[h > r] = s
-        return out
-    raise ValueError(name)
+def bin_noise(g):
+    """Sum of squares of the bins' scatter about a smooth curve, from
+    successive differences (a smooth trend adds only second-order terms)."""
+    g = np.asarray(g, dtype=np.float64)
+    nb = g.size
+    if nb < 3:
+        return 0.0
+    return 0.5 * float(np.sum(np.diff(g) ** 2)) * nb / (nb - 1)
 
 
-def _proposal(o, h0, g0, var, rng, ssill, nug, fil_nug_vg="Nug"):
-    """(range, sill) per component of permutation o for the proposal."""
-    prm = []
-    for k, name in enumerate(o):
-        if len(o) > 1 and k == 0 and name == fil_nug_vg:
-            prm.append((h0, g0))
-        elif name == "Nug":
-            prm.append((h0, ssill + nug))
-        else:
-            prm.append((rng, ssill))
-    return prm
-
-
-def warm_fit_steps(stn_x, stn_y, data, mlp, *, topk=1, fallback=0.5, range_fac=1.6,
-                   sill_fac=0.3, seed=0, opt_iters=10000, tol=0.01, nk=50, mdr=0.7,
+def warm_fit_steps(stn_x, stn_y, data, mlp, *, topk=1, fallback=4.0, span=4.0, range_fac=1.25,
+                   sill_fac=0.1, seed=0, opt_iters=10000, tol=0.01, nk=50, mdr=0.7,
                    device="cuda", points=None):
-    """Warm-started fit: the MLP's top-k permutations from narrow initial
-    boxes, the plain cold fit of all permutations where the proposal's
-    objective exceeds ``fallback`` times the bins' total sum of squares.
+    """Warm-started fit. Per step: the MLP's top-k permutations, each with its
+    proposal refined on the GPU (spi_vg_refine: least-squares sill, range
+    searched within a factor ``span`` of the network's), then the fitter's
+    differential evolution from a box of ``range_fac`` / ``sill_fac`` around
+    it. Steps whose refined top proposal has an objective above ``fallback``
+    times the bins' noise get the plain cold fit of every permutation.
     Returns (strings per step, details) like fit_steps, with
-    details["_fallback_steps"] and details["_ms"] (features, network, DE)."""
+    details["_fallback_steps"] and details["_ms"] (features + network +
+    refinement, DE, wall)."""
     from .fitvgs import step_points
     t0 = time.perf_counter()
     if points is None:
         points = step_points(stn_x, stn_y, data)
     emp = Empirical(None, None, None, nk=nk, mdr=mdr, device=device, points=points).run()
     steps = [int(s) for s in emp.steps]
+    S = len(steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     feat = step_features(points, steps, device=device)
     O = mlp.forward(feat)
-    e1.record()
     logits, pr = O[:, :mlp.n_class], O[:, mlp.n_class:]
-    warm, step_perms, fall = {}, {}, []
+    order = np.argsort(-logits, axis=1)[:, :topk]
+    probs, r0 = [], []
     for k, t in enumerate(steps):
-        h, g, _ = emp.bins(k)
-        var = emp.var2[k] / 2
-        lo_r, hi_r, lo_s, hi_s = h[0], 1e9, 1e-5, 2 * var
-        order = [int(i) for i in np.argsort(-logits[k])[:topk]]
-        rng = 10 ** (float(pr[k, 0]) + 4.0)
-        ssill = max(float(pr[k, 1]), 1e-6) * var
-        nug = max(float(pr[k, 2]), 0.0) * var
-        o = mlp.perms[order[0]]
-        prm = _proposal(o, h[0], g[0], var, rng, ssill, nug)
-        model = sum(_model(name, h, r, s) for name, (r, s) in zip(o, prm))
-        obj = np.sum((g - model) ** 2)
-        tss = np.sum((g - g.mean()) ** 2)
-        if not (obj <= fallback * tss):
+        hmax = lag_scale(points[t][0], points[t][1])
+        for i in order[k]:
+            o = mlp.perms[int(i)]
+            p = DeProblem()
+            p.step = k
+            p.n_comp = len(o)
+            for c, name in enumerate(o):
+                p.code[c] = CODES[name]
+            p.fixed_first = 1 if (len(o) > 1 and o[0] == "Nug") else 0
+            p.var2 = float(emp.var2[k])
+            probs.append(p)
+            r0.append(10 ** float(pr[k, 0]) * hmax)
+    raw = bytes((DeProblem * len(probs))(*probs))
+    d_prob = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(emp.dev)
+    d_r0 = torch.as_tensor(np.array(r0, dtype=np.float64), device=emp.dev)
+    P = len(probs)
+    x = torch.empty((P, 4), dtype=torch.float64, device=emp.dev)
+    f = torch.empty(P, dtype=torch.float64, device=emp.dev)
+    nz = torch.empty(P, dtype=torch.float64, device=emp.dev)
+    nat.call("spi_vg_refine", P, _ptr(d_prob), _ptr(emp.d_bin_off), _ptr(emp.n_bins),
+             _ptr(emp.bin_h), _ptr(emp.bin_g), _ptr(d_r0), float(span), _ptr(x), _ptr(f),
+             _ptr(nz), _stream())
+    e1.record()
+    x, f, nz = x.cpu().numpy(), f.cpu().numpy(), nz.cpu().numpy()
+    h0 = emp.bin_h[emp.d_bin_off[:S]].cpu().numpy() if S else np.zeros(0)
+    warm, step_perms, fall = {}, {}, []
+    q = 0
+    for k, t in enumerate(steps):
+        q0 = q
+        q += topk
+        if not (f[q0] <= fallback * nz[q0]):
             fall.append(t)
             continue
-        step_perms[t] = [mlp.perms[i] for i in order]
-        for i in order:
-            oi = mlp.perms[i]
+        step_perms[t] = [mlp.perms[int(i)] for i in order[k]]
+        var2 = float(emp.var2[k])
+        for j, i in enumerate(order[k]):
+            oi = mlp.perms[int(i)]
+            xi = x[q0 + j]
+            if not np.all(np.isfinite(xi)):
+                continue
             lo, hi = np.zeros(4), np.ones(4)
-            for c, ((r, sl), name) in enumerate(zip(_proposal(oi, h[0], g[0], var, rng, ssill,
-                                                              nug), oi)):
-                if len(oi) > 1 and c == 0 and name == "Nug":
+            for c in range(len(oi)):
+                if len(oi) > 1 and c == 0 and oi[0] == "Nug":
                     continue
-                if name != "Nug":
-                    lo[2 * c] = _unit(r / range_fac, lo_r, hi_r)
-                    hi[2 * c] = _unit(r * range_fac, lo_r, hi_r)
-                lo[2 * c + 1] = _unit(sl * (1 - sill_fac), lo_s, hi_s)
-                hi[2 * c + 1] = _unit(sl * (1 + sill_fac), lo_s, hi_s)
+                r, sl = xi[2 * c], xi[2 * c + 1]
+                if oi[c] != "Nug":
+                    lo[2 * c] = _unit(r / range_fac, h0[k], 1e9)
+                    hi[2 * c] = _unit(r * range_fac, h0[k], 1e9)
+                lo[2 * c + 1] = _unit(sl * (1 - sill_fac), 1e-5, var2)
+                hi[2 * c + 1] = _unit(sl * (1 + sill_fac), 1e-5, var2)
             warm[(t, oi)] = (lo, hi)
     out, det = fit_steps(stn_x, stn_y, data, seed=seed, warm=warm, step_perms=step_perms,
                          emp=emp, opt_iters=opt_iters, tol=tol, device=device,
                          return_details=True)
     torch.cuda.synchronize()
     det["_fallback_steps"] = fall
-    det["_ms"] = {"features_and_network": e0.elapsed_time(e1), "de": det["_de_ms"],
+    det["_ms"] = {"features_network_refine": e0.elapsed_time(e1), "de": det["_de_ms"],
                   "wall": (time.perf_counter() - t0) * 1e3}
     return out, det

@@ -229,3 +229,52 @@ def test_float32_fields_and_clipping():
         assert got[lab].dtype == np.float32
         assert _err(got[lab], ref[lab]) <= F32_TOL, lab
     assert np.nanmin(got["OK"]) >= 0.5 and np.nanmax(got["OK"]) <= 3.0
+
+
+def test_mixed_zeroes_the_same_entries_at_the_cut():
+    """SK zeroes covariances <= min_vg_val (OK: semivariances). Cells are
+    placed within 1e-9 relative of that cut from every station, so FP32
+    arithmetic alone would zero a different set of entries than FP64 and
+    miss by min_vg_val * |w_i|; the mixed path must agree with the oracle."""
+    spi = _spi()
+    rng = np.random.default_rng(21)
+    n, mvv, r = 40, 1e-3, 10000.0
+    sx, sy = rng.uniform(0, 2e4, n), rng.uniform(0, 2e4, n)
+    z = rng.gamma(1.2, 2.0, size=(3, n))
+    dcut = -np.log(mvv) * r / 3.0  # exp(-3 d / r) == mvv
+    k = np.repeat(np.arange(n), 50)
+    ang = rng.uniform(0, 2 * np.pi, k.size)
+    d = dcut * (1 + rng.uniform(-1e-9, 1e-9, k.size))
+    cx, cy = sx[k] + d * np.cos(ang), sy[k] + d * np.sin(ang)
+    vgs = ["1.0 Exp(10000.0)"] * 3
+    args = port.interp_args_for(["SK", "OK"], est_vars=True)
+    kw = dict(est_vars=True, min_vg_val=mvv, intrp_dtype=np.float64)
+    ref, _ = port.interp_steps(sx, sy, z, cx, cy, vgs, args, **kw)
+    got, _, info = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, precision="mixed",
+                                    return_info=True, **kw)
+    assert max(info["cond"]["SK"].values()) <= 1e7  # the FP32 tier ran
+    for lab in ref:
+        assert _err(got[lab], ref[lab]) <= MIXED_TOL, lab
+
+
+def test_mixed_vs_fp64_on_the_batched_workload():
+    """The bench's batched workload (1000 stations, per-step missingness and
+    variograms, zero-inflated values), 4 steps incl. a Gaussian one, a
+    quarter of the grid: every mixed field within 1e-5 of the FP64 GPU path.
+    SK cells whose sum of weights sits at the check's boundary are the
+    delicate case (estimate vs nearest station)."""
+    import bench
+    spi = _spi()
+    w = bench.make_workload()
+    steps = [0, 4, 150, 300]
+    cells = np.arange(0, w["cx"].size, 4)
+    args = bench.interp_args()
+    kw = dict(bench.KW)
+    z = w["z"][steps]
+    vgs = [w["vgs"][s] for s in steps]
+    f64, _ = spi.interp_steps(w["sx"], w["sy"], z, w["cx"][cells], w["cy"][cells], vgs, args,
+                              **kw)
+    mixed, _ = spi.interp_steps(w["sx"], w["sy"], z, w["cx"][cells], w["cy"][cells], vgs, args,
+                                precision="mixed", **kw)
+    for lab in f64:
+        assert _err(mixed[lab], f64[lab]) <= MIXED_TOL, lab

@@ -101,3 +101,62 @@ def test_trained_warm_start_gain():
     assert ok.sum() >= 20
     assert r_warm[ok].mean() <= 1.01 * r_plain[ok].mean(), (r_warm[ok].mean(),
                                                              r_plain[ok].mean())
+
+
+def test_refine_matches_dense_search():
+    """spi_vg_refine against a dense CPU search of the same profile (4000
+    log-ranges, closed-form clipped sill, the oracle's objective): the GPU
+    result is at least as good, its reported objective is the oracle's at
+    its parameters, and its noise is bin_noise of the bins."""
+    import ctypes
+    from spinterps_gb300 import _native as nat
+    from spinterps_gb300 import fitvgs, warmstart
+    from spinterps_gb300.steps import _ptr, _stream
+    from spinterps_gb300.train_warmstart import synth_points
+    from oracle import fitter
+    pts, _ = synth_points(3, seed=77, n_lo=300, n_hi=500)
+    emp = fitvgs.Empirical(None, None, None, points=pts).run()
+    perms = [("Sph",), ("Exp",), ("Nug", "Sph"), ("Nug", "Exp"), ("Nug",)]
+    probs, r0, keys = [], [], []
+    for k in range(emp.S):
+        for o in perms:
+            p = fitvgs.DeProblem()
+            p.step, p.n_comp = k, len(o)
+            for c, name in enumerate(o):
+                p.code[c] = fitvgs.CODES[name]
+            p.fixed_first = 1 if len(o) > 1 else 0
+            p.var2 = float(emp.var2[k])
+            probs.append(p)
+            r0.append(20e3)
+            keys.append((k, o))
+    raw = bytes((fitvgs.DeProblem * len(probs))(*probs))
+    dev = torch.device("cuda")
+    d_prob = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(dev)
+    d_r0 = torch.as_tensor(np.array(r0), device=dev)
+    P = len(probs)
+    x = torch.empty((P, 4), dtype=torch.float64, device=dev)
+    f = torch.empty(P, dtype=torch.float64, device=dev)
+    nz = torch.empty(P, dtype=torch.float64, device=dev)
+    nat.call("spi_vg_refine", P, _ptr(d_prob), _ptr(emp.d_bin_off), _ptr(emp.n_bins),
+             _ptr(emp.bin_h), _ptr(emp.bin_g), _ptr(d_r0), 4.0, _ptr(x), _ptr(f), _ptr(nz),
+             _stream())
+    x, f, nz = x.cpu().numpy(), f.cpu().numpy(), nz.cpu().numpy()
+    for q, (k, o) in enumerate(keys):
+        h, g, _ = emp.bins(k)
+        var2 = float(emp.var2[k])
+        assert abs(nz[q] - warmstart.bin_noise(g)) <= 1e-12 * warmstart.bin_noise(g)
+        names = list(o)
+        xo = x[q, :2 * len(o)]
+        assert abs(f[q] - fitter.objective(xo, names, h, g)) <= 1e-9 * max(f[q], 1e-300)
+        if o == ("Nug",):
+            best = fitter.objective(np.array([h[0], np.clip(g.mean(), 1e-5, var2)]), names, h, g)
+        else:
+            best = np.inf
+            base = g[0] if len(o) > 1 else 0.0
+            for r in np.exp(np.linspace(np.log(max(5e3, h[0])), np.log(80e3), 4000)):
+                rho = np.asarray(fitter.MODELS[o[-1]](h, (r, 1.0)), dtype=np.float64)
+                y = g - base
+                sl = np.clip(np.dot(rho, y) / np.dot(rho, rho), 1e-5, var2)
+                arg = (np.array([h[0], g[0], r, sl]) if len(o) > 1 else np.array([r, sl]))
+                best = min(best, fitter.objective(arg, names, h, g))
+        assert f[q] <= best * (1 + 1e-6) + 1e-12, (k, o, f[q], best)
