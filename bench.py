@@ -190,6 +190,37 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------- GPU side
+# The cell kernels' ceilings. The measured peaks cover HBM and the bf16
+# tensor pipe; the CUDA-core pipes are nominal (152 SMs at 2.07 GHz: FP32 128
+# FMA/clk/SM, FP64 1/64 of that).
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+FP64_NOMINAL_TFLOPS = FP32_NOMINAL_TFLOPS / 64
+KERNEL_BOUND = {
+    "var_tc": ("tensor", "spi::k_var_tc (tcgen05 3xTF32 OK-variance contraction)"),
+    "cells_fp32": ("fp32", "spi::k_krige_cells<float> (FP32 tier: estimates, sum check)"),
+    "cells_fp64": ("fp64", "spi::k_krige_cells<double> (FP64 tier: ill-conditioned and "
+                           "routed systems, the plain path's kernel)"),
+    "idw": ("fp32", "spi::k_idw"),
+}
+
+
+def roofline_for(name, k):
+    bf16, hbm, src = measured_peaks()
+    bound, kernel = KERNEL_BOUND[name]
+    if bound == "tensor":
+        peak, psrc = bf16, src + " (bf16 dense; the kernel runs 3 TF32 MMAs per product)"
+    elif bound == "fp64":
+        peak, psrc = FP64_NOMINAL_TFLOPS, "nominal FP64 pipe (not in MEASURED_PEAKS.json)"
+    else:
+        peak, psrc = FP32_NOMINAL_TFLOPS, "nominal FP32 pipe (not in MEASURED_PEAKS.json)"
+    a = k["achieved_tflops"]
+    return {"bound": bound, "kernel": kernel, "achieved": a, "peak": peak, "unit": "TFLOP/s",
+            "frac": a / peak, "traffic": None, "peak_source": psrc,
+            "per_launch_ms": k["ms"] / max(1, k["launches"]),
+            "note": "algorithmic FLOP: per (system, cell) the OK variance n(n+1) and the dual "
+                    "columns 2na, per cell-step 2n (right-hand-side generation not counted)"}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -237,7 +268,7 @@ def run_ours(args):
         start.record(stream)
         for i in range(args.steps):
             p = plans[(args.warmup + i) % n_sl]
-            kev.append(p.execute(timing=True))
+            kev.append((p, p.execute(timing=True)))
             cell_steps += p.T * C
         end.record(stream)
         torch.cuda.synchronize()
@@ -247,25 +278,22 @@ def run_ours(args):
         dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
     ms = float(t_max.item())
     value = world * cell_steps / (ms / 1e3)
-    # dominant kernel: the OK cell kernel (estimate + variance)
-    k_ms, k_fl, n_launch = 0.0, 0.0, 0
-    idw_ms = 0.0
-    for ev in kev:
-        for (a, b), fl in ev["krige_cells"]:
-            k_ms += a.elapsed_time(b)
-            k_fl += fl
-            n_launch += 1
-        for (a, b), fl in ev["idw"]:
-            idw_ms += a.elapsed_time(b)
-    launches_per_exec = sum(len(v) for v in kev[0].values())
-    bf16, hbm, src = measured_peaks()
-    achieved = k_fl / n_launch / (k_ms / n_launch / 1e3) / 1e12
-    roofline = {"bound": "tensor", "kernel": "k_krige_cells", "achieved": achieved,
-                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-                "traffic": None, "peak_source": src,
-                "note": "FP32 CUDA-core contraction (tensor-core path not yet used); "
-                        "algorithmic FLOP per launch = sum over systems and cells of "
-                        "n(n+1) + 2n*a + 2n*steps"}
+    # per-kernel times (CUDA events on the launching stream) and algorithmic
+    # FLOP; the roofline line describes the kernel that takes the most time
+    times = {}
+    for p, ev in kev:
+        for k, (t_ms, n_l, fl) in p.kernel_times(ev).items():
+            t = times.setdefault(k, [0.0, 0, 0.0])
+            t[0] += t_ms
+            t[1] += n_l
+            t[2] += fl
+    launches_per_exec = plans[0].launches_per_execute()
+    kernels = {k: {"ms": v[0], "launches": v[1], "achieved_tflops": v[2] / (v[0] / 1e3) / 1e12}
+               for k, v in times.items() if v[0] > 0}
+    dom_k = max(kernels, key=lambda k: kernels[k]["ms"])
+    roofline = roofline_for(dom_k, kernels[dom_k])
+    roofline_tc = roofline_for("var_tc", kernels["var_tc"]) if "var_tc" in kernels else None
+    idw_ms = times.get("idw", [0.0])[0]
     # e2e: public API from host arrays, fields copied back
     e2e_ms = []
     sl = slice(bounds[0], bounds[1])
@@ -328,6 +356,8 @@ def run_ours(args):
                     "ms": float(np.median(e2e_ms)) if e2e_ms else None},
             "gpu_launches": launches_per_exec * args.steps,
             "roofline": roofline,
+            "roofline_tensor_kernel": roofline_tc,
+            "kernels": kernels,
             "idw_ms_per_step": idw_ms / args.steps,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
@@ -466,7 +496,7 @@ def run_large(args):
             torch.cuda.synchronize()
             tot += a.elapsed_time(b)
             evs.append(ev)
-        cells_ms = sum(x.elapsed_time(y) for ev in evs for (x, y), _ in ev["krige_cells"])
+        cells_ms = sum(v[0] for ev in evs for v in plan.kernel_times(ev).values())
         return tot / reps, cells_ms / reps
 
     pm = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], vgs, iargs, precision="mixed",

@@ -169,6 +169,11 @@ typedef struct {
     double *s_inv;       /* per-system S^-1 [n_sys, GA * GA] */
     double *g_colsum;    /* per-system [n_sys, GA] */
     float *linv_hi, *linv_lo, *g_hi, *g_lo, *w_hi, *w_lo;
+    double *cell_yy;     /* optional [n_sys, n_cells]: |Linv c|^2 of every cell
+                            of the FP32-tier systems, written by
+                            spi_krige_var_tc and read by the precision-1 cell
+                            kernel instead of its own variance pass (NULL:
+                            the cell kernel computes it) */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -230,6 +235,17 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
                     const double *vals, const spi_krige_ws_t *ws,
                     int32_t want_var, int32_t precision, int32_t route_filter,
                     double cond_split, const spi_out_t *out, spi_stream_t stream);
+
+/* The OK variance term |Linv c|^2 of every cell of the FP32-tier systems
+ * (route 0, cond <= cond_split, kinds OK / EDK) on the tensor cores
+ * (tcgen05, 3xTF32: Linv and the right-hand sides as TF32 hi/lo pairs,
+ * FP32 accumulation in tensor memory), into ws->cell_yy [n_sys, n_cells].
+ * Requires ws->linv_hi (spi_split_f64 of linv_arena) and the domain's
+ * split coordinates. Replaces the variance half of
+ * interp/steps.py:403-435 (var = lambda'r + mu per cell and step). */
+int spi_krige_var_tc(const spi_domain_t *dom, const spi_systems_t *sys,
+                     const spi_krige_ws_t *ws, double cond_split, int32_t *err_flag,
+                     spi_stream_t stream);
 
 /* IDW (interp/steps.py:293-313, cyth/interpmthds.pyx:784-808) for every
  * cell of the listed steps. data [n_steps_total, n_stns] holds every

@@ -152,10 +152,13 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     }
     // ---- 3. OK variance |Linv c|^2, wide passes over Linv's rows
     // (triangular: a pass of rows r0..r0+63 stops at column r0+63) ----
+    // (the FP32 tier may take it from the tensor-core kernel instead:
+    // spi_krige_var_tc, ws.cell_yy)
+    const bool yy_tc = sizeof(T) == 4 && A.ws.cell_yy != nullptr;
     double yy_part[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) yy_part[c] = 0.0;
-    if (A.want_var && !prim) {
+    if (A.want_var && !prim && !yy_tc) {
       for (int r0 = 0; r0 < n; r0 += VB) {
         __syncthreads();
         for (int v = tid; v < VB; v += CT)
@@ -183,7 +186,11 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     for (int cell = tid; cell < TC; cell += CT) {
       const int64_t gc = c0 + cell;
       double yy = 0.0;
-      for (int g = 0; g < 16; ++g) yy += red[g * TC + cell];
+      if (yy_tc) {
+        if (A.want_var && gc < C) yy = A.ws.cell_yy[(int64_t)s * C + gc];
+      } else {
+        for (int g = 0; g < 16; ++g) yy += red[g * TC + cell];
+      }
       double q[GA], nu[GA], f[GA];
       for (int k = 0; k < GA; ++k) q[k] = qc[cell * GA + k];
       f[0] = 1.0;

@@ -1,0 +1,263 @@
+// The OK variance term |Linv c|^2 of every cell on the tensor cores
+// (tcgen05, sm_103a), for the FP32-tier systems of the mixed path.
+//
+// Per system: Y = C Linv' with C the cells' right-hand sides (covariances
+// to the system's stations, generated from coordinates) and Linv the
+// inverse Cholesky factor; the variance needs yy[cell] = sum_r Y[cell][r]^2
+// (n^2 flops per cell, shared by every step of the system; the rest of the
+// variance formula is in the cell kernel's FP64 epilogue).
+//
+// One CTA = 128 cells x 256 threads. The accumulator D [128 cells x 256
+// rows of Linv] lives in tensor memory (TMEM lane = cell, column = row), so
+// each lane squares and sums its own row of D. Rows of Linv go in blocks of
+// 256 (the MMA's N), the stations (K) in chunks of 32: per chunk all
+// threads stage A = the right-hand sides (128 x 32, generated, as rhs_f32
+// does for the CUDA-core path) and B = Linv's rows (256 x 32, triangular)
+// in shared memory as TF32 hi/lo pairs in the no-swizzle K-major layout
+// (8-row x 16-byte core matrices), then one thread issues 4 K-steps x 3
+// MMAs (A_hi B_hi + A_hi B_lo + A_lo B_hi, "3xTF32", FP32 accumulation in
+// TMEM) and commits them to an mbarrier that every thread waits on (with an
+// iteration limit: on expiry the kernel raises err_flag, frees its TMEM
+// and returns). 3xTF32 keeps ~22 bits of each operand; emulated on the
+// FP32-tier systems (condition <= 1e7) it stays within 2.2e-6 of the sill.
+#include "spi_cells.cuh"
+#include "spi_rhs.cuh"
+
+namespace spi {
+
+constexpr int VT_M = 128;   // cells per CTA (MMA M, TMEM lanes)
+constexpr int VT_N = 256;   // Linv rows per block (MMA N, TMEM columns)
+constexpr int VT_KC = 32;   // stations per staged chunk
+constexpr int VT_T = 256;   // threads
+constexpr long VT_SPIN = 1L << 26;   // mbarrier polls before giving up
+
+constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;
+constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;
+constexpr size_t VT_SMEM = 2 * VT_A_BYTES + 2 * VT_B_BYTES;
+
+struct VarTcArgs {
+  spi_domain_t dom;
+  spi_systems_t sys;
+  spi_krige_ws_t ws;
+  double cond_split;
+  int32_t* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major; lbo = byte stride
+// between core matrices along K, sbo = between 8-row groups.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of sm_100-class tensor cores
+  return d;
+}
+
+// Byte offset of (row, k) in an R x 32 TF32 tile (K-major, no swizzle):
+// core matrix (row / 8, k / 4) at (k / 4) * R * 16 + (row / 8) * 128.
+__device__ __forceinline__ int tile_off(int R, int row, int k) {
+  return (k >> 2) * (R * 16) + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+// TF32 keeps the top 19 bits of an FP32 value: hi = x truncated, lo = the
+// (exact) remainder, itself truncated by the tensor core.
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+  lo = x - hi;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
+  const int s = blockIdx.y;
+  const int64_t C = A.dom.n_cells;
+  const int64_t c0 = (int64_t)blockIdx.x * VT_M;
+  if (c0 >= C) return;
+  if (A.sys.kind == SPI_KIND_SK) return;
+  if (!(A.ws.route[s] == 0 && A.ws.cond[s] <= A.cond_split)) return;
+  const int64_t soff = A.sys.stn_off[s];
+  const int n = (int)(A.sys.stn_off[s + 1] - soff);
+  const int32_t* idx = A.sys.stn_idx + soff;
+  const int64_t moff = A.sys.mat_off[s];
+  const spi_vg_t vg = A.sys.vg[s];
+  const double sh = A.ws.shift[s];
+  const float* L = A.ws.linv_hi + moff;
+
+  extern __shared__ __align__(1024) unsigned char smv[];
+  unsigned char* sAh = smv;
+  unsigned char* sAl = sAh + VT_A_BYTES;
+  unsigned char* sBh = sAl + VT_A_BYTES;
+  unsigned char* sBl = sBh + VT_B_BYTES;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tbase;
+  __shared__ int fail;
+  __shared__ double half_yy[VT_M];
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tbase)),
+                 "r"(VT_N));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tbase;
+  // kind::tf32, D FP32, A/B TF32 K-major, N = 256, M = 128
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(VT_N >> 3) << 17) |
+                         ((uint32_t)(VT_M >> 4) << 24);
+
+  // staging roles: A = cell (tid % 128), stations [khalf * 16, +16) of a chunk
+  const int a_cell = tid & (VT_M - 1), khalf = tid >> 7;
+  const int64_t gc = c0 + a_cell;
+  const bool live = gc < C;
+  const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+  RhsF32 kf;
+  kf.init(vg, 0, sh, A.dom.min_vg_val);
+  const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
+  // epilogue roles: TMEM lanes of warp % 4, column half warp / 4
+  const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
+  double yy = 0.0;
+  uint32_t phase = 0;
+
+  for (int rb = 0; rb < n; rb += VT_N) {
+    const int kend = min(n, rb + VT_N);
+    for (int k0 = 0; k0 < kend; k0 += VT_KC) {
+#pragma unroll 4
+      for (int q = 0; q < 16; ++q) {
+        const int kk = khalf * 16 + q, j = k0 + kk;
+        float v = 0.f;
+        if (live && j < n) {
+          const int st = idx[j];
+          v = rhs_f32(A.dom, vg, kf, 0, sh, cp, sp4[st], gc, st);
+        }
+        float h, l;
+        tf32_split(v, h, l);
+        const int o = tile_off(VT_M, a_cell, kk);
+        *reinterpret_cast<float*>(sAh + o) = h;
+        *reinterpret_cast<float*>(sAl + o) = l;
+      }
+#pragma unroll 4
+      for (int i = 0; i < VT_N * VT_KC / VT_T; ++i) {
+        const int e = tid + VT_T * i, r = e >> 5, k = e & 31;
+        const int row = rb + r, col = k0 + k;
+        const float v = (row < n && col <= row) ? L[(int64_t)row * n + col] : 0.f;
+        float h, l;
+        tf32_split(v, h, l);
+        const int o = tile_off(VT_N, r, k);
+        *reinterpret_cast<float*>(sBh + o) = h;
+        *reinterpret_cast<float*>(sBl + o) = l;
+      }
+      asm volatile("fence.proxy.async.shared::cta;");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+        for (int ks = 0; ks < VT_KC / 8; ++ks) {
+          const uint32_t ao = 2 * ks * (VT_M * 16), bo = 2 * ks * (VT_N * 16);
+          const uint64_t ah = umma_desc(smem_u32(sAh) + ao, VT_M * 16, 128);
+          const uint64_t al = umma_desc(smem_u32(sAl) + ao, VT_M * 16, 128);
+          const uint64_t bh = umma_desc(smem_u32(sBh) + bo, VT_N * 16, 128);
+          const uint64_t bl = umma_desc(smem_u32(sBl) + bo, VT_N * 16, 128);
+          mma_tf32(tmem, ah, bh, idesc, (k0 > 0 || ks > 0) ? 1u : 0u);
+          mma_tf32(tmem, ah, bl, idesc, 1u);
+          mma_tf32(tmem, al, bh, idesc, 1u);
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&mbar)));
+      }
+      uint32_t done = 0;
+      for (long it = 0; it < VT_SPIN && !done; ++it)
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(&mbar)), "r"(phase));
+      if (!done) atomicExch(&fail, 1);
+      phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      __syncthreads();
+      if (fail) break;
+    }
+    if (fail) break;
+    // this block's rows: each lane's 128 columns of its half
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      uint32_t r[32];
+      const uint32_t addr =
+          tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(e_half * 128 + cc * 32);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+            "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+            "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+            "=r"(r[31])
+          : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const double y = (double)__uint_as_float(r[i]);
+        yy += y * y;
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+  }
+  if (e_half == 1) half_yy[e_cell] = yy;
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (fail) {
+    if (tid == 0) atomicExch(A.err, 1);
+  } else if (e_half == 0 && c0 + e_cell < C) {
+    A.ws.cell_yy[(int64_t)s * C + c0 + e_cell] = yy + half_yy[e_cell];
+  }
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(VT_N));
+}
+
+}  // namespace spi
+
+using namespace spi;
+
+extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sys,
+                                const spi_krige_ws_t* ws, double cond_split, int32_t* err_flag,
+                                spi_stream_t stream) {
+  if (!dom || !sys || !ws || !err_flag) return SPI_ERR_ARG;
+  if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
+  if (sys->n_sys == 0 || dom->n_cells == 0) return SPI_OK;
+  if (!ws->cell_yy || !ws->linv_hi || !ws->route || !ws->cond || !ws->shift ||
+      !dom->cell_split || !dom->stn_split || !sys->vg || !sys->stn_off || !sys->stn_idx ||
+      !sys->mat_off)
+    return SPI_ERR_ARG;
+  const int64_t tiles = (dom->n_cells + VT_M - 1) / VT_M;
+  if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
+  if (cudaFuncSetAttribute(k_var_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)VT_SMEM) != cudaSuccess)
+    return SPI_ERR_CUDA;
+  VarTcArgs A{*dom, *sys, *ws, cond_split, err_flag};
+  dim3 grid((unsigned)tiles, (unsigned)sys->n_sys);
+  k_var_tc<<<grid, VT_T, VT_SMEM, (cudaStream_t)stream>>>(A);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}

@@ -207,7 +207,8 @@ def _align(x, a=32):
 class _KrigeBatch:
     """One chunk of kriging systems: device descriptors and workspaces."""
 
-    def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision):
+    def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
+                 want_var=False, tensor_cores=True):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -255,11 +256,19 @@ class _KrigeBatch:
             self.split = [torch.empty(k, dtype=torch.float32, device=dev)
                           for k in (self.arena, self.arena, self.g_cols.numel(),
                                     self.g_cols.numel(), self.w_hat.numel(), self.w_hat.numel())]
+        # |Linv c|^2 per (system, cell) from the tensor cores (FP32 tier of
+        # the OK variance)
+        self.yy = None
+        self.tc_err = None
+        if precision == 1 and want_var and kind == "OK" and tensor_cores:
+            self.yy = torch.empty(len(ch) * dom.C, dtype=torch.float64, device=dev)
+            self.tc_err = torch.zeros(1, dtype=torch.int32, device=dev)
         self.ws = nat.KrigeWsT(_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
                                _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat),
                                _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv),
                                _ptr(self.g_colsum),
-                               *[_ptr(t) for t in (self.split or [None] * 6)])
+                               *[_ptr(t) for t in (self.split or [None] * 6)],
+                               _ptr(self.yy))
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
         self.n = ns
@@ -271,9 +280,40 @@ class _KrigeBatch:
             per = per + self.n * (self.n + 1)
         return float(per.sum()) * C
 
+    def kernel_flops(self, C, want_var, a, cond_split):
+        """Algorithmic FLOP of each cell kernel of the last run: the OK
+        variance n(n+1) per (system, cell), the dual columns 2na and 2n per
+        cell-step; split by where each system ran (tensor-core variance,
+        FP32 tier, FP64 tier)."""
+        route = self.route.cpu().numpy()
+        cond = self.cond.cpu().numpy()
+        var = self.n * (self.n + 1) if want_var else np.zeros_like(self.n)
+        rest = 2 * self.n * a + 2 * self.n * self.n_steps
+        ok = route != 2
+        if self.precision == 1:
+            fast = (route == 0) & (cond <= cond_split)
+            tc = self.yy is not None and want_var
+            return {"var_tc": float((var * fast).sum()) * C if tc else 0.0,
+                    "cells_fp32": float(((rest + (0 if tc else var)) * fast).sum()) * C,
+                    "cells_fp64": float(((rest + var) * (ok & ~fast)).sum()) * C}
+        return {"cells_fp64": float(((rest + var) * ok).sum()) * C}
+
     def run(self, dom, out, want_var, cond_max, cond_split, ev=None):
+        """Factor, duals, splits, cell kernels. ``ev``: a list that receives
+        (kernel name, start event, end event) per cell-kernel call."""
         s = _stream()
         ws = ctypes.byref(self.ws)
+
+        def timed(name, fn):
+            if ev is None:
+                fn()
+                return
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            ev.append((name, a, b))
+
         nat.call("spi_krige_factor", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
                  float(cond_max), s)
         nat.call("spi_krige_duals", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
@@ -283,15 +323,15 @@ class _KrigeBatch:
             nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
             nat.call("spi_split_f64", _ptr(self.g_cols), _ptr(gh), _ptr(gl), self.g_cols.numel(), s)
             nat.call("spi_split_f64", _ptr(self.w_hat), _ptr(wh), _ptr(wl), self.w_hat.numel(), s)
-        if ev is not None:
-            ev[0].record()
+        if self.yy is not None and want_var:
+            timed("var_tc", lambda: nat.call(
+                "spi_krige_var_tc", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
+                float(cond_split), _ptr(self.tc_err), s))
         passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
         for prec, filt in passes:
-            nat.call("spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy),
-                     _ptr(self.vals), ws, 1 if want_var else 0, prec, filt, float(cond_split),
-                     ctypes.byref(out), s)
-        if ev is not None:
-            ev[1].record()
+            timed("cells_fp32" if prec == 1 else "cells_fp64", lambda prec=prec, filt=filt: nat.call(
+                "spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
+                ws, 1 if want_var else 0, prec, filt, float(cond_split), ctypes.byref(out), s))
 
 
 def _chunk_systems(systems, precision, arena_budget):
@@ -321,7 +361,7 @@ class InterpPlan:
                  est_vars=False, stn_drifts=None, cell_drifts=None, min_var_thr=0.0,
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
-                 cond_max=1e13, cond_split=1e7):
+                 cond_max=1e13, cond_split=1e7, tensor_cores=True):
         dev = self.dev = _require_cuda(device)
         self.cond_max, self.cond_split = cond_max, cond_split
         prec = self.prec = PRECISION[precision]
@@ -344,6 +384,7 @@ class InterpPlan:
         for j in np.where(n_av > 0)[0]:
             means[j] = data[j, avail[j]].mean()   # numpy's pairwise mean, as the reference
         flags = ((data >= min_var_thr) & avail).any(1)
+        self.time_steps = time_steps
         self.prblm = [time_steps[j] for j in np.where(n_av == 0)[0]]
         self.single = np.where(n_av == 1)[0]
         self.single_val = np.array([data[j, avail[j]][0] for j in self.single], dtype=np.float64)
@@ -377,7 +418,8 @@ class InterpPlan:
                 val_off = np.zeros(T, dtype=np.int64)
                 beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
                 batches = [_KrigeBatch(dev, self.dom, kind, systems, ch, data, T, val_off, beta,
-                                       prec)
+                                       prec, want_var=var is not None,
+                                       tensor_cores=tensor_cores)
                            for ch in _chunk_systems(systems, prec, arena_budget)]
                 fills = (
                     _fill_args(dev, self.single, self.single_val,
@@ -408,19 +450,20 @@ class InterpPlan:
 
     def execute(self, timing=False):
         """Run the whole job on the GPU (current stream). With ``timing``,
-        returns per-stage CUDA-event pairs (kernel timing without syncs)."""
+        returns the CUDA events of every cell-kernel call (per batch:
+        (batch, want_var, a, [(kernel, start, end)])) and of the IDW calls,
+        read after a synchronisation (:meth:`kernel_times`)."""
         C = self.C
-        evs = {"krige_cells": [], "idw": []}
+        evs = {"krige": [], "idw": []}
         s = _stream()
         for kind, out, want_var, batches, fills, a in self.krig:
             for f in fills:
                 _fill_run(f, C, out, s)
             for b in batches:
-                ev = None
-                if timing:
-                    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                    evs["krige_cells"].append((ev, b.cell_flops(C, want_var, a)))
+                ev = [] if timing else None
                 b.run(self.dom, out, want_var, self.cond_max, self.cond_split, ev)
+                if timing:
+                    evs["krige"].append((b, want_var, a, ev))
         for t, out, fill, p in self.idw:
             _fill_run(fill, C, out, s)
             if not len(self.multi):
@@ -450,6 +493,8 @@ class InterpPlan:
         for kind, out, want_var, batches, fills, a in self.krig:
             failed, routed, cond = [], [], {}
             for b in batches:
+                if b.tc_err is not None and int(b.tc_err.item()):
+                    raise nat.SpiError("spi_krige_var_tc: a tensor-core wait timed out")
                 rt = b.route.cpu().numpy()
                 cn = b.cond.cpu().numpy()
                 for k, sl in enumerate(b.steps_l):
@@ -463,6 +508,54 @@ class InterpPlan:
             self.info.setdefault("exact_inverse_steps", {})[kind] = sorted(routed)
             self.info["cond"][kind] = cond
         return self.info
+
+    def launches_per_execute(self):
+        """Kernels of this library that one execute() launches: row fills;
+        per batch build + Cholesky + inverse + Gauss-Jordan, duals, the FP32
+        splits and the tensor-core variance (mixed), one cell kernel per
+        tier; per IDW / NNB field its fill, split (mixed IDW) and kernel."""
+        n = 0
+        for kind, out, want_var, batches, fills, a in self.krig:
+            n += sum(f is not None for f in fills)
+            for b in batches:
+                n += 5 + (3 if b.split is not None else 0)
+                n += 1 if (b.yy is not None and want_var) else 0
+                n += 2 if b.precision == 1 else 1
+        for t, out, fill, p in self.idw:
+            n += (fill is not None) + (len(self.multi) > 0) * (
+                1 + (t == "IDW" and self.data_hi is not None))
+        return int(n)
+
+    def kernel_times(self, evs):
+        """{kernel: [ms, launches, algorithmic FLOP]} of an execute(timing=True)."""
+        out = {}
+        for b, want_var, a, ev in evs["krige"]:
+            fl = b.kernel_flops(self.C, want_var, a, self.cond_split)
+            for name, e0, e1 in ev:
+                t = out.setdefault(name, [0.0, 0, 0.0])
+                t[0] += e0.elapsed_time(e1)
+                t[1] += 1
+                t[2] += fl.get(name, 0.0)
+        for (e0, e1), fl in evs["idw"]:
+            t = out.setdefault("idw", [0.0, 0, 0.0])
+            t[0] += e0.elapsed_time(e1)
+            t[1] += 1
+            t[2] += fl
+        return out
+
+    def problem_steps(self):
+        """The reference's prblm_time_steps after an execution: steps without
+        a present station, then steps whose kriging system is singular
+        (filled by nearest station, as the reference's pinv-failure branch,
+        interp/steps.py:362-372)."""
+        out = list(self.prblm)
+        info = self.collect_info()
+        failed = sorted({j for v in info["failed_steps"].values() for j in v})
+        for j in failed:
+            t = self.time_steps[j]
+            if t not in out:
+                out.append(t)
+        return out
 
     def fields(self, numpy=True):
         torch.cuda.current_stream().synchronize()
@@ -492,13 +585,14 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  stn_drifts=None, cell_drifts=None, min_var_thr=0.0, min_var_cut=None,
                  max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
-                 arena_budget=8 << 30, cond_max=1e13, cond_split=1e7):
+                 arena_budget=8 << 30, cond_max=1e13, cond_split=1e7, tensor_cores=True):
     """Interpolate every step onto every cell on the GPU.
 
     Same inputs and outputs as the reference step engine for one grid chunk
     (see the module docstring). ``precision`` is "fp64" (plain FP64) or
     "mixed" (FP32 right-hand sides and contractions over the FP64
-    factorisation). Returns ``(fields, problem_steps)``, plus an info dict
+    factorisation; with ``tensor_cores`` the OK variance of the FP32 tier
+    runs on tcgen05 in 3xTF32). Returns ``(fields, problem_steps)``, plus an info dict
     (failed systems, condition estimates) when ``return_info``.
     """
     plan = InterpPlan(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, est_vars=est_vars,
@@ -506,12 +600,13 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                       min_var_cut=min_var_cut, max_var_cut=max_var_cut, min_vg_val=min_vg_val,
                       intrp_dtype=intrp_dtype, time_steps=time_steps, precision=precision,
                       device=device, arena_budget=arena_budget, cond_max=cond_max,
-                      cond_split=cond_split)
+                      cond_split=cond_split, tensor_cores=tensor_cores)
     plan.execute()
     flds = plan.fields(numpy=return_numpy)
+    prblm = plan.problem_steps()
     if return_info:
-        return flds, plan.prblm, plan.collect_info()
-    return flds, plan.prblm
+        return flds, prblm, plan.collect_info()
+    return flds, prblm
 
 
 def krige_loo(stn_x, stn_y, data, vgs, *, min_vg_val=0.0, device="cuda", cond_max=1e13):
