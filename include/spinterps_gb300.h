@@ -174,6 +174,9 @@ typedef struct {
                             spi_krige_var_tc and read by the precision-1 cell
                             kernel instead of its own variance pass (NULL:
                             the cell kernel computes it) */
+    int32_t *tier;       /* optional [n_sys]: 1 = the FP32 tier of the
+                            precision-1 kernels, 0 = FP64 (spi_krige_tier);
+                            NULL: route 0 and cond <= cond_split */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -236,8 +239,23 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
                     int32_t want_var, int32_t precision, int32_t route_filter,
                     double cond_split, const spi_out_t *out, spi_stream_t stream);
 
+/* Tier of every system of a factored batch from a probe: est/var fields
+ * [rows, n_probe] (row = sys->out_row[step]) of the same probe cells
+ * computed by the FP64 kernel (route_filter 0) and by the FP32 tier
+ * (precision 1, route_filter 1, cond_split = cond_cap). tier[s] = 1 when the
+ * system is on the Cholesky path, cond <= cond_cap, and over its steps and
+ * the probe cells |est32 - est64| <= tol_est and |var32 - var64| <= tol_var
+ * (var arrays may be NULL; a NaN in one field and not the other fails). The
+ * mixed path's a-posteriori error control: the FP32 rounding of the
+ * right-hand sides enters the estimate as sum_i dc_i w_i, which the dual
+ * weights can amplify far beyond what the condition number predicts. */
+int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n_probe,
+                   const double *est64, const double *est32, const double *var64,
+                   const double *var32, double tol_est, double tol_var, double cond_cap,
+                   int32_t *tier, spi_stream_t stream);
+
 /* The OK variance term |Linv c|^2 of every cell of the FP32-tier systems
- * (route 0, cond <= cond_split, kinds OK / EDK) on the tensor cores
+ * (ws->tier, else route 0 and cond <= cond_split; kinds OK / EDK) on the tensor cores
  * (tcgen05, 3xTF32: Linv and the right-hand sides as TF32 hi/lo pairs,
  * FP32 accumulation in tensor memory), into ws->cell_yy [n_sys, n_cells].
  * Requires ws->linv_hi (spi_split_f64 of linv_arena) and the domain's

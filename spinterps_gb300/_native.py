@@ -62,7 +62,7 @@ class KrigeWsT(ctypes.Structure):
                 ("cond", c_ptr), ("shift", c_ptr), ("w_hat", c_ptr), ("beta", c_ptr),
                 ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr), ("linv_hi", c_ptr),
                 ("linv_lo", c_ptr), ("g_hi", c_ptr), ("g_lo", c_ptr), ("w_hi", c_ptr),
-                ("w_lo", c_ptr), ("cell_yy", c_ptr)]
+                ("w_lo", c_ptr), ("cell_yy", c_ptr), ("tier", c_ptr)]
 
 
 class OutT(ctypes.Structure):
@@ -92,6 +92,8 @@ _SIGS = {
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
+    "spi_krige_tier": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_i64, c_ptr, c_ptr,
+                       c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr],
     "spi_krige_var_tc": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr, c_ptr],
     "spi_krige_loo": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),

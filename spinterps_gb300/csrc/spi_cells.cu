@@ -49,7 +49,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   const int route = A.ws.route[s];
   {
     // filter 1: well-conditioned Cholesky systems; filter 2: all others
-    const bool fast = route == 0 && A.ws.cond[s] <= A.cond_split;
+    const bool fast = fp32_tier(A.ws, s, A.cond_split);
     if ((A.route_filter == 1 && !fast) || (A.route_filter == 2 && fast)) return;
   }
   const bool prim = route == 1;   // exact-inverse path: primal formulas
@@ -410,6 +410,11 @@ static int pick_tc(int max_n) {
 // streamed kernel (estimates only; the OK variance needs the stored tile).
 template <typename T, typename OutT>
 static int dispatch_cells(const CellsArgs& A, cudaStream_t st) {
+  // the mixed path's FP32 tier: double-float right-hand sides in the
+  // streamed kernel whenever no CUDA-core variance pass is needed
+  if (sizeof(T) == 4 &&
+      (A.ws.cell_yy != nullptr || !A.want_var || A.sys.kind == SPI_KIND_SK))
+    return launch_cells_stream(A, 1, st);
   int tc = pick_tc<T>(A.sys.max_n);
   if (tc == 64) return launch_cells<T, 64, OutT>(A, st);
   if (tc == 32) return launch_cells<T, 32, OutT>(A, st);
@@ -500,6 +505,55 @@ extern "C" int spi_split_coords(const double* x, const double* y, int64_t n, dou
   if (blocks > 4096) blocks = 4096;
   spi::k_split_coords<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
       x, y, n, ox, oy, reinterpret_cast<float4*>(out));
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+namespace spi {
+// One CTA per system: the largest probe discrepancy over its steps.
+__global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t ws, int64_t P,
+                                              const double* __restrict__ e64,
+                                              const double* __restrict__ e32,
+                                              const double* __restrict__ v64,
+                                              const double* __restrict__ v32, double tol_e,
+                                              double tol_v, double cap, int32_t* tier) {
+  const int s = blockIdx.x;
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const bool cand = ws.route[s] == 0 && ws.cond[s] <= cap;
+  if (cand) {
+    int b = 0;
+    for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1] && !b; ++si) {
+      const int64_t row = sys.out_row[sys.steps[si]];
+      for (int64_t c = threadIdx.x; c < P; c += blockDim.x) {
+        const double a = e32[row * P + c], r = e64[row * P + c];
+        if (isnan(a) != isnan(r) || fabs(a - r) > tol_e) b = 1;
+        if (v64 && v32) {
+          const double va = v32[row * P + c], vr = v64[row * P + c];
+          if (isnan(va) != isnan(vr) || fabs(va - vr) > tol_v) b = 1;
+        }
+      }
+    }
+    if (b) atomicOr(&bad, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) tier[s] = (cand && !bad) ? 1 : 0;
+}
+}  // namespace spi
+
+extern "C" int spi_krige_tier(const spi_systems_t* sys, const spi_krige_ws_t* ws, int64_t n_probe,
+                              const double* est64, const double* est32, const double* var64,
+                              const double* var32, double tol_est, double tol_var,
+                              double cond_cap, int32_t* tier, spi_stream_t stream) {
+  if (!sys || !ws || !tier || n_probe < 0) return SPI_ERR_ARG;
+  if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
+  if (sys->n_sys == 0) return SPI_OK;
+  if (n_probe > 0 && (!est64 || !est32)) return SPI_ERR_ARG;
+  if (!ws->route || !ws->cond || !sys->step_off || !sys->steps || !sys->out_row)
+    return SPI_ERR_ARG;
+  spi::k_tier<<<sys->n_sys, 256, 0, (cudaStream_t)stream>>>(
+      *sys, *ws, n_probe, est64, est32, var64, var32, tol_est, tol_var, cond_cap, tier);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

@@ -43,6 +43,13 @@ __device__ inline int nnb_f64_warp(const spi_domain_t& dom, const int32_t* idx, 
   return bj == 0x7fffffff ? 0 : bj;
 }
 
+// The FP32 tier of the precision-1 kernels: the probe's verdict when there
+// is one (spi_krige_tier), else the Cholesky path under cond_split.
+__device__ __forceinline__ bool fp32_tier(const spi_krige_ws_t& ws, int s, double cond_split) {
+  if (ws.tier) return ws.tier[s] != 0;
+  return ws.route[s] == 0 && ws.cond[s] <= cond_split;
+}
+
 // Host-side dispatch of the streamed kernel (spi_cells_stream.cu): systems
 // too large for the shared-memory right-hand side of k_krige_cells.
 int launch_cells_stream(const CellsArgs& A, int precision, cudaStream_t st);

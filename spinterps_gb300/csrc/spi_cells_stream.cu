@@ -12,8 +12,11 @@
 // the sum check of interp/steps.py:419) and the steps' dual weights. The 8
 // partial sums per cell are reduced in shared memory; more steps than fit
 // in one pass regenerate the right-hand side. Precision as k_krige_cells:
-// FP64 throughout, or FP32 entries against FP32 hi/lo vector pairs with
-// FP32 partials flushed to FP64 every 128 terms.
+// FP64 throughout, or (the mixed path's FP32 tier) double-float entries
+// (rhs_df, ~1e-9) against FP32 hi/lo vector pairs, accumulated in
+// double-float and flushed to FP64 every 256 terms: the estimate's error is
+// sum_i dc_i w_i, which large dual weights amplify. With ws.cell_yy (the
+// tensor-core |Linv c|^2) the FP32 tier also writes the OK variance.
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
 
@@ -31,7 +34,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   if (c0 >= C) return;
   const int route = A.ws.route[s];
   {
-    const bool fast = route == 0 && A.ws.cond[s] <= A.cond_split;
+    const bool fast = fp32_tier(A.ws, s, A.cond_split);
     if ((A.route_filter == 1 && !fast) || (A.route_filter == 2 && fast)) return;
   }
   const bool prim = route == 1;
@@ -52,6 +55,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   __shared__ double red[SNW][SSV][STC];
   __shared__ double vres[SSV][STC];
   __shared__ int okf[STC], nnb[STC];
+  __shared__ double cvar[STC];
   __shared__ const double* vp64[SSV];
   __shared__ const float* vph[SSV];
   __shared__ const float* vpl[SSV];
@@ -61,6 +65,10 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   const int64_t gc = c0 + lane;
   const bool live = gc < C;
   OutT* est_out = reinterpret_cast<OutT*>(A.out.est);
+  // the OK variance needs |Linv c|^2 per cell from the tensor-core kernel
+  const bool var_out = sizeof(T) == 4 && A.want_var && A.out.var != nullptr && !sk &&
+                       A.ws.cell_yy != nullptr;
+  OutT* var_outp = reinterpret_cast<OutT*>(A.out.var);
   auto emit = [&](int cell, int vstep, double accv) {
     const int64_t g = c0 + cell;
     if (g >= C) return;
@@ -78,6 +86,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
       e = A.vals[A.sys.val_off[j] + nnb[cell]];
     }
     est_out[row * C + g] = cast_out<OutT>(clip_est(e, A.out));
+    if (var_out) var_outp[row * C + g] = cast_out<OutT>(okf[cell] ? cvar[cell] : 0.0);
   };
   auto nearest = [&]() {
     __syncthreads();
@@ -92,7 +101,10 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   };
 
   if (failed) {
-    if (tid < STC) okf[tid] = 0;
+    if (tid < STC) {
+      okf[tid] = 0;
+      cvar[tid] = 0.0;
+    }
     if (tid == 0) any_bad = 1;
     nearest();
     for (int e = tid; e < nsteps * STC; e += STC * SNW) emit(e % STC, e / STC, 0.0);
@@ -101,7 +113,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
 
   double cx = 0.0, cy = 0.0;
   float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
-  RhsF32 kf;
+  RhsDf kd;
   if constexpr (sizeof(T) == 8) {
     if (live) {
       cx = A.dom.cell_x[gc];
@@ -109,7 +121,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
     }
   } else {
     if (live) cp = reinterpret_cast<const float4*>(A.dom.cell_split)[gc];
-    kf.init(vg, sk, sh, A.dom.min_vg_val);
+    kd.init(vg, sh);
   }
   const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
 
@@ -149,30 +161,38 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
           if (v < nv) acc[v] = fma(c, vp64[v][j], acc[v]);
       }
     } else {
-      float ph[SSV], pl[SSV];
+      // double-float entries against hi/lo vectors: the product's head by
+      // the FMA error, the cross terms, TwoSum into a double-float partial,
+      // flushed to FP64 every 256 terms
+      df pa[SSV];
 #pragma unroll
-      for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
+      for (int v = 0; v < SSV; ++v) pa[v] = df{0.f, 0.f};
       int cnt = 0;
       for (int j = warp; j < n; j += SNW) {
         const int st = idx[j];
-        const float c = live ? rhs_f32(A.dom, vg, kf, sk, sh, cp, sp4[st], gc, st) : 0.f;
+        const df c = live ? rhs_df(A.dom, vg, kd, sk, sh, cp, sp4[st], gc, st) : df{0.f, 0.f};
 #pragma unroll
         for (int v = 0; v < SSV; ++v)
           if (v < nv) {
-            ph[v] = fmaf(c, vph[v][j], ph[v]);
-            pl[v] = fmaf(c, vpl[v][j], pl[v]);
+            const float wh = vph[v][j], wl = vpl[v][j];
+            const float p = __fmul_rn(c.h, wh);
+            float e = __fmaf_rn(c.h, wh, -p);
+            e = __fmaf_rn(c.h, wl, e);
+            e = __fmaf_rn(c.l, wh, e);
+            const df s2 = two_sum(pa[v].h, p);
+            pa[v] = fast_two_sum(s2.h, s2.l + (pa[v].l + e));
           }
-        if (++cnt == 128) {
+        if (++cnt == 256) {
           cnt = 0;
 #pragma unroll
           for (int v = 0; v < SSV; ++v) {
-            acc[v] += (double)ph[v] + (double)pl[v];
-            ph[v] = pl[v] = 0.f;
+            acc[v] += (double)pa[v].h + (double)pa[v].l;
+            pa[v] = df{0.f, 0.f};
           }
         }
       }
 #pragma unroll
-      for (int v = 0; v < SSV; ++v) acc[v] += (double)ph[v] + (double)pl[v];
+      for (int v = 0; v < SSV; ++v) acc[v] += (double)pa[v].h + (double)pa[v].l;
     }
 #pragma unroll
     for (int v = 0; v < SSV; ++v) red[warp][v][lane] = acc[v];
@@ -213,6 +233,8 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
           }
           sl = q[0];
           for (int k = 0; k < a; ++k) sl -= A.ws.g_colsum[(int64_t)s * GA + k] * nu[k];
+          if (var_out && g < C)
+            cvar[cell] = sh * sl - A.ws.cell_yy[(int64_t)s * C + g] + nu[0] * q[0] - 2.0 * nu[0];
         }
         int ok = isclose_one(sl) ? 1 : 0;
         // SK's FP32 sum(lambda) within its rounding bound of the check's

@@ -60,6 +60,142 @@ __device__ __forceinline__ float rhs_f32(const spi_domain_t& dom, const spi_vg_t
   return (k.shf - cdir <= k.mvv) ? k.shf : cdir;
 }
 
+// ---- double-float (FP32 pair) arithmetic: value = hi + lo, |lo| <= ulp(hi)/2.
+// Knuth's TwoSum, Dekker's Fast2Sum and the FMA product error; explicit
+// round-to-nearest intrinsics keep the compiler from contracting them.
+struct df {
+  float h, l;
+};
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  const df s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df df_from(double x) {
+  const float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+
+// exp of a double-float argument (t <= 0 here), relative error ~1e-9:
+// t = m ln2 + r (ln2 as a 16-bit head, so m * head is exact, plus a tail),
+// |r| <= ln2 / 2, exp(r) = 1 + r + r^2/2 (double-float) + r^3 P(r) (FP32,
+// to r^8 / 8!: truncation 2e-10), then 2^m.
+__device__ __forceinline__ df df_exp(df t) {
+  if (t.h < -103.0f) return {0.f, 0.f};
+  const float m = rintf(__fmul_rn(t.h, 1.44269504088896341f));
+  const float rh0 = __fmaf_rn(-m, 0.693145751953125f, t.h);
+  const float rl0 = __fmaf_rn(-m, 1.42860682030941723e-6f, t.l);
+  const df r = fast_two_sum(rh0, rl0);
+  const float sq = __fmul_rn(r.h, r.h);
+  const float sq_l = __fmaf_rn(r.h, r.h, -sq) + 2.0f * r.h * r.l;
+  const float p = 1.0f / 6 + r.h * (1.0f / 24 + r.h * (1.0f / 120 + r.h * (1.0f / 720 +
+                  r.h * (1.0f / 5040 + r.h * (1.0f / 40320)))));
+  const float tail = sq * r.h * p;
+  const df a = two_sum(1.0f, r.h);
+  const df b = two_sum(a.h, 0.5f * sq);
+  const float lo = a.l + b.l + r.l + 0.5f * sq_l + tail;
+  const df e = fast_two_sum(b.h, lo);
+  const int mi = (int)m;
+  return {ldexpf(e.h, mi), ldexpf(e.l, mi)};
+}
+
+// Distance from split coordinates (x_hi, x_lo, y_hi, y_lo relative to a
+// common origin) as a double-float: differences by TwoSum, squares by the
+// FMA product error, one Newton step on sqrtf.
+__device__ __forceinline__ df df_dist(float4 cp, float4 sp) {
+  const df dx0 = two_sum(cp.x, -sp.x), dy0 = two_sum(cp.z, -sp.z);
+  const df dx = fast_two_sum(dx0.h, dx0.l + (cp.y - sp.y));
+  const df dy = fast_two_sum(dy0.h, dy0.l + (cp.w - sp.w));
+  const df d2 = df_add(df_mul(dx, dx), df_mul(dy, dy));
+  if (!(d2.h > 0.f)) return {0.f, 0.f};
+  const float h = sqrtf(d2.h);
+  const float rr = __fmaf_rn(-h, h, d2.h) + d2.l;
+  return fast_two_sum(h, rr / (2.0f * h));
+}
+
+// Per-component constants of rhs_df: sill and 1/range as double-floats.
+struct RhsDf {
+  df sill[SPI_MAX_VG_COMP], inv_r[SPI_MAX_VG_COMP];
+  df shift;
+  bool exact;  // every component has a double-float form below
+  __device__ __forceinline__ void init(const spi_vg_t& vg, double sh) {
+    exact = true;
+#pragma unroll
+    for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
+      sill[c] = df_from(vg.sill[c]);
+      inv_r[c] = df_from(1.0 / vg.range[c]);
+      if (c < vg.n_comp) {
+        const int k = vg.code[c];
+        if (!(k == SPI_VG_NUG || k == SPI_VG_EXP || k == SPI_VG_GAU || k == SPI_VG_SPH ||
+              k == SPI_VG_LIN))
+          exact = false;
+      }
+    }
+    shift = df_from(sh);
+  }
+};
+
+// One covariance entry (Cholesky path) as a double-float, relative error
+// ~1e-9, for the FP32 tier's estimates and dual columns, where the
+// right-hand side's rounding is amplified by the dual weights. Same
+// entries as rhs_f64 (covariance form, the min_vg_val zeroing); entries
+// within 1e-6 of the cut, and variograms with components that have no
+// double-float form here (Pow, Hol, Rng), take rhs_f64 itself.
+__device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t& vg, const RhsDf& k,
+                                     int sk, double sh, float4 cp, float4 sp, int64_t gc, int st) {
+  if (!k.exact) return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+  const df d = df_dist(cp, sp);
+  df c = {0.f, 0.f};
+#pragma unroll
+  for (int q = 0; q < SPI_MAX_VG_COMP; ++q) {
+    if (q >= vg.n_comp) break;
+    const int code = vg.code[q];
+    if (code == SPI_VG_NUG) continue;
+    const df t = df_mul(d, k.inv_r[q]);  // h / r
+    df v;
+    if (code == SPI_VG_EXP) {
+      v = df_exp(df_mul(t, df{-3.0f, 0.f}));
+    } else if (code == SPI_VG_GAU) {
+      v = df_exp(df_mul(df_mul(t, t), df{-3.0f, 0.f}));
+    } else if (code == SPI_VG_SPH) {
+      if (!(t.h < 1.0f)) continue;
+      const df u = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
+      const df w = df_add(df{1.0f, 0.f}, df{0.5f * t.h, 0.5f * t.l});
+      v = df_mul(df_mul(u, u), w);
+    } else {  // LIN
+      if (t.h > 1.0f) continue;
+      v = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
+    }
+    c = df_add(c, df_mul(k.sill[q], v));
+  }
+  const float mvv = (float)dom.min_vg_val;
+  const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
+  const float gap = (cut.h - mvv) + cut.l;
+  // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
+  // paths zero only exact zeros, which they agree on
+  if (mvv > 0.f && fabsf(gap) <= 1e-6f * mvv + (sk ? 0.f : 4e-9f * (float)sh))
+    return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+  if (sk) return gap <= 0.f ? df{0.f, 0.f} : c;
+  return gap <= 0.f ? k.shift : c;
+}
+
 // Rounding bound of an FP32-tier sum(lambda), relative to sum |u_i| c_i:
 // entries ~1e-6 (FP32 exp, double-float distance), hi/lo products, and
 // FP32 partial sums of 128 terms (up to ~8e-6 in the worst case).

@@ -193,6 +193,22 @@ class _Domain:
                               _ptr(self.ssplit), _ptr(self.csplit))
 
 
+class _DomainView:
+    """A subset of a domain's cells (the mixed path's probe cells): the same
+    stations and the same split coordinates (so FP32 entries are identical)."""
+
+    def __init__(self, dom, idx):
+        t = torch.as_tensor(np.asarray(idx, dtype=np.int64), device=dom.cx.device)
+        self.C = int(t.numel())
+        self.cx, self.cy = dom.cx[t].contiguous(), dom.cy[t].contiguous()
+        self.cd = dom.cd[:, t].contiguous() if dom.cd is not None else None
+        self.csplit = dom.csplit[t].contiguous() if dom.csplit is not None else None
+        d = dom.st
+        self.st = nat.DomainT(d.n_stns, d.stn_x, d.stn_y, self.C, _ptr(self.cx), _ptr(self.cy),
+                              d.n_drift, d.stn_drift, _ptr(self.cd), d.min_vg_val, d.stn_split,
+                              _ptr(self.csplit))
+
+
 def _out_struct(est, var, min_var_cut, max_var_cut):
     return nat.OutT(1 if est.dtype == torch.float64 else 0, _ptr(est), _ptr(var),
                     0 if min_var_cut is None else 1, 0 if max_var_cut is None else 1,
@@ -208,7 +224,7 @@ class _KrigeBatch:
     """One chunk of kriging systems: device descriptors and workspaces."""
 
     def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
-                 want_var=False, tensor_cores=True):
+                 want_var=False, tensor_cores=True, n_probe=0):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -263,12 +279,25 @@ class _KrigeBatch:
         if precision == 1 and want_var and kind == "OK" and tensor_cores:
             self.yy = torch.empty(len(ch) * dom.C, dtype=torch.float64, device=dev)
             self.tc_err = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.ws = nat.KrigeWsT(_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
-                               _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat),
-                               _ptr(self.beta), _ptr(self.g_cols), _ptr(self.s_inv),
-                               _ptr(self.g_colsum),
-                               *[_ptr(t) for t in (self.split or [None] * 6)],
-                               _ptr(self.yy))
+        # the probe (precision 1): both tiers on a few cells decide each
+        # system's tier (spi_krige_tier)
+        self.tier = self.probe = None
+        if precision == 1 and n_probe > 0:
+            n_sys = len(ch)
+            self.tier = torch.zeros(n_sys, dtype=torch.int32, device=dev)
+            f = lambda: torch.full((T, n_probe), float("nan"), dtype=torch.float64, device=dev)
+            pe64, pe32 = f(), f()
+            pv64, pv32 = (f(), f()) if want_var else (None, None)
+            pyy = (torch.empty(n_sys * n_probe, dtype=torch.float64, device=dev)
+                   if self.yy is not None else None)
+            self.probe = (pe64, pe32, pv64, pv32, pyy, _out_struct(pe64, pv64, None, None),
+                          _out_struct(pe32, pv32, None, None))
+        ptrs = [_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
+                _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat), _ptr(self.beta),
+                _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum),
+                *[_ptr(t) for t in (self.split or [None] * 6)]]
+        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier))
+        self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None)
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
         self.n = ns
@@ -291,16 +320,19 @@ class _KrigeBatch:
         rest = 2 * self.n * a + 2 * self.n * self.n_steps
         ok = route != 2
         if self.precision == 1:
-            fast = (route == 0) & (cond <= cond_split)
+            fast = ((self.tier.cpu().numpy() != 0) if self.tier is not None
+                    else (route == 0) & (cond <= cond_split))
             tc = self.yy is not None and want_var
             return {"var_tc": float((var * fast).sum()) * C if tc else 0.0,
                     "cells_fp32": float(((rest + (0 if tc else var)) * fast).sum()) * C,
                     "cells_fp64": float(((rest + var) * (ok & ~fast)).sum()) * C}
         return {"cells_fp64": float(((rest + var) * ok).sum()) * C}
 
-    def run(self, dom, out, want_var, cond_max, cond_split, ev=None):
-        """Factor, duals, splits, cell kernels. ``ev``: a list that receives
-        (kernel name, start event, end event) per cell-kernel call."""
+    def run(self, dom, out, want_var, cond_max, cond_split, ev=None, probe=None):
+        """Factor, duals, splits, (mixed) the probe that picks each system's
+        tier, cell kernels. ``ev``: a list that receives (kernel name, start
+        event, end event) per cell-kernel call; ``probe``: (probe domain,
+        estimate tolerance, variance tolerance)."""
         s = _stream()
         ws = ctypes.byref(self.ws)
 
@@ -323,6 +355,20 @@ class _KrigeBatch:
             nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
             nat.call("spi_split_f64", _ptr(self.g_cols), _ptr(gh), _ptr(gl), self.g_cols.numel(), s)
             nat.call("spi_split_f64", _ptr(self.w_hat), _ptr(wh), _ptr(wl), self.w_hat.numel(), s)
+        if self.probe is not None and probe is not None:
+            pdom, tol_e, tol_v = probe
+            pe64, pe32, pv64, pv32, pyy, o64, o32 = self.probe
+            wp = ctypes.byref(self.ws_probe)
+            if pyy is not None and want_var:
+                nat.call("spi_krige_var_tc", ctypes.byref(pdom.st), ctypes.byref(self.sy), wp,
+                         float(cond_split), _ptr(self.tc_err), s)
+            for prec, filt, o in ((1, 1, o32), (0, 0, o64)):
+                nat.call("spi_krige_cells", ctypes.byref(pdom.st), ctypes.byref(self.sy),
+                         _ptr(self.vals), wp, 1 if want_var else 0, prec, filt,
+                         float(cond_split), ctypes.byref(o), s)
+            nat.call("spi_krige_tier", ctypes.byref(self.sy), ws, pdom.C, _ptr(pe64), _ptr(pe32),
+                     _ptr(pv64 if want_var else None), _ptr(pv32 if want_var else None),
+                     float(tol_e), float(tol_v), float(cond_split), _ptr(self.tier), s)
         if self.yy is not None and want_var:
             timed("var_tc", lambda: nat.call(
                 "spi_krige_var_tc", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
@@ -361,8 +407,12 @@ class InterpPlan:
                  est_vars=False, stn_drifts=None, cell_drifts=None, min_var_thr=0.0,
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
-                 cond_max=1e13, cond_split=1e7, tensor_cores=True):
+                 cond_max=1e13, cond_split=None, tensor_cores=True, probe_cells=1024,
+                 probe_tol=2e-6):
         dev = self.dev = _require_cuda(device)
+        if cond_split is None:
+            # a cap under the probe; without it, the a-priori split
+            cond_split = 1e10 if probe_cells > 0 else 1e7
         self.cond_max, self.cond_split = cond_max, cond_split
         prec = self.prec = PRECISION[precision]
         data = np.ascontiguousarray(data, dtype=np.float64)
@@ -394,6 +444,24 @@ class InterpPlan:
                            cell_drifts if "EDK" in types else None, min_vg_val, prec)
         self.krig = []
         krig = [t for t in ("OK", "SK", "EDK") if t in types]
+        # the mixed path's probe: every system runs in both tiers on these
+        # cells first; it takes the FP32 tier only where the two agree to
+        # probe_tol of the fields' scale (the data's largest magnitude for
+        # estimates, the largest total sill for variances)
+        self.pdom = None
+        n_probe = 0
+        if krig and prec == 1 and probe_cells > 0:
+            pidx = np.unique(np.linspace(0, C - 1, min(C, int(probe_cells))).round()
+                             .astype(np.int64))
+            self.pdom = _DomainView(self.dom, pidx)
+            n_probe = self.pdom.C
+            finite = data[avail]
+            est_scale = float(np.abs(finite).max()) if finite.size else 1.0
+            sills = [sum(parse_vg(v).sill[k] for k in range(parse_vg(v).n_comp))
+                     for v in dict.fromkeys(np.asarray(vgs, dtype=object)[multi].tolist())
+                     if v is not None]
+            var_scale = max(sills) if sills else 1.0
+            self.probe_args = (self.pdom, probe_tol * est_scale, probe_tol * var_scale)
         if krig:
             vgs = np.asarray(vgs, dtype=object)
             assert np.all(vgs != "nan"), "NaN VGs not allowed!"
@@ -419,7 +487,7 @@ class InterpPlan:
                 beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
                 batches = [_KrigeBatch(dev, self.dom, kind, systems, ch, data, T, val_off, beta,
                                        prec, want_var=var is not None,
-                                       tensor_cores=tensor_cores)
+                                       tensor_cores=tensor_cores, n_probe=n_probe)
                            for ch in _chunk_systems(systems, prec, arena_budget)]
                 fills = (
                     _fill_args(dev, self.single, self.single_val,
@@ -461,7 +529,8 @@ class InterpPlan:
                 _fill_run(f, C, out, s)
             for b in batches:
                 ev = [] if timing else None
-                b.run(self.dom, out, want_var, self.cond_max, self.cond_split, ev)
+                b.run(self.dom, out, want_var, self.cond_max, self.cond_split, ev,
+                      self.probe_args if self.pdom is not None else None)
                 if timing:
                     evs["krige"].append((b, want_var, a, ev))
         for t, out, fill, p in self.idw:
@@ -504,6 +573,14 @@ class InterpPlan:
                             failed.append(int(j))
                         elif rt[k] == 1:
                             routed.append(int(j))
+            fast = []
+            for b in batches:
+                if b.tier is not None:
+                    tr = b.tier.cpu().numpy()
+                    for k, sl in enumerate(b.steps_l):
+                        if tr[k]:
+                            fast.extend(int(j) for j in sl)
+            self.info.setdefault("fp32_tier_steps", {})[kind] = sorted(fast)
             self.info["failed_steps"][kind] = sorted(failed)
             self.info.setdefault("exact_inverse_steps", {})[kind] = sorted(routed)
             self.info["cond"][kind] = cond
@@ -585,14 +662,18 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  stn_drifts=None, cell_drifts=None, min_var_thr=0.0, min_var_cut=None,
                  max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
-                 arena_budget=8 << 30, cond_max=1e13, cond_split=1e7, tensor_cores=True):
+                 arena_budget=8 << 30, cond_max=1e13, cond_split=None, tensor_cores=True,
+                 probe_cells=1024, probe_tol=2e-6):
     """Interpolate every step onto every cell on the GPU.
 
     Same inputs and outputs as the reference step engine for one grid chunk
     (see the module docstring). ``precision`` is "fp64" (plain FP64) or
     "mixed" (FP32 right-hand sides and contractions over the FP64
     factorisation; with ``tensor_cores`` the OK variance of the FP32 tier
-    runs on tcgen05 in 3xTF32). Returns ``(fields, problem_steps)``, plus an info dict
+    runs on tcgen05 in 3xTF32). In the mixed path each system first runs in
+    both tiers on ``probe_cells`` cells and takes the FP32 tier only where
+    they agree to ``probe_tol`` of the fields' scale, and only on the
+    Cholesky path with cond <= ``cond_split``. Returns ``(fields, problem_steps)``, plus an info dict
     (failed systems, condition estimates) when ``return_info``.
     """
     plan = InterpPlan(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, est_vars=est_vars,
@@ -600,7 +681,8 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                       min_var_cut=min_var_cut, max_var_cut=max_var_cut, min_vg_val=min_vg_val,
                       intrp_dtype=intrp_dtype, time_steps=time_steps, precision=precision,
                       device=device, arena_budget=arena_budget, cond_max=cond_max,
-                      cond_split=cond_split, tensor_cores=tensor_cores)
+                      cond_split=cond_split, tensor_cores=tensor_cores,
+                      probe_cells=probe_cells, probe_tol=probe_tol)
     plan.execute()
     flds = plan.fields(numpy=return_numpy)
     prblm = plan.problem_steps()

@@ -37,6 +37,6 @@ def test_large_edk_streamed():
     f64, _ = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, **kw)
     mixed, _, info = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, precision="mixed",
                                       return_info=True, **kw)
-    assert max(info["cond"]["EDK"].values()) <= 1e7  # the FP32 tier ran
+    assert info["fp32_tier_steps"]["EDK"] == [0]  # the FP32 tier ran
     assert np.abs(f64["EDK"] - ref["EDK"]).max() / scale <= 1e-9
     assert np.abs(mixed["EDK"] - ref["EDK"]).max() / scale <= 1e-5
