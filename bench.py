@@ -539,6 +539,58 @@ def run_large(args):
     print(json.dumps(line))
 
 
+def run_stress(args):
+    """The precision-stress EDK configuration: 400 Thomas-clustered stations
+    (20 parents, sigma 300 m) in a 100 km box, a Gaussian variogram of range
+    30 km with a 1e-6 micro-range nugget, one fBm elevation drift, 200 steps,
+    a 500 x 500 grid. Mixed and plain FP64 paths on the same plan inputs; the
+    mixed path's error against FP64 and the tiers its probe chose."""
+    import torch
+    from spinterps_gb300 import synth
+    from spinterps_gb300.steps import InterpPlan
+    from oracle.port import interp_args_for  # the (type, dir, label) list only
+    w = synth.stress_edk()
+    iargs = interp_args_for(["EDK"], est_vars=False)
+    C, T = w["cx"].size, w["z"].shape[0]
+    kw = dict(stn_drifts=w["stn_drift"], cell_drifts=w["cell_drift"], intrp_dtype=np.float32)
+    res = {}
+    for prec in ("mixed", "fp64"):
+        p = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], w["vgs"], iargs,
+                       precision=prec, **kw)
+        for _ in range(max(1, args.warmup)):
+            p.execute()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            p.execute()
+        b.record()
+        torch.cuda.synchronize()
+        info = p.collect_info()
+        res[prec] = (a.elapsed_time(b) / args.steps, p.flds["EDK"].double(), info)
+    f64, fm = res["fp64"][1], res["mixed"][1]
+    m = torch.isfinite(f64)
+    sc = f64[m].abs().max()
+    dd = (fm[m] - f64[m]).abs()
+    info = res["mixed"][2]
+    cond = np.array(list(info["cond"]["EDK"].values()))
+    line = {"metric": METRIC, "value": T * C / (res["mixed"][0] / 1e3), "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "dtype": "f32+f64",
+            "data": "synthetic (seeded; the reference's precision-stress configuration)",
+            "config": {"workload": "stress_edk_400stn_thomas_200steps_500x500", "stations": 400,
+                       "steps": T, "cells": C, "methods": ["EDK (fBm elevation)"],
+                       "variogram": w["vgs"][0]},
+            "fp64_path": {"value": T * C / (res["fp64"][0] / 1e3), "unit": UNIT,
+                          "ms": res["fp64"][0]},
+            "mixed_ms": res["mixed"][0], "mixed_over_fp64": res["fp64"][0] / res["mixed"][0],
+            "mixed_err_vs_fp64": {"max": float(dd.max() / sc),
+                                  "rms": float(dd.pow(2).mean().sqrt() / sc)},
+            "tiers": {"fp32_steps": len(info.get("fp32_tier_steps", {}).get("EDK", [])),
+                      "fp64_steps": T - len(info.get("fp32_tier_steps", {}).get("EDK", [])),
+                      "cond_min": float(cond.min()), "cond_max": float(cond.max())}}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -578,6 +630,8 @@ def main():
     ap.add_argument("--large", action="store_true",
                     help="the large hourly EDK configuration (one wave of steps) instead")
     ap.add_argument("--large-steps", type=int, default=152)
+    ap.add_argument("--stress", action="store_true",
+                    help="the precision-stress EDK configuration instead")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
@@ -585,6 +639,8 @@ def main():
         run_fit(args)
     elif args.large:
         run_large(args)
+    elif args.stress:
+        run_stress(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -91,6 +91,20 @@ int spi_copy_2d_arr_at_idxs(const double *arr, int64_t arr_rows, int64_t arr_col
                             double *subset, int64_t subset_cols,
                             spi_stream_t stream);
 
+/* ---- neighbour selection -------------------------------------------------
+ *
+ * Replaces SpInterpNeighborGrouping._get_nrst_neb_idxs / _get_pie_neb_idxs
+ * (interp/grps.py:147-247, with sel_equidist_refs, cyth/interpmthds.pyx:
+ * 811-890): idxs [n_dst, k] = each destination's neighbour station indices,
+ * ascending. method 1 'nrst': the k = min(n_nebs, n_ref) nearest. method 2
+ * 'pie': stations ranked by distance within n_pies angular sectors, taken
+ * nearest-of-every-sector first, k = n_nebs (requires n_pies <= n_nebs <=
+ * n_ref). Equal distances order by index (the reference: numpy's argsort).
+ * Limits: k <= 64, n_pies <= 16, n_pies * n_nebs <= 512. */
+int spi_neb_select(int32_t method, const double *dst_x, const double *dst_y, int64_t n_dst,
+                   const double *ref_x, const double *ref_y, int32_t n_ref, int32_t n_nebs,
+                   int32_t n_pies, int32_t *idxs, spi_stream_t stream);
+
 /* ---- batched step engine ------------------------------------------------
  *
  * Replaces the per-group loop of SpInterpSteps._get_interp

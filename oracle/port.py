@@ -26,6 +26,7 @@ Parity status: pinned against fixtures generated by running the reference's
 own code (tests/golden/make_golden.py); see tests/test_oracle_golden.py.
 """
 import ctypes
+import math
 
 import numpy as np
 
@@ -293,13 +294,21 @@ def interp_args_for(methods, est_vars):
 def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *,
                  est_vars=False, stn_drifts=None, cell_drifts=None,
                  min_var_thr=0.0, min_var_cut=None, max_var_cut=None,
-                 min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None):
-    """interp/steps.py:478-835 for neighbour method 'all' and one grid chunk.
+                 min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
+                 neb_sel_mthd="all", n_nebs=None, n_pies=None):
+    """interp/steps.py:478-835 for one grid chunk.
 
     data [T, N] (NaN = station missing), vgs [T] strings (or None when no
     kriging is asked for), stn_drifts [N, k], cell_drifts [k, C].
     Returns ({label: [T, C] fields}, problem time steps).
     """
+    if neb_sel_mthd != "all":
+        return _interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args,
+                                  neb_sel_mthd, n_nebs, n_pies, est_vars=est_vars,
+                                  stn_drifts=stn_drifts, cell_drifts=cell_drifts,
+                                  min_var_thr=min_var_thr, min_var_cut=min_var_cut,
+                                  max_var_cut=max_var_cut, min_vg_val=min_vg_val,
+                                  intrp_dtype=intrp_dtype, time_steps=time_steps)
     data = np.asarray(data, dtype=np.float64)
     n_steps = data.shape[0]
     n_cells = cell_x.size
@@ -368,3 +377,136 @@ def ret_mp_idxs(n_vals, n_cpus):
     if idxs.shape[0] == 1:
         idxs = np.concatenate((np.array([0]), idxs))
     return idxs
+
+
+# ---- neighbour selection 'nrst' / 'pie' (interp/grps.py:103-288) ----------
+
+def nebs_nrst(dst_xs, dst_ys, ref_xs, ref_ys, n_nebs):
+    """interp/grps.py:147-163: per destination the n_nebs nearest references
+    (numpy's argsort of the distances), as sorted indices."""
+    n = ref_xs.size
+    out = np.empty((dst_xs.size, min(n_nebs, n)), dtype=np.int64)
+    for i in range(dst_xs.size):
+        d = ((dst_xs[i] - ref_xs) ** 2 + (dst_ys[i] - ref_ys) ** 2) ** 0.5
+        out[i] = np.sort(np.argsort(d)[:n_nebs])
+    return out
+
+
+def _pie_ranks(dst_x, dst_y, ref_xs, ref_ys, n_pies):
+    """cyth/interpmthds.pyx:768-781 and 811-890 (sel_equidist_refs with
+    min_dist_thresh -1): C pow distances, the angle of every reference
+    (atan(dy/dx) with the reference's quadrant rules: dx == 0 gives 0, and
+    dx < 0 with dy == 0 stays at 0), its pie int(angle * n_pies / 2 pi), and
+    each reference's rank by distance within its pie (numpy argsort)."""
+    n = ref_xs.size
+    dists = np.array([math.pow(math.pow(dst_x - ref_xs[i], 2.0) +
+                               math.pow(dst_y - ref_ys[i], 2.0), 0.5) for i in range(n)])
+    pies = np.empty(n, dtype=np.int64)
+    two_pi = 2 * math.pi
+    for j in range(n):
+        xd, yd = ref_xs[j] - dst_x, ref_ys[j] - dst_y
+        if not xd:
+            ang = 0.0
+        else:
+            ang = math.atan(yd / xd)
+            if xd < 0 and yd > 0:
+                ang = math.pi + ang
+            elif xd < 0 and yd < 0:
+                ang = math.pi + ang
+            elif xd > 0 and yd < 0:
+                ang = two_pi + ang
+        pies[j] = int(ang * n_pies / two_pi)
+    ranks = np.full(n, -1, dtype=np.int64)
+    for j in range(n_pies):
+        if not np.any(pies == j):
+            continue
+        tem = np.where(pies == j, dists, np.inf)
+        order = np.argsort(tem)
+        for i in range(n):
+            if tem[order[i]] == np.inf:
+                break
+            ranks[order[i]] = i
+    return dists, ranks
+
+
+def nebs_pie(dst_xs, dst_ys, ref_xs, ref_ys, n_nebs, n_pies):
+    """interp/grps.py:165-247: references ordered by their rank within their
+    pie, then by distance within a rank (the nearest of every pie first);
+    the first n_nebs, as sorted indices."""
+    out = np.empty((dst_xs.size, n_nebs), dtype=np.int64)
+    for i in range(dst_xs.size):
+        dists, ranks = _pie_ranks(dst_xs[i], dst_ys[i], ref_xs, ref_ys, n_pies)
+        seq = []
+        for r in np.unique(ranks[ranks != -1]):
+            same = np.where(ranks == r)[0]
+            seq.extend(same[np.argsort(dists[same])].tolist())
+        out[i, :] = np.sort(np.array(seq)[:n_nebs])
+    return out
+
+
+def neb_groups(all_neb_idxs):
+    """interp/grps.py:103-138: destinations with identical neighbour lists,
+    groups in order of first occurrence; returns the group label of every
+    destination and the list of groups (destination indices)."""
+    _, first, inv = np.unique(all_neb_idxs, axis=0, return_index=True, return_inverse=True)
+    inv = np.asarray(inv).ravel()
+    rank = np.empty(first.size, dtype=np.int64)
+    rank[np.argsort(first)] = np.arange(first.size)
+    lab = rank[inv]
+    return lab, [np.where(lab == g)[0] for g in range(first.size)]
+
+
+def neb_idxs(method, dst_xs, dst_ys, ref_xs, ref_ys, n_nebs, n_pies):
+    """SpInterpNeighborGrouping.get_neb_idxs_and_grps (interp/grps.py:249-288)
+    for the given references: the neighbour lists of every destination."""
+    if method == "all":
+        return np.tile(np.arange(ref_xs.size), (dst_xs.size, 1))
+    if method == "nrst":
+        return nebs_nrst(dst_xs, dst_ys, ref_xs, ref_ys, n_nebs)
+    if method == "pie":
+        return nebs_pie(dst_xs, dst_ys, ref_xs, ref_ys, n_nebs, n_pies)
+    raise NotImplementedError(method)
+
+
+def _interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, method,
+                       n_nebs, n_pies, *, stn_drifts=None, cell_drifts=None, intrp_dtype=np.float32,
+                       time_steps=None, **kw):
+    """interp/steps.py:584-606 (stations that are nobody's neighbour with all
+    stations present are dropped) and 673-833 (per group of steps with the
+    same stations, every group of cells with the same neighbours is a
+    group of _get_interp with those stations)."""
+    data = np.asarray(data, dtype=np.float64)
+    T, C = data.shape[0], cell_x.size
+    if time_steps is None:
+        time_steps = np.arange(T)
+    keep = np.unique(neb_idxs(method, cell_x, cell_y, stn_x, stn_y, n_nebs, n_pies))
+    sx, sy, data = stn_x[keep], stn_y[keep], data[:, keep]
+    sd = None if stn_drifts is None else np.asarray(stn_drifts)[keep]
+    vgs = None if vgs is None else np.asarray(vgs, dtype=object)
+    labels = [a[2] for a in interp_args]
+    flds = {lab: np.full((T, C), np.nan, dtype=intrp_dtype) for lab in labels}
+    prblm = []
+    for stn_idxs, step_mask in get_grps_in_time(data):
+        sub_t = time_steps[step_mask]
+        if not stn_idxs.size:
+            for t in sub_t:
+                if t not in prblm:
+                    prblm.append(t)
+            continue
+        rows = np.where(step_mask)[0]
+        nidx = neb_idxs(method, cell_x, cell_y, sx[stn_idxs], sy[stn_idxs], n_nebs, n_pies)
+        _, groups = neb_groups(nidx)
+        for grp in groups:
+            sub = stn_idxs[nidx[grp[0]]]
+            out, pr = interp_steps(
+                sx[sub], sy[sub], data[rows][:, sub], cell_x[grp], cell_y[grp],
+                None if vgs is None else vgs[rows], interp_args,
+                stn_drifts=None if sd is None else sd[sub],
+                cell_drifts=None if cell_drifts is None else np.asarray(cell_drifts)[:, grp],
+                intrp_dtype=intrp_dtype, time_steps=sub_t, **kw)
+            for lab in labels:
+                flds[lab][np.ix_(rows, grp)] = out[lab]
+            for t in pr:
+                if t not in prblm:
+                    prblm.append(t)
+    return flds, prblm

@@ -102,6 +102,8 @@ _SIGS = {
                          c_i32, c_dbl, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
     "spi_vg_de": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_dbl, c_ptr, c_ptr, c_ptr,
                   c_ptr],
+    "spi_neb_select": [c_i32, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_i32, c_i32, c_i32, c_ptr,
+                       c_ptr],
     "spi_vg_refine": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_dbl, c_ptr, c_ptr,
                       c_ptr, c_ptr],
     "spi_vg_features": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr],

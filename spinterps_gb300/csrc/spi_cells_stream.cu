@@ -164,9 +164,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
       // double-float entries against hi/lo vectors: the product's head by
       // the FMA error, the cross terms, TwoSum into a double-float partial,
       // flushed to FP64 every 256 terms
-      df pa[SSV];
+      float ph[SSV], pl[SSV];
 #pragma unroll
-      for (int v = 0; v < SSV; ++v) pa[v] = df{0.f, 0.f};
+      for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
       int cnt = 0;
       for (int j = warp; j < n; j += SNW) {
         const int st = idx[j];
@@ -179,20 +179,21 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
             float e = __fmaf_rn(c.h, wh, -p);
             e = __fmaf_rn(c.h, wl, e);
             e = __fmaf_rn(c.l, wh, e);
-            const df s2 = two_sum(pa[v].h, p);
-            pa[v] = fast_two_sum(s2.h, s2.l + (pa[v].l + e));
+            const df s2 = two_sum(ph[v], p);
+            ph[v] = s2.h;
+            pl[v] += s2.l + e;
           }
         if (++cnt == 256) {
           cnt = 0;
 #pragma unroll
           for (int v = 0; v < SSV; ++v) {
-            acc[v] += (double)pa[v].h + (double)pa[v].l;
-            pa[v] = df{0.f, 0.f};
+            acc[v] += (double)ph[v] + (double)pl[v];
+            ph[v] = pl[v] = 0.f;
           }
         }
       }
 #pragma unroll
-      for (int v = 0; v < SSV; ++v) acc[v] += (double)pa[v].h + (double)pa[v].l;
+      for (int v = 0; v < SSV; ++v) acc[v] += (double)ph[v] + (double)pl[v];
     }
 #pragma unroll
     for (int v = 0; v < SSV; ++v) red[warp][v][lane] = acc[v];

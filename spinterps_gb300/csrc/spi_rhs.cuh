@@ -93,6 +93,12 @@ __device__ __forceinline__ df df_from(double x) {
   return {h, (float)(x - (double)h)};
 }
 
+// 2^m as an exact float product, m >= -149 (two normal powers of two).
+__device__ __forceinline__ float pow2i(int m) {
+  const int m1 = max(m, -120), m2 = m - m1;
+  return __int_as_float((m1 + 127) << 23) * __int_as_float((m2 + 127) << 23);
+}
+
 // exp of a double-float argument (t <= 0 here), relative error ~1e-9:
 // t = m ln2 + r (ln2 as a 16-bit head, so m * head is exact, plus a tail),
 // |r| <= ln2 / 2, exp(r) = 1 + r + r^2/2 (double-float) + r^3 P(r) (FP32,
@@ -112,35 +118,48 @@ __device__ __forceinline__ df df_exp(df t) {
   const df b = two_sum(a.h, 0.5f * sq);
   const float lo = a.l + b.l + r.l + 0.5f * sq_l + tail;
   const df e = fast_two_sum(b.h, lo);
-  const int mi = (int)m;
-  return {ldexpf(e.h, mi), ldexpf(e.l, mi)};
+  const float sc = pow2i((int)m);
+  return {e.h * sc, e.l * sc};
 }
 
-// Distance from split coordinates (x_hi, x_lo, y_hi, y_lo relative to a
-// common origin) as a double-float: differences by TwoSum, squares by the
-// FMA product error, one Newton step on sqrtf.
-__device__ __forceinline__ df df_dist(float4 cp, float4 sp) {
+// Squared distance from split coordinates (x_hi, x_lo, y_hi, y_lo relative
+// to a common origin) as a double-float: differences by TwoSum, squares by
+// the FMA product error.
+__device__ __forceinline__ df df_dist2(float4 cp, float4 sp) {
   const df dx0 = two_sum(cp.x, -sp.x), dy0 = two_sum(cp.z, -sp.z);
   const df dx = fast_two_sum(dx0.h, dx0.l + (cp.y - sp.y));
   const df dy = fast_two_sum(dy0.h, dy0.l + (cp.w - sp.w));
-  const df d2 = df_add(df_mul(dx, dx), df_mul(dy, dy));
-  if (!(d2.h > 0.f)) return {0.f, 0.f};
-  const float h = sqrtf(d2.h);
-  const float rr = __fmaf_rn(-h, h, d2.h) + d2.l;
-  return fast_two_sum(h, rr / (2.0f * h));
+  const float xx = __fmul_rn(dx.h, dx.h), yy = __fmul_rn(dy.h, dy.h);
+  const float ex = __fmaf_rn(dx.h, dx.h, -xx) + 2.0f * dx.h * dx.l;
+  const float ey = __fmaf_rn(dy.h, dy.h, -yy) + 2.0f * dy.h * dy.l;
+  const df s = two_sum(xx, yy);
+  return fast_two_sum(s.h, s.l + (ex + ey));
 }
 
-// Per-component constants of rhs_df: sill and 1/range as double-floats.
+// Its root: rsqrt, then one correction step (d = h + (d2 - h^2) / (2 h)).
+__device__ __forceinline__ df df_sqrt(df d2) {
+  if (!(d2.h > 0.f)) return {0.f, 0.f};
+  const float r = rsqrtf(d2.h);
+  const float h = d2.h * r;
+  const float e = __fmaf_rn(-h, h, d2.h) + d2.l;
+  return fast_two_sum(h, e * (0.5f * r));
+}
+
+// Per-component constants of rhs_df as double-floats: sill, 1 / range,
+// -3 / range and -3 / range^2.
 struct RhsDf {
-  df sill[SPI_MAX_VG_COMP], inv_r[SPI_MAX_VG_COMP];
+  df sill[SPI_MAX_VG_COMP], inv_r[SPI_MAX_VG_COMP], k1[SPI_MAX_VG_COMP], k2[SPI_MAX_VG_COMP];
   df shift;
   bool exact;  // every component has a double-float form below
   __device__ __forceinline__ void init(const spi_vg_t& vg, double sh) {
     exact = true;
 #pragma unroll
     for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
+      const double r = vg.range[c];
       sill[c] = df_from(vg.sill[c]);
-      inv_r[c] = df_from(1.0 / vg.range[c]);
+      inv_r[c] = df_from(1.0 / r);
+      k1[c] = df_from(-3.0 / r);
+      k2[c] = df_from(-3.0 / (r * r));
       if (c < vg.n_comp) {
         const int k = vg.code[c];
         if (!(k == SPI_VG_NUG || k == SPI_VG_EXP || k == SPI_VG_GAU || k == SPI_VG_SPH ||
@@ -154,46 +173,52 @@ struct RhsDf {
 
 // One covariance entry (Cholesky path) as a double-float, relative error
 // ~1e-9, for the FP32 tier's estimates and dual columns, where the
-// right-hand side's rounding is amplified by the dual weights. Same
-// entries as rhs_f64 (covariance form, the min_vg_val zeroing); entries
-// within 1e-6 of the cut, and variograms with components that have no
-// double-float form here (Pow, Hol, Rng), take rhs_f64 itself.
+// right-hand side's rounding is amplified by the dual weights, and for the
+// tensor-core variance. Same entries as rhs_f64 (covariance form, the
+// min_vg_val zeroing); entries within 1e-6 of the cut, and variograms with
+// components that have no double-float form here (Pow, Hol, Rng), take
+// rhs_f64 itself.
 __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t& vg, const RhsDf& k,
                                      int sk, double sh, float4 cp, float4 sp, int64_t gc, int st) {
   if (!k.exact) return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
-  const df d = df_dist(cp, sp);
+  const df d2 = df_dist2(cp, sp);
+  const df d = df_sqrt(d2);
   df c = {0.f, 0.f};
 #pragma unroll
   for (int q = 0; q < SPI_MAX_VG_COMP; ++q) {
-    if (q >= vg.n_comp) break;
-    const int code = vg.code[q];
-    if (code == SPI_VG_NUG) continue;
-    const df t = df_mul(d, k.inv_r[q]);  // h / r
-    df v;
-    if (code == SPI_VG_EXP) {
-      v = df_exp(df_mul(t, df{-3.0f, 0.f}));
-    } else if (code == SPI_VG_GAU) {
-      v = df_exp(df_mul(df_mul(t, t), df{-3.0f, 0.f}));
-    } else if (code == SPI_VG_SPH) {
-      if (!(t.h < 1.0f)) continue;
-      const df u = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
-      const df w = df_add(df{1.0f, 0.f}, df{0.5f * t.h, 0.5f * t.l});
-      v = df_mul(df_mul(u, u), w);
-    } else {  // LIN
-      if (t.h > 1.0f) continue;
-      v = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
+    if (q < vg.n_comp) {
+      const int code = vg.code[q];
+      df v = {0.f, 0.f};
+      if (code == SPI_VG_EXP) {
+        v = df_exp(df_mul(d, k.k1[q]));
+      } else if (code == SPI_VG_GAU) {
+        v = df_exp(df_mul(d2, k.k2[q]));
+      } else if (code == SPI_VG_SPH || code == SPI_VG_LIN) {
+        const df t = df_mul(d, k.inv_r[q]);  // h / r
+        if (t.h < 1.0f) {
+          const df u = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
+          if (code == SPI_VG_SPH) {
+            const df w = df_add(df{1.0f, 0.f}, df{0.5f * t.h, 0.5f * t.l});
+            v = df_mul(df_mul(u, u), w);
+          } else {
+            v = u;
+          }
+        }
+      }
+      if (code != SPI_VG_NUG) c = df_add(c, df_mul(k.sill[q], v));
     }
-    c = df_add(c, df_mul(k.sill[q], v));
   }
   const float mvv = (float)dom.min_vg_val;
-  const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
-  const float gap = (cut.h - mvv) + cut.l;
-  // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
-  // paths zero only exact zeros, which they agree on
-  if (mvv > 0.f && fabsf(gap) <= 1e-6f * mvv + (sk ? 0.f : 4e-9f * (float)sh))
-    return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
-  if (sk) return gap <= 0.f ? df{0.f, 0.f} : c;
-  return gap <= 0.f ? k.shift : c;
+  if (mvv > 0.f) {
+    // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
+    // paths zero only exact zeros, which they agree on
+    const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
+    const float gap = (cut.h - mvv) + cut.l;
+    if (fabsf(gap) <= 1e-6f * mvv + (sk ? 0.f : 4e-9f * (float)sh))
+      return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+    if (gap <= 0.f) return sk ? df{0.f, 0.f} : k.shift;
+  }
+  return c;
 }
 
 // Rounding bound of an FP32-tier sum(lambda), relative to sum |u_i| c_i:

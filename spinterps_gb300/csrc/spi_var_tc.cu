@@ -11,8 +11,8 @@
 // rows of Linv] lives in tensor memory (TMEM lane = cell, column = row), so
 // each lane squares and sums its own row of D. Rows of Linv go in blocks of
 // 256 (the MMA's N), the stations (K) in chunks of 32: per chunk all
-// threads stage A = the right-hand sides (128 x 32, generated, as rhs_f32
-// does for the CUDA-core path) and B = Linv's rows (256 x 32, triangular)
+// threads stage A = the right-hand sides (128 x 32, generated in
+// double-float by rhs_df) and B = Linv's rows (256 x 32, triangular)
 // in shared memory as TF32 hi/lo pairs in the no-swizzle K-major layout
 // (8-row x 16-byte core matrices), then one thread issues 4 K-steps x 3
 // MMAs (A_hi B_hi + A_hi B_lo + A_lo B_hi, "3xTF32", FP32 accumulation in
@@ -132,8 +132,8 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const bool live = gc < C;
   const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
                          : make_float4(0.f, 0.f, 0.f, 0.f);
-  RhsF32 kf;
-  kf.init(vg, 0, sh, A.dom.min_vg_val);
+  RhsDf kd;
+  kd.init(vg, sh);
   const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
   // epilogue roles: TMEM lanes of warp % 4, column half warp / 4
   const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
@@ -146,13 +146,14 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
 #pragma unroll 4
       for (int q = 0; q < 16; ++q) {
         const int kk = khalf * 16 + q, j = k0 + kk;
-        float v = 0.f;
+        df c = {0.f, 0.f};
         if (live && j < n) {
           const int st = idx[j];
-          v = rhs_f32(A.dom, vg, kf, 0, sh, cp, sp4[st], gc, st);
+          c = rhs_df(A.dom, vg, kd, 0, sh, cp, sp4[st], gc, st);
         }
         float h, l;
-        tf32_split(v, h, l);
+        tf32_split(c.h, h, l);
+        l += c.l;
         const int o = tile_off(VT_M, a_cell, kk);
         *reinterpret_cast<float*>(sAh + o) = h;
         *reinterpret_cast<float*>(sAl + o) = l;

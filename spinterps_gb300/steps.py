@@ -663,8 +663,12 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
                  arena_budget=8 << 30, cond_max=1e13, cond_split=None, tensor_cores=True,
-                 probe_cells=1024, probe_tol=2e-6):
+                 probe_cells=1024, probe_tol=2e-6, neb_sel_mthd="all", n_nebs=None,
+                 n_pies=None):
     """Interpolate every step onto every cell on the GPU.
+
+    ``neb_sel_mthd`` 'nrst' / 'pie' (with ``n_nebs``, ``n_pies``) selects
+    each cell's neighbours as the reference does (spinterps_gb300.nebs).
 
     Same inputs and outputs as the reference step engine for one grid chunk
     (see the module docstring). ``precision`` is "fp64" (plain FP64) or
@@ -676,6 +680,18 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
     Cholesky path with cond <= ``cond_split``. Returns ``(fields, problem_steps)``, plus an info dict
     (failed systems, condition estimates) when ``return_info``.
     """
+    if neb_sel_mthd != "all":
+        from .nebs import interp_steps_nebs
+        if return_info or not return_numpy:
+            raise ValueError("neighbour methods return numpy fields only")
+        return interp_steps_nebs(
+            stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_sel_mthd, n_nebs, n_pies,
+            stn_drifts=stn_drifts, cell_drifts=cell_drifts, intrp_dtype=intrp_dtype,
+            time_steps=time_steps, device=device, est_vars=est_vars, min_var_thr=min_var_thr,
+            min_var_cut=min_var_cut, max_var_cut=max_var_cut, min_vg_val=min_vg_val,
+            precision=precision, arena_budget=arena_budget, cond_max=cond_max,
+            cond_split=cond_split, tensor_cores=tensor_cores, probe_cells=probe_cells,
+            probe_tol=probe_tol)
     plan = InterpPlan(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, est_vars=est_vars,
                       stn_drifts=stn_drifts, cell_drifts=cell_drifts, min_var_thr=min_var_thr,
                       min_var_cut=min_var_cut, max_var_cut=max_var_cut, min_vg_val=min_vg_val,

@@ -165,3 +165,16 @@ def test_config1_subset(golden):
     _close(flds["OK"], g["c1_ok_est"])
     _close(flds["EST_VARS_OK"], g["c1_ok_var"], 1e-6)
     _close(flds["IDW_000"], g["c1_idw_est"], 1e-14)
+
+
+def test_oracle_neighbours_match_reference(golden):
+    """nrst / pie neighbour lists and cell groups (interp/grps.py) as the
+    reference computes them (tests/golden/nebs.npz), bit for bit."""
+    g = golden
+    sx, sy, cx, cy = g["n_sx"], g["n_sy"], g["n_cx"], g["n_cy"]
+    for mth, nn, npie in (("nrst", 8, 1), ("pie", 8, 4), ("pie", 12, 6)):
+        tag = f"{mth}_{nn}_{npie}"
+        idx = port.neb_idxs(mth, cx, cy, sx, sy, nn, npie)
+        lab, _ = port.neb_groups(idx)
+        assert np.array_equal(idx, g[f"n_{tag}_idxs"]), tag
+        assert np.array_equal(lab, g[f"n_{tag}_grp"]), tag
