@@ -253,10 +253,13 @@ def run_ours(args):
         plans[i % n_sl].execute()
     torch.cuda.synchronize()
     failed = routed = 0
+    fp32_steps = {}
     for p in plans:
         inf = p.collect_info()
         failed += len(inf["failed_steps"].get("OK", []))
         routed += len(inf.get("exact_inverse_steps", {}).get("OK", []))
+        for k, v in inf.get("fp32_tier_steps", {}).items():
+            fp32_steps[k] = fp32_steps.get(k, 0) + len(v)
     stream = torch.cuda.current_stream()
     if world > 1:
         dist.barrier()
@@ -350,7 +353,8 @@ def run_ours(args):
                        "methods": ["OK+var", "SK", "IDW p=2"], "precision": args.precision,
                        "parallelism": f"replicas x{world}",
                        "l2": "per-step working set (4.4 GB of fields + 1.6 GB factors) >> L2",
-                       "singular_steps_nnb": failed, "exact_inverse_steps": routed},
+                       "singular_steps_nnb": failed, "exact_inverse_steps": routed,
+                       "fp32_tier_steps": fp32_steps},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "ms": float(np.median(e2e_ms)) if e2e_ms else None},
@@ -470,7 +474,8 @@ def run_large(args):
     from oracle.port import interp_args_for  # the (type, dir, label) list only
     T = args.large_steps
     t0 = time.perf_counter()
-    w = synth.large_edk(n_steps=T, nx=args.large_nx, ny=args.large_nx)
+    w = synth.large_edk(n_steps=T, nx=args.large_nx, ny=args.large_nx,
+                        device="cpu" if args.synth_cpu else "cuda")
     t_gen = time.perf_counter() - t0
     pts = fitvgs.step_points(w["sx"], w["sy"], w["z"])
     mlp = warmstart.WarmStartMLP.load()
@@ -637,6 +642,8 @@ def main():
     ap.add_argument("--large-steps", type=int, default=152)
     ap.add_argument("--large-nx", type=int, default=2000,
                     help="grid side of the large configuration (2000 = the configuration's)")
+    ap.add_argument("--synth-cpu", action="store_true",
+                    help="with --large: synthesise the fields on the CPU")
     ap.add_argument("--skip-fp64", action="store_true",
                     help="with --large: skip the plain FP64 comparison (profiling runs)")
     ap.add_argument("--stress", action="store_true",
