@@ -121,7 +121,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
     }
   } else {
     if (live) cp = reinterpret_cast<const float4*>(A.dom.cell_split)[gc];
-    kd.init(vg, sh);
+    kd.init(vg, sh, A.dom.min_vg_val);
   }
   const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
 

@@ -99,27 +99,50 @@ __device__ __forceinline__ float pow2i(int m) {
   return __int_as_float((m1 + 127) << 23) * __int_as_float((m2 + 127) << 23);
 }
 
-// exp of a double-float argument (t <= 0 here), relative error ~1e-9:
-// t = m ln2 + r (ln2 as a 16-bit head, so m * head is exact, plus a tail),
-// |r| <= ln2 / 2, exp(r) = 1 + r + r^2/2 (double-float) + r^3 P(r) (FP32,
-// to r^8 / 8!: truncation 2e-10), then 2^m.
+// 2^(j/16), j = 0..15, as double-floats (one 128-byte line: the lanes of a
+// warp read it with one L1 wavefront).
+__device__ const float2 kExp2Sixteenths[16] = {
+    {1.0f, 0.0f},
+    {1.0442737340927124f, 4.8334701574503924e-08f},
+    {1.0905077457427979f, -1.3077539939843064e-08f},
+    {1.1387885808944702f, 5.386222312608879e-08f},
+    {1.1892070770263672f, 3.797635272917432e-08f},
+    {1.2418577671051025f, 4.496838101886169e-08f},
+    {1.2968395948410034f, -4.018999533172973e-08f},
+    {1.3542555570602417f, -1.0123349269974824e-08f},
+    {1.4142135381698608f, 2.4203234971764687e-08f},
+    {1.4768261909484863f, -4.500898853621038e-08f},
+    {1.5422108173370361f, 8.070904833346049e-09f},
+    {1.610490322113037f, 9.836217174097328e-09f},
+    {1.6817928552627563f, -2.4755326677450284e-08f},
+    {1.7562521696090698f, -9.235770370707996e-09f},
+    {1.8340080976486206f, -1.1239277952768134e-08f},
+    {1.9152065515518188f, 9.845328108326612e-09f},
+};
+
+// exp of a double-float argument (t <= 0 here), relative error ~1e-12:
+// t = m ln2/16 + r (ln2/16 as a 12-bit head, so m * head is exact for
+// |m| < 2^12, plus a two-float tail), |r| <= ln2/32; exp(r) = 1 + r + r^2/2
+// (double-float) + r^3 (1/6 + r/24 + r^2/120) (FP32, <= 1.7e-6, truncation
+// 1.4e-13); times 2^(j/16) from the table (j = m mod 16) and 2^(m div 16).
 __device__ __forceinline__ df df_exp(df t) {
   if (t.h < -103.0f) return {0.f, 0.f};
-  const float m = rintf(__fmul_rn(t.h, 1.44269504088896341f));
-  const float rh0 = __fmaf_rn(-m, 0.693145751953125f, t.h);
-  const float rl0 = __fmaf_rn(-m, 1.42860682030941723e-6f, t.l);
+  const float mf = rintf(__fmul_rn(t.h, 23.083120346069336f));
+  const int m = (int)mf;
+  const float rh0 = __fmaf_rn(-mf, 0.0433197021484375f, t.h);
+  const float rl0 =
+      __fmaf_rn(-mf, 1.029107354888481e-13f, __fmaf_rn(-mf, 1.9966364561696537e-06f, t.l));
   const df r = fast_two_sum(rh0, rl0);
   const float sq = __fmul_rn(r.h, r.h);
   const float sq_l = __fmaf_rn(r.h, r.h, -sq) + 2.0f * r.h * r.l;
-  const float p = 1.0f / 6 + r.h * (1.0f / 24 + r.h * (1.0f / 120 + r.h * (1.0f / 720 +
-                  r.h * (1.0f / 5040 + r.h * (1.0f / 40320)))));
-  const float tail = sq * r.h * p;
+  const float tail = sq * r.h * (1.0f / 6 + r.h * (1.0f / 24 + r.h * (1.0f / 120)));
   const df a = two_sum(1.0f, r.h);
   const df b = two_sum(a.h, 0.5f * sq);
-  const float lo = a.l + b.l + r.l + 0.5f * sq_l + tail;
-  const df e = fast_two_sum(b.h, lo);
-  const float sc = pow2i((int)m);
-  return {e.h * sc, e.l * sc};
+  const df e = fast_two_sum(b.h, a.l + b.l + r.l + 0.5f * sq_l + tail);
+  const float2 tj = __ldg(&kExp2Sixteenths[m & 15]);
+  const df v = df_mul(e, df{tj.x, tj.y});
+  const float sc = pow2i(m >> 4);
+  return {v.h * sc, v.l * sc};
 }
 
 // Squared distance from split coordinates (x_hi, x_lo, y_hi, y_lo relative
@@ -150,8 +173,14 @@ __device__ __forceinline__ df df_sqrt(df d2) {
 struct RhsDf {
   df sill[SPI_MAX_VG_COMP], inv_r[SPI_MAX_VG_COMP], k1[SPI_MAX_VG_COMP], k2[SPI_MAX_VG_COMP];
   df shift;
+  // the cut and its band in FP32, converted once: on GB300 a double <-> float
+  // conversion per entry runs on the 1/64-rate FP64 pipe
+  float mvv, band_sk, band_ok;
   bool exact;  // every component has a double-float form below
-  __device__ __forceinline__ void init(const spi_vg_t& vg, double sh) {
+  __device__ __forceinline__ void init(const spi_vg_t& vg, double sh, double min_vg_val) {
+    mvv = (float)min_vg_val;
+    band_sk = 1e-6f * mvv;
+    band_ok = 1e-6f * mvv + 4e-9f * (float)sh;
     exact = true;
 #pragma unroll
     for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
@@ -208,13 +237,12 @@ __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t& vg
       if (code != SPI_VG_NUG) c = df_add(c, df_mul(k.sill[q], v));
     }
   }
-  const float mvv = (float)dom.min_vg_val;
-  if (mvv > 0.f) {
+  if (k.mvv > 0.f) {
     // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
     // paths zero only exact zeros, which they agree on
     const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
-    const float gap = (cut.h - mvv) + cut.l;
-    if (fabsf(gap) <= 1e-6f * mvv + (sk ? 0.f : 4e-9f * (float)sh))
+    const float gap = (cut.h - k.mvv) + cut.l;
+    if (fabsf(gap) <= (sk ? k.band_sk : k.band_ok))
       return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
     if (gap <= 0.f) return sk ? df{0.f, 0.f} : k.shift;
   }

@@ -7,37 +7,35 @@
 // (n^2 flops per cell, shared by every step of the system; the rest of the
 // variance formula is in the cell kernel's FP64 epilogue).
 //
-// One CTA = 128 cells x 256 threads. The accumulator D [128 cells x 128
-// rows of Linv] lives in tensor memory (TMEM lane = cell, column = row).
-// Rows of Linv go in blocks of 128 (the MMA's N), the stations (K) in
-// chunks of 32: per chunk all threads stage A = the right-hand sides
-// (128 x 32, double-float from rhs_df) and B = Linv's rows (128 x 32,
-// triangular, from its FP32 hi/lo pair) in shared memory, each split into
-// three TF32 terms (x = x0 + x1 + x2, heads rounded to nearest), in the
-// no-swizzle K-major layout (8-row x 16-byte core matrices). One thread
-// issues 4 K-steps x 6 MMAs (the products a_i b_j with i + j <= 2, ~33
-// bits; FP32 accumulation in TMEM) and commits them to an mbarrier that
-// every thread waits on (with an iteration limit: on expiry the kernel
-// raises err_flag, frees its TMEM and returns). Every 128 stations the
-// accumulator is flushed into double-float registers (each thread: its
-// cell, 64 of the block's rows) and restarted, so no FP32 sum runs longer
-// than 128 terms; each block's rows are then squared and summed in FP64.
+// One CTA = 128 cells x 256 threads. The accumulator D [128 cells x 256
+// rows of Linv] lives in tensor memory (TMEM lane = cell, column = row), so
+// each lane squares and sums its own row of D. Rows of Linv go in blocks of
+// 256 (the MMA's N), the stations (K) in chunks of 32: per chunk all
+// threads stage A = the right-hand sides (128 x 32, generated in
+// double-float by rhs_df) and B = Linv's rows (256 x 32, triangular)
+// in shared memory as TF32 hi/lo pairs in the no-swizzle K-major layout
+// (8-row x 16-byte core matrices), then one thread issues 4 K-steps x 3
+// MMAs (A_hi B_hi + A_hi B_lo + A_lo B_hi, "3xTF32", FP32 accumulation in
+// TMEM) and commits them to an mbarrier that every thread waits on (with an
+// iteration limit: on expiry the kernel raises err_flag, frees its TMEM
+// and returns). 3xTF32 keeps ~22 bits of each operand; emulated on the
+// batched workload's well-conditioned systems it stays within 7e-7 of the
+// sill. Squares are summed in double-float (FP32 pairs: the FP64 pipe is
+// 1/64 of FP32 on GB300); the mixed path's probe checks every system.
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
 
 namespace spi {
 
 constexpr int VT_M = 128;   // cells per CTA (MMA M, TMEM lanes)
-constexpr int VT_N = 128;   // Linv rows per block (MMA N, TMEM columns)
+constexpr int VT_N = 256;   // Linv rows per block (MMA N, TMEM columns)
 constexpr int VT_KC = 32;   // stations per staged chunk
-constexpr int VT_FLUSH = 4; // chunks per FP32 accumulation (128 stations)
 constexpr int VT_T = 256;   // threads
-constexpr int VT_COLS = VT_N / 2;    // accumulator columns per thread
 constexpr long VT_SPIN = 1L << 26;   // mbarrier polls before giving up
 
 constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;
 constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;
-constexpr size_t VT_SMEM = 3 * VT_A_BYTES + 3 * VT_B_BYTES;
+constexpr size_t VT_SMEM = 2 * VT_A_BYTES + 2 * VT_B_BYTES;
 
 struct VarTcArgs {
   spi_domain_t dom;
@@ -67,18 +65,13 @@ __device__ __forceinline__ int tile_off(int R, int row, int k) {
   return (k >> 2) * (R * 16) + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4;
 }
 
-// TF32 keeps the top 19 bits of an FP32 value. A double-float x = h + l
-// as three TF32 terms: t0 = h rounded to them (half away from zero on the
-// magnitude), t1 = the remainder (h - t0) + l rounded likewise, t2 = what
-// is left (the tensor core truncates it): ~33 bits of x.
-__device__ __forceinline__ float tf32_rn(float x) {
-  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
-__device__ __forceinline__ void tf32_split3(float h, float l, float& t0, float& t1, float& t2) {
-  t0 = tf32_rn(h);
-  const float r = (h - t0) + l;
-  t1 = tf32_rn(r);
-  t2 = r - t1;
+// TF32 keeps the top 19 bits of an FP32 value: hi = x rounded to those
+// bits (half away from zero on the magnitude), lo = the exact remainder
+// (|lo| <= 2^-11 |x|), itself truncated by the tensor core. Rounding the
+// head rather than truncating it halves lo and the split's error.
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+  lo = x - hi;
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
@@ -89,7 +82,7 @@ __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uin
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
-__global__ __launch_bounds__(VT_T, 1) void k_var_tc(VarTcArgs A) {
+__global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const int s = blockIdx.y;
   const int64_t C = A.dom.n_cells;
   const int64_t c0 = (int64_t)blockIdx.x * VT_M;
@@ -102,13 +95,13 @@ __global__ __launch_bounds__(VT_T, 1) void k_var_tc(VarTcArgs A) {
   const int64_t moff = A.sys.mat_off[s];
   const spi_vg_t vg = A.sys.vg[s];
   const double sh = A.ws.shift[s];
-  const float* Lh = A.ws.linv_hi + moff;
-  const float* Ll = A.ws.linv_lo + moff;
+  const float* L = A.ws.linv_hi + moff;
 
   extern __shared__ __align__(1024) unsigned char smv[];
-  unsigned char* sA[3] = {smv, smv + VT_A_BYTES, smv + 2 * VT_A_BYTES};
-  unsigned char* sB[3] = {smv + 3 * VT_A_BYTES, smv + 3 * VT_A_BYTES + VT_B_BYTES,
-                          smv + 3 * VT_A_BYTES + 2 * VT_B_BYTES};
+  unsigned char* sAh = smv;
+  unsigned char* sAl = sAh + VT_A_BYTES;
+  unsigned char* sBh = sAl + VT_A_BYTES;
+  unsigned char* sBl = sBh + VT_B_BYTES;
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tbase;
   __shared__ int fail;
@@ -130,7 +123,7 @@ __global__ __launch_bounds__(VT_T, 1) void k_var_tc(VarTcArgs A) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tbase;
-  // kind::tf32, D FP32, A/B TF32 K-major, N = 128, M = 128
+  // kind::tf32, D FP32, A/B TF32 K-major, N = 256, M = 128
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(VT_N >> 3) << 17) |
                          ((uint32_t)(VT_M >> 4) << 24);
 
@@ -141,21 +134,16 @@ __global__ __launch_bounds__(VT_T, 1) void k_var_tc(VarTcArgs A) {
   const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
                          : make_float4(0.f, 0.f, 0.f, 0.f);
   RhsDf kd;
-  kd.init(vg, sh);
+  kd.init(vg, sh, A.dom.min_vg_val);
   const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
-  // epilogue roles: TMEM lanes of warp % 4, columns [e_half * 64, +64)
+  // epilogue roles: TMEM lanes of warp % 4, column half warp / 4
   const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
-  const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(e_half * VT_COLS);
-  float yh[VT_COLS], yl[VT_COLS];
-  double yy = 0.0;
+  df yy = {0.f, 0.f};  // sum of squares, double-float (no FP64 pipe per row)
   uint32_t phase = 0;
 
   for (int rb = 0; rb < n; rb += VT_N) {
     const int kend = min(n, rb + VT_N);
-#pragma unroll
-    for (int c = 0; c < VT_COLS; ++c) yh[c] = yl[c] = 0.f;
-    int chunk = 0;
-    for (int k0 = 0; k0 < kend; k0 += VT_KC, ++chunk) {
+    for (int k0 = 0; k0 < kend; k0 += VT_KC) {
 #pragma unroll 4
       for (int q = 0; q < 16; ++q) {
         const int kk = khalf * 16 + q, j = k0 + kk;
@@ -164,49 +152,38 @@ __global__ __launch_bounds__(VT_T, 1) void k_var_tc(VarTcArgs A) {
           const int st = idx[j];
           c = rhs_df(A.dom, vg, kd, 0, sh, cp, sp4[st], gc, st);
         }
-        float t0, t1, t2;
-        tf32_split3(c.h, c.l, t0, t1, t2);
+        float h, l;
+        tf32_split(c.h, h, l);
+        l += c.l;
         const int o = tile_off(VT_M, a_cell, kk);
-        *reinterpret_cast<float*>(sA[0] + o) = t0;
-        *reinterpret_cast<float*>(sA[1] + o) = t1;
-        *reinterpret_cast<float*>(sA[2] + o) = t2;
+        *reinterpret_cast<float*>(sAh + o) = h;
+        *reinterpret_cast<float*>(sAl + o) = l;
       }
 #pragma unroll 4
       for (int i = 0; i < VT_N * VT_KC / VT_T; ++i) {
         const int e = tid + VT_T * i, r = e >> 5, k = e & 31;
         const int row = rb + r, col = k0 + k;
-        float h = 0.f, l = 0.f;
-        if (row < n && col <= row) {
-          h = Lh[(int64_t)row * n + col];
-          l = Ll[(int64_t)row * n + col];
-        }
-        float t0, t1, t2;
-        tf32_split3(h, l, t0, t1, t2);
+        const float v = (row < n && col <= row) ? L[(int64_t)row * n + col] : 0.f;
+        float h, l;
+        tf32_split(v, h, l);
         const int o = tile_off(VT_N, r, k);
-        *reinterpret_cast<float*>(sB[0] + o) = t0;
-        *reinterpret_cast<float*>(sB[1] + o) = t1;
-        *reinterpret_cast<float*>(sB[2] + o) = t2;
+        *reinterpret_cast<float*>(sBh + o) = h;
+        *reinterpret_cast<float*>(sBl + o) = l;
       }
       asm volatile("fence.proxy.async.shared::cta;");
       __syncthreads();
       if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const bool restart = (chunk % VT_FLUSH) == 0;
 #pragma unroll
         for (int ks = 0; ks < VT_KC / 8; ++ks) {
           const uint32_t ao = 2 * ks * (VT_M * 16), bo = 2 * ks * (VT_N * 16);
-          uint64_t ad[3], bd[3];
-#pragma unroll
-          for (int t = 0; t < 3; ++t) {
-            ad[t] = umma_desc(smem_u32(sA[t]) + ao, VT_M * 16, 128);
-            bd[t] = umma_desc(smem_u32(sB[t]) + bo, VT_N * 16, 128);
-          }
-          mma_tf32(tmem, ad[0], bd[0], idesc, (restart && ks == 0) ? 0u : 1u);
-          mma_tf32(tmem, ad[0], bd[1], idesc, 1u);
-          mma_tf32(tmem, ad[1], bd[0], idesc, 1u);
-          mma_tf32(tmem, ad[0], bd[2], idesc, 1u);
-          mma_tf32(tmem, ad[2], bd[0], idesc, 1u);
-          mma_tf32(tmem, ad[1], bd[1], idesc, 1u);
+          const uint64_t ah = umma_desc(smem_u32(sAh) + ao, VT_M * 16, 128);
+          const uint64_t al = umma_desc(smem_u32(sAl) + ao, VT_M * 16, 128);
+          const uint64_t bh = umma_desc(smem_u32(sBh) + bo, VT_N * 16, 128);
+          const uint64_t bl = umma_desc(smem_u32(sBl) + bo, VT_N * 16, 128);
+          mma_tf32(tmem, ah, bh, idesc, (k0 > 0 || ks > 0) ? 1u : 0u);
+          mma_tf32(tmem, ah, bl, idesc, 1u);
+          mma_tf32(tmem, al, bh, idesc, 1u);
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -224,47 +201,45 @@ __global__ __launch_bounds__(VT_T, 1) void k_var_tc(VarTcArgs A) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       __syncthreads();
       if (fail) break;
-      // flush: every VT_FLUSH chunks and at the end of the block's stations
-      if ((chunk % VT_FLUSH) == VT_FLUSH - 1 || k0 + VT_KC >= kend) {
-#pragma unroll
-        for (int cc = 0; cc < VT_COLS / 32; ++cc) {
-          uint32_t r[32];
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-              "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-                "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
-                "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-                "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-                "=r"(r[30]), "=r"(r[31])
-              : "r"(t_row + (uint32_t)(cc * 32)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const df t = two_sum(yh[cc * 32 + i], __uint_as_float(r[i]));
-            yh[cc * 32 + i] = t.h;
-            yl[cc * 32 + i] += t.l;
-          }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-      }
     }
     if (fail) break;
+    // this block's rows: each lane's 128 columns of its half
 #pragma unroll
-    for (int c = 0; c < VT_COLS; ++c) {
-      const double y = (double)yh[c] + (double)yl[c];
-      yy += y * y;
+    for (int cc = 0; cc < 4; ++cc) {
+      uint32_t r[32];
+      const uint32_t addr =
+          tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(e_half * 128 + cc * 32);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+            "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+            "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+            "=r"(r[31])
+          : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const float y = __uint_as_float(r[i]);
+        const float p = __fmul_rn(y, y);
+        const df t = two_sum(yy.h, p);
+        yy.h = t.h;
+        yy.l += t.l + __fmaf_rn(y, y, -p);
+      }
     }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
   }
-  if (e_half == 1) half_yy[e_cell] = yy;
+  const double yy64 = (double)yy.h + (double)yy.l;
+  if (e_half == 1) half_yy[e_cell] = yy64;
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (fail) {
     if (tid == 0) atomicExch(A.err, 1);
   } else if (e_half == 0 && c0 + e_cell < C) {
-    A.ws.cell_yy[(int64_t)s * C + c0 + e_cell] = yy + half_yy[e_cell];
+    A.ws.cell_yy[(int64_t)s * C + c0 + e_cell] = yy64 + half_yy[e_cell];
   }
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(VT_N));
@@ -280,7 +255,7 @@ extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sy
   if (!dom || !sys || !ws || !err_flag) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (sys->n_sys == 0 || dom->n_cells == 0) return SPI_OK;
-  if (!ws->cell_yy || !ws->linv_hi || !ws->linv_lo || !ws->route || !ws->cond || !ws->shift ||
+  if (!ws->cell_yy || !ws->linv_hi || !ws->route || !ws->cond || !ws->shift ||
       !dom->cell_split || !dom->stn_split || !sys->vg || !sys->stn_off || !sys->stn_idx ||
       !sys->mat_off)
     return SPI_ERR_ARG;
