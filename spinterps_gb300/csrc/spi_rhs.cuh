@@ -127,8 +127,12 @@ __device__ const float2 kExp2Sixteenths[16] = {
 // 1.4e-13); times 2^(j/16) from the table (j = m mod 16) and 2^(m div 16).
 __device__ __forceinline__ df df_exp(df t) {
   if (t.h < -103.0f) return {0.f, 0.f};
-  const float mf = rintf(__fmul_rn(t.h, 23.083120346069336f));
-  const int m = (int)mf;
+  // round to an integer by adding 1.5 * 2^23 (no conversion instruction:
+  // those run on GB300's 1/64-rate FP64 / conversion pipe); |t| * 16/ln2
+  // < 2^22 here, so the integer sits in the low mantissa bits
+  const float big = __fadd_rn(__fmul_rn(t.h, 23.083120346069336f), 12582912.0f);
+  const int m = __float_as_int(big) - 0x4B400000;
+  const float mf = __fsub_rn(big, 12582912.0f);
   const float rh0 = __fmaf_rn(-mf, 0.0433197021484375f, t.h);
   const float rl0 =
       __fmaf_rn(-mf, 1.029107354888481e-13f, __fmaf_rn(-mf, 1.9966364561696537e-06f, t.l));

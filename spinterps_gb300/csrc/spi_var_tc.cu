@@ -10,18 +10,19 @@
 // One CTA = 128 cells x 256 threads. The accumulator D [128 cells x 256
 // rows of Linv] lives in tensor memory (TMEM lane = cell, column = row), so
 // each lane squares and sums its own row of D. Rows of Linv go in blocks of
-// 256 (the MMA's N), the stations (K) in chunks of 32: per chunk all
-// threads stage A = the right-hand sides (128 x 32, generated in
-// double-float by rhs_df) and B = Linv's rows (256 x 32, triangular)
-// in shared memory as TF32 hi/lo pairs in the no-swizzle K-major layout
-// (8-row x 16-byte core matrices), then one thread issues 4 K-steps x 3
-// MMAs (A_hi B_hi + A_hi B_lo + A_lo B_hi, "3xTF32", FP32 accumulation in
-// TMEM) and commits them to an mbarrier that every thread waits on (with an
-// iteration limit: on expiry the kernel raises err_flag, frees its TMEM
-// and returns). 3xTF32 keeps ~22 bits of each operand; emulated on the
-// batched workload's well-conditioned systems it stays within 7e-7 of the
-// sill. Squares are summed in double-float (FP32 pairs: the FP64 pipe is
-// 1/64 of FP32 on GB300); the mixed path's probe checks every system.
+// 256 (the MMA's N), the stations (K) in chunks of 16: per chunk all
+// threads stage A = the right-hand sides (128 x 16, generated in
+// double-float by rhs_df) and B = Linv's rows (256 x 16, triangular)
+// in shared memory in the no-swizzle K-major layout (8-row x 16-byte core
+// matrices), A as two TF32 terms (a0 + a1, ~22 bits), Linv as three
+// (b0 + b1 + b2, ~33 bits: its rounding, amplified by the cancellation in
+// Linv c, dominates the variance's error). One thread then issues 2
+// K-steps x 5 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 + a1 b1, FP32
+// accumulation in TMEM) and commits them to an mbarrier that every thread
+// waits on (with an iteration limit: on expiry the kernel raises err_flag,
+// frees its TMEM and returns). Squares are summed in double-float (FP32 pairs: the FP64
+// pipe is 1/64 of FP32 on GB300); the mixed path's probe checks every
+// system's variance against the FP64 kernel.
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
 
@@ -29,13 +30,13 @@ namespace spi {
 
 constexpr int VT_M = 128;   // cells per CTA (MMA M, TMEM lanes)
 constexpr int VT_N = 256;   // Linv rows per block (MMA N, TMEM columns)
-constexpr int VT_KC = 32;   // stations per staged chunk
+constexpr int VT_KC = 16;   // stations per staged chunk
 constexpr int VT_T = 256;   // threads
 constexpr long VT_SPIN = 1L << 26;   // mbarrier polls before giving up
 
 constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;
 constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;
-constexpr size_t VT_SMEM = 2 * VT_A_BYTES + 2 * VT_B_BYTES;
+constexpr size_t VT_SMEM = 2 * VT_A_BYTES + 3 * VT_B_BYTES;
 
 struct VarTcArgs {
   spi_domain_t dom;
@@ -59,10 +60,14 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// Byte offset of (row, k) in an R x 32 TF32 tile (K-major, no swizzle):
+// Byte offset of (row, k) in an R x KC TF32 tile (K-major, no swizzle):
 // core matrix (row / 8, k / 4) at (k / 4) * R * 16 + (row / 8) * 128.
 __device__ __forceinline__ int tile_off(int R, int row, int k) {
   return (k >> 2) * (R * 16) + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+__device__ __forceinline__ float tf32_rn(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 // TF32 keeps the top 19 bits of an FP32 value: hi = x rounded to those
@@ -95,13 +100,15 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const int64_t moff = A.sys.mat_off[s];
   const spi_vg_t vg = A.sys.vg[s];
   const double sh = A.ws.shift[s];
-  const float* L = A.ws.linv_hi + moff;
+  const float* Lh = A.ws.linv_hi + moff;
+  const float* Ll = A.ws.linv_lo + moff;
 
   extern __shared__ __align__(1024) unsigned char smv[];
   unsigned char* sAh = smv;
   unsigned char* sAl = sAh + VT_A_BYTES;
-  unsigned char* sBh = sAl + VT_A_BYTES;
-  unsigned char* sBl = sBh + VT_B_BYTES;
+  unsigned char* sB0 = sAl + VT_A_BYTES;
+  unsigned char* sB1 = sB0 + VT_B_BYTES;
+  unsigned char* sB2 = sB1 + VT_B_BYTES;
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tbase;
   __shared__ int fail;
@@ -127,7 +134,7 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(VT_N >> 3) << 17) |
                          ((uint32_t)(VT_M >> 4) << 24);
 
-  // staging roles: A = cell (tid % 128), stations [khalf * 16, +16) of a chunk
+  // staging roles: A = cell (tid % 128), stations [khalf * KC/2, +KC/2) of a chunk
   const int a_cell = tid & (VT_M - 1), khalf = tid >> 7;
   const int64_t gc = c0 + a_cell;
   const bool live = gc < C;
@@ -145,8 +152,8 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
     const int kend = min(n, rb + VT_N);
     for (int k0 = 0; k0 < kend; k0 += VT_KC) {
 #pragma unroll 4
-      for (int q = 0; q < 16; ++q) {
-        const int kk = khalf * 16 + q, j = k0 + kk;
+      for (int q = 0; q < VT_KC / 2; ++q) {
+        const int kk = khalf * (VT_KC / 2) + q, j = k0 + kk;
         df c = {0.f, 0.f};
         if (live && j < n) {
           const int st = idx[j];
@@ -161,14 +168,22 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
       }
 #pragma unroll 4
       for (int i = 0; i < VT_N * VT_KC / VT_T; ++i) {
-        const int e = tid + VT_T * i, r = e >> 5, k = e & 31;
+        const int e = tid + VT_T * i, r = e / VT_KC, k = e % VT_KC;
         const int row = rb + r, col = k0 + k;
-        const float v = (row < n && col <= row) ? L[(int64_t)row * n + col] : 0.f;
-        float h, l;
-        tf32_split(v, h, l);
+        float vh = 0.f, vl = 0.f;
+        if (row < n && col <= row) {
+          vh = Lh[(int64_t)row * n + col];
+          vl = Ll[(int64_t)row * n + col];
+        }
+        // Linv in three TF32 terms (~33 bits): its rounding, amplified by
+        // the cancellation in Linv c, dominates the variance's error
+        const float b0 = tf32_rn(vh);
+        const float r1 = (vh - b0) + vl;
+        const float b1 = tf32_rn(r1);
         const int o = tile_off(VT_N, r, k);
-        *reinterpret_cast<float*>(sBh + o) = h;
-        *reinterpret_cast<float*>(sBl + o) = l;
+        *reinterpret_cast<float*>(sB0 + o) = b0;
+        *reinterpret_cast<float*>(sB1 + o) = b1;
+        *reinterpret_cast<float*>(sB2 + o) = r1 - b1;
       }
       asm volatile("fence.proxy.async.shared::cta;");
       __syncthreads();
@@ -179,11 +194,14 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
           const uint32_t ao = 2 * ks * (VT_M * 16), bo = 2 * ks * (VT_N * 16);
           const uint64_t ah = umma_desc(smem_u32(sAh) + ao, VT_M * 16, 128);
           const uint64_t al = umma_desc(smem_u32(sAl) + ao, VT_M * 16, 128);
-          const uint64_t bh = umma_desc(smem_u32(sBh) + bo, VT_N * 16, 128);
-          const uint64_t bl = umma_desc(smem_u32(sBl) + bo, VT_N * 16, 128);
-          mma_tf32(tmem, ah, bh, idesc, (k0 > 0 || ks > 0) ? 1u : 0u);
-          mma_tf32(tmem, ah, bl, idesc, 1u);
-          mma_tf32(tmem, al, bh, idesc, 1u);
+          const uint64_t b0 = umma_desc(smem_u32(sB0) + bo, VT_N * 16, 128);
+          const uint64_t b1 = umma_desc(smem_u32(sB1) + bo, VT_N * 16, 128);
+          const uint64_t b2 = umma_desc(smem_u32(sB2) + bo, VT_N * 16, 128);
+          mma_tf32(tmem, ah, b0, idesc, (k0 > 0 || ks > 0) ? 1u : 0u);
+          mma_tf32(tmem, ah, b1, idesc, 1u);
+          mma_tf32(tmem, al, b0, idesc, 1u);
+          mma_tf32(tmem, ah, b2, idesc, 1u);
+          mma_tf32(tmem, al, b1, idesc, 1u);
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(

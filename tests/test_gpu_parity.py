@@ -278,3 +278,17 @@ def test_mixed_vs_fp64_on_the_batched_workload():
                                 precision="mixed", **kw)
     for lab in f64:
         assert _err(mixed[lab], f64[lab]) <= MIXED_TOL, lab
+
+
+def test_mixed_without_tensor_cores():
+    """The FP32 tier on CUDA cores only (tensor_cores=False: k_krige_cells
+    <float> with its own variance pass) at the mixed bar."""
+    spi = _spi()
+    sx, sy, z, cx, cy, vgs, sd, cd = _random_case(7)
+    args = port.interp_args_for(["OK", "SK", ("IDW", 2.0)], est_vars=True)
+    kw = dict(est_vars=True, min_var_thr=0.1, min_vg_val=1e-4, intrp_dtype=np.float64)
+    ref, _ = port.interp_steps(sx, sy, z, cx, cy, vgs, args, **kw)
+    got, _ = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, precision="mixed",
+                              tensor_cores=False, **kw)
+    for lab in ref:
+        assert _err(got[lab], ref[lab]) <= MIXED_TOL, lab
