@@ -253,13 +253,15 @@ def run_ours(args):
         plans[i % n_sl].execute()
     torch.cuda.synchronize()
     failed = routed = 0
-    fp32_steps = {}
+    fp32_steps, probe = {}, {}
     for p in plans:
         inf = p.collect_info()
         failed += len(inf["failed_steps"].get("OK", []))
         routed += len(inf.get("exact_inverse_steps", {}).get("OK", []))
         for k, v in inf.get("fp32_tier_steps", {}).items():
             fp32_steps[k] = fp32_steps.get(k, 0) + len(v)
+        for k, d in inf.get("probe_disc", {}).items():
+            probe.setdefault(k, []).append(d)
     stream = torch.cuda.current_stream()
     if world > 1:
         dist.barrier()
@@ -354,7 +356,12 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}",
                        "l2": "per-step working set (4.4 GB of fields + 1.6 GB factors) >> L2",
                        "singular_steps_nnb": failed, "exact_inverse_steps": routed,
-                       "fp32_tier_steps": fp32_steps},
+                       "fp32_tier_steps": fp32_steps,
+                       "probe_disc_quantiles": {
+                           k: {lab: [float(q) for q in np.nanquantile(
+                               np.concatenate(v)[:, c], [0.25, 0.5, 0.75, 0.9])]
+                               for c, lab in ((0, "est"), (1, "var"))}
+                           for k, v in probe.items()}},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "ms": float(np.median(e2e_ms)) if e2e_ms else None},

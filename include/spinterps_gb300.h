@@ -259,14 +259,17 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
  * (precision 1, route_filter 1, cond_split = cond_cap). tier[s] = 1 when the
  * system is on the Cholesky path, cond <= cond_cap, and over its steps and
  * the probe cells |est32 - est64| <= tol_est and |var32 - var64| <= tol_var
- * (var arrays may be NULL; a NaN in one field and not the other fails). The
+ * (var arrays may be NULL; a NaN in one field and not the other fails).
+ * disc (optional, [n_sys, 2]): each system's largest |est32 - est64| and
+ * |var32 - var64| over the probe (NaN for systems not on the Cholesky path
+ * under cond_cap, +inf for a NaN mismatch). The
  * mixed path's a-posteriori error control: the FP32 rounding of the
  * right-hand sides enters the estimate as sum_i dc_i w_i, which the dual
  * weights can amplify far beyond what the condition number predicts. */
 int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n_probe,
                    const double *est64, const double *est32, const double *var64,
                    const double *var32, double tol_est, double tol_var, double cond_cap,
-                   int32_t *tier, spi_stream_t stream);
+                   int32_t *tier, double *disc, spi_stream_t stream);
 
 /* The OK variance term |Linv c|^2 of every cell of the FP32-tier systems
  * (ws->tier, else route 0 and cond <= cond_split; kinds OK / EDK) on the tensor cores

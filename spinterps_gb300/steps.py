@@ -285,6 +285,7 @@ class _KrigeBatch:
         if precision == 1 and n_probe > 0:
             n_sys = len(ch)
             self.tier = torch.zeros(n_sys, dtype=torch.int32, device=dev)
+            self.disc = torch.zeros((n_sys, 2), dtype=torch.float64, device=dev)
             f = lambda: torch.full((T, n_probe), float("nan"), dtype=torch.float64, device=dev)
             pe64, pe32 = f(), f()
             pv64, pv32 = (f(), f()) if want_var else (None, None)
@@ -368,7 +369,8 @@ class _KrigeBatch:
                          float(cond_split), ctypes.byref(o), s)
             nat.call("spi_krige_tier", ctypes.byref(self.sy), ws, pdom.C, _ptr(pe64), _ptr(pe32),
                      _ptr(pv64 if want_var else None), _ptr(pv32 if want_var else None),
-                     float(tol_e), float(tol_v), float(cond_split), _ptr(self.tier), s)
+                     float(tol_e), float(tol_v), float(cond_split), _ptr(self.tier),
+                     _ptr(self.disc), s)
         if self.yy is not None and want_var:
             timed("var_tc", lambda: nat.call(
                 "spi_krige_var_tc", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
@@ -575,14 +577,18 @@ class InterpPlan:
                             failed.append(int(j))
                         elif rt[k] == 1:
                             routed.append(int(j))
-            fast = []
+            fast, disc = [], []
             for b in batches:
                 if b.tier is not None:
+                    disc.append(b.disc.cpu().numpy())
                     tr = b.tier.cpu().numpy()
                     for k, sl in enumerate(b.steps_l):
                         if tr[k]:
                             fast.extend(int(j) for j in sl)
             self.info.setdefault("fp32_tier_steps", {})[kind] = sorted(fast)
+            if disc:
+                # per system: largest probe discrepancy of estimates, variances
+                self.info.setdefault("probe_disc", {})[kind] = np.concatenate(disc)
             self.info["failed_steps"][kind] = sorted(failed)
             self.info.setdefault("exact_inverse_steps", {})[kind] = sorted(routed)
             self.info["cond"][kind] = cond
