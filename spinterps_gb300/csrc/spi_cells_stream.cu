@@ -113,7 +113,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
 
   double cx = 0.0, cy = 0.0;
   float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
-  RhsDf kd;
+  __shared__ RhsDf kd;
   if constexpr (sizeof(T) == 8) {
     if (live) {
       cx = A.dom.cell_x[gc];
@@ -121,8 +121,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
     }
   } else {
     if (live) cp = reinterpret_cast<const float4*>(A.dom.cell_split)[gc];
-    kd.init(vg, sh, A.dom.min_vg_val);
+    if (tid == 0) kd.init(vg, sh, A.dom.min_vg_val);
   }
+  const spi_vg_t* vgp = A.sys.vg + s;
   const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
 
   for (int v0 = 0; v0 < nvec; v0 += SSV) {
@@ -170,7 +171,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
       int cnt = 0;
       for (int j = warp; j < n; j += SNW) {
         const int st = idx[j];
-        const df c = live ? rhs_df(A.dom, vg, kd, sk, sh, cp, sp4[st], gc, st) : df{0.f, 0.f};
+        const df c = live ? rhs_df(A.dom, vgp, kd, sk, sh, cp, sp4[st], gc, st) : df{0.f, 0.f};
 #pragma unroll
         for (int v = 0; v < SSV; ++v)
           if (v < nv) {

@@ -298,7 +298,8 @@ __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
   double* A = l_arena + v.moff;
   extern __shared__ double gsm[];
   double* f = gsm;                                   // [m]
-  int* piv = reinterpret_cast<int*>(gsm + m);        // [m]
+  double* prow = gsm + m;                            // [m] the scaled pivot row
+  int* piv = reinterpret_cast<int*>(gsm + 2 * m);    // [m]
   __shared__ double rv[FT];
   __shared__ int ri[FT];
   __shared__ int fail;
@@ -367,15 +368,22 @@ __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
     const double dd = dk;
     for (int j = tid; j < m; j += FT) {
       double x = (j == k) ? 1.0 : A[(int64_t)k * m + j];
-      A[(int64_t)k * m + j] = x / dd;
+      x = x / dd;
+      A[(int64_t)k * m + j] = x;
+      prow[j] = x;
     }
     for (int i = tid; i < m; i += FT) f[i] = (i == k) ? 0.0 : A[(int64_t)i * m + k];
     __syncthreads();
-    for (int64_t e = tid; e < (int64_t)m * m; e += FT) {
-      int i = (int)(e / m), j = (int)(e - (int64_t)i * m);
+    // eliminate column k from every other row: a warp per row, lanes over
+    // its columns (coalesced, no index division)
+    for (int i = tid >> 5; i < m; i += FT / 32) {
       if (i == k) continue;
-      double base = (j == k) ? 0.0 : A[e];
-      A[e] = base - f[i] * A[(int64_t)k * m + j];
+      const double fi = f[i];
+      double* row = A + (int64_t)i * m;
+      for (int j = tid & 31; j < m; j += 32) {
+        const double base = (j == k) ? 0.0 : row[j];
+        row[j] = base - fi * prow[j];
+      }
     }
     __syncthreads();
   }
@@ -682,7 +690,7 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   SPI_LAUNCH_CHECK();
   k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->linv_arena, ws->status, ws->cond);
   SPI_LAUNCH_CHECK();
-  size_t gsm = (size_t)(sys->max_n + GA) * (sizeof(double) + sizeof(int));
+  size_t gsm = (size_t)(sys->max_n + GA) * (2 * sizeof(double) + sizeof(int));
   if (gsm > 200 * 1024) return SPI_ERR_TOO_LARGE;
   if (gsm > 48 * 1024 &&
       cudaFuncSetAttribute(k_gj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm) !=

@@ -174,30 +174,33 @@ __device__ __forceinline__ df df_sqrt(df d2) {
 
 // Per-component constants of rhs_df as double-floats: sill, 1 / range,
 // -3 / range and -3 / range^2.
+// Kernels keep one RhsDf per CTA in shared memory (computed by one thread):
+// held in registers, the compiler may recompute its FP64-derived constants
+// inside the hot loop, on GB300's 1/64-rate FP64 / conversion pipe.
 struct RhsDf {
   df sill[SPI_MAX_VG_COMP], inv_r[SPI_MAX_VG_COMP], k1[SPI_MAX_VG_COMP], k2[SPI_MAX_VG_COMP];
   df shift;
-  // the cut and its band in FP32, converted once: on GB300 a double <-> float
-  // conversion per entry runs on the 1/64-rate FP64 pipe
-  float mvv, band_sk, band_ok;
-  bool exact;  // every component has a double-float form below
+  float mvv, band_sk, band_ok;  // the min_vg_val cut and its bands in FP32
+  int ncomp, code[SPI_MAX_VG_COMP];
+  int exact;  // every component has a double-float form below
   __device__ __forceinline__ void init(const spi_vg_t& vg, double sh, double min_vg_val) {
     mvv = (float)min_vg_val;
     band_sk = 1e-6f * mvv;
     band_ok = 1e-6f * mvv + 4e-9f * (float)sh;
-    exact = true;
-#pragma unroll
+    ncomp = vg.n_comp;
+    exact = 1;
     for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
       const double r = vg.range[c];
       sill[c] = df_from(vg.sill[c]);
       inv_r[c] = df_from(1.0 / r);
       k1[c] = df_from(-3.0 / r);
       k2[c] = df_from(-3.0 / (r * r));
+      code[c] = vg.code[c];
       if (c < vg.n_comp) {
         const int k = vg.code[c];
         if (!(k == SPI_VG_NUG || k == SPI_VG_EXP || k == SPI_VG_GAU || k == SPI_VG_SPH ||
               k == SPI_VG_LIN))
-          exact = false;
+          exact = 0;
       }
     }
     shift = df_from(sh);
@@ -211,16 +214,17 @@ struct RhsDf {
 // min_vg_val zeroing); entries within 1e-6 of the cut, and variograms with
 // components that have no double-float form here (Pow, Hol, Rng), take
 // rhs_f64 itself.
-__device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t& vg, const RhsDf& k,
+__device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vgp, const RhsDf& k,
                                      int sk, double sh, float4 cp, float4 sp, int64_t gc, int st) {
-  if (!k.exact) return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+  if (!k.exact)
+    return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
   const df d2 = df_dist2(cp, sp);
   const df d = df_sqrt(d2);
   df c = {0.f, 0.f};
 #pragma unroll
   for (int q = 0; q < SPI_MAX_VG_COMP; ++q) {
-    if (q < vg.n_comp) {
-      const int code = vg.code[q];
+    if (q < k.ncomp) {
+      const int code = k.code[q];
       df v = {0.f, 0.f};
       if (code == SPI_VG_EXP) {
         v = df_exp(df_mul(d, k.k1[q]));
@@ -247,7 +251,7 @@ __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t& vg
     const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
     const float gap = (cut.h - k.mvv) + cut.l;
     if (fabsf(gap) <= (sk ? k.band_sk : k.band_ok))
-      return df_from(rhs_f64(dom, vg, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+      return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
     if (gap <= 0.f) return sk ? df{0.f, 0.f} : k.shift;
   }
   return c;

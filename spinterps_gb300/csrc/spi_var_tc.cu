@@ -140,8 +140,10 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const bool live = gc < C;
   const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
                          : make_float4(0.f, 0.f, 0.f, 0.f);
-  RhsDf kd;
-  kd.init(vg, sh, A.dom.min_vg_val);
+  __shared__ RhsDf kd;
+  if (tid == 0) kd.init(vg, sh, A.dom.min_vg_val);
+  __syncthreads();
+  const spi_vg_t* vgp = A.sys.vg + s;
   const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
   // epilogue roles: TMEM lanes of warp % 4, column half warp / 4
   const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
@@ -157,7 +159,7 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
         df c = {0.f, 0.f};
         if (live && j < n) {
           const int st = idx[j];
-          c = rhs_df(A.dom, vg, kd, 0, sh, cp, sp4[st], gc, st);
+          c = rhs_df(A.dom, vgp, kd, 0, sh, cp, sp4[st], gc, st);
         }
         float h, l;
         tf32_split(c.h, h, l);
