@@ -25,6 +25,7 @@ namespace spi {
 constexpr int STC = 32;  // cells per CTA (one per lane)
 constexpr int SNW = 8;   // warps per CTA (station groups)
 constexpr int SSV = 4;   // vectors per pass
+constexpr int SCH = 256; // stations per shared-memory chunk (FP32 tier)
 
 template <typename T, typename OutT>
 __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A) {
@@ -61,6 +62,8 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   __shared__ const float* vpl[SSV];
   __shared__ int any_bad;
   __shared__ int any_chk;
+  __shared__ float4 s_sp[sizeof(T) == 4 ? SCH : 1];
+  __shared__ float2 s_w[SSV][sizeof(T) == 4 ? SCH : 1];
 
   const int64_t gc = c0 + lane;
   const bool live = gc < C;
@@ -169,27 +172,40 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
 #pragma unroll
       for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
       int cnt = 0;
-      for (int j = warp; j < n; j += SNW) {
-        const int st = idx[j];
-        const df c = live ? rhs_df(A.dom, vgp, kd, sk, sh, cp, sp4[st], gc, st) : df{0.f, 0.f};
+      // stations in chunks staged in shared memory: split coordinates and
+      // the vectors' hi/lo pairs, read by every warp at a shared index
+      for (int j0 = 0; j0 < n; j0 += SCH) {
+        const int nj = min(SCH, n - j0);
+        __syncthreads();
+        for (int e = tid; e < nj; e += STC * SNW) {
+          s_sp[e] = sp4[idx[j0 + e]];
 #pragma unroll
-        for (int v = 0; v < SSV; ++v)
-          if (v < nv) {
-            const float wh = vph[v][j], wl = vpl[v][j];
-            const float p = __fmul_rn(c.h, wh);
-            float e = __fmaf_rn(c.h, wh, -p);
-            e = __fmaf_rn(c.h, wl, e);
-            e = __fmaf_rn(c.l, wh, e);
-            const df s2 = two_sum(ph[v], p);
-            ph[v] = s2.h;
-            pl[v] += s2.l + e;
-          }
-        if (++cnt == 256) {
-          cnt = 0;
+          for (int v = 0; v < SSV; ++v)
+            if (v < nv) s_w[v][e] = make_float2(vph[v][j0 + e], vpl[v][j0 + e]);
+        }
+        __syncthreads();
+        for (int jj = warp; jj < nj; jj += SNW) {
+          const df c = live ? rhs_df(A.dom, vgp, kd, sk, sh, cp, s_sp[jj], gc, idx + j0 + jj)
+                            : df{0.f, 0.f};
 #pragma unroll
-          for (int v = 0; v < SSV; ++v) {
-            acc[v] += (double)ph[v] + (double)pl[v];
-            ph[v] = pl[v] = 0.f;
+          for (int v = 0; v < SSV; ++v)
+            if (v < nv) {
+              const float2 w = s_w[v][jj];
+              const float p = __fmul_rn(c.h, w.x);
+              float e = __fmaf_rn(c.h, w.x, -p);
+              e = __fmaf_rn(c.h, w.y, e);
+              e = __fmaf_rn(c.l, w.x, e);
+              const df s2 = two_sum(ph[v], p);
+              ph[v] = s2.h;
+              pl[v] += s2.l + e;
+            }
+          if (++cnt == 256) {
+            cnt = 0;
+#pragma unroll
+            for (int v = 0; v < SSV; ++v) {
+              acc[v] += (double)ph[v] + (double)pl[v];
+              ph[v] = pl[v] = 0.f;
+            }
           }
         }
       }

@@ -183,12 +183,21 @@ struct RhsDf {
   float mvv, band_sk, band_ok;  // the min_vg_val cut and its bands in FP32
   int ncomp, code[SPI_MAX_VG_COMP];
   int exact;  // every component has a double-float form below
+  int single;  // index of the only non-nugget component, or -1
   __device__ __forceinline__ void init(const spi_vg_t& vg, double sh, double min_vg_val) {
     mvv = (float)min_vg_val;
     band_sk = 1e-6f * mvv;
     band_ok = 1e-6f * mvv + 4e-9f * (float)sh;
     ncomp = vg.n_comp;
     exact = 1;
+    int nst = 0;
+    single = -1;
+    for (int c = 0; c < vg.n_comp; ++c)
+      if (vg.code[c] != SPI_VG_NUG) {
+        ++nst;
+        single = c;
+      }
+    if (nst != 1) single = -1;
     for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
       const double r = vg.range[c];
       sill[c] = df_from(vg.sill[c]);
@@ -207,6 +216,18 @@ struct RhsDf {
   }
 };
 
+// Correlation rho(h) of one structure in double-float (Exp, Gau, Sph, Lin).
+__device__ __forceinline__ df rho_df(int code, df d, df d2, df k1, df k2, df inv_r) {
+  if (code == SPI_VG_EXP) return df_exp(df_mul(d, k1));
+  if (code == SPI_VG_GAU) return df_exp(df_mul(d2, k2));
+  const df t = df_mul(d, inv_r);  // h / r
+  if (!(t.h < 1.0f)) return {0.f, 0.f};
+  const df u = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
+  if (code == SPI_VG_LIN) return u;
+  const df w = df_add(df{1.0f, 0.f}, df{0.5f * t.h, 0.5f * t.l});
+  return df_mul(df_mul(u, u), w);
+}
+
 // One covariance entry (Cholesky path) as a double-float, relative error
 // ~1e-9, for the FP32 tier's estimates and dual columns, where the
 // right-hand side's rounding is amplified by the dual weights, and for the
@@ -215,35 +236,24 @@ struct RhsDf {
 // components that have no double-float form here (Pow, Hol, Rng), take
 // rhs_f64 itself.
 __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vgp, const RhsDf& k,
-                                     int sk, double sh, float4 cp, float4 sp, int64_t gc, int st) {
+                                     int sk, double sh, float4 cp, float4 sp, int64_t gc,
+                                     const int32_t* stp) {
   if (!k.exact)
-    return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+    return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], *stp));
   const df d2 = df_dist2(cp, sp);
   const df d = df_sqrt(d2);
   df c = {0.f, 0.f};
+  if (k.single >= 0) {
+    // the common case: one structure (plus nuggets, which add nothing to
+    // the covariance off the diagonal)
+    const int q = k.single;
+    c = df_mul(k.sill[q], rho_df(k.code[q], d, d2, k.k1[q], k.k2[q], k.inv_r[q]));
+  } else {
 #pragma unroll
-  for (int q = 0; q < SPI_MAX_VG_COMP; ++q) {
-    if (q < k.ncomp) {
-      const int code = k.code[q];
-      df v = {0.f, 0.f};
-      if (code == SPI_VG_EXP) {
-        v = df_exp(df_mul(d, k.k1[q]));
-      } else if (code == SPI_VG_GAU) {
-        v = df_exp(df_mul(d2, k.k2[q]));
-      } else if (code == SPI_VG_SPH || code == SPI_VG_LIN) {
-        const df t = df_mul(d, k.inv_r[q]);  // h / r
-        if (t.h < 1.0f) {
-          const df u = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
-          if (code == SPI_VG_SPH) {
-            const df w = df_add(df{1.0f, 0.f}, df{0.5f * t.h, 0.5f * t.l});
-            v = df_mul(df_mul(u, u), w);
-          } else {
-            v = u;
-          }
-        }
-      }
-      if (code != SPI_VG_NUG) c = df_add(c, df_mul(k.sill[q], v));
-    }
+    for (int q = 0; q < SPI_MAX_VG_COMP; ++q)
+      if (q < k.ncomp && k.code[q] != SPI_VG_NUG)
+        c = df_add(c, df_mul(k.sill[q],
+                             rho_df(k.code[q], d, d2, k.k1[q], k.k2[q], k.inv_r[q])));
   }
   if (k.mvv > 0.f) {
     // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
@@ -251,7 +261,7 @@ __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vg
     const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
     const float gap = (cut.h - k.mvv) + cut.l;
     if (fabsf(gap) <= (sk ? k.band_sk : k.band_ok))
-      return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], st));
+      return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], *stp));
     if (gap <= 0.f) return sk ? df{0.f, 0.f} : k.shift;
   }
   return c;

@@ -158,8 +158,7 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
         const int kk = khalf * (VT_KC / 2) + q, j = k0 + kk;
         df c = {0.f, 0.f};
         if (live && j < n) {
-          const int st = idx[j];
-          c = rhs_df(A.dom, vgp, kd, 0, sh, cp, sp4[st], gc, st);
+          c = rhs_df(A.dom, vgp, kd, 0, sh, cp, sp4[idx[j]], gc, idx + j);
         }
         float h, l;
         tf32_split(c.h, h, l);
