@@ -50,6 +50,12 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   const int64_t st0 = A.sys.step_off[s];
   const int nsteps = (int)(A.sys.step_off[s + 1] - st0);
   const int nvec = ndual + nsteps;
+  // OK / EDK without the variance: the dual columns feed only the sum
+  // check, and sum(lambda) = q0 - sum_k S_0k nu_k is 1 identically whatever
+  // q is (nu = S^-1 (q - f)); they need no more than FP32 (the estimates,
+  // SK's u'c and the OK variance's q0 keep double-float)
+  const bool var_needed = A.want_var && A.out.var != nullptr && !sk;
+  const int plain_duals = (sizeof(T) == 4 && !sk && !prim && !var_needed) ? ndual : 0;
   const spi_vg_t vg = A.sys.vg[s];
   const double sh = A.ws.shift[s];
 
@@ -189,7 +195,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
                             : df{0.f, 0.f};
 #pragma unroll
           for (int v = 0; v < SSV; ++v)
-            if (v < nv) {
+            if (v < nv && v0 + v < plain_duals) {
+              ph[v] = __fmaf_rn(c.h, s_w[v][jj].x, ph[v]);
+            } else if (v < nv) {
               const float2 w = s_w[v][jj];
               const float p = __fmul_rn(c.h, w.x);
               float e = __fmaf_rn(c.h, w.x, -p);
