@@ -129,10 +129,13 @@ typedef struct {
     const float *stn_split, *cell_split;
 } spi_domain_t;
 
-/* out[i] = (x_hi, x_lo, y_hi, y_lo) with x_hi = (float)(x[i] - ox) and
- * x_lo = (float)((x[i] - ox) - x_hi), likewise for y (device arrays). */
+/* out[i] = (x_hi, x_lo, y_hi, y_lo) with x_hi = (x[i] - ox) rounded to a
+ * multiple of res and x_lo = (float)((x[i] - ox) - x_hi), likewise for y
+ * (device arrays). res = 0: x_hi = (float)(x[i] - ox). With res a power of
+ * two and every |x - ox| <= 2^22 res, heads are exact floats and so are
+ * their differences: the double-float distance needs no TwoSum there. */
 int spi_split_coords(const double *x, const double *y, int64_t n, double ox,
-                     double oy, float *out, spi_stream_t stream);
+                     double oy, double res, float *out, spi_stream_t stream);
 
 /* hi[i] = (float)x[i], lo[i] = (float)(x[i] - hi[i]) (device arrays): the
  * FP32 pair of the split-precision contractions, made once per system. */

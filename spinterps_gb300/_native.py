@@ -78,7 +78,7 @@ _SIGS = {
                             c_dbl, c_ptr],
     "spi_copy_2d_arr_at_idxs": [c_ptr, c_i64, c_i64, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_i64,
                                 c_ptr],
-    "spi_split_coords": [c_ptr, c_ptr, c_i64, c_dbl, c_dbl, c_ptr, c_ptr],
+    "spi_split_coords": [c_ptr, c_ptr, c_i64, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr],
     "spi_split_f64": [c_ptr, c_ptr, c_ptr, c_i64, c_ptr],
     "spi_krige_factor": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],

@@ -486,25 +486,34 @@ extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys
 
 namespace spi {
 __global__ void k_split_coords(const double* __restrict__ x, const double* __restrict__ y,
-                               int64_t n, double ox, double oy, float4* __restrict__ out) {
+                               int64_t n, double ox, double oy, double res,
+                               float4* __restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     double dx = x[i] - ox, dy = y[i] - oy;
-    float xh = (float)dx, yh = (float)dy;
+    float xh, yh;
+    if (res > 0.0) {
+      xh = (float)(rint(dx / res) * res);
+      yh = (float)(rint(dy / res) * res);
+    } else {
+      xh = (float)dx;
+      yh = (float)dy;
+    }
     out[i] = make_float4(xh, (float)(dx - (double)xh), yh, (float)(dy - (double)yh));
   }
 }
 }  // namespace spi
 
 extern "C" int spi_split_coords(const double* x, const double* y, int64_t n, double ox,
-                                double oy, float* out, spi_stream_t stream) {
+                                double oy, double res, float* out, spi_stream_t stream) {
   if (n < 0) return SPI_ERR_ARG;
   if (n == 0) return SPI_OK;
-  if (!x || !y || !out || (reinterpret_cast<uintptr_t>(out) & 15)) return SPI_ERR_ARG;
+  if (!x || !y || !out || (reinterpret_cast<uintptr_t>(out) & 15) || !(res >= 0.0))
+    return SPI_ERR_ARG;
   int64_t blocks = (n + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   spi::k_split_coords<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
-      x, y, n, ox, oy, reinterpret_cast<float4*>(out));
+      x, y, n, ox, oy, res, reinterpret_cast<float4*>(out));
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

@@ -150,12 +150,12 @@ __device__ __forceinline__ df df_exp(df t) {
 }
 
 // Squared distance from split coordinates (x_hi, x_lo, y_hi, y_lo relative
-// to a common origin) as a double-float: differences by TwoSum, squares by
-// the FMA product error.
+// to a common origin, heads on a power-of-two grid so that their
+// difference is exact: spi_split_coords) as a double-float, squares by the
+// FMA product error.
 __device__ __forceinline__ df df_dist2(float4 cp, float4 sp) {
-  const df dx0 = two_sum(cp.x, -sp.x), dy0 = two_sum(cp.z, -sp.z);
-  const df dx = fast_two_sum(dx0.h, dx0.l + (cp.y - sp.y));
-  const df dy = fast_two_sum(dy0.h, dy0.l + (cp.w - sp.w));
+  const df dx = fast_two_sum(__fsub_rn(cp.x, sp.x), __fsub_rn(cp.y, sp.y));
+  const df dy = fast_two_sum(__fsub_rn(cp.z, sp.z), __fsub_rn(cp.w, sp.w));
   const float xx = __fmul_rn(dx.h, dx.h), yy = __fmul_rn(dy.h, dy.h);
   const float ex = __fmaf_rn(dx.h, dx.h, -xx) + 2.0f * dx.h * dx.l;
   const float ey = __fmaf_rn(dy.h, dy.h, -yy) + 2.0f * dy.h * dy.l;
@@ -184,6 +184,7 @@ struct RhsDf {
   int ncomp, code[SPI_MAX_VG_COMP];
   int exact;  // every component has a double-float form below
   int single;  // index of the only non-nugget component, or -1
+  int nug_clear;  // nuggets alone exceed the cut: OK / EDK entries never zero
   __device__ __forceinline__ void init(const spi_vg_t& vg, double sh, double min_vg_val) {
     mvv = (float)min_vg_val;
     band_sk = 1e-6f * mvv;
@@ -198,6 +199,10 @@ struct RhsDf {
         single = c;
       }
     if (nst != 1) single = -1;
+    double nug = 0.0;
+    for (int c = 0; c < vg.n_comp; ++c)
+      if (vg.code[c] == SPI_VG_NUG) nug += vg.sill[c];
+    nug_clear = nug > min_vg_val * (1.0 + 1e-3) + 1e-8 * sh;
     for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
       const double r = vg.range[c];
       sill[c] = df_from(vg.sill[c]);
@@ -255,9 +260,10 @@ __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vg
         c = df_add(c, df_mul(k.sill[q],
                              rho_df(k.code[q], d, d2, k.k1[q], k.k2[q], k.inv_r[q])));
   }
-  if (k.mvv > 0.f) {
+  if (k.mvv > 0.f && (sk || !k.nug_clear)) {
     // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
-    // paths zero only exact zeros, which they agree on
+    // paths zero only exact zeros, which they agree on; OK / EDK entries
+    // whose nuggets exceed the cut are never zeroed (gamma >= nugget)
     const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
     const float gap = (cut.h - k.mvv) + cut.l;
     if (fabsf(gap) <= (sk ? k.band_sk : k.band_ok))

@@ -182,11 +182,15 @@ class _Domain:
         if precision == 1:
             ox = float(min(self.sx.min().item(), self.cx.min().item()))
             oy = float(min(self.sy.min().item(), self.cy.min().item()))
+            ext = max(float(max(self.sx.max().item(), self.cx.max().item())) - ox,
+                      float(max(self.sy.max().item(), self.cy.max().item())) - oy, 1e-300)
+            # heads on a power-of-two grid with <= 22 significant bits
+            res = 2.0 ** (np.ceil(np.log2(ext)) - 22)
             self.ssplit = torch.empty((self.N, 4), dtype=torch.float32, device=dev)
             self.csplit = torch.empty((self.C, 4), dtype=torch.float32, device=dev)
-            nat.call("spi_split_coords", _ptr(self.sx), _ptr(self.sy), self.N, ox, oy,
+            nat.call("spi_split_coords", _ptr(self.sx), _ptr(self.sy), self.N, ox, oy, res,
                      _ptr(self.ssplit), _stream())
-            nat.call("spi_split_coords", _ptr(self.cx), _ptr(self.cy), self.C, ox, oy,
+            nat.call("spi_split_coords", _ptr(self.cx), _ptr(self.cy), self.C, ox, oy, res,
                      _ptr(self.csplit), _stream())
         self.st = nat.DomainT(self.N, _ptr(self.sx), _ptr(self.sy), self.C, _ptr(self.cx),
                               _ptr(self.cy), k, _ptr(self.sd), _ptr(self.cd), float(min_vg_val),
