@@ -608,6 +608,85 @@ def run_stress(args):
     print(json.dumps(line))
 
 
+def run_legacy(args):
+    """The single-neighbourhood classes (cyth/interpmthds.pyx:251-765):
+    OrdinaryKriging of 400 stations onto the cells of a legacy_nx^2 grid
+    (default 500 x 500 = 250 000 output points), with every array the class
+    exposes materialised (rhss, lambdas, the inverse). value: the kernels on
+    device-resident inputs (spi_legacy_system + spi_legacy_points); e2e: the
+    class call, numpy in and numpy out; cpu_baseline: the oracle's
+    restatement of the class's per-point loop (np.matmul(pinv, rhs) per
+    point, serial like the reference's class) on a sample of points."""
+    import torch
+    from spinterps_gb300 import legacy
+    from oracle import port
+    rng = np.random.default_rng(SEED + 7)
+    n, nx, box = 400, args.legacy_nx, 1e5
+    xi, yi = rng.uniform(0, box, n), rng.uniform(0, box, n)
+    zi = rng.gamma(1.2, 3.0, n)
+    cs = box / nx
+    gx = np.arange(nx) * cs + 0.5 * cs
+    cx, cy = np.meshgrid(gx, gx[::-1])
+    cx, cy = cx.ravel().copy(), cy.ravel().copy()
+    n_out, m = cx.size, n + 1
+    model = "0.1 Nug(0.0) + 0.9 Exp(30000)"
+    dv = [torch.as_tensor(a, device="cuda") for a in (xi, yi, zi, cx, cy)]
+    st = torch.cuda.current_stream()
+    for _ in range(max(3, args.warmup)):
+        r = legacy.krige_points("OK", *dv, model)
+    torch.cuda.synchronize()
+    evs = []
+    with Clocks() as clk:
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            r = legacy.krige_points("OK", *dv, model)
+            e1.record(st)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    assert r["route"] == "gj"
+    # e2e: the class, numpy in and out (copies inside)
+    t0 = time.perf_counter()
+    obj = legacy.OrdinaryKriging(xi, yi, zi, cx, cy, model=model)
+    obj.krige()
+    t_e2e = time.perf_counter() - t0
+    h2d = 8 * (3 * n + 2 * n_out)
+    d2h = 8 * (n * n + 2 * m * m + n_out * m + n_out * n + 3 * n_out)
+    # the oracle on a bounded sample of points, timed on one host core
+    samp = min(n_out, args.legacy_cpu_points)
+    sel = rng.choice(n_out, samp, replace=False)
+    t0 = time.perf_counter()
+    ref = port.legacy_krige("OrdinaryKriging", xi, yi, zi, cx[sel], cy[sel], model)
+    t_cpu = time.perf_counter() - t0
+    err = float(np.abs(obj.zk[sel] - ref["zk"]).max() / np.abs(ref["zk"]).max())
+    flop = 2.0 * m * m * n_out
+    bf16, hbm, src = measured_peaks()
+    line = {"metric": "legacy_points_per_s", "value": n_out / (ms / 1e3), "unit": "points/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"legacy_ordinary_kriging_{n}stn_{nx}x{nx}",
+                       "stations": n, "points": n_out, "variogram": model,
+                       "l2": "outputs (1.6 GB per step) exceed L2"},
+            "e2e": {"value": n_out / t_e2e, "unit": "points/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": 4 * args.steps,
+            "roofline": {"bound": "fp64", "kernel": "spi::k_leg_lambda (lambda = P r, FP64)",
+                         "achieved": flop / (ms / 1e3) / 1e12, "peak": FP64_NOMINAL_TFLOPS,
+                         "unit": "TFLOP/s", "frac": flop / (ms / 1e3) / 1e12 / FP64_NOMINAL_TFLOPS,
+                         "traffic": None,
+                         "peak_source": "nominal FP64 pipe (not in MEASURED_PEAKS.json)",
+                         "note": "2 m^2 FLOP per point over the whole step time (the "
+                                 "factorisation, right-hand sides and epilogue count "
+                                 "against it)"},
+            "cpu_baseline": {"value": samp / t_cpu, "unit": "points/s", "cores": 1,
+                             "kind": "port", "sample": f"{samp} random points of the grid, "
+                             "the per-point loop of the reference's class"},
+            "err_vs_oracle": err, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -655,8 +734,14 @@ def main():
                     help="with --large: skip the plain FP64 comparison (profiling runs)")
     ap.add_argument("--stress", action="store_true",
                     help="the precision-stress EDK configuration instead")
+    ap.add_argument("--legacy", action="store_true",
+                    help="the single-neighbourhood OrdinaryKriging class instead")
+    ap.add_argument("--legacy-nx", type=int, default=500)
+    ap.add_argument("--legacy-cpu-points", type=int, default=4000)
     args = ap.parse_args()
-    if args.profile_case:
+    if args.legacy:
+        run_legacy(args)
+    elif args.profile_case:
         run_profile_case(args)
     elif args.fit:
         run_fit(args)

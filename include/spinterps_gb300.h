@@ -469,6 +469,48 @@ int spi_krige_ok_noalloc(const spi_domain_t *dom, const int32_t *stn_idx, int32_
                          const spi_vg_t *vg, const double *vals, int32_t n_steps,
                          int32_t want_var, const spi_out_t *out, spi_stream_t stream);
 
+/* ---- the single-neighbourhood classes ----------------------------------
+ *
+ * Replace the arithmetic of OrdinaryKriging, SimpleKriging,
+ * ExternalDriftKriging, ExternalDriftKriging_MD, OrdinaryIndicatorKriging
+ * and SimpleIndicatorKriging (cyth/interpmthds.pyx:251-765): one station
+ * set, one variogram (vg: HOST pointer), kind SPI_KIND_OK / SK / EDK
+ * (EDK: n_drift >= 1; ExternalDriftKriging is n_drift = 1). Device arrays.
+ * Their semantics, unlike the step engine's: the station semivariogram
+ * matrix is 0 on its diagonal and a point's right-hand side is 0 at distance
+ * 0 (a nugget is a discontinuity), no min_vg_val cut, no sum check; the SK
+ * matrix is -gamma with a zero diagonal (SimpleKriging fills its covariance
+ * matrix with the total sill before summing it, i.e. with 0.0). */
+
+/* in_dists [n, n], lhs and lhs_inv [m, m] (m = n for SK, else n + 1 +
+ * n_drift): cyth/interpmthds.pyx:293-335 (OK), 405-445 (SK), 516-559
+ * (EDK), 644-689 (EDK_MD). lhs_inv is the Gauss-Jordan inverse standing in
+ * for numpy.linalg.pinv; *status (device int) = 0, or k + 1 when the matrix
+ * is singular at elimination step k; *cond (device double, optional) =
+ * ||lhs||_F ||lhs_inv||_F (+inf when singular), an upper bound of cond_2:
+ * while cond * m * DBL_EPSILON <= 1, pinv's cut-off drops no singular value
+ * and pinv equals this inverse; above it the caller takes an SVD
+ * pseudo-inverse. si [n_drift, n]. Limit: m <= 10240. */
+int spi_legacy_system(int32_t kind, const double *xi, const double *yi, int32_t n,
+                      const double *si, int32_t n_drift, const spi_vg_t *vg,
+                      double *in_dists, double *lhs, double *lhs_inv, int32_t *status,
+                      double *cond, spi_stream_t stream);
+
+/* Every output point k of xk, yk [n_out] (sk_drift [n_drift, n_out]):
+ * rhss [n_out, m], lambdas [n_out, n], mus [m - n, n_out] (NULL for SK),
+ * zk [n_out] = lambda'zi; est [n_out] (NULL to skip) = the OK est_vars
+ * max(0, lambda'gamma + mu) or the SK est_covars max(0, total sill -
+ * lambda'c). With ixi (the indicator values of ikrige, else NULL):
+ * ik [n_out] = max(0, lambda'ixi) and est = max(0, ik (1 - ik)).
+ * cyth/interpmthds.pyx:337-362 (OK), 447-471 (SK), 561-585 (EDK), 691-719
+ * (EDK_MD), 722-765 (indicator). */
+int spi_legacy_points(int32_t kind, const double *xi, const double *yi, const double *zi,
+                      const double *ixi, int32_t n, const double *xk, const double *yk,
+                      const double *sk_drift, int64_t n_out, int32_t n_drift,
+                      const spi_vg_t *vg, const double *lhs_inv, double *rhss,
+                      double *lambdas, double *mus, double *zk, double *est, double *ik,
+                      spi_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

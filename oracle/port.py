@@ -21,6 +21,8 @@ timing is a fair stand-in for the reference's own CPU path:
 - ``interp_steps``          interp/steps.py:478-835 (neighbour method 'all')
 - ``get_grps_in_time``      interp/grps.py:57-101 (without pandas)
 - ``ret_mp_idxs``           misc.py:601-613
+- ``legacy_krige``          cyth/interpmthds.pyx:251-765 (the single-neighbourhood
+                            kriging classes)
 
 Parity status: pinned against fixtures generated by running the reference's
 own code (tests/golden/make_golden.py); see tests/test_oracle_golden.py.
@@ -510,3 +512,135 @@ def _interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, met
                 if t not in prblm:
                     prblm.append(t)
     return flds, prblm
+
+
+# ---- the single-neighbourhood classes of cyth/interpmthds.pyx:251-765 ------
+
+LEGACY_CLASSES = ("OrdinaryKriging", "SimpleKriging", "ExternalDriftKriging",
+                  "ExternalDriftKriging_MD", "OrdinaryIndicatorKriging",
+                  "SimpleIndicatorKriging")
+
+
+def _vg_comp_arr(dists, comp):
+    """gamma of one variogram component at every entry (the reference's
+    vg_ftn(h, range, sill) of cyth/interpmthds.pyx:38-84)."""
+    code, sill, rng = comp
+    dists = np.ascontiguousarray(dists, dtype=np.float64)
+    out = np.empty_like(dists)
+    codes = np.array([code], dtype=np.int32)
+    sills = np.array([sill], dtype=np.float64)
+    ranges = np.array([rng], dtype=np.float64)
+    _build.lib().orc_fill_vg_var_arr(
+        _ptr(dists), dists.shape[0], dists.shape[1], _ptr(out), 0, 0, 1, _ptr(codes),
+        _ptr(sills), _ptr(ranges), float("-inf"))
+    return out
+
+
+def legacy_krige(cls, xi, yi, zi, xk, yk, model, si=None, sk=None, lim=None):
+    """What ``cls(...).krige()`` (``ikrige()`` for the indicator classes)
+    leaves in the object's arrays, as a dict keyed by attribute name.
+
+    Follows cyth/interpmthds.pyx:251-765:
+    - components parsed with the split rules of parse_vg_str (lines 294-303),
+      ranges clamped to max(1e-5, r);
+    - station distances for j > i, mirrored; the semivariogram matrix sums
+      the components in order for i != j and keeps 0 on the diagonal, so a
+      nugget is a discontinuity at h = 0 (not the sill, as in
+      fill_vg_var_arr);
+    - OK: [[G, 1], [1', 0]]; EDK: [[G, 1, S'], [1', 0, 0], [S, 0, 0]] with
+      S = si [k, n] (ExternalDriftKriging: k = 1); SK: the matrix starts at
+      the fill value 0.0 that __init__ gave it before krige() summed the
+      sills, so it is -G with a zero diagonal (lines 397-399, 413, 432-442);
+    - P = numpy.linalg.pinv of that matrix; per point, the right-hand side
+      sums gamma over components where the distance is not 0 (SK: total
+      sill minus them, the total sill where the distance is 0) plus 1 and
+      the point's drifts; lambda = P r by np.matmul per point;
+    - zk = sum(lambda[:n] z); OK: est_vars = max(0, lambda'r + mu);
+      SK: est_covars = max(0, total sill - lambda'c);
+    - indicator classes: ixi = (z <= lim), ik = max(0, sum(lambda ixi)),
+      est = max(0, ik (1 - ik)).
+    """
+    assert cls in LEGACY_CLASSES, cls
+    xi, yi, zi, xk, yk = (np.ascontiguousarray(a, dtype=np.float64)
+                          for a in (xi, yi, zi, xk, yk))
+    comps = parse_vg_str(model)
+    n, n_out = xi.size, xk.size
+    sk_kind = cls in ("SimpleKriging", "SimpleIndicatorKriging")
+    edk = cls.startswith("ExternalDrift")
+    if edk:
+        si = np.atleast_2d(np.asarray(si, dtype=np.float64))
+        sk = np.atleast_2d(np.asarray(sk, dtype=np.float64))
+    n_drift = si.shape[0] if edk else 0
+    a = 0 if sk_kind else 1 + n_drift
+    m = n + a
+    covar = 0.0
+    for c in comps:
+        covar += c[1]
+    in_dists = get_dists_arr(xi, yi, xi, yi)
+    off = ~np.eye(n, dtype=bool)
+    g = np.zeros((n, n))
+    for c in comps:
+        gc = _vg_comp_arr(in_dists, c)
+        if sk_kind:
+            g[off] -= gc[off]
+        else:
+            g[off] += gc[off]
+    lhs = np.zeros((m, m))
+    lhs[:n, :n] = g
+    if not sk_kind:
+        lhs[n, :n] = 1.0
+        lhs[:n, n] = 1.0
+        for k in range(n_drift):
+            lhs[n + 1 + k, :n] = si[k]
+            lhs[:n, n + 1 + k] = si[k]
+    inv = np.linalg.pinv(lhs)
+    d_out = get_dists_arr(xi, yi, xk, yk)            # [n, n_out]
+    gam = [_vg_comp_arr(d_out, c) for c in comps]
+    rhss = np.zeros((n_out, m))
+    lambdas = np.zeros((n_out, n))
+    mus = np.zeros((a, n_out))
+    zk = np.zeros(n_out)
+    est = np.zeros(n_out)
+    for k in range(n_out):
+        r = np.zeros(m)
+        for lo in range(n):
+            if d_out[lo, k] == 0.0:
+                r[lo] = covar if sk_kind else 0.0
+                continue
+            t = covar if sk_kind else 0.0
+            for gc in gam:
+                t = t - gc[lo, k] if sk_kind else t + gc[lo, k]
+            r[lo] = t
+        if not sk_kind:
+            r[n] = 1.0
+            for q in range(n_drift):
+                r[n + 1 + q] = sk[q, k]
+        lam = np.matmul(inv, r)
+        mus[:, k] = lam[n:]
+        lk = lam[:n]
+        zk[k] = np.sum(lk * zi)
+        if sk_kind:
+            est[k] = max(0.0, covar - np.sum(lk * r[:n]))
+        elif not edk:
+            est[k] = max(0.0, np.sum(lk * r[:n]) + lam[n])
+        lambdas[k] = lk
+        rhss[k] = r
+    out = dict(zk=zk, lambdas=lambdas, rhss=rhss, in_dists=in_dists, covar=covar)
+    if sk_kind:
+        out.update(est_covars=est, in_covars=lhs, in_covars_inv=inv, out_covars=rhss.copy())
+    else:
+        out.update(in_vars=lhs, in_vars_inv=inv)
+    if cls == "ExternalDriftKriging":
+        out.update(mus_1=mus[0].copy(), mus_2=mus[1].copy())
+    elif cls == "ExternalDriftKriging_MD":
+        out.update(mus_arr=mus)
+    elif not sk_kind:
+        out.update(est_vars=est, mus=mus[0].copy())
+    if cls.endswith("IndicatorKriging"):
+        ixi = np.where(zi <= lim, 1.0, 0.0)
+        ik = np.zeros(n_out)
+        for o in range(n_out):
+            ik[o] = max(0.0, np.sum(lambdas[o, :] * ixi))
+            est[o] = max(0.0, ik[o] * (1.0 - ik[o]))
+        out.update(ixi=ixi, ik=ik)
+    return out

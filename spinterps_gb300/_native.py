@@ -115,6 +115,11 @@ _SIGS = {
                      ctypes.c_float, ctypes.c_float, c_i32, c_ptr],
     "spi_krige_ok_noalloc": [ctypes.POINTER(DomainT), c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
                              c_i32, c_i32, ctypes.POINTER(OutT), c_ptr],
+    "spi_legacy_system": [c_i32, c_ptr, c_ptr, c_i32, c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
+                          c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
+    "spi_legacy_points": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_i64,
+                          c_i32, ctypes.POINTER(VgT), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                          c_ptr, c_ptr],
 }
 
 # every entry point the header declares (checked by the CPU tests)

@@ -14,6 +14,7 @@
 // staged in shared memory, and every operand read from L2 at most once per
 // 32-wide block of FMAs.
 #include "spi_common.cuh"
+#include "spi_gj.cuh"
 
 namespace spi {
 
@@ -300,10 +301,6 @@ __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
   double* f = gsm;                                   // [m]
   double* prow = gsm + m;                            // [m] the scaled pivot row
   int* piv = reinterpret_cast<int*>(gsm + 2 * m);    // [m]
-  __shared__ double rv[FT];
-  __shared__ int ri[FT];
-  __shared__ int fail;
-  __shared__ double dk;
   // saddle matrix, full storage
   for (int64_t e = tid; e < (int64_t)m * m; e += FT) {
     int i = (int)(e / m), j = (int)(e - (int64_t)i * m);
@@ -322,83 +319,8 @@ __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
     }
     A[e] = val;
   }
-  if (tid == 0) fail = 0;
   __syncthreads();
-  for (int k = 0; k < m; ++k) {
-    // pivot: first row of maximum |A[i][k]|, i >= k
-    double best = -1.0;
-    int bi = 0x7fffffff;
-    for (int i = k + tid; i < m; i += FT) {
-      double x = fabs(A[(int64_t)i * m + k]);
-      if (x > best || (x == best && i < bi) || isnan(x)) {
-        best = isnan(x) ? __longlong_as_double(0x7ff0000000000000LL) : x;
-        bi = i;
-      }
-    }
-    rv[tid] = best;
-    ri[tid] = bi;
-    __syncthreads();
-    for (int o = FT / 2; o > 0; o >>= 1) {
-      if (tid < o) {
-        double ob = rv[tid + o];
-        int oi = ri[tid + o];
-        if (ob > rv[tid] || (ob == rv[tid] && oi < ri[tid])) {
-          rv[tid] = ob;
-          ri[tid] = oi;
-        }
-      }
-      __syncthreads();
-    }
-    const int p = ri[0];
-    if (tid == 0) {
-      piv[k] = p;
-      if (!(rv[0] > 0.0) || isinf(rv[0])) fail = k + 1;
-    }
-    __syncthreads();
-    if (fail) break;
-    if (p != k)
-      for (int j = tid; j < m; j += FT) {
-        double t = A[(int64_t)k * m + j];
-        A[(int64_t)k * m + j] = A[(int64_t)p * m + j];
-        A[(int64_t)p * m + j] = t;
-      }
-    __syncthreads();
-    if (tid == 0) dk = A[(int64_t)k * m + k];
-    __syncthreads();
-    const double dd = dk;
-    for (int j = tid; j < m; j += FT) {
-      double x = (j == k) ? 1.0 : A[(int64_t)k * m + j];
-      x = x / dd;
-      A[(int64_t)k * m + j] = x;
-      prow[j] = x;
-    }
-    for (int i = tid; i < m; i += FT) f[i] = (i == k) ? 0.0 : A[(int64_t)i * m + k];
-    __syncthreads();
-    // eliminate column k from every other row: a warp per row, lanes over
-    // its columns (coalesced, no index division)
-    for (int i = tid >> 5; i < m; i += FT / 32) {
-      if (i == k) continue;
-      const double fi = f[i];
-      double* row = A + (int64_t)i * m;
-      for (int j = tid & 31; j < m; j += 32) {
-        const double base = (j == k) ? 0.0 : row[j];
-        row[j] = base - fi * prow[j];
-      }
-    }
-    __syncthreads();
-  }
-  if (!fail) {
-    for (int k = m - 1; k >= 0; --k) {
-      const int p = piv[k];
-      if (p != k)
-        for (int i = tid; i < m; i += FT) {
-          double t = A[(int64_t)i * m + k];
-          A[(int64_t)i * m + k] = A[(int64_t)i * m + p];
-          A[(int64_t)i * m + p] = t;
-        }
-      __syncthreads();
-    }
-  }
+  const int fail = gj_invert<FT>(A, m, f, prow, piv);
   if (tid == 0) route[s] = fail ? 2 : 1;
 }
 

@@ -23,6 +23,12 @@ and writes small seeded cases to tests/golden/*.npz:
 - fitter.npz    variograms/vgs.py Variogram: empirical variogram (pairs,
                 clipping, equal-count bins, robust estimator), the objective,
                 and whole fits with numpy's global RNG seeded
+- legacy.npz    the single-neighbourhood classes of cyth/interpmthds.pyx:
+                OrdinaryKriging, SimpleKriging, ExternalDriftKriging(_MD),
+                OrdinaryIndicatorKriging, SimpleIndicatorKriging
+
+``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
+legacy.npz.
 """
 import sys
 from pathlib import Path
@@ -375,8 +381,74 @@ def fitter_case(ref_root, out):
     out["f_cases"] = np.array(cases)
 
 
-def main(ref_root="/root/reference"):
+LEGACY_CASES = [
+    # (class, model, n stations, n points, n drifts, seed)
+    ("OrdinaryKriging", "0.1 Nug(0.0) + 0.9 Exp(20000)", 12, 15, 0, 71),
+    ("OrdinaryKriging", "0.5 Pow(1.2)", 10, 9, 0, 72),
+    ("OrdinaryKriging", "1.5 Hol(25000) + 0.2 Lin(40000)", 14, 11, 0, 73),
+    ("SimpleKriging", "0.2 Nug(0.0) + 1.0 Sph(30000)", 12, 15, 0, 74),
+    ("SimpleKriging", "1.0 Exp(15000)", 9, 8, 0, 75),
+    ("ExternalDriftKriging", "1.0 Gau(25000)", 11, 10, 1, 76),
+    ("ExternalDriftKriging_MD", "0.1 Nug(0.0) + 0.5 Exp(10000) + 0.4 Sph(40000)", 16, 13, 2,
+     77),
+    ("ExternalDriftKriging_MD", "1.0 Sph(35000)", 13, 12, 3, 78),
+    ("OrdinaryIndicatorKriging", "0.1 Nug(0.0) + 0.9 Exp(20000)", 12, 15, 0, 79),
+    ("SimpleIndicatorKriging", "1.0 Exp(15000)", 12, 10, 0, 80),
+    # a duplicated station: exactly singular matrices (pinv's cut-off acts)
+    ("OrdinaryKriging", "1.0 Exp(20000)", 12, 9, 0, 81),
+    ("SimpleKriging", "0.3 Nug(0.0) + 0.7 Sph(30000)", 12, 9, 0, 82),
+]
+LEGACY_DUPLICATED = (10, 11)
+
+
+def legacy_case(ref, out):
+    """The classes of cyth/interpmthds.pyx:251-765, each on small seeded
+    inputs with one output point on a station. Every readonly array the
+    class exposes after krige()/ikrige() is stored."""
+    cy = ref.cy
+    for ci, (cls, model, n, n_out, n_drift, seed) in enumerate(LEGACY_CASES):
+        rng = np.random.default_rng(seed)
+        xi, yi = rng.uniform(0, 6e4, n), rng.uniform(0, 6e4, n)
+        if ci in LEGACY_DUPLICATED:
+            xi[5], yi[5] = xi[1], yi[1]
+        zi = rng.gamma(1.5, 2.0, n)
+        xk, yk = rng.uniform(0, 6e4, n_out), rng.uniform(0, 6e4, n_out)
+        xk[0], yk[0] = xi[3], yi[3]
+        si = rng.uniform(0, 1500, (n_drift, n))
+        sk = rng.uniform(0, 1500, (n_drift, n_out))
+        lim = float(np.median(zi))
+        if cls in ("OrdinaryKriging", "SimpleKriging"):
+            obj = getattr(cy, cls)(xi, yi, zi, xk, yk, model=model)
+            obj.krige()
+        elif cls == "ExternalDriftKriging":
+            obj = cy.ExternalDriftKriging(xi, yi, zi, si[0].copy(), xk, yk, sk[0].copy(),
+                                          model=model)
+            obj.krige()
+        elif cls == "ExternalDriftKriging_MD":
+            obj = cy.ExternalDriftKriging_MD(xi, yi, zi, si, xk, yk, sk, model=model)
+            obj.krige()
+        else:
+            obj = getattr(cy, cls)(xi, yi, zi, xk, yk, lim=lim, model=model)
+            obj.ikrige()
+        p = f"l{ci}_"
+        out.update({p + "xi": xi, p + "yi": yi, p + "zi": zi, p + "xk": xk, p + "yk": yk,
+                    p + "si": si, p + "sk": sk, p + "lim": np.array(lim),
+                    p + "model": np.array(model), p + "cls": np.array(cls)})
+        for attr in ("zk", "est_vars", "est_covars", "mus", "mus_1", "mus_2", "mus_arr",
+                     "lambdas", "rhss", "in_dists", "in_vars", "in_vars_inv", "in_covars",
+                     "in_covars_inv", "out_covars", "ik", "ixi"):
+            if hasattr(obj, attr) and getattr(obj, attr) is not None:
+                out[p + attr] = np.asarray(getattr(obj, attr)).copy()
+    out["l_cases"] = np.arange(len(LEGACY_CASES))
+
+
+def main(ref_root="/root/reference", only=None):
     ref = load_reference(ref_root)
+    if only == "legacy":
+        out = {}
+        legacy_case(ref, out)
+        np.savez_compressed(HERE / "legacy.npz", **out)
+        return
     out = {}
     kernels_case(ref, out)
     np.savez_compressed(HERE / "kernels.npz", **out)
@@ -417,6 +489,9 @@ def main(ref_root="/root/reference"):
     out = {}
     fitter_case(ref_root, out)
     np.savez_compressed(HERE / "fitter.npz", **out)
+    out = {}
+    legacy_case(ref, out)
+    np.savez_compressed(HERE / "legacy.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

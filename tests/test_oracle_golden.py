@@ -178,3 +178,24 @@ def test_oracle_neighbours_match_reference(golden):
         lab, _ = port.neb_groups(idx)
         assert np.array_equal(idx, g[f"n_{tag}_idxs"]), tag
         assert np.array_equal(lab, g[f"n_{tag}_grp"]), tag
+
+
+LEGACY_INPUTS = ("xi", "yi", "zi", "xk", "yk", "si", "sk", "lim", "model", "cls")
+
+
+def test_oracle_legacy_classes_match_reference(golden):
+    """The restatement of OrdinaryKriging, SimpleKriging,
+    ExternalDriftKriging(_MD) and the indicator classes
+    (cyth/interpmthds.pyx:251-765) reproduces every array the reference's
+    compiled classes expose (tests/golden/legacy.npz), bit for bit."""
+    g = golden
+    for ci in g["l_cases"]:
+        p = f"l{ci}_"
+        cls = str(g[p + "cls"])
+        got = port.legacy_krige(cls, g[p + "xi"], g[p + "yi"], g[p + "zi"], g[p + "xk"],
+                                g[p + "yk"], str(g[p + "model"]), si=g[p + "si"],
+                                sk=g[p + "sk"], lim=float(g[p + "lim"]))
+        keys = [k[len(p):] for k in g if k.startswith(p) and k[len(p):] not in LEGACY_INPUTS]
+        assert keys, cls
+        for k in keys:
+            assert np.array_equal(np.asarray(got[k]), g[p + k]), (ci, cls, k)
