@@ -469,6 +469,40 @@ int spi_krige_ok_noalloc(const spi_domain_t *dom, const int32_t *stn_idx, int32_
                          const spi_vg_t *vg, const double *vals, int32_t n_steps,
                          int32_t want_var, const spi_out_t *out, spi_stream_t stream);
 
+/* ---- the driver flow around the step engine ------------------------------ */
+
+/* The polygon cell mask of SpInterpPrepare._select_nearby_cells
+ * (interp/prepare.py:250-288, misc.py:407-500, 617-627): inside[i] = 1 when
+ * point i, its coordinates rounded to 1e-6 as "POINT (%f %f)" prints them,
+ * lies strictly inside one of the polygons (ogr Contains: the boundary is
+ * outside). Polygon p is the single ring of vertices ring_off[p] ..
+ * ring_off[p + 1] - 1 of vx, vy, closed from its last vertex to its first;
+ * bbox [n_polys, 4] = (x_min, x_max, y_min, y_max) of each ring. Device
+ * arrays. */
+int spi_points_in_polygons(const double *px, const double *py, int64_t n_pts,
+                           int32_t n_polys, const int64_t *ring_off, const double *vx,
+                           const double *vy, const double *bbox, uint8_t *inside,
+                           spi_stream_t stream);
+
+/* Per-row statistics of fld [rows, n] (row stride ld, float or double by
+ * is_f64) over its finite entries: out [rows, 5] = (min, mean, max, std with
+ * ddof, count), as SpInterpMain._save_stats_sers computes them
+ * (interp/main.py:474-525: pandas' skip-NaN min/mean/max/std/count of the
+ * station data, ddof 1; numpy's nanmin/nanmean/nanmax/nanstd and
+ * isfinite().sum() of every interpolated field, ddof 0). A row without a
+ * finite entry gets NaN statistics and count 0; std is NaN where count <=
+ * ddof. scratch: at least 5 * (608 + rows) doubles. rows <= 65535. */
+int spi_field_stats(const void *fld, int32_t is_f64, int32_t rows, int64_t n, int64_t ld,
+                    int32_t ddof, double *scratch, int64_t scratch_len, double *out,
+                    spi_stream_t stream);
+
+/* numpy.round(fld, decimals) in place, in the field's own precision
+ * (float, or double when is_f64): the rounding to nc_nmrl_prcn decimals the
+ * reference applies before writing the fields (interp/steps.py:899-901,
+ * 920-922). |decimals| <= 22 is exact in the scale factor. */
+int spi_round_fields(void *fld, int32_t is_f64, int64_t n, int32_t decimals,
+                     spi_stream_t stream);
+
 /* ---- the single-neighbourhood classes ----------------------------------
  *
  * Replace the arithmetic of OrdinaryKriging, SimpleKriging,

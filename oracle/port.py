@@ -23,6 +23,10 @@ timing is a fair stand-in for the reference's own CPU path:
 - ``ret_mp_idxs``           misc.py:601-613
 - ``legacy_krige``          cyth/interpmthds.pyx:251-765 (the single-neighbourhood
                             kriging classes)
+- ``prepare_crds``          interp/prepare.py:148-241 (the grid)
+- ``sample_drifts``         interp/drift.py:165-227 (drift values at cells and stations)
+- ``points_in_polygons``    interp/prepare.py:244-288, misc.py:407-500, 617-627
+- ``field_stats``           interp/main.py:474-525 (per-step statistics)
 
 Parity status: pinned against fixtures generated by running the reference's
 own code (tests/golden/make_golden.py); see tests/test_oracle_golden.py.
@@ -643,4 +647,129 @@ def legacy_krige(cls, xi, yi, zi, xk, yk, model, si=None, sk=None, lim=None):
             ik[o] = max(0.0, np.sum(lambdas[o, :] * ixi))
             est[o] = max(0.0, ik[o] * (1.0 - ik[o]))
         out.update(ixi=ixi, ik=ik)
+    return out
+
+
+# ---- the driver flow around the step engine ---------------------------------
+
+def prepare_crds(x_min, x_max, y_min, y_max, cell_size, drift_bounds=None):
+    """SpInterpPrepare._prepare_crds (interp/prepare.py:148-241): the column
+    and row range of the grid (inside the drift rasters when drift_bounds =
+    (x_min, x_max, y_min, y_max) of the rasters is given, EDK), cell-centre
+    coordinates by np.linspace from (x_min + cs / 2, y_max - cs / 2), and
+    the row-major cell mesh."""
+    if drift_bounds is not None:
+        dx0, dx1, dy0, dy1 = drift_bounds
+        assert x_min >= dx0 and x_max <= dx1 and y_min >= dy0 and y_max <= dy1
+        min_col = int(math.floor((x_min - dx0) / cell_size))
+        max_col = int(math.ceil((x_max - dx0) / cell_size)) - 1
+        min_row = int(math.floor((dy1 - y_max) / cell_size))
+        max_row = int(math.ceil((dy1 - y_min) / cell_size)) - 1
+    else:
+        min_col, min_row = 0, 0
+        max_col = int(math.ceil((x_max - x_min) / cell_size)) - 1
+        max_row = int(math.ceil((y_max - y_min) / cell_size)) - 1
+    assert 0 <= min_col <= max_col and 0 <= min_row <= max_row
+    sx = x_min + 0.5 * cell_size
+    ex = sx + (max_col - min_col) * cell_size
+    sy = y_max - 0.5 * cell_size
+    ey = sy - (max_row - min_row) * cell_size
+    xs = np.linspace(sx, ex, max_col - min_col + 1)
+    ys = np.linspace(sy, ey, max_row - min_row + 1)
+    mx, my = np.meshgrid(xs, ys)
+    return dict(rc=(min_col, max_col, min_row, max_row), x_crds=xs, y_crds=ys,
+                cell_x=mx.ravel(), cell_y=my.ravel(), shape=mx.shape)
+
+
+def sample_drifts(rasters, drift_x_min, drift_y_max, cell_size, ndv, rc, stn_x, stn_y,
+                  cntn_idxs=None):
+    """KrigingDrift._prepare_stns_drift (interp/drift.py:165-227): every
+    raster read at the grid's rows and columns (no-data, by np.isclose, to
+    NaN), then at each station's cell int((x - x_min) / cs),
+    int((y_max - y) / cs); station drifts must be finite."""
+    min_col, max_col, min_row, max_row = rc
+    cm, rm = np.meshgrid(np.arange(min_col, max_col + 1), np.arange(min_row, max_row + 1))
+    cm, rm = cm.ravel(), rm.ravel()
+    if cntn_idxs is not None:
+        cm, rm = cm[cntn_idxs], rm[cntn_idxs]
+    cell = []
+    for r in rasters:
+        v = r[rm, cm]
+        v[np.isclose(ndv, v)] = np.nan
+        cell.append(v)
+    cell = np.array(cell, dtype=float)
+    stn = np.full((len(stn_x), len(rasters)), np.nan)
+    for i, (x, y) in enumerate(zip(stn_x, stn_y)):
+        col = int((x - drift_x_min) / cell_size)
+        row = int((drift_y_max - y) / cell_size)
+        for k, r in enumerate(rasters):
+            d = r[row, col]
+            stn[i, k] = np.nan if np.isclose(ndv, d) else d
+    assert np.all(np.isfinite(stn)), "Invalid value(s) of drift(s) for stations in drift rasters!"
+    return cell, stn
+
+
+def _orient(a, b, c, d):
+    """exact sign of a*b - c*d for the float64 values a, b, c, d."""
+    from fractions import Fraction
+    r = Fraction(float(a)) * Fraction(float(b)) - Fraction(float(c)) * Fraction(float(d))
+    return (r > 0) - (r < 0)
+
+
+def points_in_polygons(px, py, polygons):
+    """The cell selection of _select_nearby_cells (interp/prepare.py:244-288
+    over chk_pt_cntmnt_in_polys_mp / chk_pt_cntmnt_in_poly / cnvt_to_pt /
+    chk_cntmt, misc.py:407-500, 617-627): a point, rounded to 1e-6 as
+    "POINT (%f %f)" prints it, is kept when it lies strictly inside one of
+    the single-ring polygons (ogr Contains: boundary points are outside).
+    polygons: list of (xs, ys) vertex arrays, closed from the last vertex
+    to the first. Pure-Python loops (small cases only).
+
+    Parity unpinned against the reference itself: ogr is not importable
+    here. The crossing-number rule and the boundary test restate the
+    definition of Contains."""
+    out = np.zeros(len(px), dtype=bool)
+    for i, (x0, y0) in enumerate(zip(px, py)):
+        x = float(np.rint(x0 * 1e6) / 1e6)
+        y = float(np.rint(y0 * 1e6) / 1e6)
+        for vx, vy in polygons:
+            vx, vy = np.asarray(vx, float), np.asarray(vy, float)
+            if not (vx.min() <= x <= vx.max() and vy.min() <= y <= vy.max()):
+                continue
+            odd, onb = False, False
+            nv = len(vx)
+            for e in range(nv):
+                x1, y1 = vx[e], vy[e]
+                x2, y2 = vx[(e + 1) % nv], vy[(e + 1) % nv]
+                up1, up2 = y1 > y, y2 > y
+                inbox = min(x1, x2) <= x <= max(x1, x2) and min(y1, y2) <= y <= max(y1, y2)
+                if up1 == up2 and not inbox:
+                    continue
+                s = _orient(x2 - x1, y - y1, y2 - y1, x - x1)
+                if s == 0 and inbox:
+                    onb = True
+                    break
+                if up1 != up2 and ((s > 0) if y2 > y1 else (s < 0)):
+                    odd = not odd
+            if odd and not onb:
+                out[i] = True
+                break
+    return out
+
+
+def field_stats(fld, ddof):
+    """Per-row (min, mean, max, std, count) over the finite entries of fld
+    [rows, n] (interp/main.py:474-525): numpy's nanmin / nanmean / nanmax /
+    nanstd (ddof 0) and isfinite().sum() for the interpolated fields,
+    pandas' skip-NaN min / mean / max / std (ddof 1) / count for the station
+    data; computed in float64 here."""
+    f = np.asarray(fld, dtype=np.float64)
+    out = np.full((f.shape[0], 5), np.nan)
+    for r in range(f.shape[0]):
+        v = f[r][np.isfinite(f[r])]
+        out[r, 4] = v.size
+        if v.size:
+            out[r, 0], out[r, 1], out[r, 2] = v.min(), v.mean(), v.max()
+            if v.size > ddof:
+                out[r, 3] = v.std(ddof=ddof)
     return out

@@ -115,6 +115,10 @@ _SIGS = {
                      ctypes.c_float, ctypes.c_float, c_i32, c_ptr],
     "spi_krige_ok_noalloc": [ctypes.POINTER(DomainT), c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
                              c_i32, c_i32, ctypes.POINTER(OutT), c_ptr],
+    "spi_points_in_polygons": [c_ptr, c_ptr, c_i64, c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                               c_ptr],
+    "spi_field_stats": [c_ptr, c_i32, c_i32, c_i64, c_i64, c_i32, c_ptr, c_i64, c_ptr, c_ptr],
+    "spi_round_fields": [c_ptr, c_i32, c_i64, c_i32, c_ptr],
     "spi_legacy_system": [c_i32, c_ptr, c_ptr, c_i32, c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
                           c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
     "spi_legacy_points": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_i64,

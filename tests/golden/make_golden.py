@@ -23,12 +23,15 @@ and writes small seeded cases to tests/golden/*.npz:
 - fitter.npz    variograms/vgs.py Variogram: empirical variogram (pairs,
                 clipping, equal-count bins, robust estimator), the objective,
                 and whole fits with numpy's global RNG seeded
+- driver.npz    the driver flow's grid (SpInterpPrepare._prepare_crds,
+                interp/prepare.py:148-241) and drift sampling
+                (KrigingDrift._prepare_stns_drift, interp/drift.py:165-227)
 - legacy.npz    the single-neighbourhood classes of cyth/interpmthds.pyx:
                 OrdinaryKriging, SimpleKriging, ExternalDriftKriging(_MD),
                 OrdinaryIndicatorKriging, SimpleIndicatorKriging
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
-legacy.npz.
+legacy.npz (``driver``: only driver.npz).
 """
 import sys
 from pathlib import Path
@@ -37,7 +40,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
-from refharness import load_reference, load_variogram, make_steps  # noqa: E402
+from refharness import (LocFrame, load_prepare, load_reference, load_variogram,  # noqa: E402
+                        make_steps)
 
 VG_STRS = [
     "0.05 Nug(0.0) + 0.95 Exp(20000)",
@@ -442,8 +446,75 @@ def legacy_case(ref, out):
     out["l_cases"] = np.arange(len(LEGACY_CASES))
 
 
+DRIVER_CASES = [
+    # (edk, x_min, x_max, y_min, y_max, cell size, polygon mask)
+    (False, 1000.3, 26110.0, -5000.0, 14321.7, 500.0, False),
+    (True, 3120.0, 41200.5, 2000.0, 30750.0, 1000.0, False),
+    (True, 3120.0, 41200.5, 2000.0, 30750.0, 1000.0, True),
+]
+
+
+def driver_case(ref, out):
+    """SpInterpPrepare._prepare_crds and KrigingDrift._prepare_stns_drift on a
+    bare object with the attributes they read: a grid without drift, and
+    with two drift rasters (no-data cells included), with and without a cell
+    mask."""
+    prep = load_prepare()
+    rng = np.random.default_rng(88)
+    for ci, (edk, x0, x1, y0, y1, cs, masked) in enumerate(DRIVER_CASES):
+        obj = prep.SpInterpPrepare.__new__(prep.SpInterpPrepare)
+        obj._edk_flag = edk
+        obj._x_min, obj._x_max, obj._y_min, obj._y_max = x0, x1, y0, y1
+        obj._cell_size = cs
+        obj._plot_figs_flag = False
+        p = f"d{ci}_"
+        if edk:
+            dx0, dy1, nr, nc_ = 0.0, 40000.0, 45, 50
+            obj._drft_x_min, obj._drft_y_max = dx0, dy1
+            obj._drft_x_max = dx0 + nc_ * cs
+            obj._drft_y_min = dy1 - nr * cs
+            ndv = -9999.0
+            rasters = rng.uniform(0, 3000, (2, nr, nc_))
+            rasters[0, 30:, :4] = ndv
+            rasters[1, :3, 40:] = ndv
+            obj._drft_oarrs = [r.copy() for r in rasters]
+            obj._drft_ndv = ndv
+            out.update({p + "drift": rasters, p + "ndv": np.array(ndv),
+                        p + "drift_origin": np.array([dx0, dy1])})
+        obj._prepare_crds()
+        out.update({p + "bounds": np.array([x0, x1, y0, y1, cs]),
+                    p + "rc": np.array([obj._min_col, obj._max_col, obj._min_row,
+                                        obj._max_row]),
+                    p + "x_crds": obj._nc_x_crds, p + "y_crds": obj._nc_y_crds,
+                    p + "cell_x": obj._interp_x_crds_msh, p + "cell_y": obj._interp_y_crds_msh,
+                    p + "shape": np.array(obj._interp_crds_orig_shape)})
+        if edk:
+            n = 30
+            sx = rng.uniform(x0 + 1, x1 - 1, n)
+            sy = rng.uniform(y0 + 1, y1 - 1, n)
+            obj._crds_df = LocFrame({"X": sx, "Y": sy}, index=np.array(
+                [f"s{i}" for i in range(n)]))
+            obj._cell_sel_prms_set = masked
+            mask = None
+            if masked:
+                mask = rng.uniform(size=obj._interp_x_crds_msh.size) < 0.6
+            obj._cntn_idxs = mask
+            obj._prepare_stns_drift()
+            out.update({p + "stn_x": sx, p + "stn_y": sy,
+                        p + "cell_drift": obj._drft_arrs,
+                        p + "stn_drift": obj._stns_drft_df.values.copy()})
+            if masked:
+                out[p + "mask"] = mask
+    out["d_cases"] = np.arange(len(DRIVER_CASES))
+
+
 def main(ref_root="/root/reference", only=None):
     ref = load_reference(ref_root)
+    if only == "driver":
+        out = {}
+        driver_case(ref, out)
+        np.savez_compressed(HERE / "driver.npz", **out)
+        return
     if only == "legacy":
         out = {}
         legacy_case(ref, out)
@@ -492,6 +563,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     legacy_case(ref, out)
     np.savez_compressed(HERE / "legacy.npz", **out)
+    out = {}
+    driver_case(ref, out)
+    np.savez_compressed(HERE / "driver.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -166,6 +166,66 @@ class MiniDataFrame:
         self._a = self._a[~np.isnan(self._a).any(axis=1)]
 
 
+class LocFrame:
+    """The pandas.DataFrame operations of interp/drift.py:_prepare_stns_drift
+    on a float array with row and column labels: construction from a dict of
+    columns or from index/columns, ``.index``, ``.values``, column access,
+    and ``.loc[row, col]`` / ``.loc[row, [cols]]`` reads and
+    ``.loc[row, col] = v`` writes."""
+
+    def __init__(self, data=None, index=None, columns=None, dtype=float):
+        import numpy as np
+        if isinstance(data, dict):
+            self.columns = list(data)
+            self._a = np.column_stack([np.asarray(data[c], dtype=float) for c in data])
+            n = self._a.shape[0]
+            self.index = np.arange(n) if index is None else np.asarray(index)
+        else:
+            self.index = np.asarray(index)
+            self.columns = list(columns)
+            self._a = np.full((len(self.index), len(self.columns)), np.nan)
+        self._rows = {k: i for i, k in enumerate(self.index.tolist())}
+        outer = self
+
+        class _Loc:
+            def _ix(self, key):
+                r, c = key
+                ri = outer._rows[r]
+                if isinstance(c, (list, tuple)):
+                    return ri, [outer.columns.index(x) for x in c]
+                return ri, outer.columns.index(c)
+
+            def __getitem__(self, key):
+                ri, ci = self._ix(key)
+                return outer._a[ri, ci]
+
+            def __setitem__(self, key, v):
+                ri, ci = self._ix(key)
+                outer._a[ri, ci] = v
+
+        self.loc = _Loc()
+
+    @property
+    def values(self):
+        return self._a
+
+    def __getitem__(self, c):
+        return self._a[:, self.columns.index(c)]
+
+
+def load_prepare():
+    """The reference's SpInterpPrepare (interp/prepare.py, with KrigingDrift of
+    interp/drift.py), pandas replaced by LocFrame; call after
+    load_reference()."""
+    pd = sys.modules.get("pandas")
+    if pd is None or not hasattr(pd, "__version__"):
+        pd = _stub("pandas")
+    prep = importlib.import_module("spinterps.interp.prepare")
+    drift = importlib.import_module("spinterps.interp.drift")
+    drift.pd = types.SimpleNamespace(DataFrame=LocFrame)
+    return prep
+
+
 def load_variogram(ref_root="/root/reference"):
     """The reference's Variogram class (variograms/vgs.py) with the stand-in
     DataFrame in place of pandas."""

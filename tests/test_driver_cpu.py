@@ -1,0 +1,44 @@
+"""Host logic of the driver flow (spinterps_gb300.driver) against the
+reference's own grid and drift sampling (tests/golden/driver.npz, made by
+running SpInterpPrepare._prepare_crds and KrigingDrift._prepare_stns_drift).
+No GPU."""
+import numpy as np
+
+from spinterps_gb300 import driver
+
+
+def test_grid_and_drifts_match_reference(golden):
+    g = golden
+    for ci in g["d_cases"]:
+        p = f"d{ci}_"
+        x0, x1, y0, y1, cs = g[p + "bounds"]
+        db = None
+        if p + "drift" in g:
+            dx0, dy1 = g[p + "drift_origin"]
+            nr, nc = g[p + "drift"].shape[1:]
+            db = driver.drift_bounds(dx0, dy1, nr, nc, cs)
+        r = driver.prepare_crds(x0, x1, y0, y1, cs, drift_bounds=db)
+        assert tuple(r["rc"]) == tuple(g[p + "rc"])
+        assert tuple(r["shape"]) == tuple(g[p + "shape"])
+        for k in ("x_crds", "y_crds", "cell_x", "cell_y"):
+            assert np.array_equal(r[k], g[p + k]), (ci, k)
+        if db is not None:
+            mask = g[p + "mask"] if p + "mask" in g else None
+            cell, stn = driver.sample_drifts(list(g[p + "drift"]), db[0], db[3], cs,
+                                             float(g[p + "ndv"]), r["rc"], g[p + "stn_x"],
+                                             g[p + "stn_y"], cntn_idxs=mask)
+            assert np.array_equal(cell, g[p + "cell_drift"], equal_nan=True), ci
+            assert np.array_equal(stn, g[p + "stn_drift"]), ci
+
+
+def test_corner_coordinates_and_stats_csv(tmp_path):
+    b = driver.corner_coordinates([1.0, 5.0, 3.0], [2.0, -1.0, 4.0], cell_bdist=0.5)
+    assert b == (0.5, 5.5, -1.5, 4.5)
+    b = driver.corner_coordinates([1.0], [2.0], 1.0, poly_extent=(0.0, 10.0, 0.0, 20.0))
+    assert b == (-1.0, 11.0, -1.0, 21.0)
+    cols = {"data_min": np.array([1.0, np.nan], np.float32),
+            "OK_mean": np.array([2.5, 3.25], np.float32)}
+    f = tmp_path / "stats.csv"
+    driver.write_stats_csv(f, ["t0", "t1"], cols)
+    assert f.read_text().splitlines() == [";data_min;OK_mean", "t0;1.000000;2.500000",
+                                          "t1;;3.250000"]

@@ -199,3 +199,43 @@ def test_oracle_legacy_classes_match_reference(golden):
         assert keys, cls
         for k in keys:
             assert np.array_equal(np.asarray(got[k]), g[p + k]), (ci, cls, k)
+
+
+def test_oracle_driver_grid_and_drifts_match_reference(golden):
+    """The grid (SpInterpPrepare._prepare_crds) and the drift sampling
+    (KrigingDrift._prepare_stns_drift) as the reference computes them
+    (tests/golden/driver.npz), bit for bit."""
+    g = golden
+    for ci in g["d_cases"]:
+        p = f"d{ci}_"
+        x0, x1, y0, y1, cs = g[p + "bounds"]
+        db = None
+        if p + "drift" in g:
+            dx0, dy1 = g[p + "drift_origin"]
+            nr, nc = g[p + "drift"].shape[1:]
+            db = (dx0, dx0 + nc * cs, dy1 - nr * cs, dy1)
+        r = port.prepare_crds(x0, x1, y0, y1, cs, drift_bounds=db)
+        assert tuple(r["rc"]) == tuple(g[p + "rc"])
+        assert tuple(r["shape"]) == tuple(g[p + "shape"])
+        for k in ("x_crds", "y_crds", "cell_x", "cell_y"):
+            assert np.array_equal(r[k], g[p + k]), (ci, k)
+        if db is not None:
+            mask = g[p + "mask"] if p + "mask" in g else None
+            cell, stn = port.sample_drifts(list(g[p + "drift"]), dx0, dy1, cs,
+                                           float(g[p + "ndv"]), r["rc"], g[p + "stn_x"],
+                                           g[p + "stn_y"], cntn_idxs=mask)
+            assert np.array_equal(cell, g[p + "cell_drift"], equal_nan=True), ci
+            assert np.array_equal(stn, g[p + "stn_drift"]), ci
+
+
+def test_oracle_polygon_mask_known_answers():
+    """Strict containment after rounding to 1e-6: inside, outside, on an
+    edge, on a vertex, in and on the edge of a concave notch, and just
+    inside an edge."""
+    sq = ([0.0, 10.0, 10.0, 0.0], [0.0, 0.0, 10.0, 10.0])
+    notch = ([20.0, 30.0, 30.0, 25.0, 20.0], [0.0, 0.0, 10.0, 5.0, 10.0])
+    px = np.array([5.0, 11.0, 10.0, 0.0, 5.0, 25.0, 25.0, 9.9999996, 9.9999994, 21.0, 22.0])
+    py = np.array([5.0, 5.0, 5.0, 0.0, 10.0, 7.0, 4.0, 5.0, 5.0, 8.0, 8.0])
+    want = np.array([1, 0, 0, 0, 0, 0, 1, 0, 1, 1, 0], dtype=bool)
+    got = port.points_in_polygons(px, py, [sq, notch])
+    assert np.array_equal(got, want), got
