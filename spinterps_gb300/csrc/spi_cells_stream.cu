@@ -27,6 +27,53 @@ constexpr int SNW = 8;   // warps per CTA (station groups)
 constexpr int SSV = 4;   // vectors per pass
 constexpr int SCH = 256; // stations per shared-memory chunk (FP32 tier)
 
+// One shared-memory chunk of stations against the pass's vectors (FP32
+// tier): double-float entries (rhs_df, or rhs_df_single<CODE> for a
+// single-structure variogram) times hi/lo vector pairs, the product's head
+// by the FMA error, the cross terms, TwoSum into a double-float partial,
+// flushed to FP64 every 256 terms. Dual columns that feed only the sum
+// check (v0 + v < plain_duals) take a plain FP32 product.
+template <int CODE>
+__device__ __forceinline__ void stream_chunk(const CellsArgs& A, const spi_vg_t* vgp,
+                                             const RhsDf& kd, int sk, double sh, float4 cp,
+                                             bool live, int64_t gc, const int32_t* idxc,
+                                             const float4* s_sp, const float2 (*s_w)[SCH],
+                                             int nj, int warp, int nv, int v0, int plain_duals,
+                                             float (&ph)[SSV], float (&pl)[SSV],
+                                             double (&acc)[SSV], int& cnt) {
+  for (int jj = warp; jj < nj; jj += SNW) {
+    df c = {0.f, 0.f};
+    if (live) {
+      if constexpr (CODE < 0)
+        c = rhs_df(A.dom, vgp, kd, sk, sh, cp, s_sp[jj], gc, idxc + jj);
+      else
+        c = rhs_df_single<CODE>(A.dom, vgp, kd, sk, sh, cp, s_sp[jj], gc, idxc + jj);
+    }
+#pragma unroll
+    for (int v = 0; v < SSV; ++v)
+      if (v < nv && v0 + v < plain_duals) {
+        ph[v] = __fmaf_rn(c.h, s_w[v][jj].x, ph[v]);
+      } else if (v < nv) {
+        const float2 w = s_w[v][jj];
+        const float p = __fmul_rn(c.h, w.x);
+        float e = __fmaf_rn(c.h, w.x, -p);
+        e = __fmaf_rn(c.h, w.y, e);
+        e = __fmaf_rn(c.l, w.x, e);
+        const df s2 = two_sum(ph[v], p);
+        ph[v] = s2.h;
+        pl[v] += s2.l + e;
+      }
+    if (++cnt == 256) {
+      cnt = 0;
+#pragma unroll
+      for (int v = 0; v < SSV; ++v) {
+        acc[v] += (double)ph[v] + (double)pl[v];
+        ph[v] = pl[v] = 0.f;
+      }
+    }
+  }
+}
+
 template <typename T, typename OutT>
 __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A) {
   const int s = blockIdx.y;
@@ -171,9 +218,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
           if (v < nv) acc[v] = fma(c, vp64[v][j], acc[v]);
       }
     } else {
-      // double-float entries against hi/lo vectors: the product's head by
-      // the FMA error, the cross terms, TwoSum into a double-float partial,
-      // flushed to FP64 every 256 terms
+      // double-float entries against hi/lo vectors (stream_chunk)
       float ph[SSV], pl[SSV];
 #pragma unroll
       for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
@@ -190,31 +235,29 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
             if (v < nv) s_w[v][e] = make_float2(vph[v][j0 + e], vpl[v][j0 + e]);
         }
         __syncthreads();
-        for (int jj = warp; jj < nj; jj += SNW) {
-          const df c = live ? rhs_df(A.dom, vgp, kd, sk, sh, cp, s_sp[jj], gc, idx + j0 + jj)
-                            : df{0.f, 0.f};
-#pragma unroll
-          for (int v = 0; v < SSV; ++v)
-            if (v < nv && v0 + v < plain_duals) {
-              ph[v] = __fmaf_rn(c.h, s_w[v][jj].x, ph[v]);
-            } else if (v < nv) {
-              const float2 w = s_w[v][jj];
-              const float p = __fmul_rn(c.h, w.x);
-              float e = __fmaf_rn(c.h, w.x, -p);
-              e = __fmaf_rn(c.h, w.y, e);
-              e = __fmaf_rn(c.l, w.x, e);
-              const df s2 = two_sum(ph[v], p);
-              ph[v] = s2.h;
-              pl[v] += s2.l + e;
-            }
-          if (++cnt == 256) {
-            cnt = 0;
-#pragma unroll
-            for (int v = 0; v < SSV; ++v) {
-              acc[v] += (double)ph[v] + (double)pl[v];
-              ph[v] = pl[v] = 0.f;
-            }
-          }
+        // the single structure's model, uniform over the CTA
+        const int scode = (kd.exact && kd.single >= 0) ? kd.code[kd.single] : -1;
+        const int32_t* idxc = idx + j0;
+        switch (scode) {
+          case SPI_VG_EXP:
+            stream_chunk<SPI_VG_EXP>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
+                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+            break;
+          case SPI_VG_GAU:
+            stream_chunk<SPI_VG_GAU>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
+                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+            break;
+          case SPI_VG_SPH:
+            stream_chunk<SPI_VG_SPH>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
+                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+            break;
+          case SPI_VG_LIN:
+            stream_chunk<SPI_VG_LIN>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
+                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+            break;
+          default:
+            stream_chunk<-1>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp, nv, v0,
+                             plain_duals, ph, pl, acc, cnt);
         }
       }
 #pragma unroll

@@ -233,6 +233,24 @@ __device__ __forceinline__ df rho_df(int code, df d, df d2, df k1, df k2, df inv
   return df_mul(df_mul(u, u), w);
 }
 
+// The min_vg_val zeroing of a double-float covariance entry c (rhs_df).
+// gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
+// paths zero only exact zeros, which they agree on; OK / EDK entries whose
+// nuggets exceed the cut are never zeroed (gamma >= nugget). Entries
+// within the band of the cut take rhs_f64 itself.
+__device__ __forceinline__ df rhs_df_cut(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                         const RhsDf& k, int sk, double sh, int64_t gc,
+                                         const int32_t* stp, df c) {
+  if (k.mvv > 0.f && (sk || !k.nug_clear)) {
+    const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
+    const float gap = (cut.h - k.mvv) + cut.l;
+    if (fabsf(gap) <= (sk ? k.band_sk : k.band_ok))
+      return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], *stp));
+    if (gap <= 0.f) return sk ? df{0.f, 0.f} : k.shift;
+  }
+  return c;
+}
+
 // One covariance entry (Cholesky path) as a double-float, relative error
 // ~1e-9, for the FP32 tier's estimates and dual columns, where the
 // right-hand side's rounding is amplified by the dual weights, and for the
@@ -260,17 +278,41 @@ __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vg
         c = df_add(c, df_mul(k.sill[q],
                              rho_df(k.code[q], d, d2, k.k1[q], k.k2[q], k.inv_r[q])));
   }
-  if (k.mvv > 0.f && (sk || !k.nug_clear)) {
-    // gamma = s - c carries ~1e-9 s of c's error; with min_vg_val = 0 both
-    // paths zero only exact zeros, which they agree on; OK / EDK entries
-    // whose nuggets exceed the cut are never zeroed (gamma >= nugget)
-    const df cut = sk ? c : df_add(k.shift, df{-c.h, -c.l});
-    const float gap = (cut.h - k.mvv) + cut.l;
-    if (fabsf(gap) <= (sk ? k.band_sk : k.band_ok))
-      return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], *stp));
-    if (gap <= 0.f) return sk ? df{0.f, 0.f} : k.shift;
+  return rhs_df_cut(dom, vgp, k, sk, sh, gc, stp, c);
+}
+
+// rhs_df for a variogram with one structure (plus nuggets) of the
+// compile-time model CODE (Exp, Gau, Sph or Lin; k.single indexes it): no
+// model switch per entry, and no square root for Gau.
+template <int CODE>
+__device__ __forceinline__ df rhs_df_single(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                            const RhsDf& k, int sk, double sh, float4 cp,
+                                            float4 sp, int64_t gc, const int32_t* stp) {
+  const int q = k.single;
+  const df d2 = df_dist2(cp, sp);
+  df rho;
+  if constexpr (CODE == SPI_VG_GAU) {
+    rho = df_exp(df_mul(d2, k.k2[q]));
+  } else {
+    const df d = df_sqrt(d2);
+    if constexpr (CODE == SPI_VG_EXP) {
+      rho = df_exp(df_mul(d, k.k1[q]));
+    } else {
+      const df t = df_mul(d, k.inv_r[q]);  // h / r
+      if (!(t.h < 1.0f)) {
+        rho = df{0.f, 0.f};
+      } else {
+        const df u = df_add(df{1.0f, 0.f}, df{-t.h, -t.l});
+        if constexpr (CODE == SPI_VG_LIN) {
+          rho = u;
+        } else {
+          const df w = df_add(df{1.0f, 0.f}, df{0.5f * t.h, 0.5f * t.l});
+          rho = df_mul(df_mul(u, u), w);
+        }
+      }
+    }
   }
-  return c;
+  return rhs_df_cut(dom, vgp, k, sk, sh, gc, stp, df_mul(k.sill[q], rho));
 }
 
 // Rounding bound of an FP32-tier sum(lambda), relative to sum |u_i| c_i:

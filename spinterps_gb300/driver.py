@@ -156,10 +156,14 @@ def cells_in_polygons(cell_x, cell_y, polygons, device="cuda"):
     px, py = d(cell_x), d(cell_y)
     inside = torch.zeros(n, dtype=torch.uint8, device=device)
     if polygons:
-        nat.call("spi_points_in_polygons", _ptr(px), _ptr(py), n, len(polygons),
-                 _ptr(d(np.array(off, dtype=np.int64), torch.int64)),
-                 _ptr(d(np.concatenate(vx))), _ptr(d(np.concatenate(vy))),
-                 _ptr(d(np.array(bbox, dtype=np.float64))), _ptr(inside), _stream())
+        # every device array is held by a name until the kernel has run: a
+        # temporary freed after its pointer was taken could hand its memory
+        # to the next argument's allocation
+        t_off = d(np.array(off, dtype=np.int64), torch.int64)
+        t_vx, t_vy = d(np.concatenate(vx)), d(np.concatenate(vy))
+        t_bb = d(np.array(bbox, dtype=np.float64))
+        nat.call("spi_points_in_polygons", _ptr(px), _ptr(py), n, len(polygons), _ptr(t_off),
+                 _ptr(t_vx), _ptr(t_vy), _ptr(t_bb), _ptr(inside), _stream())
     mask = inside.cpu().numpy().astype(bool)
     assert mask.any(), "No cells selected for interpolation!"
     return mask
