@@ -174,7 +174,10 @@ typedef struct {
 typedef struct {
     double *l_arena;     /* Cholesky factor L; for routed systems the
                             inverse of the reference's saddle matrix */
-    double *linv_arena;  /* Linv = L^-1 */
+    double *linv_arena;  /* Linv = L^-1; NULL when no OK variance is wanted:
+                            spi_krige_factor then forms no inverse and
+                            estimates cond from triangular solves, and
+                            spi_krige_duals solves with L */
     int32_t *status;     /* Cholesky: 0, or the 1-based failing pivot */
     int32_t *route;      /* 0 Cholesky path, 1 exact-inverse path,
                             2 singular (nearest-station fallback) */
@@ -199,7 +202,9 @@ typedef struct {
 /* Build and factor every system of the batch in FP64.
  * Cholesky path: A = s*11' - Gamma for OK/EDK (s = total sill, Gamma
  * filled exactly as fill_vg_var_arr with covar 0, diagonal included), the
- * covariance fill for SK; A = L L', Linv = L^-1. Under sum(lambda) = 1 the
+ * covariance fill for SK; A = L L', Linv = L^-1 (with ws->linv_arena; without
+ * it, cond uses ||Linv||_F^2 = trace(A^-1) estimated as the mean of |L^-1 g|^2
+ * over 8 fixed Rademacher vectors g). Under sum(lambda) = 1 the
  * weights of [[A, F], [F', 0]] equal those of the reference's
  * [[Gamma, F], [F', 0]] (Lagrange multipliers change sign).
  * Systems whose Cholesky fails or whose cond exceeds cond_max take the

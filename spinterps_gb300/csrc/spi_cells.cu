@@ -463,9 +463,13 @@ extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys
   if (!vals || !out->est || !ws->route || !ws->shift || !ws->beta || !ws->s_inv ||
       !ws->g_colsum || !ws->l_arena || !ws->cond)
     return SPI_ERR_ARG;
-  if (!ws->linv_arena || !ws->w_hat || !ws->g_cols) return SPI_ERR_ARG;
-  if (precision == 1 && (!dom->cell_split || !dom->stn_split || !ws->linv_hi || !ws->linv_lo ||
-                         !ws->g_hi || !ws->g_lo || !ws->w_hi || !ws->w_lo))
+  if (!ws->w_hat || !ws->g_cols) return SPI_ERR_ARG;
+  // Linv (and its FP32 pair) only for the OK variance
+  if (want_var && !ws->linv_arena) return SPI_ERR_ARG;
+  if (precision == 1 && (!dom->cell_split || !dom->stn_split || !ws->g_hi || !ws->g_lo ||
+                         !ws->w_hi || !ws->w_lo))
+    return SPI_ERR_ARG;
+  if (precision == 1 && want_var && !ws->cell_yy && (!ws->linv_hi || !ws->linv_lo))
     return SPI_ERR_ARG;
   // routed systems are computed in FP64 only
   if (precision == 1 && route_filter != 1) return SPI_ERR_ARG;

@@ -375,6 +375,316 @@ __device__ void matvec_rows(const double* __restrict__ P, int m, int n,
   }
 }
 
+// S^-1 of the small a x a Schur complement by Gauss-Jordan with partial
+// pivoting (one thread), into Si and out [GA * GA], zero-padded.
+__device__ void schur_inverse(const double (*S)[GA], int a, double (*Si)[GA],
+                              double* __restrict__ out) {
+  double M[GA][2 * GA];
+  for (int i = 0; i < a; ++i)
+    for (int j = 0; j < 2 * a; ++j) M[i][j] = (j < a) ? S[i][j] : (j - a == i ? 1.0 : 0.0);
+  for (int c = 0; c < a; ++c) {
+    int p = c;
+    for (int r = c + 1; r < a; ++r)
+      if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+    if (p != c)
+      for (int j = 0; j < 2 * a; ++j) {
+        double t = M[c][j];
+        M[c][j] = M[p][j];
+        M[p][j] = t;
+      }
+    double piv = M[c][c];
+    for (int j = 0; j < 2 * a; ++j) M[c][j] /= piv;
+    for (int r = 0; r < a; ++r)
+      if (r != c) {
+        double f = M[r][c];
+        for (int j = 0; j < 2 * a; ++j) M[r][j] -= f * M[c][j];
+      }
+  }
+  for (int i = 0; i < GA; ++i)
+    for (int j = 0; j < GA; ++j) {
+      double val = (i < a && j < a) ? M[i][a + j] : 0.0;
+      Si[i][j] = val;
+      out[i * GA + j] = val;
+    }
+}
+
+// ---- triangular solves with the Cholesky factor (no inverse formed) ----
+// Systems that need no OK variance never form Linv (n^3/3 FP64 per
+// system); their dual vectors come from L by forward and backward
+// substitution, nk <= KS right-hand sides at once, held in shared memory
+// as Y[k * ldy + i]. L: row-major n x n, lower triangle (the upper one
+// still holds the matrix and is never read).
+constexpr int KS = 4;
+
+// Y_k <- L^-1 Y_k. Blocks of 32 rows: the rows' dot products with the
+// solved part (a warp per row, lanes along the row), then the 32 x 32
+// diagonal block by one warp (a lane per row).
+__device__ void trsv_lower_multi(const double* __restrict__ L, int n, double* Y, int ldy,
+                                 int nk) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i0 = 0; i0 < n; i0 += 32) {
+    const int nb = min(32, n - i0);
+    if (i0 > 0) {
+      for (int r = warp; r < nb; r += FT / 32) {
+        const double* row = L + (int64_t)(i0 + r) * n;
+        double acc[KS];
+#pragma unroll
+        for (int k = 0; k < KS; ++k) acc[k] = 0.0;
+        for (int j = lane; j < i0; j += 32) {
+          const double l = row[j];
+#pragma unroll
+          for (int k = 0; k < KS; ++k)
+            if (k < nk) acc[k] = fma(l, Y[k * ldy + j], acc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < KS; ++k)
+          for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+        if (lane == 0)
+          for (int k = 0; k < nk; ++k) Y[k * ldy + i0 + r] -= acc[k];
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      double t[KS];
+      const double* Lb = L + (int64_t)(i0 + min(lane, nb - 1)) * n + i0;  // this lane's row
+#pragma unroll
+      for (int k = 0; k < KS; ++k) t[k] = (lane < nb && k < nk) ? Y[k * ldy + i0 + lane] : 0.0;
+      for (int c = 0; c < nb; ++c) {
+        const double lcc = __shfl_sync(0xffffffffu, Lb[min(c, nb - 1)], c);
+        const double lrc = (lane > c && lane < nb) ? Lb[c] : 0.0;
+#pragma unroll
+        for (int k = 0; k < KS; ++k) {
+          const double y = __shfl_sync(0xffffffffu, t[k], c) / lcc;
+          if (lane == c) t[k] = y;
+          else t[k] -= lrc * y;
+        }
+      }
+      if (lane < nb)
+        for (int k = 0; k < nk; ++k) Y[k * ldy + i0 + lane] = t[k];
+    }
+    __syncthreads();
+  }
+}
+
+// Y_k <- L^-T Y_k. Blocks of 32 rows from the bottom: the diagonal block
+// by one warp, then every earlier entry updated by the block's solved
+// values (a thread per entry, reading the block's rows of L along them).
+__device__ void trsv_lower_t_multi(const double* __restrict__ L, int n, double* Y, int ldy,
+                                   int nk) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nblk = (n + 31) / 32;
+  for (int I = nblk - 1; I >= 0; --I) {
+    const int i0 = I * 32, nb = min(32, n - i0);
+    if (warp == 0) {
+      double t[KS];
+#pragma unroll
+      for (int k = 0; k < KS; ++k) t[k] = (lane < nb && k < nk) ? Y[k * ldy + i0 + lane] : 0.0;
+      for (int c = nb - 1; c >= 0; --c) {
+        const double* Lc = L + (int64_t)(i0 + c) * n + i0;  // row c of the block
+        const double lcc = Lc[c];
+        const double lcr = (lane < c) ? Lc[lane] : 0.0;
+#pragma unroll
+        for (int k = 0; k < KS; ++k) {
+          const double y = __shfl_sync(0xffffffffu, t[k], c) / lcc;
+          if (lane == c) t[k] = y;
+          else t[k] -= lcr * y;
+        }
+      }
+      if (lane < nb)
+        for (int k = 0; k < nk; ++k) Y[k * ldy + i0 + lane] = t[k];
+    }
+    __syncthreads();
+    for (int r = tid; r < i0; r += FT) {
+      double acc[KS];
+#pragma unroll
+      for (int k = 0; k < KS; ++k) acc[k] = 0.0;
+      for (int c = 0; c < nb; ++c) {
+        const double l = L[(int64_t)(i0 + c) * n + r];
+#pragma unroll
+        for (int k = 0; k < KS; ++k)
+          if (k < nk) acc[k] = fma(l, Y[k * ldy + i0 + c], acc[k]);
+      }
+      for (int k = 0; k < nk; ++k) Y[k * ldy + r] -= acc[k];
+    }
+    __syncthreads();
+  }
+}
+
+// A deterministic Rademacher sign for entry i of probe k of system s.
+__device__ __forceinline__ double probe_sign(int s, int k, int i) {
+  uint32_t h = (uint32_t)i * 0x9E3779B1u ^ ((uint32_t)k * 0x85EBCA77u + (uint32_t)s * 0xC2B2AE3Du);
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  return (h & 1u) ? 1.0 : -1.0;
+}
+
+// cond = n A_00 ||Linv||_F^2 without Linv: ||Linv||_F^2 = trace(A^-1) =
+// E |L^-1 g|^2 over Rademacher g (Hutchinson), the mean of KP fixed
+// probes (relative spread ~ sqrt(2 / KP) at worst, far inside the orders
+// of magnitude the routing thresholds work in). Dynamic shared memory:
+// nk x n doubles.
+constexpr int KP = 8;
+__global__ __launch_bounds__(FT) void k_cond_est(spi_systems_t sys,
+                                                const double* __restrict__ l_arena,
+                                                const int32_t* __restrict__ status,
+                                                double* __restrict__ cond, int nk) {
+  const int s = blockIdx.x;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  if (status[s] != 0) {
+    if (threadIdx.x == 0) cond[s] = __longlong_as_double(0x7ff0000000000000LL);
+    return;
+  }
+  const double* L = l_arena + v.moff;
+  extern __shared__ double ysm[];
+  __shared__ double red[FT / 32];
+  double tot = 0.0;
+  for (int k0 = 0; k0 < KP; k0 += nk) {
+    const int kk = min(nk, KP - k0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kk * n; e += FT) {
+      const int k = e / n, i = e - k * n;
+      ysm[k * n + i] = probe_sign(s, k0 + k, i);
+    }
+    __syncthreads();
+    trsv_lower_multi(L, n, ysm, n, kk);
+    for (int e = threadIdx.x; e < kk * n; e += FT) tot = fma(ysm[e], ysm[e], tot);
+  }
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = tot;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < FT / 32; ++w) t += red[w];
+    cond[s] = (double)n * (L[0] * L[0]) * (t / KP);
+  }
+}
+
+// Route-0 duals without Linv (spi_krige_duals when ws.linv_arena is NULL):
+// the same quantities as k_duals, A^-1 applied by two triangular solves.
+// Dynamic shared memory: nk x n doubles.
+__global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_systems_t sys,
+                                                   spi_krige_ws_t ws,
+                                                   const double* __restrict__ vals, int nk) {
+  const int s = blockIdx.x;
+  if (ws.route[s] != 0) return;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  const double* L = ws.l_arena + v.moff;
+  extern __shared__ double ysm[];
+  __shared__ double red[FT / 32];
+  __shared__ double S[GA][GA];
+  __shared__ double Si[GA][GA];
+  __shared__ double hb[KS][GA];
+  const int sk = sys.kind == SPI_KIND_SK;
+  const int a = sk ? 1 : extra_rows(sys.kind, dom.n_drift);
+  double* G = ws.g_cols + v.off * GA;  // column k at G + k * n
+  auto fcol = [&](int k, int i) {
+    return (k == 0) ? 1.0 : dom.stn_drift[(int64_t)v.idx[i] * dom.n_drift + (k - 1)];
+  };
+  // G_k = A^-1 F_k
+  for (int k0 = 0; k0 < a; k0 += nk) {
+    const int kk = min(nk, a - k0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kk * n; e += FT) {
+      const int k = e / n, i = e - k * n;
+      ysm[k * n + i] = fcol(k0 + k, i);
+    }
+    __syncthreads();
+    trsv_lower_multi(L, n, ysm, n, kk);
+    trsv_lower_t_multi(L, n, ysm, n, kk);
+    for (int e = threadIdx.x; e < kk * n; e += FT) G[(int64_t)k0 * n + e] = ysm[e];
+  }
+  __syncthreads();
+  // SK: |u| (u = A^-1 1) as a second column (as k_duals)
+  if (sk)
+    for (int i = threadIdx.x; i < n; i += FT) G[n + i] = fabs(G[i]);
+  // S = F'G, its inverse, 1'G
+  for (int k = 0; k < a; ++k)
+    for (int l = 0; l < a; ++l) {
+      double t = 0.0;
+      for (int i = threadIdx.x; i < n; i += FT) t = fma(fcol(k, i), G[(int64_t)l * n + i], t);
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      __syncthreads();
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double u = 0.0;
+        for (int w = 0; w < FT / 32; ++w) u += red[w];
+        S[k][l] = u;
+      }
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) schur_inverse(S, a, Si, ws.s_inv + (int64_t)s * GA * GA);
+  for (int k = 0; k < GA; ++k) {
+    double t = 0.0;
+    if (k < a)
+      for (int i = threadIdx.x; i < n; i += FT) t += G[(int64_t)k * n + i];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double u = 0.0;
+      for (int w = 0; w < FT / 32; ++w) u += red[w];
+      ws.g_colsum[(int64_t)s * GA + k] = (k < a) ? u : 0.0;
+    }
+  }
+  // per step, nk at a time: OK / EDK w_hat = A^-1 z - G beta with
+  // beta = S^-1 G'z; SK w_hat = A^-1 z
+  const int64_t sb = sys.step_off[s], se = sys.step_off[s + 1];
+  for (int64_t q0 = sb; q0 < se; q0 += nk) {
+    const int kk = (int)min((int64_t)nk, se - q0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kk * n; e += FT) {
+      const int k = e / n, i = e - k * n;
+      ysm[k * n + i] = vals[sys.val_off[sys.steps[q0 + k]] + i];
+    }
+    __syncthreads();
+    if (!sk) {
+      // h = G'z per vector, before the solves overwrite z
+      for (int k = 0; k < kk; ++k)
+        for (int l = 0; l < a; ++l) {
+          double t = 0.0;
+          for (int i = threadIdx.x; i < n; i += FT) t = fma(G[(int64_t)l * n + i], ysm[k * n + i], t);
+          for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+          __syncthreads();
+          if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            double u = 0.0;
+            for (int w = 0; w < FT / 32; ++w) u += red[w];
+            hb[k][l] = u;
+          }
+        }
+      __syncthreads();
+    }
+    trsv_lower_multi(L, n, ysm, n, kk);
+    trsv_lower_t_multi(L, n, ysm, n, kk);
+    for (int k = 0; k < kk; ++k) {
+      const int j = sys.steps[q0 + k];
+      const int64_t vo = sys.val_off[j];
+      double bt[GA];
+      for (int m = 0; m < GA; ++m) {
+        double t = 0.0;
+        if (!sk)
+          for (int l = 0; l < a; ++l) t += Si[m][l] * hb[k][l];
+        bt[m] = (m < a && !sk) ? t : 0.0;
+      }
+      for (int i = threadIdx.x; i < n; i += FT) {
+        double w = ysm[k * n + i];
+        if (!sk)
+          for (int m = 0; m < a; ++m) w -= G[(int64_t)m * n + i] * bt[m];
+        ws.w_hat[vo + i] = w;
+      }
+      if (threadIdx.x < GA) ws.beta[(int64_t)j * GA + threadIdx.x] = bt[threadIdx.x];
+    }
+  }
+}
+
 // Per-system G, S^-1, 1'G and per-step dual weights (route 0), or the
 // split dual vectors of the inverse saddle matrix (route 1). Dynamic shared
 // memory: 3 vectors of n + GA doubles.
@@ -384,6 +694,7 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
   const int s = blockIdx.x;
   const int route = ws.route[s];
   if (route == 2) return;
+  if (route == 0 && ws.linv_arena == nullptr) return;  // k_duals_solve
   SysView v = sys_view(sys, s);
   const int n = v.n;
   const double* X = ws.linv_arena + v.moff;
@@ -451,36 +762,7 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // Gauss-Jordan with partial pivoting on the small a x a Schur complement
-    double M[GA][2 * GA];
-    for (int i = 0; i < a; ++i)
-      for (int j = 0; j < 2 * a; ++j) M[i][j] = (j < a) ? S[i][j] : (j - a == i ? 1.0 : 0.0);
-    for (int c = 0; c < a; ++c) {
-      int p = c;
-      for (int r = c + 1; r < a; ++r)
-        if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
-      if (p != c)
-        for (int j = 0; j < 2 * a; ++j) {
-          double t = M[c][j];
-          M[c][j] = M[p][j];
-          M[p][j] = t;
-        }
-      double piv = M[c][c];
-      for (int j = 0; j < 2 * a; ++j) M[c][j] /= piv;
-      for (int r = 0; r < a; ++r)
-        if (r != c) {
-          double f = M[r][c];
-          for (int j = 0; j < 2 * a; ++j) M[r][j] -= f * M[c][j];
-        }
-    }
-    for (int i = 0; i < GA; ++i)
-      for (int j = 0; j < GA; ++j) {
-        double val = (i < a && j < a) ? M[i][a + j] : 0.0;
-        Si[i][j] = val;
-        ws.s_inv[(int64_t)s * GA * GA + i * GA + j] = val;
-      }
-  }
+  if (threadIdx.x == 0) schur_inverse(S, a, Si, ws.s_inv + (int64_t)s * GA * GA);
   __syncthreads();
   for (int k = 0; k < GA; ++k) {
     double cs = 0.0;
@@ -586,9 +868,20 @@ static int check_sys(const spi_domain_t* dom, const spi_systems_t* sys) {
 }
 
 static int check_ws(const spi_krige_ws_t* ws) {
-  if (!ws || !ws->l_arena || !ws->linv_arena || !ws->status || !ws->route || !ws->cond ||
-      !ws->shift || !ws->w_hat || !ws->beta || !ws->g_cols || !ws->s_inv || !ws->g_colsum)
+  if (!ws || !ws->l_arena || !ws->status || !ws->route || !ws->cond || !ws->shift ||
+      !ws->w_hat || !ws->beta || !ws->g_cols || !ws->s_inv || !ws->g_colsum)
     return SPI_ERR_ARG;
+  return SPI_OK;
+}
+
+// Right-hand sides per triangular-solve pass and the shared memory they
+// take (KS at most, within 200 KB).
+static int solve_smem(int max_n, int* nk, size_t* bytes) {
+  int k = (int)((200 * 1024) / ((size_t)max_n * sizeof(double)));
+  if (k > KS) k = KS;
+  if (k < 1) return SPI_ERR_TOO_LARGE;
+  *nk = k;
+  *bytes = (size_t)k * max_n * sizeof(double);
   return SPI_OK;
 }
 
@@ -610,7 +903,18 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   SPI_LAUNCH_CHECK();
   k_chol<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status);
   SPI_LAUNCH_CHECK();
-  k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->linv_arena, ws->status, ws->cond);
+  if (ws->linv_arena) {
+    k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->linv_arena, ws->status, ws->cond);
+  } else {
+    int nk;
+    size_t ysm;
+    if ((rc = solve_smem(sys->max_n, &nk, &ysm))) return rc;
+    if (ysm > 48 * 1024 &&
+        cudaFuncSetAttribute(k_cond_est, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ysm) != cudaSuccess)
+      return SPI_ERR_CUDA;
+    k_cond_est<<<sys->n_sys, FT, ysm, st>>>(sy, ws->l_arena, ws->status, ws->cond, nk);
+  }
   SPI_LAUNCH_CHECK();
   size_t gsm = (size_t)(sys->max_n + GA) * (2 * sizeof(double) + sizeof(int));
   if (gsm > 200 * 1024) return SPI_ERR_TOO_LARGE;
@@ -641,6 +945,18 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
   }
   k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals);
   SPI_LAUNCH_CHECK();
+  if (!ws->linv_arena) {
+    // route-0 systems without Linv: triangular solves with L
+    int nk;
+    size_t ysm;
+    if ((rc = solve_smem(sys->max_n, &nk, &ysm))) return rc;
+    if (ysm > 48 * 1024 &&
+        cudaFuncSetAttribute(k_duals_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ysm) != cudaSuccess)
+      return SPI_ERR_CUDA;
+    k_duals_solve<<<sys->n_sys, FT, ysm, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals, nk);
+    SPI_LAUNCH_CHECK();
+  }
   return SPI_OK;
 }
 
@@ -650,7 +966,7 @@ extern "C" int spi_krige_loo(const spi_domain_t* dom, const spi_systems_t* sys,
   if (rc) return rc;
   if (sys->n_sys == 0) return SPI_OK;
   if ((rc = check_ws(ws))) return rc;
-  if (!resid) return SPI_ERR_ARG;
+  if (!resid || !ws->linv_arena) return SPI_ERR_ARG;
   size_t smem = (size_t)sys->max_n * sizeof(double);
   if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
   if (smem > 48 * 1024 &&

@@ -228,7 +228,7 @@ class _KrigeBatch:
     """One chunk of kriging systems: device descriptors and workspaces."""
 
     def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
-                 want_var=False, tensor_cores=True, n_probe=0):
+                 want_var=False, tensor_cores=True, n_probe=0, need_linv=None):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -260,7 +260,12 @@ class _KrigeBatch:
                                _ptr(self.out_row), int(ns.max()))
         n_sys = len(ch)
         self.L = torch.empty(self.arena, dtype=torch.float64, device=dev)
-        self.X = torch.empty(self.arena, dtype=torch.float64, device=dev)
+        # Linv only where the OK variance (or leave-one-out) reads it; other
+        # systems get their duals and condition estimate from L by
+        # triangular solves (spi_krige_factor / spi_krige_duals)
+        if need_linv is None:
+            need_linv = bool(want_var and kind == "OK")
+        self.X = torch.empty(self.arena, dtype=torch.float64, device=dev) if need_linv else None
         self.status = torch.empty(n_sys, dtype=torch.int32, device=dev)
         self.route = torch.empty(n_sys, dtype=torch.int32, device=dev)
         self.cond = torch.empty(n_sys, dtype=torch.float64, device=dev)
@@ -273,9 +278,12 @@ class _KrigeBatch:
         self.split = None
         if precision == 1:
             # FP32 (hi, lo) pairs of Linv, G and w_hat for the split-precision kernel
+            na = self.arena if self.X is not None else 0
             self.split = [torch.empty(k, dtype=torch.float32, device=dev)
-                          for k in (self.arena, self.arena, self.g_cols.numel(),
-                                    self.g_cols.numel(), self.w_hat.numel(), self.w_hat.numel())]
+                          for k in (na, na, self.g_cols.numel(), self.g_cols.numel(),
+                                    self.w_hat.numel(), self.w_hat.numel())]
+            if self.X is None:
+                self.split[0] = self.split[1] = None
         # |Linv c|^2 per (system, cell) from the tensor cores (FP32 tier of
         # the OK variance)
         self.yy = None
@@ -357,7 +365,8 @@ class _KrigeBatch:
                  ws, s)
         if self.split is not None:
             xh, xl, gh, gl, wh, wl = self.split
-            nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
+            if self.X is not None:
+                nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
             nat.call("spi_split_f64", _ptr(self.g_cols), _ptr(gh), _ptr(gl), self.g_cols.numel(), s)
             nat.call("spi_split_f64", _ptr(self.w_hat), _ptr(wh), _ptr(wl), self.w_hat.numel(), s)
         if self.probe is not None and probe is not None:
@@ -745,7 +754,7 @@ def krige_loo(stn_x, stn_y, data, vgs, *, min_vg_val=0.0, device="cuda", cond_ma
     val_off = np.zeros(T, dtype=np.int64)
     beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
     for ch in _chunk_systems(systems, 0, 8 << 30):
-        b = _KrigeBatch(dev, dom, "OK", systems, ch, data, T, val_off, beta, 0)
+        b = _KrigeBatch(dev, dom, "OK", systems, ch, data, T, val_off, beta, 0, need_linv=True)
         s = _stream()
         ws = ctypes.byref(b.ws)
         nat.call("spi_krige_factor", ctypes.byref(dom.st), ctypes.byref(b.sy), ws,
