@@ -4,7 +4,9 @@ by running cyth/interpmthds.pyx:251-765) and against the oracle's
 restatement on larger cases.
 
 Bars:
-- distances: bit for bit;
+- distances: within 1 ulp, nearly all bit for bit (the reference's get_dist
+  takes libm pow(s, 0.5), which is 1 ulp off the correctly rounded square
+  root the GPU takes in ~0.1% of arguments);
 - matrices and right-hand sides: 1e-13 relative (device exp / sin / pow
   against the host's libm);
 - the inverse: 1e-9 of its largest entry;
@@ -47,7 +49,9 @@ def _check(key, got, ref, tag):
     got = np.asarray(got, dtype=np.float64)
     assert got.shape == ref.shape, (tag, key)
     if key in EXACT:
-        assert np.array_equal(got, ref), (tag, key)
+        ulp = np.abs(got - ref) / np.spacing(np.maximum(ref, 1e-300))
+        assert (ulp <= 1).all(), (tag, key)
+        assert (got == ref).mean() > 0.98, (tag, key)
         return
     scale = max(np.abs(ref).max(), 1e-300) if ref.size else 1.0
     if key in MATRIX:
