@@ -13,10 +13,11 @@ the reference's files:
 - the per-step statistics of ``stats.csv`` (interp/main.py:474-525, GPU).
 
 ``interpolate_grid`` strings these together. It returns full [T, rows, cols]
-float fields, NaN outside the mask, in place of the netCDF file.
+float fields, NaN outside the mask. ``write_outputs`` writes them as the
+reference's netCDF file (``ncout``, classic binary format) and stats.csv.
 
-Reading GeoTIFF rasters and shapefiles (GDAL / ogr) and writing netCDF are
-not here: those libraries are absent. Callers pass arrays: raster values
+Reading GeoTIFF rasters and shapefiles (GDAL / ogr) is not here: those
+libraries are absent. Callers pass arrays: raster values
 with their origin, cell size and no-data value, and polygon vertex lists.
 Buffering polygons (``ogr.Geometry.Buffer``) is the caller's job too.
 """
@@ -305,3 +306,23 @@ def interpolate_grid(stn_x, stn_y, data, vgs, interp_args, *, cell_size, bounds=
             full[:, mask] = h
             out[lab] = full.reshape(T, ny, nx)
     return out, plan.problem_steps(), stats, grid
+
+
+def write_outputs(out_dir, nc_name, fields, grid, stats, interp_args, time_vals, *,
+                  time_steps=None, xlab="X", ylab="Y", tlab="time", tunits=None, tcldr=None,
+                  vunits="", vlab="", settings=None, fmt=5):
+    """The reference's two output files from interpolate_grid's results:
+    the netCDF file of the fields (ncout.write_interp_nc; name as the
+    reference forms it, interp/prepare.py:308-311) and stats.csv
+    (interp/main.py:519-520). Returns the two paths."""
+    from pathlib import Path
+    from . import ncout
+    out_dir = Path(out_dir)
+    out_dir.mkdir(parents=True, exist_ok=True)
+    nc_path = out_dir / (nc_name.split(".", 1)[0] + ".nc")
+    ncout.write_interp_nc(nc_path, grid["x_crds"], grid["y_crds"], time_vals, fields,
+                          interp_args, xlab=xlab, ylab=ylab, tlab=tlab, tunits=tunits,
+                          tcldr=tcldr, vunits=vunits, vlab=vlab, settings=settings, fmt=fmt)
+    csv_path = out_dir / "stats.csv"
+    write_stats_csv(csv_path, time_steps if time_steps is not None else time_vals, stats)
+    return nc_path, csv_path

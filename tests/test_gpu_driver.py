@@ -123,6 +123,17 @@ def test_interpolate_grid_vs_oracle():
                                    rtol=1e-6, equal_nan=True), (lab, s)
     dst = port.field_stats(z, 1)
     assert np.allclose(stats["data_std"], dst[:, 3].astype(np.float32), rtol=1e-6)
+    # the output files: netCDF fields and stats.csv, read back
+    import tempfile
+    from spinterps_gb300 import ncout
+    with tempfile.TemporaryDirectory() as td:
+        nc_p, csv_p = driver.write_outputs(td, "interp.nc", out, grid, stats, args,
+                                           np.arange(T), vlab="z", settings={"cell_size": cs})
+        dims, var, gatt = ncout.read_nc(nc_p)
+        assert dims == {"dimx": nx, "dimy": ny, "dimt": T}
+        for lab in out:
+            assert np.array_equal(var[lab][1], out[lab], equal_nan=True), lab
+        assert len(open(csv_p).read().splitlines()) == T + 1
     # rounding as written: the rounded run equals numpy.round of the plain one
     out3, _, _, _ = driver.interpolate_grid(
         sx, sy, z, vgs, args, cell_size=cs, bounds=(1e3, 61e3, 1e3, 61e3), polygons=polys,
