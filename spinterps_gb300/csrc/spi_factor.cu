@@ -447,14 +447,16 @@ __device__ void trsv_lower_multi(const double* __restrict__ L, int n, double* Y,
     if (warp == 0) {
       double t[KS];
       const double* Lb = L + (int64_t)(i0 + min(lane, nb - 1)) * n + i0;  // this lane's row
+      // one reciprocal per row (divisions run on the 1/64-rate FP64 pipe)
+      const double rd = 1.0 / Lb[min(lane, nb - 1)];
 #pragma unroll
       for (int k = 0; k < KS; ++k) t[k] = (lane < nb && k < nk) ? Y[k * ldy + i0 + lane] : 0.0;
       for (int c = 0; c < nb; ++c) {
-        const double lcc = __shfl_sync(0xffffffffu, Lb[min(c, nb - 1)], c);
+        const double rcc = __shfl_sync(0xffffffffu, rd, c);
         const double lrc = (lane > c && lane < nb) ? Lb[c] : 0.0;
 #pragma unroll
         for (int k = 0; k < KS; ++k) {
-          const double y = __shfl_sync(0xffffffffu, t[k], c) / lcc;
+          const double y = __shfl_sync(0xffffffffu, t[k], c) * rcc;
           if (lane == c) t[k] = y;
           else t[k] -= lrc * y;
         }
@@ -477,15 +479,16 @@ __device__ void trsv_lower_t_multi(const double* __restrict__ L, int n, double* 
     const int i0 = I * 32, nb = min(32, n - i0);
     if (warp == 0) {
       double t[KS];
+      const double rd = 1.0 / L[(int64_t)(i0 + min(lane, nb - 1)) * n + i0 + min(lane, nb - 1)];
 #pragma unroll
       for (int k = 0; k < KS; ++k) t[k] = (lane < nb && k < nk) ? Y[k * ldy + i0 + lane] : 0.0;
       for (int c = nb - 1; c >= 0; --c) {
         const double* Lc = L + (int64_t)(i0 + c) * n + i0;  // row c of the block
-        const double lcc = Lc[c];
+        const double rcc = __shfl_sync(0xffffffffu, rd, c);
         const double lcr = (lane < c) ? Lc[lane] : 0.0;
 #pragma unroll
         for (int k = 0; k < KS; ++k) {
-          const double y = __shfl_sync(0xffffffffu, t[k], c) / lcc;
+          const double y = __shfl_sync(0xffffffffu, t[k], c) * rcc;
           if (lane == c) t[k] = y;
           else t[k] -= lcr * y;
         }
@@ -565,6 +568,7 @@ __global__ __launch_bounds__(FT) void k_cond_est(spi_systems_t sys,
 
 // Route-0 duals without Linv (spi_krige_duals when ws.linv_arena is NULL):
 // the same quantities as k_duals, A^-1 applied by two triangular solves.
+// This kernel: G, S^-1, 1'G per system; k_duals_solve_steps: the steps.
 // Dynamic shared memory: nk x n doubles.
 __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_systems_t sys,
                                                    spi_krige_ws_t ws,
@@ -578,7 +582,6 @@ __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_system
   __shared__ double red[FT / 32];
   __shared__ double S[GA][GA];
   __shared__ double Si[GA][GA];
-  __shared__ double hb[KS][GA];
   const int sk = sys.kind == SPI_KIND_SK;
   const int a = sk ? 1 : extra_rows(sys.kind, dom.n_drift);
   double* G = ws.g_cols + v.off * GA;  // column k at G + k * n
@@ -633,10 +636,33 @@ __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_system
       ws.g_colsum[(int64_t)s * GA + k] = (k < a) ? u : 0.0;
     }
   }
-  // per step, nk at a time: OK / EDK w_hat = A^-1 z - G beta with
-  // beta = S^-1 G'z; SK w_hat = A^-1 z
+}
+
+// The per-step part of the route-0 duals without Linv: CTA (g, s) takes
+// steps g * nk .. of system s (w_hat = A^-1 z - G beta with beta =
+// S^-1 G'z; SK: w_hat = A^-1 z), reading G and S^-1 from k_duals_solve.
+// Dynamic shared memory: nk x n doubles.
+__global__ __launch_bounds__(FT) void k_duals_solve_steps(spi_domain_t dom, spi_systems_t sys,
+                                                         spi_krige_ws_t ws,
+                                                         const double* __restrict__ vals,
+                                                         int nk) {
+  const int s = blockIdx.y;
+  if (ws.route[s] != 0) return;
   const int64_t sb = sys.step_off[s], se = sys.step_off[s + 1];
-  for (int64_t q0 = sb; q0 < se; q0 += nk) {
+  if (sb + (int64_t)blockIdx.x * nk >= se) return;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  const double* L = ws.l_arena + v.moff;
+  extern __shared__ double ysm[];
+  __shared__ double red[FT / 32];
+  __shared__ double Si[GA][GA];
+  __shared__ double hb[KS][GA];
+  const int sk = sys.kind == SPI_KIND_SK;
+  const int a = sk ? 1 : extra_rows(sys.kind, dom.n_drift);
+  const double* G = ws.g_cols + v.off * GA;
+  for (int e = threadIdx.x; e < GA * GA; e += FT)
+    Si[e / GA][e % GA] = ws.s_inv[(int64_t)s * GA * GA + e];
+  for (int64_t q0 = sb + (int64_t)blockIdx.x * nk; q0 < se; q0 += (int64_t)gridDim.x * nk) {
     const int kk = (int)min((int64_t)nk, se - q0);
     __syncthreads();
     for (int e = threadIdx.x; e < kk * n; e += FT) {
@@ -955,6 +981,16 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
                              (int)ysm) != cudaSuccess)
       return SPI_ERR_CUDA;
     k_duals_solve<<<sys->n_sys, FT, ysm, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals, nk);
+    SPI_LAUNCH_CHECK();
+    // the steps: groups of nk spread over gx CTAs per system
+    if (ysm > 48 * 1024 &&
+        cudaFuncSetAttribute(k_duals_solve_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ysm) != cudaSuccess)
+      return SPI_ERR_CUDA;
+    int gx = (304 + sys->n_sys - 1) / sys->n_sys;
+    gx = gx < 1 ? 1 : (gx > 64 ? 64 : gx);
+    k_duals_solve_steps<<<dim3(gx, sys->n_sys), FT, ysm, (cudaStream_t)stream>>>(*dom, *sys,
+                                                                               *ws, vals, nk);
     SPI_LAUNCH_CHECK();
   }
   return SPI_OK;
