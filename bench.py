@@ -197,6 +197,7 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 FP64_NOMINAL_TFLOPS = FP32_NOMINAL_TFLOPS / 64
 KERNEL_BOUND = {
     "var_tc": ("tensor", "spi::k_var_tc (tcgen05 3xTF32 OK-variance contraction)"),
+    "var_df": ("fp32", "spi::k_var_df (double-float OK-variance contraction, FP32 pipe)"),
     "cells_fp32": ("fp32", "spi::k_krige_cells<float> (FP32 tier: estimates, sum check)"),
     "cells_fp64": ("fp64", "spi::k_krige_cells<double> (FP64 tier: ill-conditioned and "
                            "routed systems, the plain path's kernel)"),
@@ -253,13 +254,15 @@ def run_ours(args):
         plans[i % n_sl].execute()
     torch.cuda.synchronize()
     failed = routed = 0
-    fp32_steps, probe = {}, {}
+    fp32_steps, df_steps, probe = {}, {}, {}
     for p in plans:
         inf = p.collect_info()
         failed += len(inf["failed_steps"].get("OK", []))
         routed += len(inf.get("exact_inverse_steps", {}).get("OK", []))
         for k, v in inf.get("fp32_tier_steps", {}).items():
             fp32_steps[k] = fp32_steps.get(k, 0) + len(v)
+        for k, v in inf.get("df_variance_steps", {}).items():
+            df_steps[k] = df_steps.get(k, 0) + len(v)
         for k, d in inf.get("probe_disc", {}).items():
             probe.setdefault(k, []).append(d)
     stream = torch.cuda.current_stream()
@@ -357,10 +360,11 @@ def run_ours(args):
                        "l2": "per-step working set (4.4 GB of fields + 1.6 GB factors) >> L2",
                        "singular_steps_nnb": failed, "exact_inverse_steps": routed,
                        "fp32_tier_steps": fp32_steps,
+                       "df_variance_steps": df_steps,
                        "probe_disc_quantiles": {
                            k: {lab: [float(q) for q in np.nanquantile(
                                np.concatenate(v)[:, c], [0.25, 0.5, 0.75, 0.9])]
-                               for c, lab in ((0, "est"), (1, "var"))}
+                               for c, lab in ((0, "est"), (1, "var_tc"), (2, "var_df"))}
                            for k, v in probe.items()}},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),

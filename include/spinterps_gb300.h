@@ -195,8 +195,11 @@ typedef struct {
                             kernel instead of its own variance pass (NULL:
                             the cell kernel computes it) */
     int32_t *tier;       /* optional [n_sys]: 1 = the FP32 tier of the
-                            precision-1 kernels, 0 = FP64 (spi_krige_tier);
-                            NULL: route 0 and cond <= cond_split */
+                            precision-1 kernels with the tensor-core
+                            variance, 2 = the FP32 tier with the
+                            double-float variance, 0 = FP64
+                            (spi_krige_tier); NULL: route 0 and
+                            cond <= cond_split */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -264,20 +267,24 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
 /* Tier of every system of a factored batch from a probe: est/var fields
  * [rows, n_probe] (row = sys->out_row[step]) of the same probe cells
  * computed by the FP64 kernel (route_filter 0) and by the FP32 tier
- * (precision 1, route_filter 1, cond_split = cond_cap). tier[s] = 1 when the
- * system is on the Cholesky path, cond <= cond_cap, and over its steps and
- * the probe cells |est32 - est64| <= tol_est and |var32 - var64| <= tol_var
- * (var arrays may be NULL; a NaN in one field and not the other fails).
- * disc (optional, [n_sys, 2]): each system's largest |est32 - est64| and
- * |var32 - var64| over the probe (NaN for systems not on the Cholesky path
- * under cond_cap, +inf for a NaN mismatch). The
+ * (precision 1, route_filter 1): var32 with the tensor-core variance
+ * (spi_krige_var_tc), var32_df (optional) with the double-float one
+ * (spi_krige_var_df). tier[s] = 1 when the system is on the Cholesky path,
+ * cond <= cond_cap, and over its steps and the probe cells |est32 - est64|
+ * <= tol_est and |var32 - var64| <= tol_var; else 2 when cond <= cond_cap_df
+ * and the estimates and |var32_df - var64| pass the same tolerances; else
+ * 0 (var arrays may be NULL; a NaN in one field and not the other fails).
+ * disc (optional, [n_sys, 3]): each system's largest estimate, tensor-core
+ * variance and double-float variance discrepancy over the probe (NaN where
+ * not a candidate, +inf for a NaN mismatch). The
  * mixed path's a-posteriori error control: the FP32 rounding of the
  * right-hand sides enters the estimate as sum_i dc_i w_i, which the dual
  * weights can amplify far beyond what the condition number predicts. */
 int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n_probe,
                    const double *est64, const double *est32, const double *var64,
-                   const double *var32, double tol_est, double tol_var, double cond_cap,
-                   int32_t *tier, double *disc, spi_stream_t stream);
+                   const double *var32, const double *var32_df, double tol_est,
+                   double tol_var, double cond_cap, double cond_cap_df, int32_t *tier,
+                   double *disc, spi_stream_t stream);
 
 /* The OK variance term |Linv c|^2 of every cell of the FP32-tier systems
  * (ws->tier, else route 0 and cond <= cond_split; kinds OK / EDK) on the tensor cores
@@ -289,6 +296,15 @@ int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n
 int spi_krige_var_tc(const spi_domain_t *dom, const spi_systems_t *sys,
                      const spi_krige_ws_t *ws, double cond_split, int32_t *err_flag,
                      spi_stream_t stream);
+
+/* The same term |Linv c|^2 in double-float on the FP32 pipe (every product
+ * split by FMA, sums by TwoSum: ~1e-9 of the sill), into ws->cell_yy, for
+ * the systems with ws->tier[s] == 2 (without ws->tier: route 0 and cond <=
+ * cond_cap; kinds OK / EDK): the FP32 tier's variance where the tensor-core
+ * one misses the probe's tolerance. Requires ws->linv_hi / linv_lo and the
+ * domain's split coordinates. */
+int spi_krige_var_df(const spi_domain_t *dom, const spi_systems_t *sys,
+                     const spi_krige_ws_t *ws, double cond_cap, spi_stream_t stream);
 
 /* IDW (interp/steps.py:293-313, cyth/interpmthds.pyx:784-808) for every
  * cell of the listed steps. data [n_steps_total, n_stns] holds every

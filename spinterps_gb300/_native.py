@@ -93,7 +93,9 @@ _SIGS = {
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
     "spi_krige_tier": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_i64, c_ptr, c_ptr,
-                       c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr],
+                       c_ptr, c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr],
+    "spi_krige_var_df": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
+                         ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],
     "spi_krige_var_tc": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr, c_ptr],
     "spi_krige_loo": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),

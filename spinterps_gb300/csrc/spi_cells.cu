@@ -528,45 +528,55 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
                                               const double* __restrict__ e64,
                                               const double* __restrict__ e32,
                                               const double* __restrict__ v64,
-                                              const double* __restrict__ v32, double tol_e,
-                                              double tol_v, double cap, int32_t* tier,
-                                              double* disc) {
+                                              const double* __restrict__ v32,
+                                              const double* __restrict__ v32d, double tol_e,
+                                              double tol_v, double cap, double cap_d,
+                                              int32_t* tier, double* disc) {
   const int s = blockIdx.x;
-  __shared__ double red[2][256];
-  const bool cand = ws.route[s] == 0 && ws.cond[s] <= cap;
+  __shared__ double red[3][256];
+  const bool route0 = ws.route[s] == 0;
+  const bool cand = route0 && ws.cond[s] <= cap;
+  const bool cand_d = route0 && v32d != nullptr && ws.cond[s] <= cap_d;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
-  double de = 0.0, dv = 0.0;
-  if (cand) {
+  auto gap = [&](double a, double r) {
+    return isnan(a) != isnan(r) ? inf : (isnan(a) ? 0.0 : fabs(a - r));
+  };
+  double de = 0.0, dv = 0.0, dd = 0.0;
+  if (cand || cand_d) {
     for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1]; ++si) {
       const int64_t row = sys.out_row[sys.steps[si]];
       for (int64_t c = threadIdx.x; c < P; c += blockDim.x) {
-        const double a = e32[row * P + c], r = e64[row * P + c];
-        de = fmax(de, isnan(a) != isnan(r) ? inf : (isnan(a) ? 0.0 : fabs(a - r)));
-        if (v64 && v32) {
-          const double va = v32[row * P + c], vr = v64[row * P + c];
-          dv = fmax(dv, isnan(va) != isnan(vr) ? inf : (isnan(va) ? 0.0 : fabs(va - vr)));
-        }
+        const int64_t o = row * P + c;
+        de = fmax(de, gap(e32[o], e64[o]));
+        if (v64 && v32 && cand) dv = fmax(dv, gap(v32[o], v64[o]));
+        if (v64 && cand_d) dd = fmax(dd, gap(v32d[o], v64[o]));
       }
     }
   }
   red[0][threadIdx.x] = de;
   red[1][threadIdx.x] = dv;
+  red[2][threadIdx.x] = dd;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      red[0][threadIdx.x] = fmax(red[0][threadIdx.x], red[0][threadIdx.x + o]);
-      red[1][threadIdx.x] = fmax(red[1][threadIdx.x], red[1][threadIdx.x + o]);
-    }
+    if (threadIdx.x < o)
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] = fmax(red[q][threadIdx.x], red[q][threadIdx.x + o]);
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     de = red[0][0];
     dv = red[1][0];
-    tier[s] = (cand && de <= tol_e && dv <= tol_v) ? 1 : 0;
+    dd = red[2][0];
+    int t = 0;
+    if (cand && de <= tol_e && dv <= tol_v)
+      t = 1;
+    else if (cand_d && v64 && de <= tol_e && dd <= tol_v)
+      t = 2;
+    tier[s] = t;
     if (disc) {
       const double nan = __longlong_as_double(0x7ff8000000000000LL);
-      disc[2 * s] = cand ? de : nan;
-      disc[2 * s + 1] = cand ? dv : nan;
+      disc[3 * s] = (cand || cand_d) ? de : nan;
+      disc[3 * s + 1] = cand ? dv : nan;
+      disc[3 * s + 2] = cand_d ? dd : nan;
     }
   }
 }
@@ -574,9 +584,9 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
 
 extern "C" int spi_krige_tier(const spi_systems_t* sys, const spi_krige_ws_t* ws, int64_t n_probe,
                               const double* est64, const double* est32, const double* var64,
-                              const double* var32, double tol_est, double tol_var,
-                              double cond_cap, int32_t* tier, double* disc,
-                              spi_stream_t stream) {
+                              const double* var32, const double* var32_df, double tol_est,
+                              double tol_var, double cond_cap, double cond_cap_df,
+                              int32_t* tier, double* disc, spi_stream_t stream) {
   if (!sys || !ws || !tier || n_probe < 0) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (sys->n_sys == 0) return SPI_OK;
@@ -584,7 +594,8 @@ extern "C" int spi_krige_tier(const spi_systems_t* sys, const spi_krige_ws_t* ws
   if (!ws->route || !ws->cond || !sys->step_off || !sys->steps || !sys->out_row)
     return SPI_ERR_ARG;
   spi::k_tier<<<sys->n_sys, 256, 0, (cudaStream_t)stream>>>(
-      *sys, *ws, n_probe, est64, est32, var64, var32, tol_est, tol_var, cond_cap, tier, disc);
+      *sys, *ws, n_probe, est64, est32, var64, var32, var32_df, tol_est, tol_var, cond_cap,
+      cond_cap_df, tier, disc);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

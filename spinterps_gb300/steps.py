@@ -293,11 +293,11 @@ class _KrigeBatch:
             self.tc_err = torch.zeros(1, dtype=torch.int32, device=dev)
         # the probe (precision 1): both tiers on a few cells decide each
         # system's tier (spi_krige_tier)
-        self.tier = self.probe = None
+        self.tier = self.probe = self.probe_df = None
         if precision == 1 and n_probe > 0:
             n_sys = len(ch)
             self.tier = torch.zeros(n_sys, dtype=torch.int32, device=dev)
-            self.disc = torch.zeros((n_sys, 2), dtype=torch.float64, device=dev)
+            self.disc = torch.zeros((n_sys, 3), dtype=torch.float64, device=dev)
             f = lambda: torch.full((T, n_probe), float("nan"), dtype=torch.float64, device=dev)
             pe64, pe32 = f(), f()
             pv64, pv32 = (f(), f()) if want_var else (None, None)
@@ -305,12 +305,19 @@ class _KrigeBatch:
                    if self.yy is not None else None)
             self.probe = (pe64, pe32, pv64, pv32, pyy, _out_struct(pe64, pv64, None, None),
                           _out_struct(pe32, pv32, None, None))
+            if self.yy is not None:
+                # the double-float variance on the probe cells (tier 2)
+                pyy_d = torch.empty(n_sys * n_probe, dtype=torch.float64, device=dev)
+                pe32d, pv32d = f(), f()
+                self.probe_df = (pyy_d, pe32d, pv32d, _out_struct(pe32d, pv32d, None, None))
         ptrs = [_ptr(self.L), _ptr(self.X), _ptr(self.status), _ptr(self.route),
                 _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat), _ptr(self.beta),
                 _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum),
                 *[_ptr(t) for t in (self.split or [None] * 6)]]
         self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier))
         self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None)
+        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None)
+                            if self.probe_df else None)
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
         self.n = ns
@@ -333,10 +340,12 @@ class _KrigeBatch:
         rest = 2 * self.n * a + 2 * self.n * self.n_steps
         ok = route != 2
         if self.precision == 1:
-            fast = ((self.tier.cpu().numpy() != 0) if self.tier is not None
-                    else (route == 0) & (cond <= cond_split))
+            tr = (self.tier.cpu().numpy() if self.tier is not None
+                  else ((route == 0) & (cond <= cond_split)).astype(np.int32))
+            fast = tr != 0
             tc = self.yy is not None and want_var
-            return {"var_tc": float((var * fast).sum()) * C if tc else 0.0,
+            return {"var_tc": float((var * (tr == 1)).sum()) * C if tc else 0.0,
+                    "var_df": float((var * (tr == 2)).sum()) * C if tc else 0.0,
                     "cells_fp32": float(((rest + (0 if tc else var)) * fast).sum()) * C,
                     "cells_fp64": float(((rest + var) * (ok & ~fast)).sum()) * C}
         return {"cells_fp64": float(((rest + var) * ok).sum()) * C}
@@ -376,23 +385,43 @@ class _KrigeBatch:
             if pyy is not None and want_var:
                 nat.call("spi_krige_var_tc", ctypes.byref(pdom.st), ctypes.byref(self.sy), wp,
                          float(cond_split), _ptr(self.tc_err), s)
+            # the FP32-tier estimates of every double-float candidate (cond
+            # up to cond_df); the tensor-core variance only under cond_split
+            cap = max(float(cond_split), COND_DF) if self.probe_df else float(cond_split)
             for prec, filt, o in ((1, 1, o32), (0, 0, o64)):
                 nat.call("spi_krige_cells", ctypes.byref(pdom.st), ctypes.byref(self.sy),
                          _ptr(self.vals), wp, 1 if want_var else 0, prec, filt,
-                         float(cond_split), ctypes.byref(o), s)
+                         cap if prec == 1 else float(cond_split), ctypes.byref(o), s)
+            pv32d = None
+            if self.probe_df is not None and want_var:
+                pyy_d, _, pv32d, o32d = self.probe_df
+                wpd = ctypes.byref(self.ws_probe_df)
+                nat.call("spi_krige_var_df", ctypes.byref(pdom.st), ctypes.byref(self.sy), wpd,
+                         cap, s)
+                nat.call("spi_krige_cells", ctypes.byref(pdom.st), ctypes.byref(self.sy),
+                         _ptr(self.vals), wpd, 1, 1, 1, cap, ctypes.byref(o32d), s)
             nat.call("spi_krige_tier", ctypes.byref(self.sy), ws, pdom.C, _ptr(pe64), _ptr(pe32),
                      _ptr(pv64 if want_var else None), _ptr(pv32 if want_var else None),
-                     float(tol_e), float(tol_v), float(cond_split), _ptr(self.tier),
-                     _ptr(self.disc), s)
+                     _ptr(pv32d), float(tol_e), float(tol_v), float(cond_split), cap,
+                     _ptr(self.tier), _ptr(self.disc), s)
         if self.yy is not None and want_var:
             timed("var_tc", lambda: nat.call(
                 "spi_krige_var_tc", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
                 float(cond_split), _ptr(self.tc_err), s))
+            if self.tier is not None:
+                timed("var_df", lambda: nat.call(
+                    "spi_krige_var_df", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
+                    float(cond_split), s))
         passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
         for prec, filt in passes:
             timed("cells_fp32" if prec == 1 else "cells_fp64", lambda prec=prec, filt=filt: nat.call(
                 "spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
                 ws, 1 if want_var else 0, prec, filt, float(cond_split), ctypes.byref(out), s))
+
+
+# Condition cap of the double-float variance tier: its right-hand sides
+# carry ~1e-9 relative error, which the probe checks system by system.
+COND_DF = 1e11
 
 
 def _chunk_systems(systems, precision, arena_budget):
@@ -590,7 +619,7 @@ class InterpPlan:
                             failed.append(int(j))
                         elif rt[k] == 1:
                             routed.append(int(j))
-            fast, disc = [], []
+            fast, dfv, disc = [], [], []
             for b in batches:
                 if b.tier is not None:
                     disc.append(b.disc.cpu().numpy())
@@ -598,7 +627,10 @@ class InterpPlan:
                     for k, sl in enumerate(b.steps_l):
                         if tr[k]:
                             fast.extend(int(j) for j in sl)
+                        if tr[k] == 2:
+                            dfv.extend(int(j) for j in sl)
             self.info.setdefault("fp32_tier_steps", {})[kind] = sorted(fast)
+            self.info.setdefault("df_variance_steps", {})[kind] = sorted(dfv)
             if disc:
                 # per system: largest probe discrepancy of estimates, variances
                 self.info.setdefault("probe_disc", {})[kind] = np.concatenate(disc)
@@ -618,6 +650,7 @@ class InterpPlan:
             for b in batches:
                 n += 5 + (3 if b.split is not None else 0)
                 n += 1 if (b.yy is not None and want_var) else 0
+                n += 1 if (b.yy is not None and want_var and b.tier is not None) else 0
                 n += 2 if b.precision == 1 else 1
         for t, out, fill, p in self.idw:
             n += (fill is not None) + (len(self.multi) > 0) * (
