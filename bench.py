@@ -254,7 +254,7 @@ def run_ours(args):
         plans[i % n_sl].execute()
     torch.cuda.synchronize()
     failed = routed = 0
-    fp32_steps, df_steps, probe = {}, {}, {}
+    fp32_steps, df_steps, probe, fp64_why = {}, {}, {}, {}
     for p in plans:
         inf = p.collect_info()
         failed += len(inf["failed_steps"].get("OK", []))
@@ -263,6 +263,15 @@ def run_ours(args):
             fp32_steps[k] = fp32_steps.get(k, 0) + len(v)
         for k, v in inf.get("df_variance_steps", {}).items():
             df_steps[k] = df_steps.get(k, 0) + len(v)
+        # why the OK steps outside the FP32 tiers stay in FP64
+        fast_ok = set(inf.get("fp32_tier_steps", {}).get("OK", []))
+        rt1 = set(inf.get("exact_inverse_steps", {}).get("OK", []))
+        for j, c in inf.get("cond", {}).get("OK", {}).items():
+            if j in fast_ok:
+                continue
+            why = ("exact_inverse" if j in rt1 else
+                   "cond_above_cap" if c > p.cond_df else "probe")
+            fp64_why[why] = fp64_why.get(why, 0) + 1
         for k, d in inf.get("probe_disc", {}).items():
             probe.setdefault(k, []).append(d)
     stream = torch.cuda.current_stream()
@@ -361,6 +370,7 @@ def run_ours(args):
                        "singular_steps_nnb": failed, "exact_inverse_steps": routed,
                        "fp32_tier_steps": fp32_steps,
                        "df_variance_steps": df_steps,
+                       "ok_fp64_tier_reasons": fp64_why,
                        "probe_disc_quantiles": {
                            k: {lab: [float(q) for q in np.nanquantile(
                                np.concatenate(v)[:, c], [0.25, 0.5, 0.75, 0.9])]

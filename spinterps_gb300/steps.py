@@ -49,6 +49,12 @@ def _require_cuda(device):
     return dev
 
 
+# Default condition cap of the double-float variance tier: its right-hand
+# sides carry ~1e-9 relative error, which the probe checks system by
+# system.
+COND_DF = 1e13
+
+
 def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
 
@@ -350,7 +356,8 @@ class _KrigeBatch:
                     "cells_fp64": float(((rest + var) * (ok & ~fast)).sum()) * C}
         return {"cells_fp64": float(((rest + var) * ok).sum()) * C}
 
-    def run(self, dom, out, want_var, cond_max, cond_split, ev=None, probe=None):
+    def run(self, dom, out, want_var, cond_max, cond_split, ev=None, probe=None,
+            cond_df=COND_DF):
         """Factor, duals, splits, (mixed) the probe that picks each system's
         tier, cell kernels. ``ev``: a list that receives (kernel name, start
         event, end event) per cell-kernel call; ``probe``: (probe domain,
@@ -387,7 +394,7 @@ class _KrigeBatch:
                          float(cond_split), _ptr(self.tc_err), s)
             # the FP32-tier estimates of every double-float candidate (cond
             # up to cond_df); the tensor-core variance only under cond_split
-            cap = max(float(cond_split), COND_DF) if self.probe_df else float(cond_split)
+            cap = max(float(cond_split), cond_df) if self.probe_df else float(cond_split)
             for prec, filt, o in ((1, 1, o32), (0, 0, o64)):
                 nat.call("spi_krige_cells", ctypes.byref(pdom.st), ctypes.byref(self.sy),
                          _ptr(self.vals), wp, 1 if want_var else 0, prec, filt,
@@ -419,11 +426,6 @@ class _KrigeBatch:
                 ws, 1 if want_var else 0, prec, filt, float(cond_split), ctypes.byref(out), s))
 
 
-# Condition cap of the double-float variance tier: its right-hand sides
-# carry ~1e-9 relative error, which the probe checks system by system.
-COND_DF = 1e11
-
-
 def _chunk_systems(systems, precision, arena_budget):
     order = sorted(range(len(systems)), key=lambda i: -len(systems[i][0]))
     chunks, cur, cur_bytes = [], [], 0
@@ -452,12 +454,13 @@ class InterpPlan:
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
                  cond_max=1e13, cond_split=None, tensor_cores=True, probe_cells=1024,
-                 probe_tol=2e-6):
+                 probe_tol=2e-6, cond_df=COND_DF):
         dev = self.dev = _require_cuda(device)
         if cond_split is None:
             # a cap under the probe; without it, the a-priori split
             cond_split = 1e10 if probe_cells > 0 else 1e7
         self.cond_max, self.cond_split = cond_max, cond_split
+        self.cond_df = cond_df
         prec = self.prec = PRECISION[precision]
         data = np.ascontiguousarray(data, dtype=np.float64)
         T, N = data.shape
@@ -576,7 +579,7 @@ class InterpPlan:
             for b in batches:
                 ev = [] if timing else None
                 b.run(self.dom, out, want_var, self.cond_max, self.cond_split, ev,
-                      self.probe_args if self.pdom is not None else None)
+                      self.probe_args if self.pdom is not None else None, self.cond_df)
                 if timing:
                     evs["krige"].append((b, want_var, a, ev))
         for t, out, fill, p in self.idw:
