@@ -490,6 +490,25 @@ int spi_krige_ok_noalloc(const spi_domain_t *dom, const int32_t *stn_idx, int32_
                          const spi_vg_t *vg, const double *vals, int32_t n_steps,
                          int32_t want_var, const spi_out_t *out, spi_stream_t stream);
 
+/* Interpolation from each cell's own neighbours (the neighbour methods of
+ * interp/steps.py:584-606, 673-833): for every listed step q (data row
+ * steps[q], output row out_row[q]) and cell c, the reference's _get_interp
+ * (interp/steps.py:245-401) over the stations nebs[c * k .. c * k + k)
+ * (indices into dom's stations, -1 = empty slot, the valid ones first and
+ * all present at the step): the value of a single neighbour; NNB; IDW
+ * (idw_exp) over the neighbours; OK / SK / EDK (kind SPI_KIND_*, IDW = 3,
+ * NNB = 4) from the neighbours' saddle matrix solved by Gauss-Jordan, with
+ * the mean where no value reaches min_var_thr or nug[q] (nugget-only
+ * variogram vg[q]), the sum check's nearest-neighbour fallback, and
+ * prblm[q] = 1 where a system is exactly singular (nearest neighbour). The
+ * OK variance (want_var, out->var) is lambda'r + lambda_n. data [.., ld]:
+ * station values by row. FP64. k <= 64. Device arrays. */
+int spi_local_cells(const spi_domain_t *dom, int32_t kind, int32_t k, const int32_t *nebs,
+                    int32_t n_steps, const int32_t *steps, const int32_t *out_row,
+                    const double *data, int64_t ld, const spi_vg_t *vg, const int32_t *nug,
+                    double min_var_thr, double idw_exp, int32_t want_var,
+                    const spi_out_t *out, int32_t *prblm, spi_stream_t stream);
+
 /* ---- the driver flow around the step engine ------------------------------ */
 
 /* The polygon cell mask of SpInterpPrepare._select_nearby_cells

@@ -7,6 +7,8 @@ GPU (spi_neb_select, csrc/spi_nebs.cu); cells with identical neighbour lists
 form the groups the step engine solves together, in order of first
 occurrence as the reference's hash grouping (interp/grps.py:103-138).
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -68,16 +70,28 @@ class SpInterpNeighborGrouping:
         return idx, self.groups(idx)[1]
 
 
+LOCAL_KIND = {"OK": 0, "SK": 1, "EDK": 2, "IDW": 3, "NNB": 4}
+
+
 def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_sel_mthd,
                       n_nebs, n_pies, *, stn_drifts=None, cell_drifts=None,
-                      intrp_dtype=np.float32, time_steps=None, device="cuda", **kw):
+                      intrp_dtype=np.float32, time_steps=None, device="cuda", est_vars=False,
+                      min_var_thr=0.0, min_var_cut=None, max_var_cut=None, min_vg_val=0.0,
+                      **kw):
     """The step engine with 'nrst' / 'pie' neighbours (interp/steps.py:584-606,
-    673-833): stations that are nobody's neighbour with every station present
-    are dropped; then, per group of steps with the same stations, every group
-    of cells with the same neighbours is interpolated from those neighbours
-    alone (the batched plan of spinterps_gb300.steps on that cell subset).
-    Returns (fields, problem steps) like steps.interp_steps."""
-    from .steps import InterpPlan
+    673-833). Stations that are nobody's neighbour with every station
+    present are dropped. Then, per group of steps with the same stations,
+    every cell is interpolated from its own neighbours among them: the
+    reference's _get_interp per group of cells with identical neighbour
+    lists, done by spi_local_cells with one warp per (cell, step) and a
+    system of at most 64 + 8 rows (FP64 in either precision; the other
+    keywords of steps.interp_steps do not apply). Returns (fields, problem
+    steps) like steps.interp_steps."""
+    import torch
+    from . import _native as nat
+    from .steps import (_Domain, _out_struct, _ptr, _require_cuda, _stream, _vg_tensor,
+                        check_full_nuggetness, parse_vg)
+    dev = _require_cuda(device)
     stn_x = np.ascontiguousarray(stn_x, dtype=np.float64)
     stn_y = np.ascontiguousarray(stn_y, dtype=np.float64)
     cell_x = np.ascontiguousarray(cell_x, dtype=np.float64)
@@ -88,39 +102,56 @@ def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_
         time_steps = np.arange(T)
     g = SpInterpNeighborGrouping(neb_sel_mthd, n_nebs, n_pies, cell_x, cell_y, device=device)
     keep = np.unique(g.neb_idxs(stn_x, stn_y))
-    sx, sy, data = stn_x[keep], stn_y[keep], data[:, keep]
+    keep = keep[keep >= 0]
+    sx, sy, data = stn_x[keep], stn_y[keep], np.ascontiguousarray(data[:, keep])
     sd = None if stn_drifts is None else np.asarray(stn_drifts).reshape(stn_x.size, -1)[keep]
     cd = None if cell_drifts is None else np.asarray(cell_drifts).reshape(-1, C)
-    vgs = None if vgs is None else np.asarray(vgs, dtype=object)
+    dom = _Domain(dev, sx, sy, cell_x, cell_y, sd, cd, min_vg_val, 0)
+    tdt = torch.float64 if np.dtype(intrp_dtype) == np.float64 else torch.float32
     labels = [a[2] for a in interp_args]
-    flds = {lab: np.full((T, C), np.nan, dtype=intrp_dtype) for lab in labels}
+    flds = {lab: torch.full((T, C), float("nan"), dtype=tdt, device=dev) for lab in labels}
+    d_data = torch.as_tensor(data, device=dev)
+    krig = any(a[0] in ("OK", "SK", "EDK") for a in interp_args)
+    vgt = nug = None
+    if krig:
+        vgl = [str(v) for v in vgs]
+        vgt = _vg_tensor([parse_vg(v) for v in vgl], dev).view(T, -1)
+        nug = torch.as_tensor(np.array([check_full_nuggetness(v, min_vg_val) for v in vgl],
+                                       dtype=np.int32), device=dev)
     prblm = []
+    flags = torch.zeros(T, dtype=torch.int32, device=dev)
     avail = np.isfinite(data)
     _, first, inv = np.unique(np.packbits(avail, axis=1), axis=0, return_index=True,
                               return_inverse=True)
     inv = np.asarray(inv).ravel()
+    s = _stream()
+    held = []  # device arrays in use by queued launches
     for gi in np.argsort(first):
         rows = np.where(inv == gi)[0]
         stn_idxs = np.where(avail[rows[0]])[0]
         if not stn_idxs.size:
-            for t in time_steps[rows]:
-                if t not in prblm:
-                    prblm.append(t)
+            prblm.extend(t for t in time_steps[rows] if t not in prblm)
             continue
         nidx = g.neb_idxs(sx[stn_idxs], sy[stn_idxs])
-        for grp in g.groups(nidx)[1]:
-            sub = stn_idxs[nidx[grp[0]]]
-            plan = InterpPlan(sx[sub], sy[sub], data[rows][:, sub], cell_x[grp], cell_y[grp],
-                              None if vgs is None else vgs[rows], interp_args,
-                              stn_drifts=None if sd is None else sd[sub],
-                              cell_drifts=None if cd is None else cd[:, grp],
-                              intrp_dtype=intrp_dtype, time_steps=time_steps[rows],
-                              device=device, **kw)
-            plan.execute()
-            out = plan.fields()
-            for lab in labels:
-                flds[lab][np.ix_(rows, grp)] = out[lab]
-            for t in plan.problem_steps():
-                if t not in prblm:
-                    prblm.append(t)
-    return flds, prblm
+        k = nidx.shape[1]
+        nb = np.where(nidx >= 0, stn_idxs[np.maximum(nidx, 0)], -1).astype(np.int32)
+        d_nb = torch.as_tensor(np.ascontiguousarray(nb), device=dev)
+        d_rows = torch.as_tensor(rows.astype(np.int32), device=dev)
+        d_vg = vgt[d_rows.long()].contiguous() if krig else None
+        d_nug = nug[d_rows.long()].contiguous() if krig else None
+        d_pr = torch.zeros(rows.size, dtype=torch.int32, device=dev)
+        held.append((d_nb, d_rows, d_vg, d_nug, d_pr))
+        for a in interp_args:
+            kind = LOCAL_KIND[a[0]]
+            want_var = bool(est_vars and a[0] == "OK")
+            out = _out_struct(flds[a[2]], flds["EST_VARS_OK"] if want_var else None,
+                              min_var_cut, max_var_cut)
+            nat.call("spi_local_cells", ctypes.byref(dom.st), kind, k, _ptr(d_nb), rows.size,
+                     _ptr(d_rows), _ptr(d_rows), _ptr(d_data), data.shape[1],
+                     _ptr(d_vg), _ptr(d_nug), float(min_var_thr),
+                     float(a[3]) if a[0] == "IDW" else 0.0, int(want_var), ctypes.byref(out),
+                     _ptr(d_pr), s)
+        flags.index_add_(0, d_rows.long(), d_pr)
+    bad = np.where(flags.cpu().numpy() != 0)[0]
+    prblm.extend(t for t in time_steps[bad] if t not in prblm)
+    return {lab: v.cpu().numpy() for lab, v in flds.items()}, prblm
