@@ -253,6 +253,29 @@ def run_ours(args):
     for i in range(args.warmup):
         plans[i % n_sl].execute()
     torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kev = []
+    cell_steps = 0
+    with Clocks(local) as clk:
+        start.record(stream)
+        for i in range(args.steps):
+            p = plans[(args.warmup + i) % n_sl]
+            kev.append((p, p.execute(timing=True)))
+            cell_steps += p.T * C
+        end.record(stream)
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    # tier statistics of every slice (after the timed region: slices not yet
+    # run there run once more, untimed, so that their probes have decided)
+    ran = {i % n_sl for i in range(args.warmup + args.steps)}
+    for k in range(n_sl):
+        if k not in ran:
+            plans[k].execute()
+    torch.cuda.synchronize()
     failed = routed = 0
     fp32_steps, df_steps, probe, fp64_why = {}, {}, {}, {}
     for p in plans:
@@ -274,22 +297,6 @@ def run_ours(args):
             fp64_why[why] = fp64_why.get(why, 0) + 1
         for k, d in inf.get("probe_disc", {}).items():
             probe.setdefault(k, []).append(d)
-    stream = torch.cuda.current_stream()
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kev = []
-    cell_steps = 0
-    with Clocks(local) as clk:
-        start.record(stream)
-        for i in range(args.steps):
-            p = plans[(args.warmup + i) % n_sl]
-            kev.append((p, p.execute(timing=True)))
-            cell_steps += p.T * C
-        end.record(stream)
-        torch.cuda.synchronize()
-    ms = start.elapsed_time(end)
     t_max = torch.tensor([ms], device="cuda")
     if world > 1:
         dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
@@ -701,6 +708,59 @@ def run_legacy(args):
     print(json.dumps(line))
 
 
+def run_nebs(args):
+    """The neighbour methods (interp/steps.py:584-833): the batched
+    workload's stations and first steps, OK+var / IDW from each cell's 16
+    nearest present stations ('nrst') on a nebs_nx^2 grid. value: through
+    interp_steps (spi_neb_select + spi_local_cells, device time of the whole
+    call including its host work per step group); cpu_baseline: the
+    oracle's restatement (the reference's per-group loop) on a sample."""
+    import torch
+    import spinterps_gb300 as spi
+    from oracle import port
+    w = make_workload()
+    T, nx = args.nebs_steps, args.nebs_nx
+    box = 250e3
+    g = (np.arange(nx) + 0.5) * (box / nx)
+    cx, cy = np.meshgrid(g, g[::-1])
+    cx, cy = cx.ravel().copy(), cy.ravel().copy()
+    z, vgs = w["z"][:T], w["vgs"][:T]
+    iargs = port.interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
+    kw = dict(est_vars=True, min_vg_val=1e-4, intrp_dtype=np.float32, neb_sel_mthd="nrst",
+              n_nebs=16, n_pies=1)
+    spi.interp_steps(w["sx"], w["sy"], z[:2], cx[:1000], cy[:1000], vgs[:2], iargs, **kw)
+    torch.cuda.synchronize()
+    with Clocks() as clk:
+        t0 = time.perf_counter()
+        out, _ = spi.interp_steps(w["sx"], w["sy"], z, cx, cy, vgs, iargs, **kw)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    C = cx.size
+    # the oracle on a small block of cells and steps
+    rng = np.random.default_rng(5)
+    sel = rng.choice(C, args.nebs_cpu_cells, replace=False)
+    ts = 2
+    t0 = time.perf_counter()
+    ref, _ = port.interp_steps(w["sx"], w["sy"], z[:ts], cx[sel], cy[sel], vgs[:ts], iargs,
+                               **kw)
+    t_cpu = time.perf_counter() - t0
+    got, _ = spi.interp_steps(w["sx"], w["sy"], z[:ts], cx[sel], cy[sel], vgs[:ts], iargs, **kw)
+    err = {lab: float(np.nanmax(np.abs(got[lab] - ref[lab])) / np.nanmax(np.abs(ref[lab])))
+           for lab in ref}
+    line = {"metric": "cell-steps/s, neighbour method nrst (16), OK+var and IDW",
+            "value": T * C / dt, "unit": "cell-steps/s", "n_gpus": 1, "steps": 1,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"nebs_nrst16_1000stn_{T}steps_{nx}x{nx}", "stations": 1000,
+                       "steps": T, "cells": C, "methods": ["OK+var", "IDW p=2"]},
+            "seconds": dt,
+            "cpu_baseline": {"value": ts * sel.size / t_cpu, "unit": "cell-steps/s",
+                             "cores": 1, "kind": "port",
+                             "sample": f"{sel.size} random cells x {ts} steps, the oracle's "
+                                       "per-group loop"},
+            "err_vs_oracle_on_sample": err, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -752,8 +812,15 @@ def main():
                     help="the single-neighbourhood OrdinaryKriging class instead")
     ap.add_argument("--legacy-nx", type=int, default=500)
     ap.add_argument("--legacy-cpu-points", type=int, default=4000)
+    ap.add_argument("--nebs", action="store_true",
+                    help="the neighbour method 'nrst' (per-cell systems) instead")
+    ap.add_argument("--nebs-nx", type=int, default=500)
+    ap.add_argument("--nebs-steps", type=int, default=73)
+    ap.add_argument("--nebs-cpu-cells", type=int, default=2000)
     args = ap.parse_args()
-    if args.legacy:
+    if args.nebs:
+        run_nebs(args)
+    elif args.legacy:
         run_legacy(args)
     elif args.profile_case:
         run_profile_case(args)

@@ -142,8 +142,10 @@ def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_
         d_pr = torch.zeros(rows.size, dtype=torch.int32, device=dev)
         held.append((d_nb, d_rows, d_vg, d_nug, d_pr))
         for a in interp_args:
+            if a[0] == "EST_VARS_OK":  # written by the OK launch
+                continue
             kind = LOCAL_KIND[a[0]]
-            want_var = bool(est_vars and a[0] == "OK")
+            want_var = bool(est_vars and a[0] == "OK" and "EST_VARS_OK" in flds)
             out = _out_struct(flds[a[2]], flds["EST_VARS_OK"] if want_var else None,
                               min_var_cut, max_var_cut)
             nat.call("spi_local_cells", ctypes.byref(dom.st), kind, k, _ptr(d_nb), rows.size,
