@@ -190,11 +190,9 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------- GPU side
-# The cell kernels' ceilings. The measured peaks cover HBM and the bf16
-# tensor pipe; the CUDA-core pipes are nominal (152 SMs at 2.07 GHz: FP32 128
-# FMA/clk/SM, FP64 1/64 of that).
-FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
-FP64_NOMINAL_TFLOPS = FP32_NOMINAL_TFLOPS / 64
+# The cell kernels' ceilings: the measured peaks for HBM and the
+# bf16 tensor pipe; the CUDA-core FP32 / FP64 FMA rates measured here
+# (fma_peak_tflops).
 KERNEL_BOUND = {
     "var_tc": ("tensor", "spi::k_var_tc (tcgen05 3xTF32 OK-variance contraction)"),
     "var_df": ("fp32", "spi::k_var_df (double-float OK-variance contraction, FP32 pipe)"),
@@ -205,15 +203,47 @@ KERNEL_BOUND = {
 }
 
 
+_FMA_PEAKS = {}
+
+
+def fma_peak_tflops(f64):
+    """CUDA-core FMA throughput measured on this GPU (spi_peak_fma: 8
+    independent chains per thread, 16 CTAs of 256 threads per SM, timed
+    with CUDA events; best of 3 after a warm-up launch). MEASURED_PEAKS.json
+    covers HBM and the bf16 tensor pipe only."""
+    import ctypes
+    import torch
+    from spinterps_gb300 import _native as nat
+    if f64 in _FMA_PEAKS:
+        return _FMA_PEAKS[f64]
+    sink = torch.empty(152 * 16 * 256, dtype=torch.float64 if f64 else torch.float32,
+                       device="cuda")
+    thr = ctypes.c_int64(0)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    iters = 20000 if f64 else 200000
+    best = 0.0
+    for rep in range(4):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        nat.call("spi_peak_fma", 1 if f64 else 0, iters, ctypes.c_void_p(sink.data_ptr()),
+                 ctypes.byref(thr), st)
+        b.record()
+        torch.cuda.synchronize()
+        if rep:
+            best = max(best, 2 * 8 * iters * thr.value / (a.elapsed_time(b) / 1e3) / 1e12)
+    _FMA_PEAKS[f64] = best
+    return best
+
+
 def roofline_for(name, k):
     bf16, hbm, src = measured_peaks()
     bound, kernel = KERNEL_BOUND[name]
     if bound == "tensor":
         peak, psrc = bf16, src + " (bf16 dense; the kernel runs 3 TF32 MMAs per product)"
     elif bound == "fp64":
-        peak, psrc = FP64_NOMINAL_TFLOPS, "nominal FP64 pipe (not in MEASURED_PEAKS.json)"
+        peak, psrc = fma_peak_tflops(True), "measured FP64 FMA rate (spi_peak_fma, bench.py)"
     else:
-        peak, psrc = FP32_NOMINAL_TFLOPS, "nominal FP32 pipe (not in MEASURED_PEAKS.json)"
+        peak, psrc = fma_peak_tflops(False), "measured FP32 FMA rate (spi_peak_fma, bench.py)"
     a = k["achieved_tflops"]
     return {"bound": bound, "kernel": kernel, "achieved": a, "peak": peak, "unit": "TFLOP/s",
             "frac": a / peak, "traffic": None, "peak_source": psrc,
@@ -694,10 +724,11 @@ def run_legacy(args):
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 4 * args.steps,
             "roofline": {"bound": "fp64", "kernel": "spi::k_leg_lambda (lambda = P r, FP64)",
-                         "achieved": flop / (ms / 1e3) / 1e12, "peak": FP64_NOMINAL_TFLOPS,
-                         "unit": "TFLOP/s", "frac": flop / (ms / 1e3) / 1e12 / FP64_NOMINAL_TFLOPS,
+                         "achieved": flop / (ms / 1e3) / 1e12, "peak": fma_peak_tflops(True),
+                         "unit": "TFLOP/s",
+                         "frac": flop / (ms / 1e3) / 1e12 / fma_peak_tflops(True),
                          "traffic": None,
-                         "peak_source": "nominal FP64 pipe (not in MEASURED_PEAKS.json)",
+                         "peak_source": "measured FP64 FMA rate (spi_peak_fma, bench.py)",
                          "note": "2 m^2 FLOP per point over the whole step time (the "
                                  "factorisation, right-hand sides and epilogue count "
                                  "against it)"},

@@ -271,9 +271,10 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
  * (spi_krige_var_tc), var32_df (optional) with the double-float one
  * (spi_krige_var_df). tier[s] = 1 when the system is on the Cholesky path,
  * cond <= cond_cap, and over its steps and the probe cells |est32 - est64|
- * <= tol_est and |var32 - var64| <= tol_var; else 2 when cond <= cond_cap_df
- * and the estimates and |var32_df - var64| pass the same tolerances; else
- * 0 (var arrays may be NULL; a NaN in one field and not the other fails).
+ * <= tol_est and |var32 - var64| <= tol_var; else, up to cond <= cond_cap_df,
+ * 1 for estimates alone (var64 NULL) that pass, or 2 when the estimates and
+ * |var32_df - var64| pass the same tolerances; else 0 (var arrays may be
+ * NULL; a NaN in one field and not the other fails).
  * disc (optional, [n_sys, 3]): each system's largest estimate, tensor-core
  * variance and double-float variance discrepancy over the probe (NaN where
  * not a candidate, +inf for a NaN mismatch). The
@@ -584,6 +585,16 @@ int spi_legacy_points(int32_t kind, const double *xi, const double *yi, const do
                       const spi_vg_t *vg, const double *lhs_inv, double *rhss,
                       double *lambdas, double *mus, double *zk, double *est, double *ik,
                       spi_stream_t stream);
+
+/* ---- measurement ------------------------------------------------------ */
+
+/* No counterpart in the reference: a CUDA-core FMA throughput kernel (FP64
+ * when f64, else FP32) for the roofline of the FP64 / FP32 kernels: *threads
+ * threads each run 8 independent FMA chains for iters rounds (2 * 8 * iters
+ * * threads FLOP); the caller times the launch. sink: [*threads] elements of
+ * the type, device (152 * 16 * 256 of them). */
+int spi_peak_fma(int32_t f64, int64_t iters, void *sink, int64_t *threads,
+                 spi_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -124,6 +124,7 @@ _SIGS = {
     "spi_local_cells": [ctypes.POINTER(DomainT), c_i32, c_i32, c_ptr, c_i32, c_ptr, c_ptr, c_ptr,
                         c_i64, c_ptr, c_ptr, c_dbl, c_dbl, c_i32, ctypes.POINTER(OutT), c_ptr,
                         c_ptr],
+    "spi_peak_fma": [c_i32, c_i64, c_ptr, ctypes.POINTER(c_i64), c_ptr],
     "spi_legacy_system": [c_i32, c_ptr, c_ptr, c_i32, c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
                           c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
     "spi_legacy_points": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_i64,

@@ -392,9 +392,11 @@ class _KrigeBatch:
             if pyy is not None and want_var:
                 nat.call("spi_krige_var_tc", ctypes.byref(pdom.st), ctypes.byref(self.sy), wp,
                          float(cond_split), _ptr(self.tc_err), s)
-            # the FP32-tier estimates of every double-float candidate (cond
-            # up to cond_df); the tensor-core variance only under cond_split
-            cap = max(float(cond_split), cond_df) if self.probe_df else float(cond_split)
+            # the FP32-tier estimates of every candidate up to cond_df (the
+            # double-float variance, or no variance); the tensor-core
+            # variance only under cond_split
+            cap = (max(float(cond_split), cond_df) if (self.probe_df or not want_var)
+                   else float(cond_split))
             for prec, filt, o in ((1, 1, o32), (0, 0, o64)):
                 nat.call("spi_krige_cells", ctypes.byref(pdom.st), ctypes.byref(self.sy),
                          _ptr(self.vals), wp, 1 if want_var else 0, prec, filt,
