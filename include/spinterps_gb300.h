@@ -271,10 +271,9 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
  * (spi_krige_var_tc), var32_df (optional) with the double-float one
  * (spi_krige_var_df). tier[s] = 1 when the system is on the Cholesky path,
  * cond <= cond_cap, and over its steps and the probe cells |est32 - est64|
- * <= tol_est and |var32 - var64| <= tol_var; else, up to cond <= cond_cap_df,
- * 1 for estimates alone (var64 NULL) that pass, or 2 when the estimates and
- * |var32_df - var64| pass the same tolerances; else 0 (var arrays may be
- * NULL; a NaN in one field and not the other fails).
+ * <= tol_est and |var32 - var64| <= tol_var; else 2 when cond <= cond_cap_df
+ * and the estimates and |var32_df - var64| pass the same tolerances; else
+ * 0 (var arrays may be NULL; a NaN in one field and not the other fails).
  * disc (optional, [n_sys, 3]): each system's largest estimate, tensor-core
  * variance and double-float variance discrepancy over the probe (NaN where
  * not a candidate, +inf for a NaN mismatch). The

@@ -536,8 +536,7 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
   __shared__ double red[3][256];
   const bool route0 = ws.route[s] == 0;
   const bool cand = route0 && ws.cond[s] <= cap;
-  // up to cap_d: the double-float variance, or estimates alone (no variance)
-  const bool cand_d = route0 && (v32d != nullptr || v64 == nullptr) && ws.cond[s] <= cap_d;
+  const bool cand_d = route0 && v32d != nullptr && ws.cond[s] <= cap_d;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
   auto gap = [&](double a, double r) {
     return isnan(a) != isnan(r) ? inf : (isnan(a) ? 0.0 : fabs(a - r));
@@ -550,7 +549,7 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
         const int64_t o = row * P + c;
         de = fmax(de, gap(e32[o], e64[o]));
         if (v64 && v32 && cand) dv = fmax(dv, gap(v32[o], v64[o]));
-        if (v64 && v32d && cand_d) dd = fmax(dd, gap(v32d[o], v64[o]));
+        if (v64 && cand_d) dd = fmax(dd, gap(v32d[o], v64[o]));
       }
     }
   }
@@ -570,8 +569,6 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
     int t = 0;
     if (cand && de <= tol_e && dv <= tol_v)
       t = 1;
-    else if (cand_d && !v64 && de <= tol_e)
-      t = 1;  // estimates only: the FP32 tier needs no variance kernel
     else if (cand_d && v64 && de <= tol_e && dd <= tol_v)
       t = 2;
     tier[s] = t;

@@ -345,6 +345,9 @@ class _KrigeBatch:
         var = self.n * (self.n + 1) if want_var else np.zeros_like(self.n)
         rest = 2 * self.n * a + 2 * self.n * self.n_steps
         ok = route != 2
+        # the exact-inverse path's variance (P r per cell) runs only on tiles
+        # where a cell passes the sum check: not counted (a lower bound)
+        var = np.where(route == 1, 0, var)
         if self.precision == 1:
             tr = (self.tier.cpu().numpy() if self.tier is not None
                   else ((route == 0) & (cond <= cond_split)).astype(np.int32))
@@ -392,11 +395,12 @@ class _KrigeBatch:
             if pyy is not None and want_var:
                 nat.call("spi_krige_var_tc", ctypes.byref(pdom.st), ctypes.byref(self.sy), wp,
                          float(cond_split), _ptr(self.tc_err), s)
-            # the FP32-tier estimates of every candidate up to cond_df (the
-            # double-float variance, or no variance); the tensor-core
-            # variance only under cond_split
-            cap = (max(float(cond_split), cond_df) if (self.probe_df or not want_var)
-                   else float(cond_split))
+            # the FP32-tier estimates of every double-float candidate (cond
+            # up to cond_df); the tensor-core variance, and systems without
+            # a variance, only under cond_split (the streamed estimate kernel
+            # regenerates the right-hand sides for every four dual vectors:
+            # slower than FP64 on systems shared by hundreds of steps)
+            cap = max(float(cond_split), cond_df) if self.probe_df else float(cond_split)
             for prec, filt, o in ((1, 1, o32), (0, 0, o64)):
                 nat.call("spi_krige_cells", ctypes.byref(pdom.st), ctypes.byref(self.sy),
                          _ptr(self.vals), wp, 1 if want_var else 0, prec, filt,
