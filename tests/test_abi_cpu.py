@@ -43,6 +43,8 @@ def test_struct_layout_matches_header(tmp_path):
 int main(void) {
   printf("spi_vg_t %zu\nspi_domain_t %zu\nspi_systems_t %zu\nspi_out_t %zu\n",
          sizeof(spi_vg_t), sizeof(spi_domain_t), sizeof(spi_systems_t), sizeof(spi_out_t));
+  printf("spi_krige_ws_t %zu\n", sizeof(spi_krige_ws_t));
+  P(spi_krige_ws_t, cell_yy) P(spi_krige_ws_t, tier)
   P(spi_vg_t, sill) P(spi_vg_t, range) P(spi_domain_t, n_drift) P(spi_domain_t, min_vg_val)
   P(spi_domain_t, stn_split) P(spi_domain_t, cell_split) P(spi_systems_t, max_n)
   P(spi_systems_t, out_row) P(spi_out_t, clip_min) P(spi_out_t, clip_max)
@@ -56,6 +58,9 @@ int main(void) {
     assert int(got["spi_domain_t"]) == ctypes.sizeof(nat.DomainT)
     assert int(got["spi_systems_t"]) == ctypes.sizeof(nat.SystemsT)
     assert int(got["spi_out_t"]) == ctypes.sizeof(nat.OutT)
+    assert int(got["spi_krige_ws_t"]) == ctypes.sizeof(nat.KrigeWsT)
+    assert int(got["spi_krige_ws_t.cell_yy"]) == nat.KrigeWsT.cell_yy.offset
+    assert int(got["spi_krige_ws_t.tier"]) == nat.KrigeWsT.tier.offset
     assert int(got["spi_vg_t.sill"]) == nat.VgT.sill.offset
     assert int(got["spi_vg_t.range"]) == nat.VgT.range.offset
     assert int(got["spi_domain_t.n_drift"]) == nat.DomainT.n_drift.offset
@@ -145,3 +150,46 @@ def test_noalloc_limits_match_header():
     stns = int(re.search(r"#define SPI_NOALLOC_MAX_STNS (\d+)", txt).group(1))
     steps = int(re.search(r"#define SPI_NOALLOC_MAX_STEPS (\d+)", txt).group(1))
     assert (stns, steps) == (nat.SPI_NOALLOC_MAX_STNS, nat.SPI_NOALLOC_MAX_STEPS)
+
+
+def test_entry_points_check_arguments_before_any_gpu_work():
+    """Invalid arguments come back as status codes (no GPU is touched): the
+    per-cell neighbourhood kernel, the single-neighbourhood classes, the
+    driver-flow kernels, the double-float variance, the tier decision and
+    the FMA-rate kernel."""
+    lib = nat.load()
+    c_i64 = ctypes.c_int64
+    dom = nat.DomainT()
+    out = nat.OutT()
+    vg = nat.VgT()
+    vg.n_comp = 1
+    dummy = ctypes.c_void_p(8)  # never dereferenced on these paths
+    ARG, TOO_LARGE, VG = 1, 5, 2
+    assert lib.spi_local_cells(None, 0, 8, None, 1, None, None, None, 0, None, None, 0.0, 2.0,
+                               0, None, None, None) == ARG
+    assert lib.spi_local_cells(ctypes.byref(dom), 0, 65, dummy, 1, dummy, dummy, dummy, 1,
+                               dummy, dummy, 0.0, 2.0, 0, ctypes.byref(out), dummy,
+                               None) == TOO_LARGE
+    assert lib.spi_local_cells(ctypes.byref(dom), 7, 8, dummy, 1, dummy, dummy, dummy, 1, dummy,
+                               dummy, 0.0, 2.0, 0, ctypes.byref(out), dummy, None) == ARG
+    assert lib.spi_legacy_system(9, dummy, dummy, 5, None, 0, ctypes.byref(vg), dummy, dummy,
+                                 dummy, dummy, None, None) == ARG
+    vg0 = nat.VgT()
+    assert lib.spi_legacy_system(0, dummy, dummy, 5, None, 0, ctypes.byref(vg0), dummy, dummy,
+                                 dummy, dummy, None, None) == VG
+    assert lib.spi_legacy_points(0, dummy, dummy, dummy, None, 5, dummy, dummy, None, -1, 0,
+                                 ctypes.byref(vg), dummy, dummy, dummy, dummy, dummy, None,
+                                 None, None) == ARG
+    assert lib.spi_points_in_polygons(dummy, dummy, -1, 0, None, None, None, None, dummy,
+                                      None) == ARG
+    assert lib.spi_points_in_polygons(dummy, dummy, 0, 0, None, None, None, None, dummy,
+                                      None) == 0
+    assert lib.spi_field_stats(dummy, 0, -1, 10, 10, 0, dummy, 10, dummy, None) == ARG
+    assert lib.spi_field_stats(dummy, 0, 70000, 10, 10, 0, dummy, 10, dummy, None) == TOO_LARGE
+    assert lib.spi_round_fields(dummy, 0, -1, 3, None) == ARG
+    assert lib.spi_round_fields(dummy, 0, 10, 400, None) == ARG
+    assert lib.spi_round_fields(dummy, 0, 0, 3, None) == 0
+    assert lib.spi_krige_var_df(None, None, None, 1e10, None) == ARG
+    assert lib.spi_krige_tier(None, None, 0, None, None, None, None, None, 0.0, 0.0, 0.0, 0.0,
+                              None, None, None) == ARG
+    assert lib.spi_peak_fma(1, 0, dummy, ctypes.byref(c_i64()), None) == ARG
