@@ -252,6 +252,18 @@ def roofline_for(name, k):
                     "columns 2na, per cell-step 2n (right-hand-side generation not counted)"}
 
 
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time: every rank passes its own timed milliseconds
+    (replicas, one per GPU); the job's time is their maximum."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -327,10 +339,7 @@ def run_ours(args):
             fp64_why[why] = fp64_why.get(why, 0) + 1
         for k, d in inf.get("probe_disc", {}).items():
             probe.setdefault(k, []).append(d)
-    t_max = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    ms = float(t_max.item())
+    ms = max_over_ranks(ms, world, "cuda")
     value = world * cell_steps / (ms / 1e3)
     # per-kernel times (CUDA events on the launching stream) and algorithmic
     # FLOP; the roofline line describes the kernel that takes the most time
