@@ -200,6 +200,11 @@ typedef struct {
                             double-float variance, 0 = FP64
                             (spi_krige_tier); NULL: route 0 and
                             cond <= cond_split */
+    int32_t *var_cells;  /* optional [n_sys]: the FP64 cell kernel adds the
+                            cells of every tile whose exact-inverse
+                            variance pass (P r, 2 m^2 FLOP per cell) ran;
+                            it runs only where a cell of the tile passes
+                            the sum check (NULL: not counted) */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.

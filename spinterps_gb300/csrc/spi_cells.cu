@@ -254,6 +254,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     if constexpr (sizeof(T) == 8) {
       if (prim && A.want_var && !sk && any_ok) {
         const int m = n + a;
+        // cells whose tile ran this pass (the FLOP count of the roofline)
+        if (tid == 0 && A.ws.var_cells)
+          atomicAdd(A.ws.var_cells + s, (int)min((int64_t)TC, C - c0));
         double vpart[CPT];
 #pragma unroll
         for (int c = 0; c < CPT; ++c) vpart[c] = 0.0;

@@ -320,9 +320,12 @@ class _KrigeBatch:
                 _ptr(self.cond), _ptr(self.shift), _ptr(self.w_hat), _ptr(self.beta),
                 _ptr(self.g_cols), _ptr(self.s_inv), _ptr(self.g_colsum),
                 *[_ptr(t) for t in (self.split or [None] * 6)]]
-        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier))
-        self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None)
-        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None)
+        # cells of the exact-inverse variance passes that ran (main pass only)
+        self.var_cells = torch.zeros(len(ch), dtype=torch.int32, device=dev)
+        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells))
+        self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None,
+                                     None)
+        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None, None)
                             if self.probe_df else None)
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
@@ -345,8 +348,12 @@ class _KrigeBatch:
         var = self.n * (self.n + 1) if want_var else np.zeros_like(self.n)
         rest = 2 * self.n * a + 2 * self.n * self.n_steps
         ok = route != 2
-        # the exact-inverse path's variance (P r per cell) runs only on tiles
-        # where a cell passes the sum check: not counted (a lower bound)
+        # the exact-inverse path's variance (P r: 2 m^2 per cell) runs only
+        # on tiles where a cell passes the sum check: counted from the
+        # cells of the passes that ran (var_cells, last execution)
+        vc = self.var_cells.cpu().numpy().astype(np.float64)
+        m = self.n + (a if want_var else 0)
+        prim_var = np.where(route == 1, 2.0 * m * m * vc, 0.0) if want_var else 0.0 * vc
         var = np.where(route == 1, 0, var)
         if self.precision == 1:
             tr = (self.tier.cpu().numpy() if self.tier is not None
@@ -356,8 +363,9 @@ class _KrigeBatch:
             return {"var_tc": float((var * (tr == 1)).sum()) * C if tc else 0.0,
                     "var_df": float((var * (tr == 2)).sum()) * C if tc else 0.0,
                     "cells_fp32": float(((rest + (0 if tc else var)) * fast).sum()) * C,
-                    "cells_fp64": float(((rest + var) * (ok & ~fast)).sum()) * C}
-        return {"cells_fp64": float(((rest + var) * ok).sum()) * C}
+                    "cells_fp64": float(((rest + var) * (ok & ~fast)).sum()) * C
+                    + float((prim_var * (ok & ~fast)).sum())}
+        return {"cells_fp64": float(((rest + var) * ok).sum()) * C + float((prim_var * ok).sum())}
 
     def run(self, dom, out, want_var, cond_max, cond_split, ev=None, probe=None,
             cond_df=COND_DF):
@@ -425,6 +433,7 @@ class _KrigeBatch:
                 timed("var_df", lambda: nat.call(
                     "spi_krige_var_df", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
                     float(cond_split), s))
+        self.var_cells.zero_()
         passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
         for prec, filt in passes:
             timed("cells_fp32" if prec == 1 else "cells_fp64", lambda prec=prec, filt=filt: nat.call(
