@@ -594,7 +594,8 @@ int spi_legacy_points(int32_t kind, const double *xi, const double *yi, const do
 
 /* No counterpart in the reference: a CUDA-core FMA throughput kernel (FP64
  * when f64, else FP32) for the roofline of the FP64 / FP32 kernels: *threads
- * threads each run 8 independent FMA chains for iters rounds (2 * 8 * iters
+ * threads each run 8 independent FMA chains for iters rounds (iters a
+ * multiple of 8; 2 * 8 * iters
  * * threads FLOP); the caller times the launch. sink: [*threads] elements of
  * the type, device (152 * 16 * 256 of them). */
 int spi_peak_fma(int32_t f64, int64_t iters, void *sink, int64_t *threads,
