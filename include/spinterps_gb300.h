@@ -247,11 +247,14 @@ typedef struct {
 } spi_out_t;
 
 /* Kriging estimates (and OK variances when want_var) for every cell of
- * every step of a system batch. precision 0: FP64 throughout; 1: FP32
- * right-hand sides, split-FP32 contractions against the FP32 (hi, lo)
- * pairs of the FP64 factor and duals in ws (FP64 accumulation every 64
- * terms). route_filter: 0 all systems;
- * 1 only route-0 systems with cond <= cond_split; 2 every other system. A
+ * every step of a system batch. precision 0: FP64 throughout; 1: the FP32
+ * tier, double-float right-hand sides against the FP32 (hi, lo) pairs of
+ * the FP64 duals in ws, accumulated as double-floats (the streamed kernel;
+ * the OK variance from ws->cell_yy, or, without it, a split-FP32 pass over
+ * Linv's pair). ws->linv_arena (and its pair) is needed only with
+ * want_var. route_filter: 0 all systems; 1 the FP32-tier systems
+ * (ws->tier != 0, or without ws->tier route 0 with cond <= cond_split);
+ * 2 every other system. A
  * mixed-precision job runs precision 1 with filter 1, then precision 0 with
  * filter 2: ill-conditioned and routed systems are always computed in FP64
  * (precision 1 accepts only filter 1).
