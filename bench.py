@@ -66,7 +66,7 @@ def make_workload(seed=SEED, n_stns=1000, n_steps=365, nx=1000, ny=1000, cell=25
 
 
 def interp_args():
-    from oracle.port import interp_args_for  # the (type, dir, label[, exp]) list only
+    from spinterps_gb300.steps import interp_args_for
     return interp_args_for(["OK", "SK", ("IDW", 2.0)], est_vars=True)
 
 
@@ -538,7 +538,7 @@ def run_large(args):
     import torch
     from spinterps_gb300 import fitvgs, synth, warmstart
     from spinterps_gb300.steps import InterpPlan
-    from oracle.port import interp_args_for  # the (type, dir, label) list only
+    from spinterps_gb300.steps import interp_args_for
     T = args.large_steps
     t0 = time.perf_counter()
     w = synth.large_edk(n_steps=T, nx=args.large_nx, ny=args.large_nx,
@@ -625,7 +625,7 @@ def run_stress(args):
     import torch
     from spinterps_gb300 import synth
     from spinterps_gb300.steps import InterpPlan
-    from oracle.port import interp_args_for  # the (type, dir, label) list only
+    from spinterps_gb300.steps import interp_args_for
     w = synth.stress_edk()
     iargs = interp_args_for(["EDK"], est_vars=False)
     C, T = w["cx"].size, w["z"].shape[0]
@@ -765,7 +765,8 @@ def run_nebs(args):
     cx, cy = np.meshgrid(g, g[::-1])
     cx, cy = cx.ravel().copy(), cy.ravel().copy()
     z, vgs = w["z"][:T], w["vgs"][:T]
-    iargs = port.interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
+    from spinterps_gb300.steps import interp_args_for
+    iargs = interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
     kw = dict(est_vars=True, min_vg_val=1e-4, intrp_dtype=np.float32, neb_sel_mthd="nrst",
               n_nebs=16, n_pies=1)
     spi.interp_steps(w["sx"], w["sy"], z[:2], cx[:1000], cy[:1000], vgs[:2], iargs, **kw)

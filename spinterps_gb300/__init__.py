@@ -7,11 +7,13 @@ variogram strings, per-method estimate and variance fields).
 The compute path is CUDA only (``csrc/``, built by ``build.py`` into
 ``_lib/``), reached through the C ABI of ``include/spinterps_gb300.h``.
 """
-from .steps import SpInterpSteps, interp_steps, parse_vg, check_full_nuggetness  # noqa: F401
+from .steps import (  # noqa: F401
+    SpInterpSteps, interp_steps, interp_args_for, parse_vg, check_full_nuggetness)
 from .legacy import (  # noqa: F401
     OrdinaryKriging, SimpleKriging, ExternalDriftKriging, ExternalDriftKriging_MD,
     OrdinaryIndicatorKriging, SimpleIndicatorKriging)
 
-__all__ = ["SpInterpSteps", "interp_steps", "parse_vg", "check_full_nuggetness",
+__all__ = ["SpInterpSteps", "interp_steps", "interp_args_for", "parse_vg",
+           "check_full_nuggetness",
            "OrdinaryKriging", "SimpleKriging", "ExternalDriftKriging",
            "ExternalDriftKriging_MD", "OrdinaryIndicatorKriging", "SimpleIndicatorKriging"]

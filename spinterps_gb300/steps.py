@@ -730,6 +730,26 @@ def _fill_run(f, C, out, s):
     nat.call("spi_fill_rows", n, _ptr(r), _ptr(v), _ptr(vv), C, ctypes.byref(out), s)
 
 
+def interp_args_for(methods, est_vars=False, fig_dir=None):
+    """The reference's interpolation tuples (interp/prepare.py:638-695) for
+    a list of methods like ['OK', 'SK', 'EDK', ('IDW', 2.0), 'NNB']:
+    (type, figure directory, label[, idw_exp]) in the reference's order,
+    IDW labels 'IDW_000', 'IDW_001', ... in the order of their exponents,
+    and ('EST_VARS_OK', ...) last when est_vars."""
+    args = []
+    for t in ("OK", "SK", "EDK"):
+        if t in methods:
+            args.append((t, fig_dir, t))
+    idw = [m[1] for m in methods if isinstance(m, tuple) and m[0] == "IDW"]
+    for i, e in enumerate(idw):
+        args.append(("IDW", fig_dir, f"IDW_{i:03d}", float(e)))
+    if "NNB" in methods:
+        args.append(("NNB", fig_dir, "NNB"))
+    if est_vars:
+        args.append(("EST_VARS_OK", fig_dir, "EST_VARS_OK"))
+    return args
+
+
 def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_vars=False,
                  stn_drifts=None, cell_drifts=None, min_var_thr=0.0, min_var_cut=None,
                  max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32, time_steps=None,

@@ -193,3 +193,12 @@ def test_entry_points_check_arguments_before_any_gpu_work():
     assert lib.spi_krige_tier(None, None, 0, None, None, None, None, None, 0.0, 0.0, 0.0, 0.0,
                               None, None, None) == ARG
     assert lib.spi_peak_fma(1, 0, dummy, ctypes.byref(c_i64()), None) == ARG
+
+
+def test_interp_args_match_the_oracle():
+    """The product's interpolation tuples (interp/prepare.py:638-695) equal
+    the oracle's for every method mix."""
+    from spinterps_gb300.steps import interp_args_for
+    for methods in (["OK"], ["OK", "SK", ("IDW", 2.0), ("IDW", 1.0), "NNB"], ["EDK"]):
+        for ev in (False, True):
+            assert interp_args_for(methods, est_vars=ev) == port.interp_args_for(methods, ev)
