@@ -658,15 +658,25 @@ class InterpPlan:
         return self.info
 
     def launches_per_execute(self):
-        """Kernels of this library that one execute() launches: row fills;
-        per batch build + Cholesky + inverse + Gauss-Jordan, duals, the FP32
-        splits and the tensor-core variance (mixed), one cell kernel per
-        tier; per IDW / NNB field its fill, split (mixed IDW) and kernel."""
+        """Kernels of this library that one execute() launches, call by call
+        as _KrigeBatch.run makes them: row fills; per batch the build,
+        Cholesky, inverse (or condition estimate) and Gauss-Jordan, the duals
+        (plus two triangular-solve kernels without the inverse), the FP32
+        splits, the probe (tensor-core and double-float variances, both
+        tiers' cell kernels, the tier pick), the main variance kernels and
+        one cell kernel per tier; per IDW / NNB field its fill, split (mixed
+        IDW) and kernel."""
         n = 0
         for kind, out, want_var, batches, fills, a in self.krig:
             n += sum(f is not None for f in fills)
             for b in batches:
-                n += 5 + (3 if b.split is not None else 0)
+                n += 4
+                n += 1 if b.X is not None else 3
+                if b.split is not None:
+                    n += 2 + (b.X is not None)
+                if b.probe is not None and self.pdom is not None:
+                    n += (b.probe[4] is not None and want_var) + 2 + 1
+                    n += 2 if (b.probe_df is not None and want_var) else 0
                 n += 1 if (b.yy is not None and want_var) else 0
                 n += 1 if (b.yy is not None and want_var and b.tier is not None) else 0
                 n += 2 if b.precision == 1 else 1
