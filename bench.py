@@ -817,7 +817,9 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "methods": ["OK+var", "SK", "IDW p=2"]},
+            "config": {"workload": WORKLOAD, "stations": int(w["sx"].size),
+                       "steps": int(w["z"].shape[0]), "cells": int(w["cx"].size),
+                       "methods": ["OK+var", "SK", "IDW p=2"]},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
