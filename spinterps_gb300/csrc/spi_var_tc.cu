@@ -20,7 +20,8 @@
 // K-steps x 5 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 + a1 b1, FP32
 // accumulation in TMEM) and commits them to an mbarrier that every thread
 // waits on (with an iteration limit: on expiry the kernel raises err_flag,
-// frees its TMEM and returns). Squares are summed in double-float (FP32 pairs: the FP64
+// waits once more, with the same limit, for the MMAs in flight, frees its
+// TMEM and returns). Squares are summed in double-float (FP32 pairs: the FP64
 // pipe is 1/64 of FP32 on GB300); the mixed path's probe checks every
 // system's variance against the FP64 kernel.
 #include "spi_cells.cuh"
@@ -85,6 +86,19 @@ __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uin
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// polls the mbarrier until the phase of the given parity has completed, at
+// most VT_SPIN times; false if it never did
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+  uint32_t done = 0;
+  for (long it = 0; it < VT_SPIN && !done; ++it)
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity));
+  return done != 0;
 }
 
 __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
@@ -209,14 +223,7 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 smem_u32(&mbar)));
       }
-      uint32_t done = 0;
-      for (long it = 0; it < VT_SPIN && !done; ++it)
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            "selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(&mbar)), "r"(phase));
-      if (!done) atomicExch(&fail, 1);
+      if (!mbar_wait_bounded(smem_u32(&mbar), phase)) atomicExch(&fail, 1);
       phase ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;");
       __syncthreads();
@@ -251,6 +258,12 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+  }
+  if (fail) {
+    // the timed-out MMAs may still be writing tensor memory: wait for their
+    // commit once more, with the same limit, before the columns are freed
+    mbar_wait_bounded(smem_u32(&mbar), phase ^ 1u);
+    asm volatile("tcgen05.fence::after_thread_sync;");
   }
   const double yy64 = (double)yy.h + (double)yy.l;
   if (e_half == 1) half_yy[e_cell] = yy64;
