@@ -28,7 +28,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .steps import InterpPlan
+from .steps import InterpPlan, _require_cuda
 
 
 def _ptr(t):
@@ -140,6 +140,7 @@ def cells_in_polygons(cell_x, cell_y, polygons, device="cuda"):
     its last vertex to its first. Each polygon needs at least 3 vertices
     and a nonzero area, as the reference asserts. Raises AssertionError
     when no cell is selected, as the reference does."""
+    device = _require_cuda(device)
     vx, vy, off, bbox = [], [], [0], []
     for xs, ys in polygons:
         xs, ys = np.asarray(xs, float).ravel(), np.asarray(ys, float).ravel()
@@ -205,6 +206,7 @@ def stats_table(data, flds, interp_args, device="cuda"):
     station values (ddof 1). {label}_* are numpy's nan-statistics of every
     field except EST_VARS_OK (ddof 0). flds: label -> CUDA [T, C] tensor of
     the selected cells, already rounded as written."""
+    device = _require_cuda(device)
     cols = {}
     dt = torch.as_tensor(np.ascontiguousarray(data, dtype=np.float64), device=device)
     st = field_stats(dt, ddof=1)

@@ -44,6 +44,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from .steps import _require_cuda
 
 _CODES = {b"Rng": 0, b"Nug": 1, b"Sph": 2, b"Exp": 3, b"Lin": 4, b"Gau": 5, b"Pow": 6,
           b"Hol": 7}
@@ -100,7 +101,7 @@ def krige_points(kind, xi, yi, zi, xk, yk, model, si=None, sk=None, ixi=None, wa
     comps = parse_model(model) if not isinstance(model, list) else model
     vg = _vg_struct(comps)
     code = nat.KIND[kind]
-    dev = xi.device
+    dev = _require_cuda(xi.device)
     n, n_out = int(xi.shape[0]), int(xk.shape[0])
     n_drift = int(si.shape[0]) if kind == "EDK" else 0
     a = 0 if kind == "SK" else 1 + n_drift
@@ -164,6 +165,7 @@ class _LegacyKriging:
             raise RuntimeError(
                 "krige() runs once per object (a second call on the reference's class "
                 "kriges a different system); make a new object")
+        _require_cuda("cuda")
         comps = parse_model(self.model)
         for name, sill, rng in comps:
             self.vgs.append(name)

@@ -140,9 +140,25 @@ def test_host_mirror_has_no_cpu_fallback():
     import spinterps_gb300 as spi
     if torch.cuda.is_available():
         pytest.skip("GPU present")
-    with pytest.raises(RuntimeError, match="no CPU fallback"):
-        spi.interp_steps(np.zeros(3), np.zeros(3), np.zeros((1, 3)), np.zeros(2), np.zeros(2),
-                         ["1.0 Exp(10)"], [("OK", None, "OK")])
+    from spinterps_gb300 import driver, fitvgs, steps, warmstart
+    x, y, z = np.array([0.0, 1e3, 2e3]), np.array([0.0, 5e2, 2e3]), np.array([[1.0, 2.0, 3.0]])
+    calls = {
+        "interp_steps": lambda: spi.interp_steps(x, y, z, x[:2], y[:2], ["1.0 Exp(10)"],
+                                                 [("OK", None, "OK")]),
+        "SpInterpSteps": lambda: spi.SpInterpSteps(),
+        "OrdinaryKriging": lambda: spi.OrdinaryKriging(x, y, z[0], x, y,
+                                                       model="1.0 Exp(1000)").krige(),
+        "cells_in_polygons": lambda: driver.cells_in_polygons(x, y, [(x, y)]),
+        "stats_table": lambda: driver.stats_table(z, {}, []),
+        "interpolate_grid": lambda: driver.interpolate_grid(
+            x, y, z, ["1.0 Exp(1000)"], [("OK", None, "OK")], cell_size=250.0),
+        "fit_steps": lambda: fitvgs.fit_steps(x, y, z),
+        "krige_loo": lambda: steps.krige_loo(x, y, z, ["1.0 Exp(1000)"]),
+        "warm_fit_steps": lambda: warmstart.warm_fit_steps(x, y, z, None),
+    }
+    for name, fn in calls.items():
+        with pytest.raises(RuntimeError, match="no CPU fallback"):
+            fn()
 
 
 def test_noalloc_limits_match_header():
