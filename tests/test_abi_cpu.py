@@ -140,12 +140,16 @@ def test_host_mirror_has_no_cpu_fallback():
     import spinterps_gb300 as spi
     if torch.cuda.is_available():
         pytest.skip("GPU present")
-    from spinterps_gb300 import driver, fitvgs, steps, warmstart
+    from spinterps_gb300 import driver, fitvgs, nebs, steps, warmstart
     x, y, z = np.array([0.0, 1e3, 2e3]), np.array([0.0, 5e2, 2e3]), np.array([[1.0, 2.0, 3.0]])
     calls = {
         "interp_steps": lambda: spi.interp_steps(x, y, z, x[:2], y[:2], ["1.0 Exp(10)"],
                                                  [("OK", None, "OK")]),
         "SpInterpSteps": lambda: spi.SpInterpSteps(),
+        "interp_steps nrst": lambda: spi.interp_steps(
+            x, y, z, x[:2], y[:2], ["1.0 Exp(10)"], [("OK", None, "OK")], neb_sel_mthd="nrst",
+            n_nebs=2),
+        "SpInterpNeighborGrouping": lambda: nebs.SpInterpNeighborGrouping("nrst", 2, None, x, y),
         "OrdinaryKriging": lambda: spi.OrdinaryKriging(x, y, z[0], x, y,
                                                        model="1.0 Exp(1000)").krige(),
         "cells_in_polygons": lambda: driver.cells_in_polygons(x, y, [(x, y)]),
