@@ -350,7 +350,9 @@ def run_ours(args):
             t[0] += t_ms
             t[1] += n_l
             t[2] += fl
-    launches_per_exec = plans[0].launches_per_execute()
+    # this library's kernels in the timed region: each timed execution's own count
+    launches = sum(plans[(args.warmup + i) % n_sl].launches_per_execute()
+                   for i in range(args.steps))
     kernels = {k: {"ms": v[0], "launches": v[1], "achieved_tflops": v[2] / (v[0] / 1e3) / 1e12}
                for k, v in times.items() if v[0] > 0}
     dom_k = max(kernels, key=lambda k: kernels[k]["ms"])
@@ -425,7 +427,7 @@ def run_ours(args):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "ms": float(np.median(e2e_ms)) if e2e_ms else None},
-            "gpu_launches": launches_per_exec * args.steps,
+            "gpu_launches": launches,
             "roofline": roofline,
             "roofline_tensor_kernel": roofline_tc,
             "kernels": kernels,
