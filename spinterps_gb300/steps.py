@@ -577,7 +577,10 @@ class InterpPlan:
                 fill = _fill_args(dev, self.single, self.single_val, None)
                 p = float(interp_args[i][3]) if t == "IDW" else 0.0
                 self.idw.append((t, out, fill, p))
-            self.idw_flops = 4.0 * N * len(multi) * C
+            # algorithmic work: 4 FLOP per present station and cell-step
+            # (weighted values and weight sums); masked-out stations are not
+            # counted
+            self.idw_flops = 4.0 * float(n_present.sum()) * C
         self.info = {"failed_steps": {}, "cond": {}}
 
     def execute(self, timing=False):
@@ -619,7 +622,7 @@ class InterpPlan:
                          ctypes.byref(out), s)
             if timing:
                 ev[1].record()
-                evs["idw"].append((ev, self.idw_flops))
+                evs["idw"].append(("idw", ev, self.idw_flops) if t == "IDW" else ("nnb", ev, 0.0))
         return evs
 
     def collect_info(self):
@@ -695,8 +698,8 @@ class InterpPlan:
                 t[0] += e0.elapsed_time(e1)
                 t[1] += 1
                 t[2] += fl.get(name, 0.0)
-        for (e0, e1), fl in evs["idw"]:
-            t = out.setdefault("idw", [0.0, 0, 0.0])
+        for name, (e0, e1), fl in evs["idw"]:
+            t = out.setdefault(name, [0.0, 0, 0.0])
             t[0] += e0.elapsed_time(e1)
             t[1] += 1
             t[2] += fl
