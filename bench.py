@@ -581,7 +581,9 @@ def run_large(args):
     info = pm.collect_info()
     cond = np.array(list(info["cond"]["EDK"].values()))
     fm = pm.flds["EDK"]
-    n_fast = int(np.sum(cond <= pm.cond_split))
+    # the tier each step ran in, as the probe decided it
+    n_fast = len(info.get("fp32_tier_steps", {}).get("EDK", []))
+    n_cap = int(np.sum(cond <= pm.cond_split))
     del pm
     torch.cuda.empty_cache()
     if args.skip_fp64:
@@ -611,6 +613,7 @@ def run_large(args):
                           "cells_kernel_ms": cells_64},
             "mixed_over_fp64": ms_64 / ms_m, "mixed_err_vs_fp64": err,
             "tiers": {"fp32": n_fast, "fp64": int(cond.size - n_fast),
+                      "cond_under_cap": n_cap,
                       "cond_median": float(np.median(cond)), "cond_max": float(cond.max())},
             "fit": {"seconds": t_fit, "fallback_steps": len(det["_fallback_steps"]),
                     "de_ms": det["_de_ms"], "ms": det["_ms"]},
