@@ -757,8 +757,9 @@ def run_nebs(args):
     """The neighbour methods (interp/steps.py:584-833): the batched
     workload's stations and first steps, OK+var / IDW from each cell's 16
     nearest present stations ('nrst') on a nebs_nx^2 grid. value: through
-    interp_steps (spi_neb_select + spi_local_cells, device time of the whole
-    call including its host work per step group); cpu_baseline: the
+    interp_steps (spi_neb_select + spi_local_cells): wall time of the whole
+    call, numpy in and out, its host work per step group included;
+    cpu_baseline: the
     oracle's restatement (the reference's per-group loop) on a sample."""
     import torch
     import spinterps_gb300 as spi
