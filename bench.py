@@ -759,8 +759,8 @@ def run_nebs(args):
     nearest present stations ('nrst') on a nebs_nx^2 grid. value: through
     interp_steps (spi_neb_select + spi_local_cells): wall time of the whole
     call, numpy in and out, its host work per step group included;
-    cpu_baseline: the
-    oracle's restatement (the reference's per-group loop) on a sample."""
+    cpu_baseline: the oracle's restatement (the reference's per-group loop)
+    on a sample."""
     import torch
     import spinterps_gb300 as spi
     from oracle import port
