@@ -61,3 +61,22 @@ def test_launch_count_follows_run(monkeypatch, kind, prec, want_var, n_probe, tc
     plan = types.SimpleNamespace(krig=[(kind, out, want_var, [b], [None], 1)], idw=[],
                                  multi=[], pdom=pdom, data_hi=None)
     assert steps.InterpPlan.launches_per_execute(plan) == launched, calls
+
+
+class _Ev:
+    def __init__(self, t):
+        self.t = t
+
+    def elapsed_time(self, other):
+        return other.t - self.t
+
+
+def test_kernel_times_keeps_nnb_apart_from_idw():
+    """IDW carries its algorithmic FLOP (present stations only); NNB has its
+    own entry and no FLOP."""
+    evs = {"krige": [], "idw": [("idw", (_Ev(0.0), _Ev(2.0)), 40.0),
+                                ("nnb", (_Ev(2.0), _Ev(3.0)), 0.0),
+                                ("idw", (_Ev(3.0), _Ev(4.0)), 40.0)]}
+    plan = types.SimpleNamespace(C=10, cond_split=1e10)
+    out = steps.InterpPlan.kernel_times(plan, evs)
+    assert out == {"idw": [3.0, 2, 80.0], "nnb": [1.0, 1, 0.0]}
