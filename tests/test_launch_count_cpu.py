@@ -1,8 +1,11 @@
-"""The bench's kernel-launch claim: InterpPlan.launches_per_execute must
-equal the kernels that _KrigeBatch.run actually launches. The batches are
-built on the CPU and run with the entry points recorded instead of called;
-each recorded entry point is then counted by the kernels its C source
-launches."""
+"""The bench's kernel accounting, on the CPU.
+
+- InterpPlan.launches_per_execute must equal the kernels that
+  _KrigeBatch.run actually launches. The batches are built on the CPU and
+  run with the entry points recorded instead of called; each recorded entry
+  point is then counted by the kernels its C source launches.
+- InterpPlan.kernel_times files IDW and NNB under their own names, with
+  IDW's algorithmic FLOP only."""
 import types
 
 import numpy as np
