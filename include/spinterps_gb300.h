@@ -55,7 +55,9 @@ enum { SPI_KIND_OK = 0, SPI_KIND_SK = 1, SPI_KIND_EDK = 2 };
 /* ---- host helpers ------------------------------------------------------ */
 
 /* Parse 's1 M1(r1) + s2 M2(r2)' with the split rules of fill_vg_var_arr
- * (replaces the parse in cyth/interpmthds.pyx:174-184). */
+ * (replaces the parse in cyth/interpmthds.pyx:174-184): Python bytes.split
+ * semantics, numbers in Python float()'s grammar, at most SPI_MAX_VG_COMP
+ * components (SPI_ERR_TOO_LARGE otherwise, before any other check). */
 int spi_parse_vg(const char *vg_str, spi_vg_t *out);
 
 /* misc.py:1074-1105 check_full_nuggetness: *out = 1 when the total sill or

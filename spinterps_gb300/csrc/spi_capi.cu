@@ -1,5 +1,6 @@
 // Host-side entry points of the C ABI: variogram string parsing and the
 // nugget-only check. Pure C++ (no device code); errors are status codes.
+#include <cctype>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -34,14 +35,63 @@ std::vector<std::string> split(const std::string& s, char sep) {
   return out;
 }
 
-// Python float(): surrounding whitespace allowed, the rest must parse whole.
+bool is_digit(char c) { return c >= '0' && c <= '9'; }
+
+// Python float() of a bytes token. ASCII whitespace may surround it; the
+// rest must be, in full, [sign] followed by
+//   digitpart ["." [digitpart]] | "." digitpart, then [("e"|"E") [sign] digitpart],
+// with digitpart = digit (["_"] digit)*, or by "inf", "infinity" or "nan" in
+// any case. No hexadecimal, no "nan(...)". The token without its
+// underscores then goes to strtod, which rounds correctly as Python does.
 bool py_float(const std::string& tok, double* out) {
-  std::string t = strip(tok);
-  if (t.empty()) return false;
-  char* end = nullptr;
-  double v = std::strtod(t.c_str(), &end);
-  if (end != t.c_str() + t.size()) return false;
-  *out = v;
+  const std::string t = strip(tok);
+  const size_t n = t.size();
+  size_t i = 0;
+  std::string clean;
+  bool neg = false;
+  if (i < n && (t[i] == '+' || t[i] == '-')) {
+    neg = t[i] == '-';
+    clean += t[i++];
+  }
+  std::string word;
+  for (size_t j = i; j < n; ++j) word += (char)std::tolower((unsigned char)t[j]);
+  if (word == "inf" || word == "infinity") {
+    *out = neg ? -HUGE_VAL : HUGE_VAL;
+    return true;
+  }
+  if (word == "nan") {
+    *out = std::copysign(std::nan(""), neg ? -1.0 : 1.0);
+    return true;
+  }
+  auto digitpart = [&]() {
+    if (i >= n || !is_digit(t[i])) return false;
+    clean += t[i++];
+    while (i < n) {
+      if (is_digit(t[i])) {
+        clean += t[i++];
+      } else if (t[i] == '_' && i + 1 < n && is_digit(t[i + 1])) {
+        ++i;
+      } else {
+        break;
+      }
+    }
+    return true;
+  };
+  const bool whole = digitpart();
+  if (i < n && t[i] == '.') {
+    clean += t[i++];
+    const bool frac = digitpart();
+    if (!whole && !frac) return false;
+  } else if (!whole) {
+    return false;
+  }
+  if (i < n && (t[i] == 'e' || t[i] == 'E')) {
+    clean += t[i++];
+    if (i < n && (t[i] == '+' || t[i] == '-')) clean += t[i++];
+    if (!digitpart()) return false;
+  }
+  if (i != n) return false;
+  *out = std::strtod(clean.c_str(), nullptr);
   return true;
 }
 

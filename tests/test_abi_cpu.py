@@ -222,3 +222,70 @@ def test_interp_args_match_the_oracle():
     for methods in (["OK"], ["OK", "SK", ("IDW", 2.0), ("IDW", 1.0), "NNB"], ["EDK"]):
         for ev in (False, True):
             assert interp_args_for(methods, est_vars=ev) == port.interp_args_for(methods, ev)
+
+
+# Tokens the reference's string rules meet in float(): Python accepts
+# surrounding whitespace, digit-group underscores, inf / infinity / nan in
+# any case; it rejects hexadecimal, 'nan(...)', a lone '.', empty tokens.
+_SILLS = ["1", "0.5", ".5", "5.", "1e3", "1E-3", "-0.2", "+0.2", "inf", "-inf", "nan", "NaN",
+          "Infinity", "1_0", "1__0", "_1", "1_", "0x10", "1.5e", "", "1.0\t", "\t1.0", "1d3",
+          "1e400", "1e-400", "1.0.0", "1.5_0", "1e1_0"]
+_NAMES = ["Nug", "Sph", "Exp", "Lin", "Gau", "Pow", "Hol", "Rng", "Foo", "exp", ""]
+_RANGES = ["0", "10", "1e5", "-5", "1e-9", " 5", "\t5", "5\t", "1_000", "inf", "nan", "",
+           "1e+5", "3)x", "3))", "(3", "0x1p3", "nan(1)"]
+
+
+def _fuzz_strings(n, seed):
+    import random
+    rng = random.Random(seed)
+    for _ in range(n):
+        comps = []
+        for _ in range(rng.choice([1, 1, 2, 2, 3, 4, 5])):
+            comps.append(rng.choice(["", " ", "\t"]) + rng.choice(_SILLS) +
+                         rng.choice([" ", "  ", "\t", ""]) + rng.choice(_NAMES) + "(" +
+                         rng.choice(_RANGES) + rng.choice([")", ")", ")x", ""]))
+        s = comps[0]
+        for c in comps[1:]:
+            s += rng.choice(["+", " + ", "+ ", " +", "++"]) + c
+        yield s
+
+
+def _same(a, b):
+    return a == b or (np.isnan(a) and np.isnan(b))
+
+
+def test_parse_vg_fuzz_matches_reference_rules():
+    """spi_parse_vg against the oracle's restatement of
+    cyth/interpmthds.pyx:174-184 on seeded random strings: the same
+    components, or an error where the reference raises."""
+    for s in _fuzz_strings(6000, 7):
+        try:
+            ref = port.parse_vg_str(s)
+        except (ValueError, KeyError):
+            ref = None
+        rc, v = _parse(s)
+        if len(s.encode().split(b"+")) > 4:
+            assert rc == 5, s  # at most 4 components, checked before the parse
+        elif ref is None:
+            assert rc == 2, s
+        else:
+            assert rc == 0 and v.n_comp == len(ref), s
+            for k, (code, sill, rng) in enumerate(ref):
+                assert v.code[k] == code and _same(v.sill[k], sill) and v.range[k] == rng, s
+
+
+def test_nuggetness_fuzz_matches_reference_rules():
+    """spi_check_full_nuggetness against the oracle's restatement of
+    misc.py:1074-1105 on the same kind of strings."""
+    for s in _fuzz_strings(3000, 11):
+        for mvv in (0.0, 1e-4):
+            try:
+                ref = port.check_full_nuggetness(s, mvv)
+            except (ValueError, IndexError):
+                ref = None
+            out = nat.c_i32(-1)
+            rc = nat.lib().spi_check_full_nuggetness(s.encode(), mvv, ctypes.byref(out))
+            if ref is None:
+                assert rc == 2, s
+            else:
+                assert rc == 0 and bool(out.value) == bool(ref), (s, mvv)
