@@ -25,7 +25,9 @@ and writes small seeded cases to tests/golden/*.npz:
                 and whole fits with numpy's global RNG seeded
 - driver.npz    the driver flow's grid (SpInterpPrepare._prepare_crds,
                 interp/prepare.py:148-241) and drift sampling
-                (KrigingDrift._prepare_stns_drift, interp/drift.py:165-227)
+                (KrigingDrift._prepare_stns_drift, interp/drift.py:165-227),
+                plus a sweep of 400 seeded grids (ranges, shapes, digests of
+                the coordinate vectors, and where the reference asserts)
 - legacy.npz    the single-neighbourhood classes of cyth/interpmthds.pyx:
                 OrdinaryKriging, SimpleKriging, ExternalDriftKriging(_MD),
                 OrdinaryIndicatorKriging, SimpleIndicatorKriging
@@ -506,6 +508,63 @@ def driver_case(ref, out):
             if masked:
                 out[p + "mask"] = mask
     out["d_cases"] = np.arange(len(DRIVER_CASES))
+    driver_sweep(prep, out)
+
+
+def driver_sweep(prep, out, n_cases=400, seed=404):
+    """SpInterpPrepare._prepare_crds over seeded random extents and cell
+    sizes, half of them inside drift rasters (EDK), some with the grid
+    reaching outside the rasters (the reference asserts). Stored compactly:
+    the inputs, whether the reference raised, the row / column range, the
+    shape and SHA-256 digests of the x and y coordinate vectors."""
+    import hashlib
+    rng = np.random.default_rng(seed)
+    sizes = [0.5, 1.0, 25.0, 100.0, 250.0, 333.3, 500.0, 1000.0, 1234.567]
+    params = np.zeros((n_cases, 10))
+    raised = np.zeros(n_cases, dtype=bool)
+    rcs = np.full((n_cases, 4), -1, dtype=np.int64)
+    shapes = np.zeros((n_cases, 2), dtype=np.int64)
+    digests = np.zeros((n_cases, 2, 32), dtype=np.uint8)
+    for i in range(n_cases):
+        cs = float(sizes[rng.integers(len(sizes))])
+        x0 = round(float(rng.uniform(-2e5, 2e5)), int(rng.integers(0, 4)))
+        y0 = round(float(rng.uniform(-2e5, 2e5)), int(rng.integers(0, 4)))
+        if rng.uniform() < 0.3:  # extents on the cell lattice: ceil at its edge
+            w, h = cs * int(rng.integers(1, 150)), cs * int(rng.integers(1, 150))
+        else:
+            w, h = cs * float(rng.uniform(0.3, 150)), cs * float(rng.uniform(0.3, 150))
+        x1, y1 = x0 + w, y0 + h
+        edk = bool(rng.uniform() < 0.5)
+        db = (np.nan,) * 4
+        obj = prep.SpInterpPrepare.__new__(prep.SpInterpPrepare)
+        obj._edk_flag = edk
+        obj._x_min, obj._x_max, obj._y_min, obj._y_max = x0, x1, y0, y1
+        obj._cell_size = cs
+        obj._plot_figs_flag = False
+        if edk:
+            off = lambda: cs * int(rng.integers(0, 4)) + (  # noqa: E731
+                float(rng.uniform(0, cs)) if rng.uniform() < 0.5 else 0.0)
+            dx0, dy1 = x0 - off(), y1 + off()
+            nc = int(np.ceil((x1 - dx0) / cs)) + int(rng.integers(0, 4))
+            nr = int(np.ceil((dy1 - y0) / cs)) + int(rng.integers(0, 4))
+            if rng.uniform() < 0.1:  # the grid reaches outside the rasters
+                nc = max(1, nc - int(rng.integers(2, 6)))
+            db = (dx0, dx0 + nc * cs, dy1 - nr * cs, dy1)
+            obj._drft_x_min, obj._drft_x_max, obj._drft_y_min, obj._drft_y_max = db
+        params[i] = [x0, x1, y0, y1, cs, float(edk), *db]
+        try:
+            obj._prepare_crds()
+        except AssertionError:
+            raised[i] = True
+            continue
+        rcs[i] = [obj._min_col, obj._max_col, obj._min_row, obj._max_row]
+        shapes[i] = obj._interp_crds_orig_shape
+        for k, v in enumerate((obj._nc_x_crds, obj._nc_y_crds)):
+            digests[i, k] = np.frombuffer(
+                hashlib.sha256(np.ascontiguousarray(v, dtype="<f8").tobytes()).digest(),
+                dtype=np.uint8)
+    out.update(sw_params=params, sw_raised=raised, sw_rc=rcs, sw_shape=shapes,
+               sw_digest=digests)
 
 
 def main(ref_root="/root/reference", only=None):

@@ -42,3 +42,27 @@ def test_corner_coordinates_and_stats_csv(tmp_path):
     driver.write_stats_csv(f, ["t0", "t1"], cols)
     assert f.read_text().splitlines() == [";data_min;OK_mean", "t0;1.000000;2.500000",
                                           "t1;;3.250000"]
+
+
+def test_grid_sweep_matches_reference(golden):
+    """400 seeded extents and cell sizes, half inside drift rasters: the
+    same row / column range, shape and coordinate vectors (by SHA-256 of
+    their bytes) as the reference's _prepare_crds, and an AssertionError
+    wherever the reference asserted (a grid outside its rasters)."""
+    import hashlib
+
+    import pytest
+    g = golden
+    for i, p in enumerate(g["sw_params"]):
+        x0, x1, y0, y1, cs, edk = (float(v) for v in p[:6])
+        db = tuple(float(v) for v in p[6:]) if edk else None
+        if g["sw_raised"][i]:
+            with pytest.raises(AssertionError):
+                driver.prepare_crds(x0, x1, y0, y1, cs, drift_bounds=db)
+            continue
+        r = driver.prepare_crds(x0, x1, y0, y1, cs, drift_bounds=db)
+        assert tuple(r["rc"]) == tuple(g["sw_rc"][i]), i
+        assert tuple(r["shape"]) == tuple(g["sw_shape"][i]), i
+        for k, key in enumerate(("x_crds", "y_crds")):
+            d = hashlib.sha256(np.ascontiguousarray(r[key], dtype="<f8").tobytes()).digest()
+            assert d == bytes(g["sw_digest"][i, k]), (i, key)
