@@ -26,8 +26,10 @@ and writes small seeded cases to tests/golden/*.npz:
 - driver.npz    the driver flow's grid (SpInterpPrepare._prepare_crds,
                 interp/prepare.py:148-241) and drift sampling
                 (KrigingDrift._prepare_stns_drift, interp/drift.py:165-227),
-                plus a sweep of 400 seeded grids (ranges, shapes, digests of
-                the coordinate vectors, and where the reference asserts)
+                plus sweeps of 400 seeded grids (ranges, shapes, digests of
+                the coordinate vectors, and where the reference asserts) and
+                of 150 drift windows (inputs from sweeps.py, digests of the
+                cell and station drifts, the reference's exceptions)
 - legacy.npz    the single-neighbourhood classes of cyth/interpmthds.pyx:
                 OrdinaryKriging, SimpleKriging, ExternalDriftKriging(_MD),
                 OrdinaryIndicatorKriging, SimpleIndicatorKriging
@@ -565,6 +567,82 @@ def driver_sweep(prep, out, n_cases=400, seed=404):
                 dtype=np.uint8)
     out.update(sw_params=params, sw_raised=raised, sw_rc=rcs, sw_shape=shapes,
                sw_digest=digests)
+    drift_sweep(prep, out)
+
+
+def drift_sweep(prep, out, n_cases=150, n_stn=15, seed=505):
+    """KrigingDrift._prepare_stns_drift over seeded grids inside drift
+    rasters made by sweeps.drift_rasters (no-data cells, values at the edge
+    of np.isclose's reach), stations on cell edges and inside cells, with
+    and without the cell mask of sweeps.cell_mask. Stored: the inputs but
+    the rasters, whether the reference raised (AssertionError: a station on
+    no-data; IndexError: rounding put the window's last column or row past
+    the rasters), and digests of the cell and station drift arrays."""
+    from sweeps import NDV, cell_mask, digest, drift_rasters
+    rng = np.random.default_rng(seed)
+    sizes = [1.0, 25.0, 100.0, 250.0, 333.3, 1000.0]
+    params = np.zeros((n_cases, 12))  # cs, dx0, dy1, nr, nc, k, phase, x0, x1, y0, y1, masked
+    stn = np.zeros((n_cases, 2, n_stn))
+    raised = np.zeros(n_cases, dtype=np.int8)  # 1 AssertionError, 2 IndexError
+    digests = np.zeros((n_cases, 2, 32), dtype=np.uint8)
+    for i in range(n_cases):
+        cs = float(sizes[rng.integers(len(sizes))])
+        dx0 = round(float(rng.uniform(-1e5, 1e5)), int(rng.integers(0, 3)))
+        dy1 = round(float(rng.uniform(-1e5, 1e5)), int(rng.integers(0, 3)))
+        nr, nc = int(rng.integers(6, 40)), int(rng.integers(6, 40))
+        k = int(rng.integers(1, 3))
+        phase = float(rng.uniform(0, 6))
+        # the grid: a window of the rasters, its edges on or off the lattice
+        c0, r0 = int(rng.integers(0, 3)), int(rng.integers(0, 3))
+        fx = float(rng.uniform(0, 0.9)) if rng.uniform() < 0.5 else 0.0
+        fy = float(rng.uniform(0, 0.9)) if rng.uniform() < 0.5 else 0.0
+        x0 = dx0 + (c0 + fx) * cs
+        y1 = dy1 - (r0 + fy) * cs
+        x1 = dx0 + (nc - int(rng.integers(0, 3))) * cs
+        y0 = dy1 - (nr - int(rng.integers(0, 3))) * cs
+        masked = bool(rng.uniform() < 0.3)
+        params[i] = [cs, dx0, dy1, nr, nc, k, phase, x0, x1, y0, y1, float(masked)]
+        # stations: in cells that hold a value in every raster (a station on
+        # an edge may still read its neighbour, as the reference's int()
+        # rounds), half on cell edges (exact lattice points), half inside
+        rasters = drift_rasters(nr, nc, k, phase)
+        ok = np.all([~np.isclose(NDV, r) for r in rasters], axis=0)
+        ok[:r0 + 1, :] = False
+        ok[:, :c0 + 1] = False
+        ok[nr - 2:, :] = False
+        ok[:, nc - 2:] = False
+        cand = np.argwhere(ok)
+        pick = cand[rng.integers(len(cand), size=n_stn)]
+        rows, cols = pick[:, 0], pick[:, 1]
+        on_edge = rng.uniform(size=n_stn) < 0.5
+        sx = dx0 + (cols + np.where(on_edge, 0.0, rng.uniform(0.05, 0.95, n_stn))) * cs
+        sy = dy1 - (rows + np.where(on_edge, 0.0, rng.uniform(0.05, 0.95, n_stn))) * cs
+        stn[i] = [sx, sy]
+        obj = prep.SpInterpPrepare.__new__(prep.SpInterpPrepare)
+        obj._edk_flag = True
+        obj._x_min, obj._x_max, obj._y_min, obj._y_max = x0, x1, y0, y1
+        obj._cell_size = cs
+        obj._plot_figs_flag = False
+        obj._drft_x_min, obj._drft_y_max = dx0, dy1
+        obj._drft_x_max, obj._drft_y_min = dx0 + nc * cs, dy1 - nr * cs
+        obj._drft_oarrs = rasters
+        obj._drft_ndv = NDV
+        obj._prepare_crds()
+        obj._crds_df = LocFrame({"X": sx, "Y": sy},
+                                index=np.array([f"s{j}" for j in range(n_stn)]))
+        obj._cell_sel_prms_set = masked
+        obj._cntn_idxs = cell_mask(obj._interp_x_crds_msh.size) if masked else None
+        try:
+            obj._prepare_stns_drift()
+        except AssertionError:
+            raised[i] = 1
+            continue
+        except IndexError:  # the window's last column or row past the rasters
+            raised[i] = 2
+            continue
+        digests[i, 0] = np.frombuffer(digest(obj._drft_arrs), dtype=np.uint8)
+        digests[i, 1] = np.frombuffer(digest(obj._stns_drft_df.values), dtype=np.uint8)
+    out.update(dw_params=params, dw_stn=stn, dw_raised=raised, dw_digest=digests)
 
 
 def main(ref_root="/root/reference", only=None):

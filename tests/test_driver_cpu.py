@@ -66,3 +66,36 @@ def test_grid_sweep_matches_reference(golden):
         for k, key in enumerate(("x_crds", "y_crds")):
             d = hashlib.sha256(np.ascontiguousarray(r[key], dtype="<f8").tobytes()).digest()
             assert d == bytes(g["sw_digest"][i, k]), (i, key)
+
+
+def test_drift_sweep_matches_reference(golden):
+    """150 seeded drift windows (rasters from tests/golden/sweeps.py with
+    no-data cells and values at the edge of np.isclose's reach; stations on
+    cell edges and inside cells; with and without a cell mask): the same
+    cell and station drifts as the reference's _prepare_stns_drift (by
+    SHA-256), and the same exception where it raised."""
+    import sys
+    from pathlib import Path
+
+    import pytest
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from sweeps import NDV, cell_mask, digest, drift_rasters
+    g = golden
+    for i, p in enumerate(g["dw_params"]):
+        cs, dx0, dy1, nr, nc, k, phase, x0, x1, y0, y1, masked = (float(v) for v in p)
+        nr, nc, k = int(nr), int(nc), int(k)
+        r = driver.prepare_crds(x0, x1, y0, y1, cs,
+                                drift_bounds=(dx0, dx0 + nc * cs, dy1 - nr * cs, dy1))
+        mask = cell_mask(r["cell_x"].size) if masked else None
+        sx, sy = g["dw_stn"][i]
+        run = lambda: driver.sample_drifts(  # noqa: E731
+            drift_rasters(nr, nc, k, phase), dx0, dy1, cs, NDV, r["rc"], sx, sy,
+            cntn_idxs=mask)
+        if g["dw_raised"][i]:
+            exc = AssertionError if g["dw_raised"][i] == 1 else IndexError
+            with pytest.raises(exc):
+                run()
+            continue
+        cell, stn = run()
+        assert digest(cell) == bytes(g["dw_digest"][i, 0]), i
+        assert digest(stn) == bytes(g["dw_digest"][i, 1]), i
