@@ -33,9 +33,12 @@ and writes small seeded cases to tests/golden/*.npz:
 - legacy.npz    the single-neighbourhood classes of cyth/interpmthds.pyx:
                 OrdinaryKriging, SimpleKriging, ExternalDriftKriging(_MD),
                 OrdinaryIndicatorKriging, SimpleIndicatorKriging
+- interp_sweep.npz  SpInterpSteps._get_interp on 80 seeded random one-group
+                cases (every model, nests of up to three, all five methods)
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
-legacy.npz (``driver``: only driver.npz).
+legacy.npz (``driver``: only driver.npz; ``interp_sweep``: only
+interp_sweep.npz).
 """
 import sys
 from pathlib import Path
@@ -645,6 +648,63 @@ def drift_sweep(prep, out, n_cases=150, n_stn=15, seed=505):
     out.update(dw_params=params, dw_stn=stn, dw_raised=raised, dw_digest=digests)
 
 
+SWEEP_MODELS = ["Nug", "Sph", "Exp", "Lin", "Gau", "Pow", "Hol", "Rng"]
+SWEEP_TYPES = ["OK", "SK", "EDK", "IDW", "NNB"]
+
+
+def interp_sweep(ref, out, n_cases=80, seed=606):
+    """SpInterpSteps._get_interp on one group over seeded random cases: 2 to
+    35 stations, 5 to 40 cells (some on stations), 1 to 4 steps, each step
+    a random nest of 1 to 3 of the eight models, flags off on some steps
+    (nugget-only steps follow from the strings), OK / SK / EDK (1 to 3
+    drifts) / IDW (exponents 0.5 to 3.7) / NNB in turn. Stored: the inputs,
+    the estimates, the OK variances and the problem steps."""
+    rng = np.random.default_rng(seed)
+    st = make_steps(ref, min_vg_val=1e-4, est_vars=True)
+    for i in range(n_cases):
+        itype = SWEEP_TYPES[i % len(SWEEP_TYPES)]
+        n, c, t = int(rng.integers(2, 36)), int(rng.integers(5, 41)), int(rng.integers(1, 5))
+        box = float(rng.uniform(1e3, 2e5))
+        sx, sy = rng.uniform(0, box, n), rng.uniform(0, box, n)
+        cx, cy = rng.uniform(0, box, c), rng.uniform(0, box, c)
+        on = int(rng.integers(0, 3))
+        cx[:on], cy[:on] = sx[:on], sy[:on]
+        z = rng.normal(3.0, 2.0, (t, n))
+        vgs = []
+        for _ in range(t):
+            comps = []
+            for _ in range(int(rng.integers(1, 4))):
+                nm = SWEEP_MODELS[rng.integers(len(SWEEP_MODELS))]
+                sill = round(float(rng.uniform(0.01, 2.0)), 4)
+                if nm == "Nug":
+                    r = 0.0
+                elif nm == "Pow":
+                    r = round(float(rng.uniform(0.1, 1.9)), 3)
+                else:
+                    r = round(float(rng.uniform(0.02, 1.0)) * box, 1)
+                comps.append(f"{sill} {nm}({r})")
+            vgs.append(" + ".join(comps))
+        flags = rng.uniform(size=t) < 0.85
+        sd = cd = None
+        if itype == "EDK":
+            kd = int(rng.integers(1, 4))
+            sd = rng.uniform(0, 1000, (n, kd))
+            cd = rng.uniform(0, 1000, (kd, c))
+        idw_exp = float(rng.choice([0.5, 1.0, 2.0, 3.7]))
+        est, var, prblm = interp_one(ref, st, sx, sy, cx, cy, z, itype, vgs, idw_exp=idw_exp,
+                                     flags=flags, drifts=sd, cell_drifts=cd)
+        p = f"w{i}_"
+        out.update({p + "sx": sx, p + "sy": sy, p + "cx": cx, p + "cy": cy, p + "z": z,
+                    p + "vgs": np.array(vgs), p + "flags": flags,
+                    p + "type": np.array(itype), p + "idw_exp": np.array(idw_exp),
+                    p + "est": est, p + "prblm": np.array(sorted(prblm), dtype=np.int64)})
+        if var is not None:
+            out[p + "var"] = var
+        if sd is not None:
+            out.update({p + "sd": sd, p + "cd": cd})
+    out["w_cases"] = np.arange(n_cases)
+
+
 def main(ref_root="/root/reference", only=None):
     ref = load_reference(ref_root)
     if only == "driver":
@@ -656,6 +716,11 @@ def main(ref_root="/root/reference", only=None):
         out = {}
         legacy_case(ref, out)
         np.savez_compressed(HERE / "legacy.npz", **out)
+        return
+    if only == "interp_sweep":
+        out = {}
+        interp_sweep(ref, out)
+        np.savez_compressed(HERE / "interp_sweep.npz", **out)
         return
     out = {}
     kernels_case(ref, out)
@@ -703,6 +768,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     driver_case(ref, out)
     np.savez_compressed(HERE / "driver.npz", **out)
+    out = {}
+    interp_sweep(ref, out)
+    np.savez_compressed(HERE / "interp_sweep.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

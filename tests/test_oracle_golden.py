@@ -239,3 +239,36 @@ def test_oracle_polygon_mask_known_answers():
     want = np.array([1, 0, 0, 0, 0, 0, 1, 0, 1, 1, 0], dtype=bool)
     got = port.points_in_polygons(px, py, [sq, notch])
     assert np.array_equal(got, want), got
+
+
+def test_get_interp_sweep(golden):
+    """The oracle's get_interp against the reference's _get_interp on 80
+    seeded random one-group cases (tests/golden/interp_sweep.npz): every
+    variogram model in nests of up to three, flags off and nugget-only
+    steps, OK / SK / EDK with 1 to 3 drifts / IDW / NNB."""
+    g = golden
+    for i in g["w_cases"]:
+        p = f"w{i}_"
+        itype = str(g[p + "type"])
+        sx, sy, cx, cy, z = (g[p + k] for k in ("sx", "sy", "cx", "cy", "z"))
+        vgs = [str(v) for v in g[p + "vgs"]]
+        t = z.shape[0]
+        krig = itype in ("OK", "SK", "EDK")
+        d_cs = port.get_dists_arr(cx, cy, sx, sy)
+        d_ss = port.get_dists_arr(sx, sy, sx, sy)
+        uv = list(dict.fromkeys(vgs))
+        rr = port.get_svars_arr(d_ss, uv, [itype], 1, 1e-4) if krig else None
+        dr = port.get_svars_arr(d_cs, uv, [itype], 0, 1e-4) if krig else None
+        nug = np.array([port.check_full_nuggetness(v, 1e-4) for v in vgs])
+        prblm = []
+        est, var = port.get_interp(
+            z.copy("c"), itype, g.get(p + "sd"), g.get(p + "cd"), float(g[p + "idw_exp"]),
+            np.array(vgs, dtype=object), g[p + "flags"], nug, np.arange(t), prblm, d_cs.copy(),
+            rr, dr, np.arange(sx.size), np.arange(cx.size), est_vars_flag=True)
+        assert sorted(prblm) == g[p + "prblm"].tolist(), i
+        if itype == "NNB":
+            assert np.array_equal(est, g[p + "est"], equal_nan=True), i
+        else:
+            _close(est, g[p + "est"], 1e-15 if itype == "IDW" else KRIG_RTOL)
+        if p + "var" in g:
+            _close(var, g[p + "var"], 1e-6)   # float32 storage
