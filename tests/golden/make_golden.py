@@ -35,10 +35,11 @@ and writes small seeded cases to tests/golden/*.npz:
                 OrdinaryIndicatorKriging, SimpleIndicatorKriging
 - interp_sweep.npz  SpInterpSteps._get_interp on 80 seeded random one-group
                 cases (every model, nests of up to three, all five methods)
+- nebs_sweep.npz    SpInterpNeighborGrouping on 60 seeded random station and
+                cell sets, 'nrst' and 'pie'
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
-legacy.npz (``driver``: only driver.npz; ``interp_sweep``: only
-interp_sweep.npz).
+legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``: only that file).
 """
 import sys
 from pathlib import Path
@@ -323,6 +324,40 @@ def nebs_case(ref, out):
         for gi, gr in enumerate(grps):
             lab[gr] = gi
         out[f"n_{tag}_grp"] = lab
+
+
+def nebs_sweep(ref, out, n_cases=60, seed=707):
+    """SpInterpNeighborGrouping.get_neb_idxs_and_grps over seeded random
+    station and cell sets (3 to 50 stations, 5 to 60 cells, some cells on
+    stations), 'nrst' with 1 to 16 neighbours and 'pie' with 1 to 8 sectors.
+    Stored: the inputs, the neighbour lists and the cell groups (int16)."""
+    ref.grps.np = _NumpyLLP64()
+    rng = np.random.default_rng(seed)
+    for i in range(n_cases):
+        n, c = int(rng.integers(3, 51)), int(rng.integers(5, 61))
+        box = float(rng.uniform(1e3, 1e5))
+        sx, sy = rng.uniform(0, box, n), rng.uniform(0, box, n)
+        cx, cy = rng.uniform(0, box, c), rng.uniform(0, box, c)
+        on = int(rng.integers(0, 3))
+        cx[:on], cy[:on] = sx[:on], sy[:on]
+        if i % 2 == 0:
+            mth, npie = "nrst", 1
+            nn = int(rng.integers(1, min(16, n) + 1))
+        else:
+            mth = "pie"
+            npie = int(rng.integers(1, min(8, n) + 1))
+            nn = int(rng.integers(npie, min(16, n) + 1))
+        g = ref.grps.SpInterpNeighborGrouping(mth, nn, npie, cx.copy(), cy.copy(),
+                                              verbose=False)
+        idxs, grps = g.get_neb_idxs_and_grps(sx.copy(), sy.copy())
+        lab = np.full(c, -1, dtype=np.int16)
+        for gi, gr in enumerate(grps):
+            lab[gr] = gi
+        p = f"ns{i}_"
+        out.update({p + "sx": sx, p + "sy": sy, p + "cx": cx, p + "cy": cy,
+                    p + "cfg": np.array([0 if mth == "nrst" else 1, nn, npie]),
+                    p + "idxs": idxs.astype(np.int16), p + "grp": lab})
+    out["ns_cases"] = np.arange(n_cases)
 
 
 def fitter_case(ref_root, out):
@@ -722,6 +757,11 @@ def main(ref_root="/root/reference", only=None):
         interp_sweep(ref, out)
         np.savez_compressed(HERE / "interp_sweep.npz", **out)
         return
+    if only == "nebs_sweep":
+        out = {}
+        nebs_sweep(ref, out)
+        np.savez_compressed(HERE / "nebs_sweep.npz", **out)
+        return
     out = {}
     kernels_case(ref, out)
     np.savez_compressed(HERE / "kernels.npz", **out)
@@ -771,6 +811,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     interp_sweep(ref, out)
     np.savez_compressed(HERE / "interp_sweep.npz", **out)
+    out = {}
+    nebs_sweep(ref, out)
+    np.savez_compressed(HERE / "nebs_sweep.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

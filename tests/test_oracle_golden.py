@@ -180,6 +180,20 @@ def test_oracle_neighbours_match_reference(golden):
         assert np.array_equal(lab, g[f"n_{tag}_grp"]), tag
 
 
+def test_oracle_neighbour_sweep_matches_reference(golden):
+    """nrst / pie neighbour lists and cell groups on 60 seeded random station
+    and cell sets (tests/golden/nebs_sweep.npz), bit for bit."""
+    g = golden
+    for i in g["ns_cases"]:
+        p = f"ns{i}_"
+        kind, nn, npie = (int(v) for v in g[p + "cfg"])
+        mth = "nrst" if kind == 0 else "pie"
+        idx = port.neb_idxs(mth, g[p + "cx"], g[p + "cy"], g[p + "sx"], g[p + "sy"], nn, npie)
+        lab, _ = port.neb_groups(idx)
+        assert np.array_equal(idx, g[p + "idxs"].astype(np.int64)), (i, mth, nn, npie)
+        assert np.array_equal(lab, g[p + "grp"].astype(np.int64)), (i, mth, nn, npie)
+
+
 LEGACY_INPUTS = ("xi", "yi", "zi", "xk", "yk", "si", "sk", "lim", "model", "cls")
 
 
