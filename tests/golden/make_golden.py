@@ -37,9 +37,12 @@ and writes small seeded cases to tests/golden/*.npz:
                 cases (every model, nests of up to three, all five methods)
 - nebs_sweep.npz    SpInterpNeighborGrouping on 60 seeded random station and
                 cell sets, 'nrst' and 'pie'
+- legacy_sweep.npz  the six single-neighbourhood classes on 48 seeded random
+                cases (model nests, drifts, indicator limits)
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
-legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``: only that file).
+legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``, ``legacy_sweep``:
+only that file).
 """
 import sys
 from pathlib import Path
@@ -488,6 +491,65 @@ def legacy_case(ref, out):
     out["l_cases"] = np.arange(len(LEGACY_CASES))
 
 
+LEGACY_CLASSES = ["OrdinaryKriging", "SimpleKriging", "ExternalDriftKriging",
+                  "ExternalDriftKriging_MD", "OrdinaryIndicatorKriging",
+                  "SimpleIndicatorKriging"]
+LEGACY_SWEEP_OUT = ("zk", "est_vars", "est_covars", "mus", "mus_1", "mus_2", "mus_arr",
+                    "lambdas", "ik")
+
+
+def legacy_sweep(ref, out, n_cases=48, seed=808):
+    """The six classes in turn on seeded random cases: 3 to 16 stations, 1 to
+    16 output points (one on a station), nests of 1 to 3 of the eight
+    models, 1 to 3 drifts for ExternalDriftKriging_MD, the median as the
+    indicator limit. Stored: the inputs and the outputs callers read
+    (estimates, variances, multipliers, weights, indicators)."""
+    cy = ref.cy
+    rng = np.random.default_rng(seed)
+    for i in range(n_cases):
+        cls = LEGACY_CLASSES[i % len(LEGACY_CLASSES)]
+        n, n_out = int(rng.integers(3, 17)), int(rng.integers(1, 17))
+        box = float(rng.uniform(1e3, 1e5))
+        xi, yi = rng.uniform(0, box, n), rng.uniform(0, box, n)
+        zi = rng.gamma(1.5, 2.0, n)
+        xk, yk = rng.uniform(0, box, n_out), rng.uniform(0, box, n_out)
+        xk[0], yk[0] = xi[1], yi[1]
+        comps = []
+        for _ in range(int(rng.integers(1, 4))):
+            nm = SWEEP_MODELS[rng.integers(len(SWEEP_MODELS))]
+            sill = round(float(rng.uniform(0.05, 2.0)), 4)
+            r = (0.0 if nm == "Nug" else round(float(rng.uniform(0.1, 1.9)), 3) if nm == "Pow"
+                 else round(float(rng.uniform(0.05, 1.0)) * box, 1))
+            comps.append(f"{sill} {nm}({r})")
+        model = " + ".join(comps)
+        n_drift = int(rng.integers(1, 4)) if cls == "ExternalDriftKriging_MD" else (
+            1 if cls == "ExternalDriftKriging" else 0)
+        si = rng.uniform(0, 1500, (n_drift, n))
+        sk = rng.uniform(0, 1500, (n_drift, n_out))
+        lim = float(np.median(zi))
+        if cls in ("OrdinaryKriging", "SimpleKriging"):
+            obj = getattr(cy, cls)(xi, yi, zi, xk, yk, model=model)
+            obj.krige()
+        elif cls == "ExternalDriftKriging":
+            obj = cy.ExternalDriftKriging(xi, yi, zi, si[0].copy(), xk, yk, sk[0].copy(),
+                                          model=model)
+            obj.krige()
+        elif cls == "ExternalDriftKriging_MD":
+            obj = cy.ExternalDriftKriging_MD(xi, yi, zi, si, xk, yk, sk, model=model)
+            obj.krige()
+        else:
+            obj = getattr(cy, cls)(xi, yi, zi, xk, yk, lim=lim, model=model)
+            obj.ikrige()
+        p = f"ls{i}_"
+        out.update({p + "xi": xi, p + "yi": yi, p + "zi": zi, p + "xk": xk, p + "yk": yk,
+                    p + "si": si, p + "sk": sk, p + "lim": np.array(lim),
+                    p + "model": np.array(model), p + "cls": np.array(cls)})
+        for attr in LEGACY_SWEEP_OUT:
+            if hasattr(obj, attr) and getattr(obj, attr) is not None:
+                out[p + attr] = np.asarray(getattr(obj, attr)).copy()
+    out["ls_cases"] = np.arange(n_cases)
+
+
 DRIVER_CASES = [
     # (edk, x_min, x_max, y_min, y_max, cell size, polygon mask)
     (False, 1000.3, 26110.0, -5000.0, 14321.7, 500.0, False),
@@ -762,6 +824,11 @@ def main(ref_root="/root/reference", only=None):
         nebs_sweep(ref, out)
         np.savez_compressed(HERE / "nebs_sweep.npz", **out)
         return
+    if only == "legacy_sweep":
+        out = {}
+        legacy_sweep(ref, out)
+        np.savez_compressed(HERE / "legacy_sweep.npz", **out)
+        return
     out = {}
     kernels_case(ref, out)
     np.savez_compressed(HERE / "kernels.npz", **out)
@@ -814,6 +881,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     nebs_sweep(ref, out)
     np.savez_compressed(HERE / "nebs_sweep.npz", **out)
+    out = {}
+    legacy_sweep(ref, out)
+    np.savez_compressed(HERE / "legacy_sweep.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -215,6 +215,23 @@ def test_oracle_legacy_classes_match_reference(golden):
             assert np.array_equal(np.asarray(got[k]), g[p + k]), (ci, cls, k)
 
 
+def test_oracle_legacy_sweep_matches_reference(golden):
+    """The same restatement on 48 seeded random cases of the six classes
+    (tests/golden/legacy_sweep.npz: model nests, drifts, indicator limits):
+    estimates, variances, multipliers, weights and indicators bit for bit."""
+    g = golden
+    for ci in g["ls_cases"]:
+        p = f"ls{ci}_"
+        cls = str(g[p + "cls"])
+        got = port.legacy_krige(cls, g[p + "xi"], g[p + "yi"], g[p + "zi"], g[p + "xk"],
+                                g[p + "yk"], str(g[p + "model"]), si=g[p + "si"],
+                                sk=g[p + "sk"], lim=float(g[p + "lim"]))
+        keys = [k[len(p):] for k in g if k.startswith(p) and k[len(p):] not in LEGACY_INPUTS]
+        assert "zk" in keys or "ik" in keys, (ci, cls)
+        for k in keys:
+            assert np.array_equal(np.asarray(got[k]), g[p + k]), (ci, cls, k)
+
+
 def test_oracle_driver_grid_and_drifts_match_reference(golden):
     """The grid (SpInterpPrepare._prepare_crds) and the drift sampling
     (KrigingDrift._prepare_stns_drift) as the reference computes them
