@@ -39,10 +39,12 @@ and writes small seeded cases to tests/golden/*.npz:
                 cell sets, 'nrst' and 'pie'
 - legacy_sweep.npz  the six single-neighbourhood classes on 48 seeded random
                 cases (model nests, drifts, indicator limits)
+- vg_edges.npz      fill_vg_var_arr at every model's branch points (h = 0,
+                subnormal, the range and its neighbouring doubles, inf)
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
-legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``, ``legacy_sweep``:
-only that file).
+legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``, ``legacy_sweep``,
+``vg_edges``: only that file).
 """
 import sys
 from pathlib import Path
@@ -130,6 +132,42 @@ def kernels_case(ref, out):
     out["k_nug_1e-4"] = np.array(
         [ref.misc.check_full_nuggetness(s, 1e-4) for s in nug_cases])
     out["k_nug_0"] = np.array([ref.misc.check_full_nuggetness(s, 0.0) for s in nug_cases])
+
+
+VG_EDGE_STRS = [
+    "1.0 Nug(0.0)", "0.7 Sph(1000.0)", "1.3 Exp(2500.5)", "0.4 Lin(777.0)", "2.0 Gau(3000.0)",
+    "0.5 Pow(0.5)", "0.5 Pow(1.0)", "0.5 Pow(1.9)", "1.5 Hol(1200.0)", "2.0 Rng(1.0)",
+    "1.0 Sph(1e-07)", "1.0 Exp(0.0)", "0.2 Nug(0.0) + 0.5 Sph(1000.0) + 0.3 Lin(777.0)",
+]
+
+
+def vg_edges(ref, out):
+    """fill_vg_var_arr at the models' branch points: for each string, the
+    distances 0, the smallest subnormal, each component's range and its two
+    neighbouring doubles, half and twice the range, 1e300 and inf; covariance
+    and semivariance, min_vg_val 0 and 0.05, as a row (diag flag 0) and as a
+    symmetric square of the same values (diag flag 1)."""
+    cy = ref.cy
+    for vi, vg in enumerate(VG_EDGE_STRS):
+        rs = []
+        for part in vg.split("+"):
+            r = max(1e-5, float(part.strip().split("(")[1].split(")")[0]))
+            rs += [r, np.nextafter(r, 0.0), np.nextafter(r, np.inf), 0.5 * r, 2.0 * r]
+        h = np.array([0.0, 5e-324, *rs, 1e300, np.inf])
+        row = h[None, :].copy()
+        with np.errstate(invalid="ignore"):  # inf - inf
+            sq = np.abs(h[:, None] - h[None, :])
+        sq[~np.isfinite(sq)] = np.inf
+        out[f"ve_h_{vi}"] = h
+        for covar in (0, 1):
+            for mvv in (0.0, 0.05):
+                a = np.full_like(row, np.nan)
+                cy.fill_vg_var_arr(row, a, covar, 0, vg, mvv)
+                b = np.full_like(sq, np.nan)
+                cy.fill_vg_var_arr(sq, b, covar, 1, vg, mvv)
+                out[f"ve_row_{vi}_{covar}_{mvv:g}"] = a
+                out[f"ve_sq_{vi}_{covar}_{mvv:g}"] = b
+    out["ve_vgs"] = np.array(VG_EDGE_STRS)
 
 
 def interp_one(ref, st, sx, sy, cx, cy, z, itype, vgs, *, idw_exp=5.0,
@@ -829,6 +867,11 @@ def main(ref_root="/root/reference", only=None):
         legacy_sweep(ref, out)
         np.savez_compressed(HERE / "legacy_sweep.npz", **out)
         return
+    if only == "vg_edges":
+        out = {}
+        vg_edges(ref, out)
+        np.savez_compressed(HERE / "vg_edges.npz", **out)
+        return
     out = {}
     kernels_case(ref, out)
     np.savez_compressed(HERE / "kernels.npz", **out)
@@ -884,6 +927,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     legacy_sweep(ref, out)
     np.savez_compressed(HERE / "legacy_sweep.npz", **out)
+    out = {}
+    vg_edges(ref, out)
+    np.savez_compressed(HERE / "vg_edges.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

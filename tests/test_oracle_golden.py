@@ -303,3 +303,24 @@ def test_get_interp_sweep(golden):
             _close(est, g[p + "est"], 1e-15 if itype == "IDW" else KRIG_RTOL)
         if p + "var" in g:
             _close(var, g[p + "var"], 1e-6)   # float32 storage
+
+
+def test_vg_fill_edges_bit_exact(golden):
+    """The C restatement of fill_vg_var_arr at every model's branch points
+    (tests/golden/vg_edges.npz): h = 0, the smallest subnormal, each range
+    and its neighbouring doubles, 1e300 and inf, ranges under the 1e-5 clamp."""
+    g = golden
+    for vi, vg in enumerate(g["ve_vgs"]):
+        h = g[f"ve_h_{vi}"]
+        row = h[None, :].copy()
+        with np.errstate(invalid="ignore"):  # inf - inf
+            sq = np.abs(h[:, None] - h[None, :])
+        sq[~np.isfinite(sq)] = np.inf
+        for covar in (0, 1):
+            for mvv in (0.0, 0.05):
+                a = port.fill_vg_var_arr(row, covar, 0, str(vg), mvv)
+                assert np.array_equal(a, g[f"ve_row_{vi}_{covar}_{mvv:g}"], equal_nan=True), \
+                    (vg, covar, mvv)
+                b = port.fill_vg_var_arr(sq, covar, 1, str(vg), mvv)
+                assert np.array_equal(b, g[f"ve_sq_{vi}_{covar}_{mvv:g}"], equal_nan=True), \
+                    (vg, covar, mvv)
