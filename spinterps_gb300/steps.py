@@ -747,8 +747,8 @@ def interp_args_for(methods, est_vars=False, fig_dir=None):
     """The reference's interpolation tuples (interp/prepare.py:638-695) for
     a list of methods like ['OK', 'SK', 'EDK', ('IDW', 2.0), 'NNB']:
     (type, figure directory, label[, idw_exp]) in the reference's order,
-    IDW labels 'IDW_000', 'IDW_001', ... in the order of their exponents,
-    and ('EST_VARS_OK', ...) last when est_vars."""
+    IDW labels 'IDW_000', 'IDW_001', ... in the order the exponents are
+    given (not sorted), and ('EST_VARS_OK', ...) last when est_vars."""
     args = []
     for t in ("OK", "SK", "EDK"):
         if t in methods:
