@@ -57,3 +57,41 @@ def test_cdf5_round_trip_int64_time(tmp_path):
     assert gatt["sett_idw_exps"] == "[2.0]"
     with open(p, "rb") as f:
         assert f.read(4) == b"CDF\x05"
+
+
+def test_cdf2_fuzz_read_by_scipy(tmp_path):
+    """Seeded random files (1 to 4 dimensions, scalar to 3-d variables of
+    every classic type, odd byte counts that need padding, numeric and text
+    attributes) written as CDF-2 and read back by scipy's independent
+    netCDF-3 reader, value for value."""
+    sio = pytest.importorskip("scipy.io")
+    rng = np.random.default_rng(17)
+    types = [np.int8, np.int16, np.int32, np.float32, np.float64]
+    for case in range(40):
+        dims = {f"d{k}": int(rng.integers(1, 7)) for k in range(int(rng.integers(1, 5)))}
+        names = list(dims)
+        variables = []
+        for v in range(int(rng.integers(1, 5))):
+            nd = int(rng.integers(0, min(3, len(names)) + 1))
+            dn = tuple(rng.choice(names, nd, replace=False)) if nd else ()
+            dt = types[rng.integers(len(types))]
+            shape = tuple(dims[d] for d in dn)
+            if np.issubdtype(dt, np.integer):
+                arr = rng.integers(np.iinfo(dt).min, np.iinfo(dt).max, shape, endpoint=True)
+            else:
+                arr = rng.normal(size=shape) * 1e3
+            attrs = {"units": "mm" * int(rng.integers(0, 3)) or "x",
+                     "scale": np.array(rng.normal(size=int(rng.integers(1, 4))), dt)}
+            variables.append((f"v{v}", dn, np.asarray(arr, dt), attrs))
+        gatt = {"title": f"case {case}", "ver": np.int32(case)}
+        p = tmp_path / f"f{case}.nc"
+        ncout.write_nc(p, dims, variables, gatt, fmt=2)
+        with sio.netcdf_file(p, "r", mmap=False) as f:
+            assert {k: f.dimensions[k] for k in dims} == dims, case
+            assert f.title == b"case %d" % case and f.ver == case
+            for name, dn, arr, attrs in variables:
+                got = f.variables[name]
+                assert tuple(got.dimensions) == dn, (case, name)
+                assert np.array_equal(got[...] if arr.ndim else got.getValue(), arr), (case, name)
+                assert got.units.decode() == attrs["units"]
+                assert np.array_equal(np.atleast_1d(got.scale), attrs["scale"]), (case, name)
