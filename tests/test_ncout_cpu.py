@@ -59,11 +59,11 @@ def test_cdf5_round_trip_int64_time(tmp_path):
         assert f.read(4) == b"CDF\x05"
 
 
-def test_cdf2_fuzz_read_by_scipy(tmp_path):
+def test_classic_fuzz_read_by_scipy(tmp_path):
     """Seeded random files (1 to 4 dimensions, scalar to 3-d variables of
     every classic type, odd byte counts that need padding, numeric and text
-    attributes) written as CDF-2 and read back by scipy's independent
-    netCDF-3 reader, value for value."""
+    attributes) written as CDF-1 and CDF-2 in turn and read back by scipy's
+    independent netCDF-3 reader, value for value."""
     sio = pytest.importorskip("scipy.io")
     rng = np.random.default_rng(17)
     types = [np.int8, np.int16, np.int32, np.float32, np.float64]
@@ -85,7 +85,7 @@ def test_cdf2_fuzz_read_by_scipy(tmp_path):
             variables.append((f"v{v}", dn, np.asarray(arr, dt), attrs))
         gatt = {"title": f"case {case}", "ver": np.int32(case)}
         p = tmp_path / f"f{case}.nc"
-        ncout.write_nc(p, dims, variables, gatt, fmt=2)
+        ncout.write_nc(p, dims, variables, gatt, fmt=1 if case % 2 else 2)
         with sio.netcdf_file(p, "r", mmap=False) as f:
             assert {k: f.dimensions[k] for k in dims} == dims, case
             assert f.title == b"case %d" % case and f.ver == case
