@@ -5,7 +5,10 @@
   run with the entry points recorded instead of called; each recorded entry
   point is then counted by the kernels its C source launches.
 - InterpPlan.kernel_times files IDW and NNB under their own names, with
-  IDW's algorithmic FLOP only."""
+  IDW's algorithmic FLOP only.
+- A whole plan runs its host logic end to end (construction, execute with
+  and without timing, counters, problem steps) with the entry points
+  recorded instead of called."""
 import types
 
 import numpy as np
@@ -83,3 +86,66 @@ def test_kernel_times_keeps_nnb_apart_from_idw():
     plan = types.SimpleNamespace(C=10, cond_split=1e10)
     out = steps.InterpPlan.kernel_times(plan, evs)
     assert out == {"idw": [3.0, 2, 80.0], "nnb": [1.0, 1, 0.0]}
+
+
+class _FakeEvent:
+    """Stands in for torch.cuda.Event on the CPU."""
+    _t = 0.0
+
+    def __init__(self, enable_timing=False):
+        self.t = 0.0
+
+    def record(self, stream=None):
+        _FakeEvent._t += 1.0
+        self.t = _FakeEvent._t
+
+    def elapsed_time(self, other):
+        return other.t - self.t
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_plan_dry_run(monkeypatch, precision):
+    """A whole InterpPlan (OK + variance, SK, IDW, NNB; missing stations, a
+    step without stations, a single-station step) built and executed with
+    the entry points recorded instead of called: the host logic runs end to
+    end, the launch count equals the kernels behind the recorded calls, and
+    the timed execution files every kernel it times."""
+    calls = []
+    monkeypatch.setattr(steps, "_require_cuda", lambda device: torch.device("cpu"))
+    monkeypatch.setattr(nat, "call", lambda name, *a: calls.append((name, a)))
+    monkeypatch.setattr(steps, "_stream", lambda: None)
+    monkeypatch.setattr(torch.cuda, "Event", _FakeEvent)
+    rng = np.random.default_rng(3)
+    N, T, C = 30, 6, 200
+    sx, sy = rng.uniform(0, 1e5, N), rng.uniform(0, 1e5, N)
+    z = rng.normal(size=(T, N))
+    z[rng.uniform(size=(T, N)) < 0.2] = np.nan
+    z[2] = np.nan
+    z[3] = np.nan
+    z[3, 4] = 1.0
+    cx, cy = rng.uniform(0, 1e5, C), rng.uniform(0, 1e5, C)
+    vgs = ["0.1 Nug(0.0) + 0.9 Exp(20000)", "1.0 Gau(30000)"] * (T // 2)
+    args = steps.interp_args_for(["OK", "SK", ("IDW", 2.0), "NNB"], est_vars=True)
+    plan = steps.InterpPlan(sx, sy, z, cx, cy, vgs, args, est_vars=True, precision=precision,
+                            min_vg_val=1e-4)
+
+    def kernels(name, a):
+        if name == "spi_krige_factor":
+            return 4
+        if name == "spi_krige_duals":
+            return 1 if a[3]._obj.linv_arena else 3
+        return 1
+
+    for timing in (False, True):
+        calls.clear()
+        evs = plan.execute(timing=timing)
+        assert plan.launches_per_execute() == sum(kernels(n, a) for n, a in calls)
+    names = {n for n, _ in calls}
+    assert {"spi_krige_factor", "spi_krige_duals", "spi_krige_cells", "spi_idw_cells",
+            "spi_nnb_cells", "spi_fill_rows"} <= names
+    if precision == "mixed":
+        assert {"spi_krige_tier", "spi_krige_var_tc", "spi_krige_var_df"} <= names
+    times = plan.kernel_times(evs)
+    assert {"idw", "nnb"} <= set(times)
+    assert times["nnb"][2] == 0.0 and times["idw"][2] > 0.0
+    assert plan.problem_steps()[0] == 2
