@@ -149,3 +149,41 @@ def test_plan_dry_run(monkeypatch, precision):
     assert {"idw", "nnb"} <= set(times)
     assert times["nnb"][2] == 0.0 and times["idw"][2] > 0.0
     assert plan.problem_steps()[0] == 2
+
+
+def test_legacy_and_polygon_dry_run(monkeypatch):
+    """The legacy classes and the polygon mask run their host logic with the
+    entry points recorded instead of called (no GPU)."""
+    from spinterps_gb300 import driver, legacy
+    calls = []
+    cpu = torch.device("cpu")
+
+    class _Stream:
+        cuda_stream = 0
+
+        def synchronize(self):
+            pass
+
+    for mod in (steps, legacy, driver):
+        monkeypatch.setattr(mod, "_require_cuda", lambda device: cpu)
+    monkeypatch.setattr(driver, "_stream", lambda: None)
+    monkeypatch.setattr(nat, "call", lambda name, *a: calls.append(name))
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda *a, **k: _Stream())
+    monkeypatch.setattr(legacy, "_dev", lambda a: torch.as_tensor(
+        np.ascontiguousarray(a, dtype=np.float64)))
+    rng = np.random.default_rng(4)
+    xi, yi, zi = rng.uniform(0, 5e4, 12), rng.uniform(0, 5e4, 12), rng.normal(size=12)
+    xk, yk = rng.uniform(0, 5e4, 20), rng.uniform(0, 5e4, 20)
+    for cls in ("OrdinaryKriging", "SimpleKriging", "OrdinaryIndicatorKriging"):
+        obj = getattr(legacy, cls)(xi, yi, zi, xk, yk, model="0.1 Nug(0.0) + 0.9 Exp(20000)")
+        if "Indicator" in cls:
+            obj.ikrige()
+        else:
+            obj.krige()
+        assert obj.pinv_route == "gj" and obj.zk.shape == (20,)
+    assert calls.count("spi_legacy_system") == 3 and calls.count("spi_legacy_points") == 3
+    calls.clear()
+    ring = (np.array([0.0, 5e4, 5e4, 0.0]), np.array([0.0, 0.0, 5e4, 5e4]))
+    with pytest.raises(AssertionError, match="No cells selected"):
+        driver.cells_in_polygons(xk, yk, [ring])  # the recorded kernel selects nothing
+    assert calls == ["spi_points_in_polygons"]
