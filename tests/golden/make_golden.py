@@ -41,10 +41,12 @@ and writes small seeded cases to tests/golden/*.npz:
                 cases (model nests, drifts, indicator limits)
 - vg_edges.npz      fill_vg_var_arr at every model's branch points (h = 0,
                 subnormal, the range and its neighbouring doubles, inf)
+- empirical_sweep.npz  the Variogram's empirical variogram on 40 seeded random
+                station sets (lattices with tied distances, nk, mdr)
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
 legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``, ``legacy_sweep``,
-``vg_edges``: only that file).
+``vg_edges``, ``empirical_sweep``: only that file).
 """
 import sys
 from pathlib import Path
@@ -399,6 +401,41 @@ def nebs_sweep(ref, out, n_cases=60, seed=707):
                     p + "cfg": np.array([0 if mth == "nrst" else 1, nn, npie]),
                     p + "idxs": idxs.astype(np.int16), p + "grp": lab})
     out["ns_cases"] = np.arange(n_cases)
+
+
+def empirical_sweep(ref_root, out, n_cases=40, seed=909):
+    """The reference Variogram's empirical variogram (_max_dist_est and
+    _vg_var_raw, variograms/vgs.py:320-520, 597-659) on seeded random
+    station sets: 5 to 80 stations, a third of them on a lattice (many tied
+    distances), nk 10 / 25 / 50, mdr 0.3 to 1.0. Stored: the inputs, the bin
+    distances, the robust semivariances, the pair counts, the max distance."""
+    vgs_mod = load_variogram(ref_root)
+    rng = np.random.default_rng(seed)
+    for i in range(n_cases):
+        n = int(rng.integers(5, 81))
+        box = float(rng.uniform(1e3, 1e5))
+        if i % 3 == 0:
+            m = int(np.ceil(np.sqrt(n))) + 1
+            pts = rng.choice(m * m, n, replace=False)
+            x, y = (pts % m) * box / m, (pts // m) * box / m
+        else:
+            x, y = rng.uniform(0, box, n), rng.uniform(0, box, n)
+        z = rng.gamma(1.2, 2.0, n)
+        nk = int(rng.choice([10, 25, 50]))
+        mdr = float(rng.choice([0.3, 0.5, 0.7, 1.0]))
+        v = vgs_mod.Variogram(x=x, y=y, z=z, mdr=mdr, nk=nk, typ="var", perm_r_list=[1, 2],
+                              fil_nug_vg="Nug", ld=None, uh=None, h_itrs=100,
+                              opt_meth="L-BFGS-B", opt_iters=10000, fit_vgs=["Sph", "Exp"],
+                              n_best=1, evg_name="robust", use_wts=False, ngp=5,
+                              fit_thresh=0.01)
+        v._max_dist_est()
+        v._vg_var_raw()
+        p = f"fe{i}_"
+        out.update({p + "x": x, p + "y": y, p + "z": z, p + "nk": np.array(nk),
+                    p + "mdr": np.array(mdr), p + "h": v.vg_h_arr.copy(),
+                    p + "g": v.vg_vg_arr.copy(), p + "np": v.pairs_no.copy(),
+                    p + "maxd": np.array(v.max_dist)})
+    out["fe_cases"] = np.arange(n_cases)
 
 
 def fitter_case(ref_root, out):
@@ -872,6 +909,11 @@ def main(ref_root="/root/reference", only=None):
         vg_edges(ref, out)
         np.savez_compressed(HERE / "vg_edges.npz", **out)
         return
+    if only == "empirical_sweep":
+        out = {}
+        empirical_sweep(ref_root, out)
+        np.savez_compressed(HERE / "empirical_sweep.npz", **out)
+        return
     out = {}
     kernels_case(ref, out)
     np.savez_compressed(HERE / "kernels.npz", **out)
@@ -930,6 +972,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     vg_edges(ref, out)
     np.savez_compressed(HERE / "vg_edges.npz", **out)
+    out = {}
+    empirical_sweep(ref_root, out)
+    np.savez_compressed(HERE / "empirical_sweep.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -24,6 +24,21 @@ def test_empirical_variogram_exact(golden):
         assert max_dist == g[f"f{c}_maxd"]
 
 
+def test_empirical_variogram_sweep_exact(golden):
+    """The same on 40 seeded random station sets (tests/golden/
+    empirical_sweep.npz): lattices with many tied distances, nk 10 / 25 /
+    50, mdr 0.3 to 1.0."""
+    g = golden
+    for c in g["fe_cases"]:
+        p = f"fe{c}_"
+        h, gam, cnt, max_dist, _ = fitter.empirical(g[p + "x"], g[p + "y"], g[p + "z"],
+                                                    nk=int(g[p + "nk"]), mdr=float(g[p + "mdr"]))
+        assert np.array_equal(h, g[p + "h"]), c
+        assert np.array_equal(gam, g[p + "g"]), c
+        assert np.array_equal(cnt, g[p + "np"]), c
+        assert max_dist == g[p + "maxd"], c
+
+
 def test_objective_exact(golden):
     g = golden
     for c in _cases(g):
