@@ -1,0 +1,100 @@
+"""The CUDA path against the golden sweeps made by running the reference
+(tests/golden/*_sweep.npz, vg_edges.npz). Opt-in: these run only with
+SPI_GPU_SWEEPS=1 until a GPU run has confirmed them.
+
+Bars:
+- neighbour lists and cell groups: exact;
+- the variogram fill at the branch points: 1e-13 relative (device exp / sin
+  / pow against the host's libm), the same non-finite entries;
+- the legacy classes' outputs: 1e-9 of the field's largest magnitude, on
+  the cases whose matrix condition is under 1e6. Above that, the
+  reference's pinv and the Gauss-Jordan inverse both carry errors near
+  cond * eps.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytest.importorskip("torch")
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("SPI_GPU_SWEEPS") != "1",
+                                 reason="opt-in: set SPI_GPU_SWEEPS=1")]
+
+from oracle import port  # noqa: E402
+
+
+def test_neb_select_sweep(golden):
+    from spinterps_gb300 import nebs
+    g = golden
+    for i in g["ns_cases"]:
+        p = f"ns{i}_"
+        kind, nn, npie = (int(v) for v in g[p + "cfg"])
+        mth = "nrst" if kind == 0 else "pie"
+        grp = nebs.SpInterpNeighborGrouping(mth, nn, npie, g[p + "cx"], g[p + "cy"])
+        idxs, grps = grp.get_neb_idxs_and_grps(g[p + "sx"], g[p + "sy"])
+        lab = np.full(g[p + "cx"].size, -1, dtype=np.int64)
+        for gi, gr in enumerate(grps):
+            lab[gr] = gi
+        assert np.array_equal(np.asarray(idxs, np.int64), g[p + "idxs"].astype(np.int64)), i
+        assert np.array_equal(lab, g[p + "grp"].astype(np.int64)), i
+
+
+def test_vg_fill_edges(golden):
+    import spinterps_gb300 as spi
+    g = golden
+    for vi, vg in enumerate(g["ve_vgs"]):
+        h = g[f"ve_h_{vi}"]
+        row = h[None, :].copy()
+        with np.errstate(invalid="ignore"):  # inf - inf
+            sq = np.abs(h[:, None] - h[None, :])
+        sq[~np.isfinite(sq)] = np.inf
+        for covar, types in ((0, ["OK"]), (1, ["SK"])):
+            for mvv in (0.0, 0.05):
+                st = spi.SpInterpSteps(min_vg_val=mvv)
+                for arr, diag, key in ((row, 0, "row"), (sq, 1, "sq")):
+                    got = st._get_svars_arr(arr, [str(vg)], types, diag)[(str(vg), covar)]
+                    ref = g[f"ve_{key}_{vi}_{covar}_{mvv:g}"]
+                    fin = np.isfinite(ref)
+                    assert np.array_equal(np.isfinite(got), fin), (vg, covar, mvv, key)
+                    assert np.array_equal(got[~fin], ref[~fin], equal_nan=True), (vg, key)
+                    assert np.all(np.abs(got[fin] - ref[fin])
+                                  <= 1e-13 * np.abs(ref[fin]) + 1e-300), (vg, covar, mvv, key)
+
+
+def test_legacy_sweep(golden):
+    import spinterps_gb300 as spi
+    g = golden
+    checked = 0
+    for ci in g["ls_cases"]:
+        p = f"ls{ci}_"
+        cls = str(g[p + "cls"])
+        args = (g[p + "xi"], g[p + "yi"], g[p + "zi"], g[p + "xk"], g[p + "yk"])
+        model, si, sk, lim = str(g[p + "model"]), g[p + "si"], g[p + "sk"], float(g[p + "lim"])
+        mats = port.legacy_krige(cls, *args, model, si=si, sk=sk, lim=lim)
+        a = mats.get("in_vars", mats.get("in_covars"))
+        if a is None or np.linalg.cond(a) > 1e6:
+            continue
+        c = getattr(spi, cls)
+        if cls == "ExternalDriftKriging":
+            obj = c(*args[:3], si[0].copy(), *args[3:], sk[0].copy(), model=model)
+            obj.krige()
+        elif cls == "ExternalDriftKriging_MD":
+            obj = c(*args[:3], si, *args[3:], sk, model=model)
+            obj.krige()
+        elif cls.endswith("IndicatorKriging"):
+            obj = c(*args, lim=lim, model=model)
+            obj.ikrige()
+        else:
+            obj = c(*args, model=model)
+            obj.krige()
+        for k in ("zk", "est_vars", "est_covars", "mus", "mus_1", "mus_2", "mus_arr",
+                  "lambdas", "ik"):
+            if p + k not in g:
+                continue
+            ref = g[p + k]
+            got = np.asarray(getattr(obj, k), dtype=np.float64)
+            scale = max(np.abs(ref).max(), 1e-300) if ref.size else 1.0
+            assert np.abs(got - ref).max() <= 1e-9 * scale if ref.size else True, (ci, cls, k)
+        checked += 1
+    assert checked >= 20, checked
