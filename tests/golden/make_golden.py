@@ -43,10 +43,12 @@ and writes small seeded cases to tests/golden/*.npz:
                 subnormal, the range and its neighbouring doubles, inf)
 - empirical_sweep.npz  the Variogram's empirical variogram on 40 seeded random
                 station sets (lattices with tied distances, nk, mdr)
+- steps_sweep.npz   16 multi-step runs as steps.npz with seeded random settings
+                (methods, missingness, thresholds, cut-offs)
 
 ``python tests/golden/make_golden.py REFERENCE_ROOT legacy`` writes only
 legacy.npz (``driver``, ``interp_sweep``, ``nebs_sweep``, ``legacy_sweep``,
-``vg_edges``, ``empirical_sweep``: only that file).
+``vg_edges``, ``empirical_sweep``, ``steps_sweep``: only that file).
 """
 import sys
 from pathlib import Path
@@ -333,6 +335,41 @@ def steps_case(ref, out, tag, *, n, t, nx, ny, cs, box, p_miss, vgs, methods,
     out[f"s_{tag}_prblm"] = np.array(sorted(set(prblm)), dtype=np.int64)
     for lab, f in flds.items():
         out[f"s_{tag}_out_{lab}"] = f
+
+
+STEPS_SWEEP_VGS = ["0.05 Nug(0.0) + 0.95 Exp(20000)", "1.0 Sph(30000)",
+                   "0.2 Nug(0.0) + 0.8 Gau(15000)", "1.0 Nug(0.0)", "0.7 Lin(40000)",
+                   "0.1 Nug(0.0) + 0.5 Exp(8000) + 0.4 Sph(50000)"]
+
+
+def steps_sweep(ref, out, n_cases=16, seed=1010):
+    """steps_case with seeded random settings: 8 to 40 stations, 6 to 10
+    steps, grids of 4 to 10 cells a side, missingness 0 to 0.35, per-step
+    variograms from STEPS_SWEEP_VGS (nugget-only steps among them), a random
+    subset of OK / SK / EDK / IDW (one or two exponents) / NNB, min_var_thr
+    and both cut-offs on or off."""
+    rng = np.random.default_rng(seed)
+    tags = []
+    for i in range(n_cases):
+        n, t = int(rng.integers(8, 41)), int(rng.integers(6, 11))
+        nx, ny = int(rng.integers(4, 11)), int(rng.integers(4, 11))
+        box = float(rng.uniform(3e4, 1.5e5))
+        methods = [m for m in ("OK", "SK", "EDK") if rng.uniform() < 0.5]
+        for e in rng.choice([0.5, 1.0, 2.0, 3.0], int(rng.integers(0, 3)), replace=False):
+            methods.append(("IDW", float(e)))
+        if rng.uniform() < 0.4 or not methods:
+            methods.append("NNB")
+        vgs = [STEPS_SWEEP_VGS[k] for k in rng.integers(len(STEPS_SWEEP_VGS), size=t)]
+        thr = float(rng.choice([0.0, 0.5, 3.0]))
+        mn = float(rng.choice([0.0, 1.0])) if rng.uniform() < 0.5 else None
+        mx = float(rng.choice([4.0, 6.0])) if rng.uniform() < 0.5 else None
+        tag = f"sw{i}"
+        steps_case(ref, out, tag, n=n, t=t, nx=nx, ny=ny, cs=box / max(nx, ny), box=box,
+                   p_miss=float(rng.choice([0.0, 0.15, 0.35])), vgs=vgs, methods=methods,
+                   seed=int(rng.integers(1 << 30)), min_var_thr=thr, min_var_cut=mn,
+                   max_var_cut=mx, edk="EDK" in methods)
+        tags.append(tag)
+    out["ss_tags"] = np.array(tags)
 
 
 class _NumpyLLP64:
@@ -914,6 +951,11 @@ def main(ref_root="/root/reference", only=None):
         empirical_sweep(ref_root, out)
         np.savez_compressed(HERE / "empirical_sweep.npz", **out)
         return
+    if only == "steps_sweep":
+        out = {}
+        steps_sweep(ref, out)
+        np.savez_compressed(HERE / "steps_sweep.npz", **out)
+        return
     out = {}
     kernels_case(ref, out)
     np.savez_compressed(HERE / "kernels.npz", **out)
@@ -975,6 +1017,9 @@ def main(ref_root="/root/reference", only=None):
     out = {}
     empirical_sweep(ref_root, out)
     np.savez_compressed(HERE / "empirical_sweep.npz", **out)
+    out = {}
+    steps_sweep(ref, out)
+    np.savez_compressed(HERE / "steps_sweep.npz", **out)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

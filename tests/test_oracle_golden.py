@@ -134,6 +134,18 @@ def test_get_interp_idw_nnb_one(golden):
 
 @pytest.mark.parametrize("tag", ["okidw", "edk"])
 def test_interp_steps(golden, tag):
+    _check_steps(golden, tag)
+
+
+def test_interp_steps_sweep(golden):
+    """16 multi-step runs with seeded random settings
+    (tests/golden/steps_sweep.npz): methods, missingness, thresholds and
+    cut-offs."""
+    for tag in golden["ss_tags"]:
+        _check_steps(golden, str(tag))
+
+
+def _check_steps(golden, tag):
     g = golden
     p = f"s_{tag}_"
     methods = []
