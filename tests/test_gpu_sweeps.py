@@ -9,7 +9,9 @@ Bars:
 - the legacy classes' outputs: 1e-9 of the field's largest magnitude, on
   the cases whose matrix condition is under 1e6. Above that, the
   reference's pinv and the Gauss-Jordan inverse both carry errors near
-  cond * eps.
+  cond * eps;
+- the multi-step runs: 2e-6 (float32 fields) on the FP64 path, 1e-5 on the
+  mixed path.
 """
 import os
 
@@ -98,3 +100,41 @@ def test_legacy_sweep(golden):
             assert np.abs(got - ref).max() <= 1e-9 * scale if ref.size else True, (ci, cls, k)
         checked += 1
     assert checked >= 20, checked
+
+
+def _err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(b)
+    if not m.any():
+        return 0.0
+    return float(np.abs(a[m] - b[m]).max() / max(np.abs(b[m]).max(), 1e-300))
+
+
+def test_multi_step_sweep(golden):
+    """The step engine on the 16 random multi-step runs
+    (tests/golden/steps_sweep.npz), FP64 path at the float32 fields' bar and
+    mixed path at 1e-5, as the hand-built multi-step cases."""
+    import spinterps_gb300 as spi
+    g = golden
+    for tag in g["ss_tags"]:
+        p = f"s_{tag}_"
+        methods = []
+        for m in g[p + "methods"]:
+            m = str(m)
+            methods.append(("IDW", float(m.split(":")[1])) if m.startswith("IDW:") else m)
+        thr, mn, mx, mvv = g[p + "params"]
+        args = port.interp_args_for(methods, est_vars="OK" in methods)
+        for precision, tol in (("fp64", 2e-6), ("mixed", 1e-5)):
+            flds, prblm = spi.interp_steps(
+                g[p + "sx"], g[p + "sy"], g[p + "z"], g[p + "cx"], g[p + "cy"],
+                [str(v) for v in g[p + "vgs"]], args, est_vars="OK" in methods,
+                stn_drifts=g.get(p + "sd"), cell_drifts=g.get(p + "cd"), min_var_thr=thr,
+                min_var_cut=None if np.isnan(mn) else mn,
+                max_var_cut=None if np.isnan(mx) else mx, min_vg_val=mvv, precision=precision)
+            assert sorted(set(prblm)) == g[p + "prblm"].tolist(), (tag, precision)
+            for lab, f in flds.items():
+                e = _err(f, g[p + "out_" + lab])
+                assert e <= tol, (tag, precision, lab, e)
