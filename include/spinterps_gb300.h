@@ -286,15 +286,18 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
  * 0 (var arrays may be NULL; a NaN in one field and not the other fails).
  * disc (optional, [n_sys, 3]): each system's largest estimate, tensor-core
  * variance and double-float variance discrepancy over the probe (NaN where
- * not a candidate, +inf for a NaN mismatch). The
+ * not a candidate, +inf for a NaN mismatch). tc_err (optional, device):
+ * the err_flag given to spi_krige_var_tc for the probe; when it is set, a
+ * tensor-core wait timed out and var32 is incomplete, so every system gets
+ * tier 0. The
  * mixed path's a-posteriori error control: the FP32 rounding of the
  * right-hand sides enters the estimate as sum_i dc_i w_i, which the dual
  * weights can amplify far beyond what the condition number predicts. */
 int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n_probe,
                    const double *est64, const double *est32, const double *var64,
                    const double *var32, const double *var32_df, double tol_est,
-                   double tol_var, double cond_cap, double cond_cap_df, int32_t *tier,
-                   double *disc, spi_stream_t stream);
+                   double tol_var, double cond_cap, double cond_cap_df,
+                   const int32_t *tc_err, int32_t *tier, double *disc, spi_stream_t stream);
 
 /* The OK variance term |Linv c|^2 of every cell of the FP32-tier systems
  * (ws->tier, else route 0 and cond <= cond_split; kinds OK / EDK) on the tensor cores
@@ -491,14 +494,24 @@ int spi_mlp_adam(float *params, const float *grad, float *m, float *v, int64_t n
  * stn_idx [n] (device): the stations' indices into dom; vals [n_steps, n]
  * (device): their values per step; vg (host): the variogram; est / var of
  * out: [n_steps, dom->n_cells], row j = step j. dom->n_drift is ignored.
+ * It needs 2 <= n: a step with one present station is the reference's
+ * copy of that station's value (interp/steps.py:282-283), which the caller
+ * does itself (spi_fill_rows), and n < 2 returns SPI_ERR_ARG.
  * Sizes above the limits return SPI_ERR_TOO_LARGE. The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress, with
  * that device current); make that first call before any stream capture.
  * Every call shares the one array: calls that overlap on the GPU (other
- * streams or host threads) race and must be serialised by the caller. */
+ * streams or host threads) race and must be serialised by the caller.
+ * route_out (optional, device, one int32): the system's route, written in
+ * stream order -- 0 Cholesky, 1 exact inverse, 2 exactly singular: every
+ * cell then took its nearest station and the estimate variance is 0, and
+ * the step is one the reference reports as a problem step
+ * (interp/steps.py:363-384). Without route_out such steps are not
+ * reported. */
 int spi_krige_ok_noalloc(const spi_domain_t *dom, const int32_t *stn_idx, int32_t n,
                          const spi_vg_t *vg, const double *vals, int32_t n_steps,
-                         int32_t want_var, const spi_out_t *out, spi_stream_t stream);
+                         int32_t want_var, const spi_out_t *out, spi_stream_t stream,
+                         int32_t *route_out);
 
 /* Interpolation from each cell's own neighbours (the neighbour methods of
  * interp/steps.py:584-606, 673-833): for every listed step q (data row

@@ -12,7 +12,11 @@ producing inf/NaN), then compiles it with g++ against numpy's headers.
 
 Usage (only where the reference tree exists, i.e. not on the GPU host)::
 
-    python oracle/build_ref.py [REFERENCE_ROOT]
+    python oracle/build_ref.py REFERENCE_ROOT
+
+or with the root in the environment variable SPINTERPS_REFERENCE_ROOT
+(``build()`` without an argument reads it, and builds nothing when it is
+unset).
 """
 import os
 import subprocess
@@ -22,12 +26,23 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_REF = Path("/root/reference")
+ENV = "SPINTERPS_REFERENCE_ROOT"
 
 
-def build(ref_root=DEFAULT_REF, force=False):
-    """Build ``oracle/_ref/interpmthds*.so``; return its directory or None."""
-    ref_root = Path(ref_root)
+def reference_root(ref_root=None):
+    """The reference tree: the argument, else $SPINTERPS_REFERENCE_ROOT, else
+    None."""
+    if ref_root is None:
+        ref_root = os.environ.get(ENV)
+    return Path(ref_root) if ref_root else None
+
+
+def build(ref_root=None, force=False):
+    """Build ``oracle/_ref/interpmthds*.so``; return its directory or None
+    (no reference tree given, or Cython absent)."""
+    ref_root = reference_root(ref_root)
+    if ref_root is None:
+        return None
     pyx = ref_root / "cyth" / "interpmthds.pyx"
     if not pyx.exists():
         return None
@@ -64,7 +79,5 @@ def build(ref_root=DEFAULT_REF, force=False):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(
-        "SPINTERPS_REFERENCE", str(DEFAULT_REF))
-    out = build(root, force=True)
+    out = build(sys.argv[1] if len(sys.argv) > 1 else None, force=True)
     print("built" if out else "reference not present", out)

@@ -93,7 +93,8 @@ _SIGS = {
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
     "spi_krige_tier": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_i64, c_ptr, c_ptr,
-                       c_ptr, c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr],
+                       c_ptr, c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr,
+                       c_ptr],
     "spi_krige_var_df": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],
     "spi_krige_var_tc": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
@@ -116,7 +117,7 @@ _SIGS = {
     "spi_mlp_adam": [c_ptr, c_ptr, c_ptr, c_ptr, c_i64, ctypes.c_float, ctypes.c_float,
                      ctypes.c_float, ctypes.c_float, c_i32, c_ptr],
     "spi_krige_ok_noalloc": [ctypes.POINTER(DomainT), c_ptr, c_i32, ctypes.POINTER(VgT), c_ptr,
-                             c_i32, c_i32, ctypes.POINTER(OutT), c_ptr],
+                             c_i32, c_i32, ctypes.POINTER(OutT), c_ptr, c_ptr],
     "spi_points_in_polygons": [c_ptr, c_ptr, c_i64, c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                c_ptr],
     "spi_field_stats": [c_ptr, c_i32, c_i32, c_i64, c_i64, c_i32, c_ptr, c_i64, c_ptr, c_ptr],

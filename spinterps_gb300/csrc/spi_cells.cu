@@ -534,10 +534,13 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
                                               const double* __restrict__ v32,
                                               const double* __restrict__ v32d, double tol_e,
                                               double tol_v, double cap, double cap_d,
+                                              const int32_t* __restrict__ tc_err,
                                               int32_t* tier, double* disc) {
   const int s = blockIdx.x;
   __shared__ double red[3][256];
-  const bool route0 = ws.route[s] == 0;
+  // a timed-out tensor-core wait (spi_krige_var_tc) leaves var32 partly
+  // unwritten: every system then stays in FP64
+  const bool route0 = ws.route[s] == 0 && !(tc_err && *tc_err);
   const bool cand = route0 && ws.cond[s] <= cap;
   const bool cand_d = route0 && v32d != nullptr && ws.cond[s] <= cap_d;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
@@ -589,7 +592,8 @@ extern "C" int spi_krige_tier(const spi_systems_t* sys, const spi_krige_ws_t* ws
                               const double* est64, const double* est32, const double* var64,
                               const double* var32, const double* var32_df, double tol_est,
                               double tol_var, double cond_cap, double cond_cap_df,
-                              int32_t* tier, double* disc, spi_stream_t stream) {
+                              const int32_t* tc_err, int32_t* tier, double* disc,
+                              spi_stream_t stream) {
   if (!sys || !ws || !tier || n_probe < 0) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (sys->n_sys == 0) return SPI_OK;
@@ -598,7 +602,7 @@ extern "C" int spi_krige_tier(const spi_systems_t* sys, const spi_krige_ws_t* ws
     return SPI_ERR_ARG;
   spi::k_tier<<<sys->n_sys, 256, 0, (cudaStream_t)stream>>>(
       *sys, *ws, n_probe, est64, est32, var64, var32, var32_df, tol_est, tol_var, cond_cap,
-      cond_cap_df, tier, disc);
+      cond_cap_df, tc_err, tier, disc);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

@@ -9,6 +9,9 @@
 // take a caller-provided workspace; this one instead keeps its workspace
 // (factor arenas, dual weights, system descriptors) in one file-scope
 // static device array, so the caller passes only inputs and outputs.
+// The system's route (route_out, optional) tells the caller whether the
+// step is one the reference would report as a problem step: route 2 means
+// the system was exactly singular and every cell took its nearest station.
 //
 // The array holds one system of at most SPI_NOALLOC_MAX_STNS stations and
 // SPI_NOALLOC_MAX_STEPS steps (see spinterps_gb300.h); it is reserved on
@@ -105,12 +108,17 @@ __global__ void k_noalloc_setup(unsigned char* base, int n, int n_steps, spi_vg_
   for (int i = t; i < MAXT * GA; i += blockDim.x) beta[i] = 0.0;
 }
 
+// The system's route, copied out of the scratch in stream order.
+__global__ void k_noalloc_route(const unsigned char* base, int32_t* route_out) {
+  *route_out = *reinterpret_cast<const int32_t*>(base + OFF_ROUTE);
+}
+
 }  // namespace
 
 extern "C" int spi_krige_ok_noalloc(const spi_domain_t* dom, const int32_t* stn_idx,
                                     int32_t n, const spi_vg_t* vg, const double* vals,
                                     int32_t n_steps, int32_t want_var, const spi_out_t* out,
-                                    spi_stream_t stream) {
+                                    spi_stream_t stream, int32_t* route_out) {
   if (!dom || !stn_idx || !vg || !vals || !out || !out->est) return SPI_ERR_ARG;
   if (n < 2 || n_steps < 1) return SPI_ERR_ARG;
   if (n > MAXN || n_steps > MAXT) return SPI_ERR_TOO_LARGE;
@@ -149,5 +157,10 @@ extern "C" int spi_krige_ok_noalloc(const spi_domain_t* dom, const int32_t* stn_
   d.n_drift = 0;  // ordinary kriging: the unbiasedness row only
   if ((rc = spi_krige_factor(&d, &sy, &ws, 1e13, stream))) return rc;
   if ((rc = spi_krige_duals(&d, &sy, vals, &ws, stream))) return rc;
-  return spi_krige_cells(&d, &sy, vals, &ws, want_var, 0, 0, 1e7, out, stream);
+  if ((rc = spi_krige_cells(&d, &sy, vals, &ws, want_var, 0, 0, 1e7, out, stream))) return rc;
+  if (route_out) {
+    k_noalloc_route<<<1, 1, 0, st>>>(base, route_out);
+    SPI_LAUNCH_CHECK();
+  }
+  return SPI_OK;
 }

@@ -424,7 +424,7 @@ class _KrigeBatch:
             nat.call("spi_krige_tier", ctypes.byref(self.sy), ws, pdom.C, _ptr(pe64), _ptr(pe32),
                      _ptr(pv64 if want_var else None), _ptr(pv32 if want_var else None),
                      _ptr(pv32d), float(tol_e), float(tol_v), float(cond_split), cap,
-                     _ptr(self.tier), _ptr(self.disc), s)
+                     _ptr(self.tc_err), _ptr(self.tier), _ptr(self.disc), s)
         if self.yy is not None and want_var:
             timed("var_tc", lambda: nat.call(
                 "spi_krige_var_tc", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,

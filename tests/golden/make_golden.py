@@ -2,7 +2,9 @@
 
 TEST INFRASTRUCTURE. Run only where the reference tree exists::
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
+
+(or with the root in $SPINTERPS_REFERENCE_ROOT)
 
 It loads the unmodified reference (interp/steps.py, interp/grps.py, misc.py
 and cyth/interpmthds.pyx compiled by oracle/build_ref.py, see refharness.py)
@@ -914,7 +916,7 @@ def interp_sweep(ref, out, n_cases=80, seed=606):
     out["w_cases"] = np.arange(n_cases)
 
 
-def main(ref_root="/root/reference", only=None):
+def main(ref_root=None, only=None):
     ref = load_reference(ref_root)
     if only == "driver":
         out = {}

@@ -35,9 +35,18 @@ def _stub(name, **attrs):
     return mod
 
 
-def load_reference(ref_root="/root/reference"):
+def _root(ref_root):
+    from oracle import build_ref
+    root = build_ref.reference_root(ref_root)
+    if root is None:
+        raise RuntimeError(f"give the reference tree as an argument or in ${build_ref.ENV}")
+    return root
+
+
+def load_reference(ref_root=None):
     """Return a namespace with the reference's step engine and kernels."""
-    ref_root = Path(ref_root)
+    sys.path.insert(0, str(REPO))
+    ref_root = _root(ref_root)
     sys.path.insert(0, str(REPO))
     from oracle import build_ref
 
@@ -226,11 +235,12 @@ def load_prepare():
     return prep
 
 
-def load_variogram(ref_root="/root/reference"):
+def load_variogram(ref_root=None):
     """The reference's Variogram class (variograms/vgs.py) with the stand-in
     DataFrame in place of pandas."""
     import importlib.util
-    ref_root = Path(ref_root)
+    sys.path.insert(0, str(REPO))
+    ref_root = _root(ref_root)
     pd = sys.modules.get("pandas")
     if pd is None or not hasattr(pd, "__version__"):
         pd = _stub("pandas")

@@ -211,7 +211,7 @@ def test_entry_points_check_arguments_before_any_gpu_work():
     assert lib.spi_round_fields(dummy, 0, 0, 3, None) == 0
     assert lib.spi_krige_var_df(None, None, None, 1e10, None) == ARG
     assert lib.spi_krige_tier(None, None, 0, None, None, None, None, None, 0.0, 0.0, 0.0, 0.0,
-                              None, None, None) == ARG
+                              None, None, None, None) == ARG
     assert lib.spi_peak_fma(1, 0, dummy, ctypes.byref(c_i64()), None) == ARG
 
 

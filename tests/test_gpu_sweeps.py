@@ -1,6 +1,5 @@
 """The CUDA path against the golden sweeps made by running the reference
-(tests/golden/*_sweep.npz, vg_edges.npz). Opt-in: these run only with
-SPI_GPU_SWEEPS=1 until a GPU run has confirmed them.
+(tests/golden/*_sweep.npz, vg_edges.npz).
 
 Bars:
 - neighbour lists and cell groups: exact;
@@ -11,19 +10,22 @@ Bars:
   reference's pinv and the Gauss-Jordan inverse both carry errors near
   cond * eps;
 - the multi-step runs: 2e-6 (float32 fields) on the FP64 path, 1e-5 on the
-  mixed path.
+  mixed path;
+- the one-group runs of _get_interp (interp_sweep.npz): 1e-9 on regular
+  systems (or 10x the reference's own spread under 1e-15 perturbations of
+  its matrix, where that is larger), exact for NNB; systems that pinv
+  treats as singular are set apart and held to the reference's outcomes
+  under those perturbations (tests/envelope.py).
 """
-import os
-
 import numpy as np
 import pytest
 
 pytest.importorskip("torch")
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("SPI_GPU_SWEEPS") != "1",
-                                 reason="opt-in: set SPI_GPU_SWEEPS=1")]
+pytestmark = pytest.mark.gpu
 
 from oracle import port  # noqa: E402
+
+import envelope  # noqa: E402
 
 
 def test_neb_select_sweep(golden):
@@ -138,3 +140,75 @@ def test_multi_step_sweep(golden):
             for lab, f in flds.items():
                 e = _err(f, g[p + "out_" + lab])
                 assert e <= tol, (tag, precision, lab, e)
+
+
+def test_interp_sweep(golden):
+    """The step engine on the 80 one-group _get_interp runs
+    (tests/golden/interp_sweep.npz): OK (with variance) / SK / EDK with 1
+    to 3 drifts / IDW / NNB, nests of up to three of the eight models,
+    cells on stations, flag-off and nugget-only steps. The reference got
+    its per-step flags as an argument; here the flagged steps come from a
+    run with min_value_to_interp_thresh -inf and the others from a run with
+    +inf (every step then takes the step mean)."""
+    import spinterps_gb300 as spi
+    g = golden
+    mvv = 1e-4
+    n_regular = n_singular = 0
+    sing_cells = sing_ok = 0
+    for i in g["w_cases"]:
+        p = f"w{i}_"
+        itype = str(g[p + "type"])
+        sx, sy, cx, cy, z = (g[p + k] for k in ("sx", "sy", "cx", "cy", "z"))
+        vgs = [str(v) for v in g[p + "vgs"]]
+        flags = g[p + "flags"].astype(bool)
+        sd, cd = g.get(p + "sd"), g.get(p + "cd")
+        ref_est = g[p + "est"]
+        ref_var = g.get(p + "var")
+        m = ("IDW", float(g[p + "idw_exp"])) if itype == "IDW" else itype
+        args = port.interp_args_for([m], est_vars=itype == "OK")
+        lab = args[0][2]
+        kw = dict(est_vars=itype == "OK", stn_drifts=sd, cell_drifts=cd, min_vg_val=mvv,
+                  intrp_dtype=np.float64)
+        on, prblm = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, min_var_thr=-np.inf, **kw)
+        off, _ = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, min_var_thr=np.inf, **kw)
+        want_prblm = g[p + "prblm"].tolist()
+        assert sorted(j for j in prblm if flags[j]) == want_prblm, i
+        for j in range(z.shape[0]):
+            got = (on if flags[j] else off)[lab][j]
+            want = ref_est[j]
+            if itype == "NNB":
+                assert np.array_equal(got, want, equal_nan=True), (i, j)
+                continue
+            scale = max(float(np.nanmax(np.abs(want))), 1e-300) if np.isfinite(want).any() \
+                else 1.0
+            assert np.array_equal(np.isnan(got), np.isnan(want)), (i, j)
+            if itype == "IDW" or not flags[j] or port.check_full_nuggetness(vgs[j], mvv):
+                assert np.nanmax(np.abs(got - want), initial=0.0) <= 1e-9 * scale, (i, j)
+                if ref_var is not None and not flags[j]:
+                    assert np.all((on if flags[j] else off)["EST_VARS_OK"][j] == 0.0)
+                continue
+            idx = np.arange(sx.size)
+            lhs, rhs, d_cs = envelope.system(itype, sx, sy, idx, cx, cy, vgs[j], mvv, sd, cd)
+            sing, _ = envelope.singular_to_pinv(lhs)
+            rs = envelope.runs(lhs, rhs, sx.size, z[j][None], d_cs, itype == "OK", k=4,
+                               seed=int(i) * 10 + j)
+            if not sing:
+                n_regular += 1
+                de, dv = envelope.spread(rs, scale)
+                assert np.nanmax(np.abs(got - want), initial=0.0) \
+                    <= max(1e-9, 10 * de) * scale, (i, j, itype, vgs[j])
+                if ref_var is not None:
+                    gv = on["EST_VARS_OK"][j]
+                    vs = max(float(np.abs(ref_var[j]).max()), 1e-300)
+                    # the reference stores its variance in float32
+                    assert np.abs(gv - ref_var[j]).max() <= max(1e-6, 10 * dv) * vs, (i, j)
+            else:
+                n_singular += 1
+                ok = envelope.consistent(got[None], rs, z[j][None], d_cs, 1e-9 * scale)[0]
+                sing_cells += ok.size
+                sing_ok += int(ok.sum())
+    print(f"\ninterp sweep: {n_regular} regular kriging steps, {n_singular} singular "
+          f"({sing_ok} of {sing_cells} cells inside the reference's perturbed outcomes)")
+    assert n_regular >= 40
+    if sing_cells:
+        assert sing_ok >= 0.9 * sing_cells
