@@ -75,33 +75,62 @@ KW = dict(est_vars=True, min_var_thr=0.0, min_var_cut=0.0, max_var_cut=None, min
 
 # ---------------------------------------------------------------- CPU side
 def _cpu_worker(args):
-    """One worker of the CPU baseline: the oracle on a block of cells for a
-    few steps (BLAS pinned to one thread, as the reference's driver does)."""
+    """One worker of the CPU baseline: the oracle on one step of the workload
+    over two cell samples (BLAS pinned to one thread, as the reference's
+    driver does). Returns the two wall times."""
     os.environ["OMP_NUM_THREADS"] = "1"
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
     os.environ["MKL_NUM_THREADS"] = "1"
-    sx, sy, z, cx, cy, vgs, iargs = args
+    sx, sy, z, cx, cy, vgs, iargs, sizes = args
     from oracle import port
-    t0 = time.perf_counter()
-    port.interp_steps(sx, sy, z, cx, cy, vgs, iargs, **KW)
-    return time.perf_counter() - t0, z.shape[0] * cx.size
+    out = []
+    for c in sizes:
+        t0 = time.perf_counter()
+        port.interp_steps(sx, sy, z, cx[:c], cy[:c], vgs, iargs, **KW)
+        out.append(time.perf_counter() - t0)
+    return out
 
 
-def cpu_baseline(w, n_cells=4096, steps_per_worker=4, cores=None):
-    """Time the oracle over all host cores on a bounded sample: each worker
-    takes steps_per_worker different steps and a contiguous block of
-    n_cells cells (spread over the grid)."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    import platform
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline(w, sizes=(512, 4096), cores=None, step0=0):
+    """The oracle (the reference's algorithm, its per-cell pinv loop
+    included) over all host cores, one step per worker process, each step
+    run on two cell samples of the workload's grid. Per worker the step's
+    fixed cost a (station matrices, the two pinv SVDs of OK and SK) and its
+    per-cell cost b are fitted from the two timings, and a whole step of the
+    workload's C cells costs a + b C: throughput = cores C / mean(a + b C).
+    The system solves are thus spread over all C cells, as in a real run."""
     import multiprocessing as mp
     cores = cores or os.cpu_count()
     iargs = interp_args()
     jobs = []
     C = w["cx"].size
-    for k in range(cores):
-        steps = [(k * steps_per_worker + i) % w["z"].shape[0] for i in range(steps_per_worker)]
-        c0 = (k * 7919 * n_cells) % (C - n_cells)
-        sl = slice(c0, c0 + n_cells)
-        jobs.append((w["sx"], w["sy"], w["z"][steps], w["cx"][sl], w["cy"][sl],
-                     [w["vgs"][s] for s in steps], iargs))
+    T = w["z"].shape[0]
+    steps = [(step0 + k * 37) % T for k in range(cores)]
+    for k, st in enumerate(steps):
+        # a contiguous block of the grid (rows of cells), spread over workers
+        c0 = (k * 7919 * max(sizes)) % (C - max(sizes))
+        sl = slice(c0, c0 + max(sizes))
+        jobs.append((w["sx"], w["sy"], w["z"][[st]], w["cx"][sl], w["cy"][sl],
+                     [w["vgs"][st]], iargs, tuple(sizes)))
     ctx = mp.get_context("spawn")
     # one BLAS thread per worker process (the reference's driver does the
     # same, interp/main.py:31-33); set before the children import numpy
@@ -120,11 +149,21 @@ def cpu_baseline(w, n_cells=4096, steps_per_worker=4, cores=None):
                 os.environ.pop(k, None)
             else:
                 os.environ[k] = v
-    cell_steps = sum(r[1] for r in res)
-    return {"value": cell_steps / wall, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} workers x {steps_per_worker} steps x {n_cells} cells "
-                      f"({cell_steps} cell-steps, OK+var, SK, IDW p=2; oracle restating the "
-                      f"reference's per-cell pinv loop), wall {wall:.1f} s"}
+    c1, c2 = sizes
+    b = np.array([max((t2 - t1) / (c2 - c1), 0.0) for t1, t2 in res])
+    a = np.array([max(t1 - bb * c1, 0.0) for (t1, _), bb in zip(res, b)])
+    t_step = a + b * C
+    value = cores * C / float(np.mean(t_step))
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(), "seed": SEED,
+            "sample": f"{cores} workers, one step each (steps {steps[0]}, {steps[1]}, ...), "
+                      f"each run on {c1} and {c2} cells of the grid (OK+var, SK, IDW p=2; the "
+                      f"oracle restating the reference's per-cell pinv loop); per step a fixed "
+                      f"cost a (mean {np.mean(a):.2f} s: station matrices and the OK and SK "
+                      f"pinv) and a per-cell cost b (mean {np.mean(b) * 1e3:.3f} ms) fitted per "
+                      f"worker, extrapolated to the workload's {C} cells per step: "
+                      f"cores * C / mean(a + b C); wall {wall:.1f} s",
+            "fixed_s_per_step": float(np.mean(a)), "ms_per_cell": float(np.mean(b) * 1e3)}
 
 
 # ---------------------------------------------------------------- clocks
@@ -393,16 +432,22 @@ def run_ours(args):
                         **KW)
         pm.execute()
         fm = pm.fields(numpy=False)
-        errs = {}
-        for lab in f64:
-            x, y = fm[lab].double(), f64[lab].double()
-            m = torch.isfinite(y)
-            sc = y[m].abs().max()
-            d = (x[m] - y[m]).abs()
-            errs[lab] = {"max": float(d.max() / sc), "rms": float(d.pow(2).mean().sqrt() / sc)}
+        errs = {lab: field_errors(fm[lab], f64[lab]) for lab in f64}
         fp64 = {"value": len(sub) * C / (a.elapsed_time(b) / 1e3), "unit": UNIT,
                 "sample": f"{len(sub)} evenly spaced steps, all cells",
-                "mixed_err_vs_fp64": errs}
+                "mixed_err_vs_fp64": errs,
+                "error_definition": "max / rms: |mixed - fp64| over the field's largest "
+                                    "magnitude; per_cell: |mixed - fp64| / |fp64| over cells "
+                                    "above the stated floor"}
+        del p64, pm
+    # the largest configuration (4000 stations, EDK with two drifts, 2000 x
+    # 2000 cells, learned variograms), one wave of its steps
+    large = None
+    if rank == 0 and not args.no_large:
+        del plans
+        torch.cuda.empty_cache()
+        large = large_leg(args, args.large_reps, fp64_every=args.large_fp64_every, e2e=True,
+                          clocks=False)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -426,7 +471,9 @@ def run_ours(args):
                            for k, v in probe.items()}},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
-                    "ms": float(np.median(e2e_ms)) if e2e_ms else None},
+                    "ms": float(np.median(e2e_ms)) if e2e_ms else None,
+                    "repeats_ms": [float(x) for x in e2e_ms],
+                    "statistic": f"median of {len(e2e_ms)} calls"},
             "gpu_launches": launches,
             "roofline": roofline,
             "roofline_tensor_kernel": roofline_tc,
@@ -435,6 +482,7 @@ def run_ours(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "fp64_path": fp64,
+            "large": large,
         }
         print(json.dumps(line))
     if world > 1:
@@ -530,15 +578,37 @@ def run_fit(args):
     print(json.dumps(line))
 
 
-def run_large(args):
+def field_errors(x, y, floor_frac=1e-3):
+    """Errors of field x against the FP64 field y (torch tensors, NaN =
+    no value): max and RMS of |x - y| relative to y's largest magnitude,
+    and per-cell relative errors |x - y| / |y| over the cells with |y| at
+    least floor_frac of that magnitude."""
+    import torch
+    x, y = x.double(), y.double()
+    m = torch.isfinite(y)
+    sc = y[m].abs().max()
+    d = (x[m] - y[m]).abs()
+    yy = y[m].abs()
+    big = yy >= floor_frac * sc
+    rel = d[big] / yy[big]
+    return {"max": float(d.max() / sc), "rms": float(d.pow(2).mean().sqrt() / sc),
+            "per_cell": {"floor": f"|y| >= {floor_frac:g} x max|y|", "cells": int(big.sum()),
+                         "max": float(rel.max()) if rel.numel() else None,
+                         "rms": float(rel.pow(2).mean().sqrt()) if rel.numel() else None}}
+
+
+def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
     """The large hourly EDK configuration on one wave of steps: 4000
     stations in a 500 km box, per-station missingness U(0.05, 0.5), two
     drifts (fBm elevation, easting), a 2000 x 2000 grid at 250 m, float32
     fields; each step's variogram from the learned warm start with cold-fit
-    fallback (timed apart). Mixed and plain FP64 paths run the same plan;
-    the line reports both, their ratio and the mixed path's error."""
+    fallback (timed apart). The mixed path runs the whole wave ``reps``
+    times; the plain FP64 path runs every ``fp64_every``-th step of it once
+    (both rates are per cell-step: every step has its own system), and the
+    mixed fields of those steps are compared with it."""
     import torch
     from spinterps_gb300 import fitvgs, synth, warmstart
+    import spinterps_gb300 as spi
     from spinterps_gb300.steps import InterpPlan
     from spinterps_gb300.steps import interp_args_for
     T = args.large_steps
@@ -559,65 +629,105 @@ def run_large(args):
     kw = dict(stn_drifts=w["stn_drift"], cell_drifts=w["cell_drift"], min_vg_val=1e-4,
               intrp_dtype=np.float32, arena_budget=96 << 30)
 
-    def timed(plan, reps):
-        evs, tot = [], 0.0
-        for _ in range(reps):
+    def timed(plan, n):
+        evs, tot = [], []
+        for _ in range(n):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             a.record()
             ev = plan.execute(timing=True)
             b.record()
             torch.cuda.synchronize()
-            tot += a.elapsed_time(b)
+            tot.append(a.elapsed_time(b))
             evs.append(ev)
-        cells_ms = sum(v[0] for ev in evs for v in plan.kernel_times(ev).values())
-        return tot / reps, cells_ms / reps
+        times = {}
+        for ev in evs:
+            for k, (t_ms, n_l, fl) in plan.kernel_times(ev).items():
+                t = times.setdefault(k, [0.0, 0, 0.0])
+                t[0] += t_ms
+                t[1] += n_l
+                t[2] += fl
+        return float(np.median(tot)), tot, times
 
     pm = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], vgs, iargs, precision="mixed",
                     **kw)
     pm.execute()
-    with Clocks(0) as clk:
-        ms_m, cells_m = timed(pm, args.steps)
+    clk = Clocks(0) if clocks else None
+    if clk:
+        clk.__enter__()
+    ms_m, all_m, times_m = timed(pm, reps)
+    if clk:
+        clk.__exit__()
+    launches = pm.launches_per_execute()
     info = pm.collect_info()
     cond = np.array(list(info["cond"]["EDK"].values()))
-    fm = pm.flds["EDK"]
-    # the tier each step ran in, as the probe decided it
     n_fast = len(info.get("fp32_tier_steps", {}).get("EDK", []))
     n_cap = int(np.sum(cond <= pm.cond_split))
+    sub = np.arange(0, T, fp64_every)
+    fm = pm.flds["EDK"][torch.as_tensor(sub, device=pm.flds["EDK"].device)].clone()
     del pm
     torch.cuda.empty_cache()
-    if args.skip_fp64:
-        ms_64 = cells_64 = float("nan")
-        err = None
-    else:
-        p64 = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], vgs, iargs,
-                         precision="fp64", **kw)
-        ms_64, cells_64 = timed(p64, 1)
-        f64 = p64.flds["EDK"]
-        m = torch.isfinite(f64)
-        sc = f64[m].double().abs().max()
-        dd = (fm[m].double() - f64[m].double()).abs()
-        err = {"max": float(dd.max() / sc), "rms": float(dd.pow(2).mean().sqrt() / sc)}
-    n_av = np.isfinite(w["z"]).sum(1)
-    line = {"metric": METRIC, "value": T * C / (ms_m / 1e3), "unit": UNIT, "n_gpus": 1,
+    err = fp64 = None
+    if not args.skip_fp64:
+        p64 = InterpPlan(w["sx"], w["sy"], w["z"][sub], w["cx"], w["cy"], [vgs[i] for i in sub],
+                         iargs, precision="fp64", **kw)
+        ms_64, _, times_64 = timed(p64, 1)
+        err = field_errors(fm, p64.flds["EDK"])
+        fp64 = {"value": len(sub) * C / (ms_64 / 1e3), "unit": UNIT, "ms": ms_64,
+                "sample": f"every {fp64_every}th step of the wave ({len(sub)} steps), all cells",
+                "kernels_ms": {k: v[0] for k, v in times_64.items()}}
+        del p64
+        torch.cuda.empty_cache()
+    e2e_val = None
+    if e2e:
+        zh = np.asarray(w["z"].cpu().numpy() if hasattr(w["z"], "cpu") else w["z"])
+        host = {k: (v.cpu().numpy() if hasattr(v, "cpu") else np.asarray(v))
+                for k, v in w.items() if k in ("sx", "sy", "cx", "cy", "stn_drift",
+                                               "cell_drift")}
+        kwh = dict(kw, stn_drifts=host["stn_drift"], cell_drifts=host["cell_drift"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        spi.interp_steps(host["sx"], host["sy"], zh, host["cx"], host["cy"], vgs, iargs,
+                         precision="mixed", **kwh)
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3
+        e2e_val = {"value": T * C / (e2e_ms / 1e3), "unit": UNIT, "ms": e2e_ms,
+                   "h2d_bytes_per_step": int(zh.nbytes + sum(v.nbytes for v in host.values())),
+                   "d2h_bytes_per_step": int(4 * T * C)}
+    kernels = {k: {"ms": v[0], "launches": v[1], "achieved_tflops": v[2] / (v[0] / 1e3) / 1e12}
+               for k, v in times_m.items() if v[0] > 0}
+    dom_k = max(kernels, key=lambda k: kernels[k]["ms"])
+    n_av = np.isfinite(np.asarray(w["z"].cpu() if hasattr(w["z"], "cpu") else w["z"])).sum(1)
+    out = {"value": T * C / (ms_m / 1e3), "unit": UNIT, "ms_per_execution": ms_m,
+           "executions_ms": all_m,
+           "config": {"workload": f"large_edk_4000stn_{T}of8760steps_{args.large_nx}x"
+                                  f"{args.large_nx}", "stations": 4000,
+                      "steps": T, "cells": C, "methods": ["EDK (elevation, easting)"],
+                      "stations_per_step": [int(n_av.min()), int(n_av.max())],
+                      "output": "float32", "vgs": "learned warm start, cold-fit fallback"},
+           "fp64_path": fp64,
+           "mixed_over_fp64": (T * C / (ms_m / 1e3)) / fp64["value"] if fp64 else None,
+           "mixed_err_vs_fp64": err, "e2e": e2e_val, "gpu_launches": launches,
+           "kernels": kernels, "roofline": roofline_for(dom_k, kernels[dom_k]),
+           "tiers": {"fp32": n_fast, "fp64": int(cond.size - n_fast), "cond_under_cap": n_cap,
+                     "cond_median": float(np.median(cond)), "cond_max": float(cond.max())},
+           "fit": {"seconds": t_fit, "fallback_steps": len(det["_fallback_steps"]),
+                   "de_ms": det["_de_ms"], "ms": det["_ms"]},
+           "synthesis_s": t_gen}
+    if clk:
+        out["clocks"] = clk.summary()
+    return out
+
+
+def run_large(args):
+    """The large configuration alone: its own JSON line (every step through
+    both paths)."""
+    d = large_leg(args, args.steps, fp64_every=1, e2e=False)
+    line = {"metric": METRIC, "value": d["value"], "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "higher_is_better": True, "dtype": "f32+f64",
             "data": "synthetic (seeded; shapes and distributions of the reference's large hourly "
-                    "configuration)",
-            "config": {"workload": f"large_edk_4000stn_{T}of8760steps_{args.large_nx}x"
-                                   f"{args.large_nx}", "stations": 4000,
-                       "steps": T, "cells": C, "methods": ["EDK (elevation, easting)"],
-                       "stations_per_step": [int(n_av.min()), int(n_av.max())],
-                       "output": "float32", "vgs": "learned warm start, cold-fit fallback"},
-            "ms_per_execution": ms_m, "cells_kernel_ms": cells_m,
-            "fp64_path": {"value": T * C / (ms_64 / 1e3), "unit": UNIT, "ms": ms_64,
-                          "cells_kernel_ms": cells_64},
-            "mixed_over_fp64": ms_64 / ms_m, "mixed_err_vs_fp64": err,
-            "tiers": {"fp32": n_fast, "fp64": int(cond.size - n_fast),
-                      "cond_under_cap": n_cap,
-                      "cond_median": float(np.median(cond)), "cond_max": float(cond.max())},
-            "fit": {"seconds": t_fit, "fallback_steps": len(det["_fallback_steps"]),
-                    "de_ms": det["_de_ms"], "ms": det["_ms"]},
-            "synthesis_s": t_gen, "clocks": clk.summary()}
+                    "configuration)"}
+    line.update({k: v for k, v in d.items() if k not in ("value", "unit")})
     print(json.dumps(line))
 
 
@@ -814,8 +924,10 @@ def run_reference(args):
         return
     w = make_workload()
     vals = []
-    for _ in range(args.warmup + args.steps):
-        vals.append(cpu_baseline(w, steps_per_worker=1))  # ~3 s of work per core per step
+    for i in range(args.warmup + args.steps):
+        # each bench step: one pool over all host cores, a different step
+        # of the workload per worker (about 5 s)
+        vals.append(cpu_baseline(w, step0=i))
     timed = vals[args.warmup:]
     v = float(np.median([x["value"] for x in timed]))
     cb = dict(timed[0])
@@ -838,7 +950,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-large", action="store_true",
+                    help="leave the large configuration out of the default line")
+    ap.add_argument("--large-reps", type=int, default=2)
+    ap.add_argument("--large-fp64-every", type=int, default=4)
     ap.add_argument("--fp64-steps", type=int, default=4)
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--fit", action="store_true",

@@ -165,6 +165,13 @@ typedef struct {
 
 /* Maximum drifts of EDK (a = 1 + n_drift Lagrange/drift rows). */
 #define SPI_MAX_DRIFT 7
+/* Largest exact-inverse system (rows m = n + Lagrange / drift rows) that
+ * spi_krige_factor checks against numpy.linalg.pinv's cut-off, and the
+ * scratch (doubles) that check needs: SPI_PINV_SLOTS systems at once, each
+ * two m x m matrices. */
+#define SPI_PINV_MAX_M 256
+#define SPI_PINV_SLOTS 16
+#define SPI_PINV_SCRATCH_DOUBLES (SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M)
 
 /* Per-batch workspace of the kriging entry points (device arrays, caller
  * owned). Arenas hold one matrix per system at sys->mat_off[s], sized for
@@ -207,6 +214,13 @@ typedef struct {
                             variance pass (P r, 2 m^2 FLOP per cell) ran;
                             it runs only where a cell of the tile passes
                             the sum check (NULL: not counted) */
+    double *pinv_scratch; /* optional, SPI_PINV_SCRATCH_DOUBLES doubles: lets
+                            spi_krige_factor take numpy.linalg.pinv's answer
+                            for exact-inverse systems of m <= SPI_PINV_MAX_M
+                            rows that pinv treats as singular (see
+                            spi_krige_factor); NULL: Gauss-Jordan only */
+    int32_t *pinv_used;  /* optional [n_sys]: 1 where that pinv replaced the
+                            Gauss-Jordan inverse, else 0 */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -221,8 +235,24 @@ typedef struct {
  * exact-inverse path (route 1): the reference's own saddle matrix
  * (interp/steps.py:170-243) is inverted in place by Gauss-Jordan with
  * partial pivoting, i.e. numpy.linalg.pinv (interp/steps.py:351) without
- * its 1e-15 singular-value cut-off, which is the same matrix whenever the
- * cut-off removes nothing. An exactly singular saddle matrix gives route 2. */
+ * its singular-value cut-off (1e-15 * s_max, numpy's default rcond), which
+ * is the same matrix whenever the cut-off removes nothing. On the
+ * exact-inverse path ws->cond holds ||M||_F ||P||_F (M the saddle matrix,
+ * P its computed inverse), an upper bound of M's condition number.
+ * With ws->pinv_scratch, a system of m <= SPI_PINV_MAX_M rows whose
+ * Gauss-Jordan inverse failed (a zero pivot) or whose ||M||_F ||P||_F
+ * exceeds 1e15 -- those pinv may cut -- is also diagonalised by a
+ * parallel cyclic Jacobi eigen-decomposition (M is symmetric, so its
+ * singular values are the |eigenvalues|). When the spectrum has
+ * eigenvalues under pinv's cut-off 1e-15 max|lambda| and none within a
+ * factor 30 of it either side (a rank deficiency with a gap: duplicated
+ * stations, drifts collinear with the constant, badly scaled unbounded
+ * models), pinv's answer is stable and the truncated pseudo-inverse
+ * V diag(1/lambda) V' replaces the Gauss-Jordan inverse (route 1,
+ * ws->pinv_used = 1); without a gap the cut falls inside rounding noise, no
+ * solver reproduces the reference's pinv there, and the Gauss-Jordan
+ * inverse is kept. Without the scratch (or above SPI_PINV_MAX_M), an exactly
+ * singular saddle matrix gives route 2. */
 int spi_krige_factor(const spi_domain_t *dom, const spi_systems_t *sys,
                      const spi_krige_ws_t *ws, double cond_max,
                      spi_stream_t stream);
@@ -480,7 +510,7 @@ int spi_mlp_adam(float *params, const float *grad, float *m, float *v, int64_t n
 /* Limits of spi_krige_ok_noalloc and the size of its static scratch. */
 #define SPI_NOALLOC_MAX_STNS 512
 #define SPI_NOALLOC_MAX_STEPS 64
-#define SPI_NOALLOC_SCRATCH_BYTES 4629248  /* 4.4 MiB on every GPU that loads the library */
+#define SPI_NOALLOC_SCRATCH_BYTES 5678080  /* 5.4 MiB on every GPU that loads the library */
 
 /* No counterpart in the reference. Ordinary kriging (estimate, and the OK
  * variance when want_var) of ONE station set, n <= SPI_NOALLOC_MAX_STNS
@@ -503,7 +533,9 @@ int spi_mlp_adam(float *params, const float *grad, float *m, float *v, int64_t n
  * Every call shares the one array: calls that overlap on the GPU (other
  * streams or host threads) race and must be serialised by the caller.
  * route_out (optional, device, one int32): the system's route, written in
- * stream order -- 0 Cholesky, 1 exact inverse, 2 exactly singular: every
+ * stream order -- 0 Cholesky, 1 exact inverse (numpy.linalg.pinv's
+ * truncated inverse where spi_krige_factor's pinv check takes it: systems
+ * of up to SPI_PINV_MAX_M rows), 2 singular without that check: every
  * cell then took its nearest station and the estimate variance is 0, and
  * the step is one the reference reports as a problem step
  * (interp/steps.py:363-384). Without route_out such steps are not

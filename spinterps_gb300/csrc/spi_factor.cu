@@ -15,8 +15,13 @@
 // 32-wide block of FMAs.
 #include "spi_common.cuh"
 #include "spi_gj.cuh"
+#include "spi_saddle.cuh"
 
 namespace spi {
+
+// Resolves routes 3 / 4 left by k_gj (spi_pinv.cu).
+int launch_pinv(const spi_domain_t& dom, const spi_systems_t& sys, const spi_krige_ws_t& ws,
+                cudaStream_t st);
 
 constexpr int NB = 32;        // panel width of the blocked factorisations
 constexpr int FT = 256;       // threads per factor CTA
@@ -36,6 +41,19 @@ __device__ __forceinline__ SysView sys_view(const spi_systems_t& sys, int s) {
   v.idx = sys.stn_idx + v.off;
   v.moff = sys.mat_off[s];
   return v;
+}
+
+// Sum of one value per thread over the block (all threads call it).
+__device__ double block_sum(double t, double* red) {
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = t;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += red[w];
+  __syncthreads();
+  return r;
 }
 
 // A[i, j] for i >= j. The reference fills the upper triangle of the full
@@ -276,14 +294,19 @@ __global__ __launch_bounds__(FT) void k_trinv(spi_systems_t sys, const double* _
 // [[Gamma, F], [F', 0]] (interp/steps.py:170-243; SK: the covariance
 // matrix) inverted in place by Gauss-Jordan with partial pivoting (first
 // row of maximum |pivot|), columns unscrambled in reverse pivot order.
-// That is numpy.linalg.pinv (interp/steps.py:351) whenever pinv's 1e-15
-// singular-value cut-off removes nothing. Dynamic shared memory: m pivot
-// factors + m pivot indices.
+// That is numpy.linalg.pinv (interp/steps.py:351) whenever pinv's
+// singular-value cut-off (1e-15 s_max, numpy's default) removes nothing,
+// which holds while ||M||_F ||P||_F <= 1e15; cond[s] receives that
+// product. With
+// pinv_on, systems of m <= SPI_PINV_MAX_M rows above it (or with a zero
+// pivot) are left to k_pinv (route 3: inverse valid, 4: Gauss-Jordan
+// failed). Dynamic shared memory: m pivot factors + m pivot indices.
 __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
                                           double* __restrict__ l_arena,
                                           const int32_t* __restrict__ status,
-                                          const double* __restrict__ cond,
-                                          int32_t* __restrict__ route, double cond_max) {
+                                          double* __restrict__ cond,
+                                          int32_t* __restrict__ route, double cond_max,
+                                          int pinv_on) {
   const int s = blockIdx.x;
   const int tid = threadIdx.x;
   if (status[s] == 0 && cond[s] <= cond_max) {
@@ -301,27 +324,31 @@ __global__ __launch_bounds__(FT) void k_gj(spi_domain_t dom, spi_systems_t sys,
   double* f = gsm;                                   // [m]
   double* prow = gsm + m;                            // [m] the scaled pivot row
   int* piv = reinterpret_cast<int*>(gsm + 2 * m);    // [m]
-  // saddle matrix, full storage
+  __shared__ double red[FT / 32];
+  // saddle matrix, full storage, and its squared Frobenius norm
+  double fm = 0.0;
   for (int64_t e = tid; e < (int64_t)m * m; e += FT) {
-    int i = (int)(e / m), j = (int)(e - (int64_t)i * m);
-    double val;
-    if (i < n && j < n) {
-      int lo = min(i, j), hi = max(i, j);
-      int sl = v.idx[lo], sh = v.idx[hi];
-      double d = dist_f64(dom.stn_x[sl], dom.stn_y[sl], dom.stn_x[sh], dom.stn_y[sh]);
-      val = vg_fill_f64(vg, d, sk, dom.min_vg_val);
-    } else if (i >= n && j >= n) {
-      val = 0.0;
-    } else {
-      int st = (i < n) ? v.idx[i] : v.idx[j];
-      int k = (i < n) ? (j - n) : (i - n);
-      val = (k == 0) ? 1.0 : dom.stn_drift[(int64_t)st * dom.n_drift + (k - 1)];
-    }
+    const int i = (int)(e / m), j = (int)(e - (int64_t)i * m);
+    const double val = saddle_entry(dom, vg, v.idx, n, sk, i, j);
     A[e] = val;
+    fm += val * val;
   }
-  __syncthreads();
+  fm = block_sum(fm, red);
   const int fail = gj_invert<FT>(A, m, f, prow, piv);
-  if (tid == 0) route[s] = fail ? 2 : 1;
+  double fp = 0.0;
+  if (!fail)
+    for (int64_t e = tid; e < (int64_t)m * m; e += FT) fp += A[e] * A[e];
+  fp = block_sum(fp, red);
+  if (tid == 0) {
+    const double cg = sqrt(fm) * sqrt(fp);
+    cond[s] = fail ? __longlong_as_double(0x7ff0000000000000LL) : cg;
+    // pinv (default rcond 1e-15) cuts nothing while cond_2 <= cg <= 1e15
+    const bool suspect = fail || !(cg <= 1e15);
+    if (pinv_on && m <= SPI_PINV_MAX_M && suspect)
+      route[s] = fail ? 4 : 3;
+    else
+      route[s] = fail ? 2 : 1;
+  }
 }
 
 // y = X x (X lower, row-major n x n): warp per row, lanes along the row.
@@ -948,9 +975,16 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
       cudaFuncSetAttribute(k_gj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm) !=
           cudaSuccess)
     return SPI_ERR_CUDA;
+  const int pinv_on = ws->pinv_scratch != nullptr;
   k_gj<<<sys->n_sys, FT, gsm, st>>>(d, sy, ws->l_arena, ws->status, ws->cond, ws->route,
-                                    cond_max);
+                                    cond_max, pinv_on);
   SPI_LAUNCH_CHECK();
+  if (ws->pinv_used) {
+    if (cudaMemsetAsync(ws->pinv_used, 0, sizeof(int32_t) * (size_t)sys->n_sys, st) !=
+        cudaSuccess)
+      return SPI_ERR_CUDA;
+  }
+  if (pinv_on) return launch_pinv(d, sy, *ws, st);
   return SPI_OK;
 }
 

@@ -14,7 +14,9 @@
 // the system was exactly singular and every cell took its nearest station.
 //
 // The array holds one system of at most SPI_NOALLOC_MAX_STNS stations and
-// SPI_NOALLOC_MAX_STEPS steps (see spinterps_gb300.h); it is reserved on
+// SPI_NOALLOC_MAX_STEPS steps, and one slot of the pinv check that
+// spi_krige_factor runs on exact-inverse systems of up to SPI_PINV_MAX_M
+// rows (see spinterps_gb300.h); it is reserved on
 // every GPU that loads this library, until the process exits. Every call
 // shares it: calls whose work overlaps on the GPU (other streams, other
 // host threads) race on it and must be serialised by the caller.
@@ -50,7 +52,11 @@ constexpr size_t OFF_VALOFF = OFF_STEPOFF + al(2 * 8);
 constexpr size_t OFF_STEPS = OFF_VALOFF + al((size_t)MAXT * 8);
 constexpr size_t OFF_OUTROW = OFF_STEPS + al((size_t)MAXT * 4);
 constexpr size_t OFF_VG = OFF_OUTROW + al((size_t)MAXT * 4);
-constexpr size_t SCRATCH_BYTES = OFF_VG + al(sizeof(spi_vg_t));
+// one slot of the pinv check (spi_krige_factor): a one-system batch uses
+// slot 0 only
+constexpr size_t OFF_PINV = OFF_VG + al(sizeof(spi_vg_t));
+constexpr size_t OFF_PUSED = OFF_PINV + al((size_t)2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M * 8);
+constexpr size_t SCRATCH_BYTES = OFF_PUSED + al(4);
 
 static_assert(SCRATCH_BYTES == SPI_NOALLOC_SCRATCH_BYTES,
               "SPI_NOALLOC_SCRATCH_BYTES in spinterps_gb300.h is out of date");
@@ -153,6 +159,8 @@ extern "C" int spi_krige_ok_noalloc(const spi_domain_t* dom, const int32_t* stn_
   ws.g_cols = reinterpret_cast<double*>(base + OFF_GCOLS);
   ws.s_inv = reinterpret_cast<double*>(base + OFF_SINV);
   ws.g_colsum = reinterpret_cast<double*>(base + OFF_GSUM);
+  ws.pinv_scratch = reinterpret_cast<double*>(base + OFF_PINV);
+  ws.pinv_used = reinterpret_cast<int32_t*>(base + OFF_PUSED);
   spi_domain_t d = *dom;
   d.n_drift = 0;  // ordinary kriging: the unbiasedness row only
   if ((rc = spi_krige_factor(&d, &sy, &ws, 1e13, stream))) return rc;

@@ -234,7 +234,7 @@ class _KrigeBatch:
     """One chunk of kriging systems: device descriptors and workspaces."""
 
     def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
-                 want_var=False, tensor_cores=True, n_probe=0, need_linv=None):
+                 want_var=False, tensor_cores=True, n_probe=0, need_linv=None, pinv=None):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -281,6 +281,7 @@ class _KrigeBatch:
         self.g_colsum = torch.zeros(n_sys * nat.GA, dtype=torch.float64, device=dev)
         self.w_hat = torch.zeros_like(self.vals)
         self.beta = beta
+        self.pinv = pinv
         self.split = None
         if precision == 1:
             # FP32 (hi, lo) pairs of Linv, G and w_hat for the split-precision kernel
@@ -322,10 +323,15 @@ class _KrigeBatch:
                 *[_ptr(t) for t in (self.split or [None] * 6)]]
         # cells of the exact-inverse variance passes that ran (main pass only)
         self.var_cells = torch.zeros(len(ch), dtype=torch.int32, device=dev)
-        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells))
+        # numpy.linalg.pinv's cut-off on the exact-inverse systems
+        # (spi_krige_factor with a pinv scratch): shared by the plan's
+        # batches, which run in stream order
+        self.pinv_used = torch.zeros(len(ch), dtype=torch.int32, device=dev)
+        pv = (_ptr(pinv), _ptr(self.pinv_used))
+        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells), *pv)
         self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None,
-                                     None)
-        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None, None)
+                                     None, *pv)
+        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None, None, *pv)
                             if self.probe_df else None)
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
@@ -526,6 +532,9 @@ class InterpPlan:
             # variances get 2.5x the estimates' tolerance (still 2x under the
             # 1e-5 bar): the tensor-core 3xTF32 term carries ~2e-6 of the sill
             self.probe_args = (self.pdom, probe_tol * est_scale, 2.5 * probe_tol * var_scale)
+        # scratch of the pinv check of exact-inverse systems (spi_krige_factor)
+        self.pinv = (torch.empty(nat.SPI_PINV_SCRATCH_DOUBLES, dtype=torch.float64, device=dev)
+                     if krig else None)
         if krig:
             vgs = np.asarray(vgs, dtype=object)
             assert np.all(vgs != "nan"), "NaN VGs not allowed!"
@@ -551,7 +560,8 @@ class InterpPlan:
                 beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
                 batches = [_KrigeBatch(dev, self.dom, kind, systems, ch, data, T, val_off, beta,
                                        prec, want_var=var is not None,
-                                       tensor_cores=tensor_cores, n_probe=n_probe)
+                                       tensor_cores=tensor_cores, n_probe=n_probe,
+                                       pinv=self.pinv)
                            for ch in _chunk_systems(systems, prec, arena_budget)]
                 fills = (
                     _fill_args(dev, self.single, self.single_val,
@@ -627,12 +637,13 @@ class InterpPlan:
 
     def collect_info(self):
         for kind, out, want_var, batches, fills, a in self.krig:
-            failed, routed, cond = [], [], {}
+            failed, routed, cond, pinv = [], [], {}, []
             for b in batches:
                 if b.tc_err is not None and int(b.tc_err.item()):
                     raise nat.SpiError("spi_krige_var_tc: a tensor-core wait timed out")
                 rt = b.route.cpu().numpy()
                 cn = b.cond.cpu().numpy()
+                pu = b.pinv_used.cpu().numpy()
                 for k, sl in enumerate(b.steps_l):
                     for j in sl:
                         cond[int(j)] = float(cn[k])
@@ -640,6 +651,8 @@ class InterpPlan:
                             failed.append(int(j))
                         elif rt[k] == 1:
                             routed.append(int(j))
+                            if pu[k]:
+                                pinv.append(int(j))
             fast, dfv, disc = [], [], []
             for b in batches:
                 if b.tier is not None:
@@ -657,13 +670,16 @@ class InterpPlan:
                 self.info.setdefault("probe_disc", {})[kind] = np.concatenate(disc)
             self.info["failed_steps"][kind] = sorted(failed)
             self.info.setdefault("exact_inverse_steps", {})[kind] = sorted(routed)
+            # exact-inverse steps whose inverse is pinv's truncated one
+            self.info.setdefault("pinv_steps", {})[kind] = sorted(pinv)
             self.info["cond"][kind] = cond
         return self.info
 
     def launches_per_execute(self):
         """Kernels of this library that one execute() launches, call by call
         as _KrigeBatch.run makes them: row fills; per batch the build,
-        Cholesky, inverse (or condition estimate) and Gauss-Jordan, the duals
+        Cholesky, inverse (or condition estimate), Gauss-Jordan and the pinv
+        check of the exact-inverse systems, the duals
         (plus two triangular-solve kernels without the inverse), the FP32
         splits, the probe (tensor-core and double-float variances, both
         tiers' cell kernels, the tier pick), the main variance kernels and
@@ -673,7 +689,7 @@ class InterpPlan:
         for kind, out, want_var, batches, fills, a in self.krig:
             n += sum(f is not None for f in fills)
             for b in batches:
-                n += 4
+                n += 4 + (b.pinv is not None)
                 n += 1 if b.X is not None else 3
                 if b.split is not None:
                     n += 2 + (b.X is not None)

@@ -23,9 +23,6 @@ import numpy as np
 
 from oracle import port
 
-EPS = np.finfo(np.float64).eps
-
-
 def system(kind, sx, sy, idx, cx, cy, vg, min_vg_val, stn_drifts=None, cell_drifts=None):
     """The reference's system for station subset ``idx``: (LHS [m, m], cell
     right-hand sides [C, m], cell-station distances [C, n]), built with the
@@ -43,10 +40,15 @@ def system(kind, sx, sy, idx, cx, cy, vg, min_vg_val, stn_drifts=None, cell_drif
 
 
 def singular_to_pinv(lhs):
-    """Whether pinv's default cut-off (max(M, N) * eps * s_max) drops a
-    singular value of ``lhs``, and its condition number."""
-    s = np.linalg.svd(lhs, compute_uv=False)
-    return bool((s <= max(lhs.shape) * EPS * s[0]).any()), float(s[0] / max(s[-1], 1e-300))
+    """Whether numpy.linalg.pinv's default cut-off (rcond 1e-15: singular
+    values <= 1e-15 s_max are dropped) drops a singular value of ``lhs``,
+    and its condition number. The singular values come from the same SVD
+    call pinv makes (with singular vectors): for an exactly singular
+    matrix the null singular value is rounding noise of a few eps s_max,
+    near the cut-off, and the SVD without vectors computes a different
+    one."""
+    s = np.linalg.svd(lhs, full_matrices=False)[1]
+    return bool((s <= 1e-15 * s[0]).any()), float(s[0] / max(s[-1], 1e-300))
 
 
 def outcome(P, rhs, n, vals, d_cs, want_var):

@@ -292,3 +292,58 @@ def test_mixed_without_tensor_cores():
                               tensor_cores=False, **kw)
     for lab in ref:
         assert _err(got[lab], ref[lab]) <= MIXED_TOL, lab
+
+
+def test_pinv_route_on_rank_deficient_systems():
+    """Exactly singular systems: a duplicated station (OK and SK with Exp,
+    Sph and Gau variograms) and an EDK drift equal to a constant. The
+    reference inverts them with numpy.linalg.pinv (interp/steps.py:351),
+    which drops singular values <= 1e-15 s_max; the null direction's
+    computed singular value is rounding noise of a few eps s_max, so
+    whether pinv drops it depends on the rounding of its SVD. Where the
+    oracle's pinv drops it (checked with the same SVD call) its answer is
+    the truncated pseudo-inverse's, which the exact-inverse route must give
+    (spi_krige_factor's pinv check), not a problem step: 1e-9 against the
+    oracle. Where it does not, the reference's answer is that of a matrix
+    with a ~1e15 entry-scale inverse, and the GPU's answer must be one of
+    the reference's outcomes under 1e-15 perturbations (tests/envelope.py)."""
+    import envelope
+    spi = _spi()
+    rng = np.random.default_rng(31)
+    n = 60
+    sx, sy = rng.uniform(0, 6e4, n), rng.uniform(0, 6e4, n)
+    sx[7], sy[7] = sx[6], sy[6]
+    gx, gy = np.meshgrid(np.arange(24) * 2500.0 + 1250.0, 6e4 - 1250.0 - np.arange(24) * 2500.0)
+    cx, cy = gx.ravel(), gy.ravel()
+    vgs = ["0.1 Nug(0.0) + 0.9 Exp(15000)", "1.2 Sph(25000)", "0.05 Nug(0.0) + 0.8 Gau(12000)"]
+    t = len(vgs)
+    z = 3.0 + rng.normal(size=(t, n))
+    const = dict(stn_drifts=np.full((n, 1), 5.0), cell_drifts=np.full((1, cx.size), 5.0))
+    zc = z.copy()
+    zc[:, 7] = np.nan  # no duplicate: the constant drift alone is singular
+    matched = 0
+    for kind, zz, drifts in (("OK", z, {}), ("SK", z, {}), ("EDK", zc, const)):
+        args = port.interp_args_for([kind], est_vars=kind == "OK")
+        kw = dict(est_vars=kind == "OK", min_var_thr=-np.inf, min_vg_val=1e-4,
+                  intrp_dtype=np.float64, **drifts)
+        ref, rp = port.interp_steps(sx, sy, zz, cx, cy, vgs, args, **kw)
+        got, gp, info = spi.interp_steps(sx, sy, zz, cx, cy, vgs, args, return_info=True, **kw)
+        assert gp == rp == [], kind
+        assert info["pinv_steps"][kind] == [0, 1, 2], (kind, info["pinv_steps"])
+        idx = np.where(np.isfinite(zz[0]))[0]
+        for j, vg in enumerate(vgs):
+            lhs, rhs, d_cs = envelope.system(kind, sx, sy, idx, cx, cy, vg, 1e-4,
+                                             drifts.get("stn_drifts"),
+                                             drifts.get("cell_drifts"))
+            cut, _ = envelope.singular_to_pinv(lhs)
+            if cut:
+                matched += 1
+                for lab in ref:
+                    scale = max(float(np.abs(ref[lab][j]).max()), 1e-300)
+                    e = float(np.abs(got[lab][j] - ref[lab][j]).max()) / scale
+                    assert e <= FP64_TOL, (kind, vg, lab, e)
+            else:
+                rs = envelope.runs(lhs, rhs, idx.size, zz[j, idx][None], d_cs, kind == "OK")
+                ok = envelope.consistent(got[kind][j][None], rs, zz[j, idx][None], d_cs, 1e-9)
+                assert ok.mean() >= 0.98, (kind, vg, ok.mean())
+    assert matched >= 3

@@ -23,7 +23,10 @@ def entry_kernels(name, batch):
     """Kernel launches per call of each entry point _KrigeBatch.run uses
     (csrc/spi_factor.cu, spi_cells.cu, spi_var_tc.cu, spi_var_df.cu)."""
     if name == "spi_krige_factor":
-        return 4  # build, Cholesky, inverse or condition estimate, Gauss-Jordan
+        # build, Cholesky, inverse or condition estimate, Gauss-Jordan, and
+        # the pinv check of exact-inverse systems when the batch has its
+        # scratch
+        return 4 + (batch.pinv is not None)
     if name == "spi_krige_duals":
         return 1 if batch.X is not None else 3  # + the two triangular-solve kernels
     return {"spi_split_f64": 1, "spi_krige_var_tc": 1, "spi_krige_var_df": 1,
@@ -39,8 +42,10 @@ def make_batch(kind, precision, want_var, n_probe, tensor_cores=True):
     dom = types.SimpleNamespace(C=C, st=nat.DomainT())
     val_off = np.zeros(T, dtype=np.int64)
     beta = torch.zeros(T * nat.GA, dtype=torch.float64)
+    pinv = torch.empty(8, dtype=torch.float64)
     b = steps._KrigeBatch("cpu", dom, kind, systems, [0, 1], data, T, val_off, beta, precision,
-                          want_var=want_var, tensor_cores=tensor_cores, n_probe=n_probe)
+                          want_var=want_var, tensor_cores=tensor_cores, n_probe=n_probe,
+                          pinv=pinv)
     return dom, b
 
 
@@ -131,7 +136,8 @@ def test_plan_dry_run(monkeypatch, precision):
 
     def kernels(name, a):
         if name == "spi_krige_factor":
-            return 4
+            # + the pinv check when the workspace carries its scratch
+            return 4 + bool(a[2]._obj.pinv_scratch)
         if name == "spi_krige_duals":
             return 1 if a[3]._obj.linv_arena else 3
         return 1
