@@ -65,6 +65,122 @@ def make_workload(seed=SEED, n_stns=1000, n_steps=365, nx=1000, ny=1000, cell=25
     return dict(sx=sx, sy=sy, z=vals, cx=gx.ravel().copy(), cy=gy.ravel().copy(), vgs=vgs)
 
 
+def make_small_workload(seed=20261206, n_stns=150, n_steps=24, nx=200, ny=200, cell=500.0,
+                        box=100e3):
+    """The small configuration: 150 stations uniform in a 100 km box (seeded
+    float64 metre coordinates), 24 steps with every station present, values
+    5 + a Gaussian random field with the variogram '0.05 Nug(0.0) + 0.95
+    Exp(20000)' drawn by Cholesky of the station covariance, a 200 x 200
+    grid at 500 m (cell centres, rows from the top)."""
+    rng = np.random.default_rng(seed)
+    sx, sy = rng.uniform(0, box, n_stns), rng.uniform(0, box, n_stns)
+    d = np.hypot(sx[:, None] - sx[None], sy[:, None] - sy[None])
+    cov = 0.95 * np.exp(-3 * d / 20000.0) + 0.05 * np.eye(n_stns)
+    vals = 5.0 + (np.linalg.cholesky(cov) @ rng.standard_normal((n_stns, n_steps))).T
+    xs = cell / 2 + cell * np.arange(nx)
+    ys = box - cell / 2 - cell * np.arange(ny)
+    gx, gy = np.meshgrid(xs, ys)
+    return dict(sx=sx, sy=sy, z=vals, cx=gx.ravel().copy(), cy=gy.ravel().copy(),
+                vgs=["0.05 Nug(0.0) + 0.95 Exp(20000)"] * n_steps)
+
+
+def _small_cpu_worker(args):
+    os.environ["OMP_NUM_THREADS"] = "1"
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["MKL_NUM_THREADS"] = "1"
+    sx, sy, z, cx, cy, vgs, iargs = args
+    from oracle import port
+    t0 = time.perf_counter()
+    f, _ = port.interp_steps(sx, sy, z, cx, cy, vgs, iargs, est_vars=True, min_vg_val=1e-4,
+                             intrp_dtype=np.float64)
+    return time.perf_counter() - t0, f
+
+
+def small_leg(args, reps=20):
+    """The small configuration (150 stations, 24 steps, 200 x 200 cells, OK
+    estimate + variance and IDW p=2), where launch overhead matters: the
+    whole job per execution, plain FP64 and mixed, eager (one host call per
+    kernel) and replayed from a captured CUDA graph, after the cell-tile
+    autotuner; e2e through interp_steps; the oracle over all host cores on
+    the whole job (cells split across workers), with the GPU's error
+    against it."""
+    import multiprocessing as mp
+    import torch
+    import spinterps_gb300 as spi
+    from spinterps_gb300.steps import InterpPlan, interp_args_for
+    w = make_small_workload()
+    iargs = interp_args_for(["OK", ("IDW", 2.0)], est_vars=True)
+    kw = dict(est_vars=True, min_vg_val=1e-4, intrp_dtype=np.float32)
+    T, C = w["z"].shape[0], w["cx"].size
+    out = {"config": {"workload": "small_ok_idw_150stn_24steps_200x200", "stations": 150,
+                      "steps": T, "cells": C, "methods": ["OK+var", "IDW p=2"],
+                      "vg": w["vgs"][0]}}
+
+    def per_exec(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    for prec in ("fp64", "mixed"):
+        plan = InterpPlan(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], w["vgs"], iargs,
+                          precision=prec, **kw)
+        plan.execute()
+        torch.cuda.synchronize()
+        ms_default = per_exec(plan.execute)
+        tiles = plan.autotune()
+        ms_eager = per_exec(plan.execute)
+        plan.capture()
+        ms_graph = per_exec(plan.replay)
+        out[prec] = {"eager_ms": ms_eager, "graph_ms": ms_graph,
+                     "untuned_eager_ms": ms_default,
+                     "value_eager": T * C / (ms_eager / 1e3),
+                     "value_graph": T * C / (ms_graph / 1e3), "unit": UNIT,
+                     "tiles": {f"{k[0]}:{k[2][0]}{k[2][1]}": v for k, v in tiles.items()},
+                     "gpu_launches": plan.launches_per_execute()}
+        if prec == "fp64":
+            f64 = plan.fields()
+    e2e = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        spi.interp_steps(w["sx"], w["sy"], w["z"], w["cx"], w["cy"], w["vgs"], iargs, **kw)
+        torch.cuda.synchronize()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    out["e2e"] = {"value": T * C / (np.median(e2e) / 1e3), "unit": UNIT,
+                  "ms": float(np.median(e2e)), "statistic": "median of 3 interp_steps calls",
+                  "h2d_bytes_per_step": int(w["z"].nbytes + 16 * (150 + C)),
+                  "d2h_bytes_per_step": int(4 * 3 * T * C)}
+    if not args.no_cpu:
+        cores = os.cpu_count()
+        blocks = np.array_split(np.arange(C), cores)
+        jobs = [(w["sx"], w["sy"], w["z"], w["cx"][b], w["cy"][b], w["vgs"], iargs)
+                for b in blocks]
+        t0 = time.perf_counter()
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(_small_cpu_worker, jobs, chunksize=1)
+        wall = time.perf_counter() - t0
+        ref = {lab: np.concatenate([r[1][lab] for r in res], axis=1) for lab in res[0][1]}
+        errs = {}
+        for lab in ref:
+            sc = float(np.nanmax(np.abs(ref[lab])))
+            errs[lab] = float(np.nanmax(np.abs(f64[lab].astype(np.float64) - ref[lab])) / sc)
+        out["cpu_baseline"] = {"value": T * C / wall, "unit": UNIT, "cores": cores,
+                               "kind": "port", "cpu_model": cpu_model(), "seed": 20261206,
+                               "sample": f"the whole job ({T} steps x {C} cells, OK+var and "
+                                         f"IDW p=2), cells split over {cores} workers, wall "
+                                         f"{wall:.1f} s (pool start-up included)"}
+        out["fp64_err_vs_oracle"] = {"max_rel_to_field_max": errs,
+                                     "note": "float32 fields against the oracle's float64"}
+    return out
+
+
 def interp_args():
     from spinterps_gb300.steps import interp_args_for
     return interp_args_for(["OK", "SK", ("IDW", 2.0)], est_vars=True)
@@ -334,6 +450,17 @@ def run_ours(args):
     for i in range(args.warmup):
         plans[i % n_sl].execute()
     torch.cuda.synchronize()
+    # the cell-tile autotuner on the warmed slices (its choices are cached
+    # per station-count bucket and reused by the other slices)
+    warmed = {i % n_sl for i in range(args.warmup)}
+    tiles = {}
+    for k in sorted(warmed):
+        tiles.update({f"slice{k}:{kk[0]}:{kk[2][0]}{kk[2][1]}": v
+                      for kk, v in plans[k].autotune().items()})
+    for k in range(n_sl):
+        if k not in warmed:
+            plans[k].autotune(cached_only=True)
+    torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     if world > 1:
         dist.barrier()
@@ -440,6 +567,11 @@ def run_ours(args):
                                     "magnitude; per_cell: |mixed - fp64| / |fp64| over cells "
                                     "above the stated floor"}
         del p64, pm
+    # the small configuration (150 stations, 24 steps, 200 x 200 cells):
+    # launch overhead, CUDA graph, tile autotuner
+    small = None
+    if rank == 0 and not args.no_small:
+        small = small_leg(args)
     # the largest configuration (4000 stations, EDK with two drifts, 2000 x
     # 2000 cells, learned variograms), one wave of its steps
     large = None
@@ -459,6 +591,7 @@ def run_ours(args):
                        "steps_per_bench_step": T, "cells": C,
                        "methods": ["OK+var", "SK", "IDW p=2"], "precision": args.precision,
                        "parallelism": f"replicas x{world}",
+                       "cell_tiles_autotuned": tiles,
                        "l2": "per-step working set (4.4 GB of fields + 1.6 GB factors) >> L2",
                        "singular_steps_nnb": failed, "exact_inverse_steps": routed,
                        "fp32_tier_steps": fp32_steps,
@@ -482,6 +615,7 @@ def run_ours(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "fp64_path": fp64,
+            "small": small,
             "large": large,
         }
         print(json.dumps(line))
@@ -953,6 +1087,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-large", action="store_true",
                     help="leave the large configuration out of the default line")
+    ap.add_argument("--no-small", action="store_true",
+                    help="leave the small configuration out of the default line")
+    ap.add_argument("--small", action="store_true",
+                    help="the small configuration alone (CUDA graph and autotuner)")
     ap.add_argument("--large-reps", type=int, default=2)
     ap.add_argument("--large-fp64-every", type=int, default=4)
     ap.add_argument("--fp64-steps", type=int, default=4)
@@ -983,6 +1121,9 @@ def main():
     ap.add_argument("--nebs-steps", type=int, default=73)
     ap.add_argument("--nebs-cpu-cells", type=int, default=2000)
     args = ap.parse_args()
+    if args.small:
+        print(json.dumps(dict(small_leg(args), metric=METRIC, unit=UNIT, n_gpus=1)))
+        return
     if args.nebs:
         run_nebs(args)
     elif args.legacy:

@@ -210,10 +210,11 @@ typedef struct {
                             (spi_krige_tier); NULL: route 0 and
                             cond <= cond_split */
     int32_t *var_cells;  /* optional [n_sys]: the FP64 cell kernel adds the
-                            cells of every tile whose exact-inverse
-                            variance pass (P r, 2 m^2 FLOP per cell) ran;
-                            it runs only where a cell of the tile passes
-                            the sum check (NULL: not counted) */
+                            cells whose exact-inverse variance (lambda =
+                            P r, 2 m^2 FLOP per cell) it computed: only the
+                            cells that pass the sum check where few of a
+                            tile do, every cell of the tile where more than
+                            a quarter do (NULL: not counted) */
     double *pinv_scratch; /* optional, SPI_PINV_SCRATCH_DOUBLES doubles: lets
                             spi_krige_factor take numpy.linalg.pinv's answer
                             for exact-inverse systems of m <= SPI_PINV_MAX_M
@@ -303,6 +304,18 @@ int spi_krige_cells(const spi_domain_t *dom, const spi_systems_t *sys,
                     const double *vals, const spi_krige_ws_t *ws,
                     int32_t want_var, int32_t precision, int32_t route_filter,
                     double cond_split, const spi_out_t *out, spi_stream_t stream);
+
+/* spi_krige_cells with the cell tile of the shared-memory kernel chosen by
+ * the caller: tile 0 = the largest of 64 / 32 / 16 cells whose right-hand
+ * sides fit in shared memory (spi_krige_cells itself), 16 / 32 / 64 = that
+ * tile, SPI_ERR_TOO_LARGE when it does not fit (nothing is launched). Used
+ * by the host's autotuner, which times the tiles on a plan's first
+ * execution per station-count bucket. No reference counterpart (the
+ * reference has no tiles). */
+int spi_krige_cells_tiled(const spi_domain_t *dom, const spi_systems_t *sys,
+                          const double *vals, const spi_krige_ws_t *ws, int32_t want_var,
+                          int32_t precision, int32_t route_filter, double cond_split,
+                          const spi_out_t *out, int32_t tile, spi_stream_t stream);
 
 /* Tier of every system of a factored batch from a probe: est/var fields
  * [rows, n_probe] (row = sys->out_row[step]) of the same probe cells

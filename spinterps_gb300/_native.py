@@ -36,6 +36,9 @@ STATUS = {
 }
 
 
+SPI_ERR_TOO_LARGE = 5
+
+
 class SpiError(RuntimeError):
     def __init__(self, fn, code):
         super().__init__(f"{fn} returned {STATUS.get(code, code)}")
@@ -96,6 +99,9 @@ _SIGS = {
     "spi_nnb_cells": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr,
                       ctypes.POINTER(OutT), c_ptr],
     "spi_fill_rows": [c_i32, c_ptr, c_ptr, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr],
+    "spi_krige_cells_tiled": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT), c_ptr,
+                              ctypes.POINTER(KrigeWsT), c_i32, c_i32, c_i32, c_dbl,
+                              ctypes.POINTER(OutT), c_i32, c_ptr],
     "spi_krige_tier": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_i64, c_ptr, c_ptr,
                        c_ptr, c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr,
                        c_ptr],

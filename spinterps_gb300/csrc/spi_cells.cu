@@ -84,6 +84,8 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   __shared__ int any_bad;
   __shared__ int any_ok;
   __shared__ int any_chk;
+  __shared__ int n_ok;
+  __shared__ double wred[CT / 32];
 
   // vector v of the next pass: FP64 base + off, or its FP32 hi / lo copies
   auto setv = [&](int v, const double* b64, const float* bh, const float* bl, int64_t off,
@@ -101,6 +103,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     any_bad = failed ? 1 : 0;
     any_ok = 0;
     any_chk = 0;
+    n_ok = 0;
   }
   for (int e = tid; e < TC * GA; e += CT) qc[e] = 0.0;
 
@@ -112,15 +115,48 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       const bool live = gc < C;
       if constexpr (sizeof(T) == 8) {
         const double cx = live ? A.dom.cell_x[gc] : 0.0, cy = live ? A.dom.cell_y[gc] : 0.0;
+        // the nearest station of the cell comes with its distances (the
+        // same FP64 distances as nnb_f64_warp: first index of the minimum)
+        double best = __longlong_as_double(0x7ff0000000000000LL);
+        int bj = 0x7fffffff;
         for (int j = jg; j < npad; j += njg) {
           double v = 0.0;
-          if (live && j < n) v = rhs_f64(A.dom, vg, sk, prim, sh, cx, cy, idx[j]);
+          if (live && j < n) {
+            const int st = idx[j];
+            const double d = dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
+            if (d < best) {
+              best = d;
+              bj = j;
+            }
+            const double g = vg_fill_f64(vg, d, sk, A.dom.min_vg_val);
+            v = (sk || prim) ? g : __dsub_rn(sh, g);
+          }
           if (prim && live && j >= n && j < n + a) {
             const int k = j - n;  // r = [gamma, 1, drifts] rows of the saddle system
             v = (k == 0) ? 1.0 : A.dom.cell_drift[(int64_t)(k - 1) * C + gc];
           }
           cvT[(int64_t)j * TC + cell] = (T)v;
         }
+        // per cell, the minimum over the thread groups (Bs is free until
+        // the contractions below)
+        double* bd = reinterpret_cast<double*>(Bs);
+        bd[jg * TC + cell] = best;
+        bd[CT + jg * TC + cell] = (double)bj;
+        __syncthreads();
+        if (tid < TC) {
+          double b = bd[tid];
+          int bi = (int)bd[CT + tid];
+          for (int g = 1; g < njg; ++g) {
+            const double ob = bd[g * TC + tid];
+            const int oi = (int)bd[CT + g * TC + tid];
+            if (ob < b || (ob == b && oi < bi)) {
+              b = ob;
+              bi = oi;
+            }
+          }
+          nnb[tid] = bi == 0x7fffffff ? 0 : bi;
+        }
+        __syncthreads();
       } else {
         const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
                                : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -228,7 +264,10 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       okf[cell] = ok;
       cvar[cell] = ok == 1 ? vv : 0.0;
       if (!ok && gc < C) atomicOr(&any_bad, 1);
-      if (ok == 1 && gc < C) atomicOr(&any_ok, 1);
+      if (ok == 1 && gc < C) {
+        atomicOr(&any_ok, 1);
+        atomicAdd(&n_ok, 1);
+      }
     }
     __syncthreads();
     if constexpr (sizeof(T) == 4) {
@@ -248,12 +287,43 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       }
     }
     // ---- 4b. exact-inverse path, OK variance of the cells that pass the
-    // check: lambda = P r, var = lambda'r + lambda_n, wide passes over P's
-    // rows; skipped when no cell of the tile passes ----
+    // check: lambda = P r, var = lambda'r + lambda_n. A few passing cells
+    // (numerically singular systems: the sum check passes on ~1% of
+    // cells) take lambda = P r one cell at a time, a warp per row of P;
+    // tiles where many pass take wide passes over P's rows for the whole
+    // tile; skipped when no cell of the tile passes ----
     __syncthreads();
     if constexpr (sizeof(T) == 8) {
-      if (prim && A.want_var && !sk && any_ok) {
-        const int m = n + a;
+      const int m_prim = n + a;
+      if (prim && A.want_var && !sk && any_ok && n_ok <= TC / 4 && m_prim <= KC * BSTR) {
+        const int m = m_prim;
+        if (tid == 0 && A.ws.var_cells) atomicAdd(A.ws.var_cells + s, n_ok);
+        double* rv = reinterpret_cast<double*>(Bs);  // [m] the cell's r
+        const double* P = A.ws.l_arena + moff;
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int cell = 0; cell < TC; ++cell) {
+          if (okf[cell] != 1 || c0 + cell >= C) continue;
+          __syncthreads();
+          for (int j = tid; j < m; j += CT) rv[j] = (double)cvT[(int64_t)j * TC + cell];
+          __syncthreads();
+          double part = 0.0;
+          for (int i = warp; i < m; i += CT / 32) {
+            const double* row = P + (int64_t)i * m;
+            double t = 0.0;
+            for (int j = lane; j < m; j += 32) t = fma(row[j], rv[j], t);
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            part += t * rv[i] + (i == n ? t : 0.0);
+          }
+          if (lane == 0) wred[warp] = part;
+          __syncthreads();
+          if (tid == 0) {
+            double vv = 0.0;
+            for (int w = 0; w < CT / 32; ++w) vv += wred[w];
+            cvar[cell] = vv;
+          }
+        }
+      } else if (prim && A.want_var && !sk && any_ok) {
+        const int m = m_prim;
         // cells whose tile ran this pass (the FLOP count of the roofline)
         if (tid == 0 && A.ws.var_cells)
           atomicAdd(A.ws.var_cells + s, (int)min((int64_t)TC, C - c0));
@@ -297,8 +367,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     }
   }
   __syncthreads();
-  // ---- 5. nearest station, only for cells that fall back ----
-  if (any_bad) {
+  // ---- 5. nearest station, only for cells that fall back (the FP64 path
+  // found it with the right-hand sides) ----
+  if (any_bad && (sizeof(T) == 4 || failed)) {
     const int warp = tid >> 5, lane = tid & 31;
     for (int cell = warp; cell < TC; cell += CT / 32) {
       const int64_t gc = c0 + cell;
@@ -411,13 +482,24 @@ static int pick_tc(int max_n) {
 
 // Systems whose right-hand-side tile does not fit in shared memory take the
 // streamed kernel (estimates only; the OK variance needs the stored tile).
+// tile: 0 = the largest cell tile that fits; 16, 32 or 64 = that tile
+// (SPI_ERR_TOO_LARGE when it does not fit), the choice of the host's
+// autotuner.
 template <typename T, typename OutT>
-static int dispatch_cells(const CellsArgs& A, cudaStream_t st) {
+static int dispatch_cells(const CellsArgs& A, int tile, cudaStream_t st) {
   // the mixed path's FP32 tier: double-float right-hand sides in the
   // streamed kernel whenever no CUDA-core variance pass is needed
   if (sizeof(T) == 4 &&
       (A.ws.cell_yy != nullptr || !A.want_var || A.sys.kind == SPI_KIND_SK))
     return launch_cells_stream(A, 1, st);
+  if (tile) {
+    const int npad = (A.sys.max_n + GA + KC - 1) / KC * KC;
+    const size_t cap = 227 * 1024;
+    if (tile == 64 && cells_smem<T, 64>(npad) <= cap) return launch_cells<T, 64, OutT>(A, st);
+    if (tile == 32 && cells_smem<T, 32>(npad) <= cap) return launch_cells<T, 32, OutT>(A, st);
+    if (tile == 16 && cells_smem<T, 16>(npad) <= cap) return launch_cells<T, 16, OutT>(A, st);
+    return SPI_ERR_TOO_LARGE;
+  }
   int tc = pick_tc<T>(A.sys.max_n);
   if (tc == 64) return launch_cells<T, 64, OutT>(A, st);
   if (tc == 32) return launch_cells<T, 32, OutT>(A, st);
@@ -453,11 +535,13 @@ extern "C" int spi_split_f64(const double* x, float* hi, float* lo, int64_t n,
   return SPI_OK;
 }
 
-extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys,
-                               const double* vals, const spi_krige_ws_t* ws, int32_t want_var,
-                               int32_t precision, int32_t route_filter, double cond_split,
-                               const spi_out_t* out, spi_stream_t stream) {
+extern "C" int spi_krige_cells_tiled(const spi_domain_t* dom, const spi_systems_t* sys,
+                                     const double* vals, const spi_krige_ws_t* ws,
+                                     int32_t want_var, int32_t precision, int32_t route_filter,
+                                     double cond_split, const spi_out_t* out, int32_t tile,
+                                     spi_stream_t stream) {
   if (!dom || !sys || !out || !ws) return SPI_ERR_ARG;
+  if (tile != 0 && tile != 16 && tile != 32 && tile != 64) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (dom->n_drift < 0 || dom->n_drift > SPI_MAX_DRIFT) return SPI_ERR_TOO_LARGE;
   if (route_filter < 0 || route_filter > 2) return SPI_ERR_ARG;
@@ -487,8 +571,18 @@ extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys
   A.out = *out;
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == 0)
-    return out->out_f64 ? dispatch_cells<double, double>(A, st) : dispatch_cells<double, float>(A, st);
-  return out->out_f64 ? dispatch_cells<float, double>(A, st) : dispatch_cells<float, float>(A, st);
+    return out->out_f64 ? dispatch_cells<double, double>(A, tile, st)
+                        : dispatch_cells<double, float>(A, tile, st);
+  return out->out_f64 ? dispatch_cells<float, double>(A, tile, st)
+                      : dispatch_cells<float, float>(A, tile, st);
+}
+
+extern "C" int spi_krige_cells(const spi_domain_t* dom, const spi_systems_t* sys,
+                               const double* vals, const spi_krige_ws_t* ws, int32_t want_var,
+                               int32_t precision, int32_t route_filter, double cond_split,
+                               const spi_out_t* out, spi_stream_t stream) {
+  return spi_krige_cells_tiled(dom, sys, vals, ws, want_var, precision, route_filter,
+                               cond_split, out, 0, stream);
 }
 
 namespace spi {

@@ -24,8 +24,9 @@
 // even), each rotating m / 2 disjoint index pairs (p, q) at once: the 2 x 2
 // rotations are computed from W, then applied to the pairs' rows, then to
 // their columns (W <- J' W J) and to V's columns (V <- V J). Sweeps stop
-// when the off-diagonal Frobenius norm is under 0.1 eps ||M||_F, after at
-// most kSweeps. One CTA per scratch slot (SPI_PINV_SLOTS), each taking the
+// when the off-diagonal Frobenius norm reaches the rounding floor of the
+// rotations (sqrt(8 m) eps ||M||_F, or no longer falls by 4x a sweep once
+// under 1e-12 ||M||_F), after at most kSweeps. One CTA per scratch slot (SPI_PINV_SLOTS), each taking the
 // candidates s = slot, slot + slots, ...; W and V live in the slot's
 // scratch (global memory, L2-resident at m <= SPI_PINV_MAX_M = 256).
 #include "spi_common.cuh"
@@ -107,6 +108,7 @@ __global__ __launch_bounds__(PT) void k_pinv(spi_domain_t dom, spi_systems_t sys
     fm = cta_sum(fm, red);
     const int mm = m + (m & 1);
     bool conv = false;
+    double prev = __longlong_as_double(0x7ff0000000000000LL);
     for (int sweep = 0; sweep < kSweeps; ++sweep) {
       double off2 = 0.0;
       for (int e = tid; e < m * m; e += PT) {
@@ -114,10 +116,13 @@ __global__ __launch_bounds__(PT) void k_pinv(spi_domain_t dom, spi_systems_t sys
         if (i != j) off2 += W[e] * W[e];
       }
       off2 = cta_sum(off2, red);
-      if (off2 <= 1e-2 * kEps * kEps * fm) {
+      // converged: each off-diagonal entry at the rounding level of its
+      // rotations (~eps times its row's diagonal), or stalled there
+      if (off2 <= 8.0 * m * kEps * kEps * fm || (off2 <= 1e-24 * fm && off2 > 0.25 * prev)) {
         conv = true;
         break;
       }
+      prev = off2;
       for (int r = 0; r < mm - 1; ++r) {
         // the round's rotations
         if (tid < mm / 2) {

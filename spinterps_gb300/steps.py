@@ -65,6 +65,8 @@ def _stream():
 
 _VG_CACHE = {}
 _NUG_CACHE = {}
+# the autotuner's cell tiles (InterpPlan.autotune)
+_TILE_CACHE = {}
 
 
 def parse_vg(vg_str):
@@ -282,6 +284,9 @@ class _KrigeBatch:
         self.w_hat = torch.zeros_like(self.vals)
         self.beta = beta
         self.pinv = pinv
+        # cell tile per pass, from InterpPlan.autotune (0: the largest that
+        # fits)
+        self.tiles = {}
         self.split = None
         if precision == 1:
             # FP32 (hi, lo) pairs of Linv, G and w_hat for the split-precision kernel
@@ -440,11 +445,25 @@ class _KrigeBatch:
                     "spi_krige_var_df", ctypes.byref(dom.st), ctypes.byref(self.sy), ws,
                     float(cond_split), s))
         self.var_cells.zero_()
-        passes = [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
-        for prec, filt in passes:
-            timed("cells_fp32" if prec == 1 else "cells_fp64", lambda prec=prec, filt=filt: nat.call(
-                "spi_krige_cells", ctypes.byref(dom.st), ctypes.byref(self.sy), _ptr(self.vals),
-                ws, 1 if want_var else 0, prec, filt, float(cond_split), ctypes.byref(out), s))
+        for prec, filt in self.passes():
+            tile = self.tiles.get((prec, filt), 0)
+            timed("cells_fp32" if prec == 1 else "cells_fp64", lambda prec=prec, filt=filt,
+                  tile=tile: nat.call(
+                "spi_krige_cells_tiled", ctypes.byref(dom.st), ctypes.byref(self.sy),
+                _ptr(self.vals), ws, 1 if want_var else 0, prec, filt, float(cond_split),
+                ctypes.byref(out), tile, s))
+
+    def passes(self):
+        """The cell-kernel passes of run(): (precision, route filter)."""
+        return [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
+
+    def tiled(self, prec, want_var):
+        """Whether the pass takes the shared-memory tile kernel (the FP32
+        tier with a tensor-core variance, without a variance or SK, and
+        systems too large for shared memory take the streamed kernel)."""
+        if prec == 1 and (self.yy is not None or not want_var or self.kind == "SK"):
+            return False
+        return True
 
 
 def _chunk_systems(systems, precision, arena_budget):
@@ -634,6 +653,74 @@ class InterpPlan:
                 ev[1].record()
                 evs["idw"].append(("idw", ev, self.idw_flops) if t == "IDW" else ("nnb", ev, 0.0))
         return evs
+
+    def autotune(self, tiles=(16, 32, 64), cached_only=False):
+        """Pick the cell tile of the shared-memory cell kernel per batch and
+        pass: each candidate of ``tiles`` runs that pass (after one
+        execute(): factors, duals and tiers in place; the pass rewrites the
+        same fields), timed with CUDA events on the current stream after a
+        warm-up launch of its own; the fastest is kept. Choices are cached
+        process-wide per (precision, pass, kind, variance, station-count
+        bucket of the next power of two), so later plans of the same shape
+        reuse them untimed (``cached_only``: take cached choices only, for a
+        plan not yet executed). Returns {(kind, batch, pass): tile}."""
+        s = _stream()
+        chosen = {}
+        for kind, out, want_var, batches, fills, a in self.krig:
+            for bi, b in enumerate(batches):
+                bucket = 1 << int(np.ceil(np.log2(max(int(b.n.max()), 2))))
+                for prec, filt in b.passes():
+                    if not b.tiled(prec, want_var):
+                        continue
+                    key = (b.precision, prec, filt, kind, bool(want_var), bucket)
+                    if key not in _TILE_CACHE and cached_only:
+                        continue
+                    if key not in _TILE_CACHE:
+                        best, best_ms = 0, None
+                        for tc in tiles:
+                            ms = []
+                            for _ in range(2):
+                                e0 = torch.cuda.Event(enable_timing=True)
+                                e1 = torch.cuda.Event(enable_timing=True)
+                                e0.record()
+                                rc = nat.lib().spi_krige_cells_tiled(
+                                    ctypes.byref(self.dom.st), ctypes.byref(b.sy),
+                                    _ptr(b.vals), ctypes.byref(b.ws), 1 if want_var else 0,
+                                    prec, filt, float(self.cond_split), ctypes.byref(out), tc, s)
+                                e1.record()
+                                if rc:
+                                    break
+                                torch.cuda.synchronize()
+                                ms.append(e0.elapsed_time(e1))
+                            if rc == nat.SPI_ERR_TOO_LARGE:
+                                continue
+                            if rc:
+                                raise nat.SpiError("spi_krige_cells_tiled", rc)
+                            if best_ms is None or ms[-1] < best_ms:
+                                best, best_ms = tc, ms[-1]
+                        _TILE_CACHE[key] = best
+                    b.tiles[(prec, filt)] = _TILE_CACHE[key]
+                    chosen[(kind, bi, (prec, filt))] = _TILE_CACHE[key]
+        return chosen
+
+    def capture(self):
+        """Record execute() in a CUDA graph (after one plain execution on the
+        current stream, which sets the kernels' shared-memory attributes);
+        replay() then runs the whole job with one launch from the host.
+        The graph keeps the plan's device buffers and inputs: replay
+        recomputes the same fields."""
+        self.execute()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="thread_local"):
+            self.execute()
+        torch.cuda.synchronize()
+        self._graph = g
+        return g
+
+    def replay(self):
+        """Run the captured job (capture() first) on the current stream."""
+        self._graph.replay()
 
     def collect_info(self):
         for kind, out, want_var, batches, fills, a in self.krig:

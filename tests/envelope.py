@@ -10,8 +10,11 @@ fallback, est = lambda[:n] . z, var = lambda . r + lambda[n]). Where the
 matrix is badly conditioned that answer is set by rounding. This module
 measures how far: it re-runs the same per-cell formulas with pinv of the
 matrix under K symmetric relative perturbations of 1e-15 (a few ulp of
-every entry) and returns every run, so a test can ask whether the GPU's
-answer lies inside the reference's own spread.
+every entry), with numpy's cut-off and with one at 1e-13 (singular values
+that close to zero are rounding noise, and where they fall against the
+1e-15 cut-off depends on the platform's LAPACK), and returns every run, so
+a test can ask whether the GPU's answer lies inside the reference's own
+spread.
 
 The per-cell formulas are applied to all cells at once (one matrix
 product) instead of the reference's cell loop; that changes only the
@@ -39,16 +42,39 @@ def system(kind, sx, sy, idx, cx, cy, vg, min_vg_val, stn_drifts=None, cell_drif
     return lhs, rhs, d_cs
 
 
+# numpy.linalg.pinv's default cut-off, and the widest cut-off within
+# rounding reach of it: an exactly singular matrix's null singular values
+# come out of the SVD as rounding noise of about eps to 16 eps times s_max
+# (the LAPACK build and the platform decide where), on either side of
+# numpy's 1e-15
+RCOND = 1e-15
+RCOND_NOISE = 1e-13
+
+
 def singular_to_pinv(lhs):
-    """Whether numpy.linalg.pinv's default cut-off (rcond 1e-15: singular
-    values <= 1e-15 s_max are dropped) drops a singular value of ``lhs``,
-    and its condition number. The singular values come from the same SVD
-    call pinv makes (with singular vectors): for an exactly singular
-    matrix the null singular value is rounding noise of a few eps s_max,
-    near the cut-off, and the SVD without vectors computes a different
-    one."""
+    """Whether ``lhs`` has singular values within rounding reach of
+    numpy.linalg.pinv's cut-off (<= 1e-13 s_max; pinv itself drops those
+    <= 1e-15 s_max, decided there by rounding), and its condition number."""
     s = np.linalg.svd(lhs, full_matrices=False)[1]
-    return bool((s <= 1e-15 * s[0]).any()), float(s[0] / max(s[-1], 1e-300))
+    return bool((s <= RCOND_NOISE * s[0]).any()), float(s[0] / max(s[-1], 1e-300))
+
+
+def pinv_cuts(lhs):
+    """Whether numpy.linalg.pinv (rcond 1e-15) drops a singular value of
+    ``lhs`` on this platform: the same SVD call pinv makes."""
+    s = np.linalg.svd(lhs, full_matrices=False)[1]
+    return bool((s <= RCOND * s[0]).any())
+
+
+def _pinvs(m, rconds):
+    """numpy.linalg.pinv's computation (the SVD with vectors, singular
+    values <= rcond s_max dropped) for several cut-offs from one SVD."""
+    u, s, vt = np.linalg.svd(m, full_matrices=False)
+    out = []
+    for rc in rconds:
+        inv = np.where(s > rc * s[0], 1.0 / np.where(s > 0, s, 1.0), 0.0)
+        out.append((vt.T * inv) @ u.T)
+    return out
 
 
 def outcome(P, rhs, n, vals, d_cs, want_var):
@@ -66,29 +92,36 @@ def outcome(P, rhs, n, vals, d_cs, want_var):
 
 def runs(lhs, rhs, n, vals, d_cs, want_var, k=4, seed=0):
     """The reference's outcome on the matrix as given, then under ``k``
-    symmetric relative perturbations of 1e-15 (a pinv failure gives the
-    reference's nearest-station fill for every cell)."""
+    symmetric relative perturbations of 1e-15, each with numpy's cut-off
+    (1e-15) and, after those, each again with the cut-off at 1e-13 (an
+    SVD failure gives the reference's nearest-station fill for every
+    cell). Runs 0 .. k are numpy.linalg.pinv's own; the others add the
+    outcomes in which the singular values within rounding reach of the
+    cut-off are dropped."""
     rng = np.random.default_rng(seed)
-    out = []
+    own, wide = [], []
+    c = d_cs.shape[0]
+    fail = (vals[:, np.argmin(d_cs, 1)], np.zeros(c) if want_var else None,
+            np.zeros(c, dtype=bool))
     for i in range(k + 1):
         m = lhs
         if i:
             e = rng.standard_normal(lhs.shape)
             m = lhs * (1.0 + 1e-15 * (e + e.T) / 2)
         try:
-            P = np.linalg.pinv(m)
+            P, Pw = _pinvs(m, (RCOND, RCOND_NOISE))
         except np.linalg.LinAlgError:
-            c = d_cs.shape[0]
-            out.append((vals[:, np.argmin(d_cs, 1)], np.zeros(c) if want_var else None,
-                        np.zeros(c, dtype=bool)))
+            own.append(fail)
+            wide.append(fail)
             continue
-        out.append(outcome(P, rhs, n, vals, d_cs, want_var))
-    return out
+        own.append(outcome(P, rhs, n, vals, d_cs, want_var))
+        wide.append(outcome(Pw, rhs, n, vals, d_cs, want_var))
+    return own + wide
 
 
 def spread(rs, scale):
-    """Largest change of the estimates (and variances) over the perturbed
-    runs, relative to ``scale`` (estimates) and the variance's largest
+    """Largest change of the estimates (and variances) over the runs,
+    relative to ``scale`` (estimates) and the variance's largest
     magnitude."""
     e0, v0, _ = rs[0]
     de = max(float(np.abs(r[0] - e0).max()) for r in rs[1:]) / scale

@@ -30,7 +30,7 @@ def entry_kernels(name, batch):
     if name == "spi_krige_duals":
         return 1 if batch.X is not None else 3  # + the two triangular-solve kernels
     return {"spi_split_f64": 1, "spi_krige_var_tc": 1, "spi_krige_var_df": 1,
-            "spi_krige_cells": 1, "spi_krige_tier": 1}[name]
+            "spi_krige_cells": 1, "spi_krige_cells_tiled": 1, "spi_krige_tier": 1}[name]
 
 
 def make_batch(kind, precision, want_var, n_probe, tensor_cores=True):
@@ -147,7 +147,7 @@ def test_plan_dry_run(monkeypatch, precision):
         evs = plan.execute(timing=timing)
         assert plan.launches_per_execute() == sum(kernels(n, a) for n, a in calls)
     names = {n for n, _ in calls}
-    assert {"spi_krige_factor", "spi_krige_duals", "spi_krige_cells", "spi_idw_cells",
+    assert {"spi_krige_factor", "spi_krige_duals", "spi_krige_cells_tiled", "spi_idw_cells",
             "spi_nnb_cells", "spi_fill_rows"} <= names
     if precision == "mixed":
         assert {"spi_krige_tier", "spi_krige_var_tc", "spi_krige_var_df"} <= names
