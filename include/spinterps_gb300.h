@@ -222,6 +222,12 @@ typedef struct {
                             spi_krige_factor); NULL: Gauss-Jordan only */
     int32_t *pinv_used;  /* optional [n_sys]: 1 where that pinv replaced the
                             Gauss-Jordan inverse, else 0 */
+    double *gj_scratch;  /* optional, 2 * (total stations) + (2 * GA + 1) *
+                            n_sys doubles: spi_krige_factor then runs the
+                            exact-inverse path's Gauss-Jordan elimination
+                            step by step over the whole GPU (two launches per
+                            step, the same arithmetic); NULL: one CTA per
+                            system */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.

@@ -69,7 +69,7 @@ class KrigeWsT(ctypes.Structure):
                 ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr), ("linv_hi", c_ptr),
                 ("linv_lo", c_ptr), ("g_hi", c_ptr), ("g_lo", c_ptr), ("w_hi", c_ptr),
                 ("w_lo", c_ptr), ("cell_yy", c_ptr), ("tier", c_ptr), ("var_cells", c_ptr),
-                ("pinv_scratch", c_ptr), ("pinv_used", c_ptr)]
+                ("pinv_scratch", c_ptr), ("pinv_used", c_ptr), ("gj_scratch", c_ptr)]
 
 
 class OutT(ctypes.Structure):

@@ -19,6 +19,10 @@
 
 namespace spi {
 
+// The exact-inverse path's elimination over the whole GPU (spi_gj_multi.cu).
+int launch_gj_multi(const spi_domain_t& dom, const spi_systems_t& sys, const spi_krige_ws_t& ws,
+                    double cond_max, int pinv_on, cudaStream_t st);
+
 // Resolves routes 3 / 4 left by k_gj (spi_pinv.cu).
 int launch_pinv(const spi_domain_t& dom, const spi_systems_t& sys, const spi_krige_ws_t& ws,
                 cudaStream_t st);
@@ -976,9 +980,13 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
           cudaSuccess)
     return SPI_ERR_CUDA;
   const int pinv_on = ws->pinv_scratch != nullptr;
-  k_gj<<<sys->n_sys, FT, gsm, st>>>(d, sy, ws->l_arena, ws->status, ws->cond, ws->route,
-                                    cond_max, pinv_on);
-  SPI_LAUNCH_CHECK();
+  if (ws->gj_scratch) {
+    if ((rc = launch_gj_multi(d, sy, *ws, cond_max, pinv_on, st))) return rc;
+  } else {
+    k_gj<<<sys->n_sys, FT, gsm, st>>>(d, sy, ws->l_arena, ws->status, ws->cond, ws->route,
+                                      cond_max, pinv_on);
+    SPI_LAUNCH_CHECK();
+  }
   if (ws->pinv_used) {
     if (cudaMemsetAsync(ws->pinv_used, 0, sizeof(int32_t) * (size_t)sys->n_sys, st) !=
         cudaSuccess)

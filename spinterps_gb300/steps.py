@@ -67,6 +67,10 @@ _VG_CACHE = {}
 _NUG_CACHE = {}
 # the autotuner's cell tiles (InterpPlan.autotune)
 _TILE_CACHE = {}
+# systems of at least this many rows (stations + Lagrange / drift rows) take
+# the step-by-step Gauss-Jordan elimination over the whole GPU on the
+# exact-inverse path (2 launches per row); smaller ones one CTA each
+GJ_MULTI_MIN_M = 256
 
 
 def parse_vg(vg_str):
@@ -332,7 +336,16 @@ class _KrigeBatch:
         # (spi_krige_factor with a pinv scratch): shared by the plan's
         # batches, which run in stream order
         self.pinv_used = torch.zeros(len(ch), dtype=torch.int32, device=dev)
-        pv = (_ptr(pinv), _ptr(self.pinv_used))
+        # exact-inverse systems of hundreds of rows: their Gauss-Jordan
+        # elimination spread over the GPU, step by step (spi_gj_multi.cu);
+        # smaller systems keep one CTA each
+        self.a_rows = 0 if kind == "SK" else (1 + dom.st.n_drift if kind == "EDK" else 1)
+        self.max_m = int(ns.max()) + self.a_rows
+        self.gj = None
+        if self.max_m >= GJ_MULTI_MIN_M:
+            self.gj = torch.empty(2 * int(stn_off[-1]) + (2 * nat.GA + 1) * len(ch),
+                                  dtype=torch.float64, device=dev)
+        pv = (_ptr(pinv), _ptr(self.pinv_used), _ptr(self.gj))
         self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells), *pv)
         self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None,
                                      None, *pv)
@@ -776,7 +789,10 @@ class InterpPlan:
         for kind, out, want_var, batches, fills, a in self.krig:
             n += sum(f is not None for f in fills)
             for b in batches:
-                n += 4 + (b.pinv is not None)
+                # build, Cholesky, inverse or condition estimate, the
+                # exact-inverse elimination (one kernel, or set-up + 2 per
+                # row + finish), the pinv check
+                n += 3 + (2 * b.max_m + 2 if b.gj is not None else 1) + (b.pinv is not None)
                 n += 1 if b.X is not None else 3
                 if b.split is not None:
                     n += 2 + (b.X is not None)

@@ -348,3 +348,44 @@ def test_pinv_route_on_rank_deficient_systems():
                 assert ok.mean() >= 0.98, (kind, vg, ok.mean())
     print(f"\npinv route: {matched} of 9 systems cut by this platform's pinv, checked at "
           "1e-9; the others inside the reference's rounding envelope")
+
+
+@pytest.mark.parametrize("case", ["singular_gau_750", "duplicate_60"])
+def test_step_by_step_elimination_is_bit_identical(monkeypatch, case):
+    """The exact-inverse path's Gauss-Jordan elimination spread over the GPU
+    (spi_gj_multi.cu, systems of >= 256 rows) performs gj_invert's
+    operations one for one: forcing either form on the same systems gives
+    identical fields, problem steps and routes."""
+    import bench
+    from spinterps_gb300 import steps as st
+    spi = _spi()
+    if case == "singular_gau_750":
+        w = bench.make_workload()
+        sel = [4, 10]   # Gaussian variograms, numerically singular OK systems
+        sx, sy, z = w["sx"], w["sy"], w["z"][sel]
+        vgs = [w["vgs"][s] for s in sel]
+        cells = np.arange(0, w["cx"].size, 997)
+        cx, cy = w["cx"][cells], w["cy"][cells]
+        kw = dict(bench.KW, intrp_dtype=np.float64)
+        args = bench.interp_args()
+    else:
+        rng = np.random.default_rng(4)
+        sx, sy = rng.uniform(0, 5e4, 60), rng.uniform(0, 5e4, 60)
+        sx[9], sy[9] = sx[8], sy[8]
+        gx, gy = np.meshgrid(np.arange(30) * 1700.0, np.arange(20) * 2500.0)
+        cx, cy = gx.ravel(), gy.ravel()
+        z = 2.0 + rng.normal(size=(2, 60))
+        vgs = ["0.1 Nug(0.0) + 0.9 Exp(15000)", "1.0 Gau(9000)"]
+        kw = dict(est_vars=True, min_vg_val=1e-4, intrp_dtype=np.float64)
+        args = port.interp_args_for(["OK", "SK"], est_vars=True)
+    out = []
+    for min_m in (10 ** 9, 0):
+        monkeypatch.setattr(st, "GJ_MULTI_MIN_M", min_m)
+        f, p, info = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, return_info=True, **kw)
+        out.append((f, p, info))
+    (f0, p0, i0), (f1, p1, i1) = out
+    assert p0 == p1
+    assert i0["exact_inverse_steps"] == i1["exact_inverse_steps"]
+    assert any(i0["exact_inverse_steps"].values())
+    for lab in f0:
+        assert np.array_equal(f0[lab], f1[lab], equal_nan=True), lab

@@ -23,10 +23,11 @@ def entry_kernels(name, batch):
     """Kernel launches per call of each entry point _KrigeBatch.run uses
     (csrc/spi_factor.cu, spi_cells.cu, spi_var_tc.cu, spi_var_df.cu)."""
     if name == "spi_krige_factor":
-        # build, Cholesky, inverse or condition estimate, Gauss-Jordan, and
-        # the pinv check of exact-inverse systems when the batch has its
-        # scratch
-        return 4 + (batch.pinv is not None)
+        # build, Cholesky, inverse or condition estimate, Gauss-Jordan (one
+        # kernel, or set-up + 2 per row + finish over the GPU), and the pinv
+        # check of exact-inverse systems when the batch has its scratch
+        gj = 2 * batch.max_m + 2 if batch.gj is not None else 1
+        return 3 + gj + (batch.pinv is not None)
     if name == "spi_krige_duals":
         return 1 if batch.X is not None else 3  # + the two triangular-solve kernels
     return {"spi_split_f64": 1, "spi_krige_var_tc": 1, "spi_krige_var_df": 1,
@@ -136,8 +137,14 @@ def test_plan_dry_run(monkeypatch, precision):
 
     def kernels(name, a):
         if name == "spi_krige_factor":
-            # + the pinv check when the workspace carries its scratch
-            return 4 + bool(a[2]._obj.pinv_scratch)
+            # + the pinv check when the workspace carries its scratch; the
+            # step-by-step elimination with its scratch (systems >= 256 rows)
+            ws, sy = a[2]._obj, a[1]._obj
+            gj = 1
+            if ws.gj_scratch:
+                gj = 2 * (sy.max_n + (0 if sy.kind == 1 else 1 + a[0]._obj.n_drift
+                                      if sy.kind == 2 else 1)) + 2
+            return 3 + gj + bool(ws.pinv_scratch)
         if name == "spi_krige_duals":
             return 1 if a[3]._obj.linv_arena else 3
         return 1
