@@ -88,18 +88,38 @@ class _Header:
         return b"".join(self.parts)
 
 
+class Deferred:
+    """A variable whose data write_nc leaves to later slab writes
+    (write_slab): only its shape and dtype are given; its region of the
+    file is reserved (sparse, reading as zeros until written)."""
+
+    def __init__(self, shape, dtype):
+        self.shape = tuple(int(v) for v in shape)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape, dtype=np.int64)) * self.dtype.itemsize
+
+
+def _meta(arr):
+    if isinstance(arr, Deferred):
+        return arr.shape, arr.dtype, arr.nbytes
+    a = np.asarray(arr)
+    return a.shape, a.dtype, a.nbytes
+
+
 def write_nc(path, dims, variables, global_attrs=None, fmt=5):
     """A netCDF classic file with fixed-size (non-record) variables.
 
-    dims: {name: length}; variables: list of (name, dim names, numpy array,
-    attrs dict); all arrays are written big-endian, each padded to 4 bytes.
-    fmt: 1 (CDF-1), 2 (CDF-2, 64-bit offsets) or 5 (CDF-5, 64-bit data)."""
+    dims: {name: length}; variables: list of (name, dim names, numpy array
+    or Deferred, attrs dict); all arrays are written big-endian, each padded
+    to 4 bytes. fmt: 1 (CDF-1), 2 (CDF-2, 64-bit offsets) or 5 (CDF-5,
+    64-bit data). Returns the path; the byte offset of every variable's data
+    is in ``write_nc.begins`` (name -> offset) after the call."""
     dim_names = list(dims)
     for name, dn, arr, _ in variables:
         shape = tuple(dims[d] for d in dn)
-        assert tuple(np.shape(arr)) == shape, (name, np.shape(arr), shape)
+        assert tuple(_meta(arr)[0]) == shape, (name, _meta(arr)[0], shape)
         if fmt != 5:
-            assert np.asarray(arr).dtype != np.int64, f"{name}: int64 needs CDF-5"
+            assert _meta(arr)[1] != np.int64, f"{name}: int64 needs CDF-5"
 
     def header(begins):
         h = _Header(fmt)
@@ -119,15 +139,15 @@ def write_nc(path, dims, variables, global_attrs=None, fmt=5):
             h.tag(NC_VARIABLE)
             h.count(len(variables))
             for (name, dn, arr, attrs), beg in zip(variables, begins):
-                a = np.asarray(arr)
-                t, _ = NC_TYPES[a.dtype]
+                _, dt, nb = _meta(arr)
+                t, _ = NC_TYPES[dt]
                 h.name(name)
                 h.count(len(dn))
                 for d in dn:
                     h.count(dim_names.index(d))
                 h.attrs(attrs or {})
                 h.tag(t)
-                vsize = a.nbytes + ((-a.nbytes) % 4)
+                vsize = nb + ((-nb) % 4)
                 if fmt != 5 and vsize > 2**32 - 4:
                     vsize = 2**32 - 1
                 h.count(vsize)
@@ -142,16 +162,33 @@ def write_nc(path, dims, variables, global_attrs=None, fmt=5):
     begins, pos = [], hlen
     for _, _, arr, _ in variables:
         begins.append(pos)
-        n = np.asarray(arr).nbytes
+        n = _meta(arr)[2]
         pos += n + ((-n) % 4)
     with open(path, "wb") as f:
         f.write(header(begins))
         for _, _, arr, _ in variables:
+            nb = _meta(arr)[2]
+            if isinstance(arr, Deferred):
+                f.seek(nb + ((-nb) % 4), 1)
+                continue
             a = np.ascontiguousarray(arr)
             be = a.astype(NC_TYPES[a.dtype][1], copy=False)
             f.write(be.tobytes())
             f.write(b"\x00" * ((-a.nbytes) % 4))
+        f.truncate(pos)
+    write_nc.begins = {v[0]: b for v, b in zip(variables, begins)}
     return path
+
+
+def write_slab(path, begin, block, first):
+    """Write ``block`` (leading axis = the variable's first dimension) into
+    a Deferred variable whose data starts at byte ``begin``, from index
+    ``first`` of its first dimension on (big-endian, as write_nc)."""
+    a = np.ascontiguousarray(block)
+    per = int(np.prod(a.shape[1:], dtype=np.int64)) * a.dtype.itemsize
+    with open(path, "r+b") as f:
+        f.seek(int(begin) + int(first) * per)
+        f.write(a.astype(NC_TYPES[a.dtype][1], copy=False).tobytes())
 
 
 def write_interp_nc(path, x_crds, y_crds, time_vals, fields, interp_args, *, xlab="X",
@@ -161,8 +198,10 @@ def write_interp_nc(path, x_crds, y_crds, time_vals, fields, interp_args, *, xla
     and variables, one per interpolation label (interp_args: the reference's
     (type, dir, label[, idw_exp]) tuples), with units and standard_name as
     _initiate_nc sets them (IDW: '{vlab} ({label[:3]}_exp_{exp})').
-    fields: label -> [T, ny, nx] array; settings: name -> value, written as
-    'sett_<name>' string attributes; Source = the file's path."""
+    fields: label -> [T, ny, nx] array, or a Deferred of that shape whose
+    steps come later through write_slab (offsets in write_nc.begins);
+    settings: name -> value, written as 'sett_<name>' string attributes;
+    Source = the file's path."""
     T, ny, nx = len(time_vals), len(y_crds), len(x_crds)
     dims = {"dimx": nx, "dimy": ny, "dimt": T}
     tv = np.asarray(time_vals)
@@ -178,7 +217,9 @@ def write_interp_nc(path, x_crds, y_crds, time_vals, fields, interp_args, *, xla
     for a in interp_args:
         lab = a[2]
         std = f"{vlab} ({lab[:3]}_exp_{a[3]})" if a[0] == "IDW" else f"{vlab} ({lab})"
-        variables.append((lab, ("dimt", "dimy", "dimx"), np.asarray(fields[lab]),
+        fl = fields[lab]
+        variables.append((lab, ("dimt", "dimy", "dimx"),
+                          fl if isinstance(fl, Deferred) else np.asarray(fl),
                           {"units": str(vunits), "standard_name": std}))
     gatt = {f"sett_{k}": str(v) for k, v in (settings or {}).items()}
     gatt["Source"] = str(path)
