@@ -169,6 +169,9 @@ typedef struct {
  * spi_krige_factor checks against numpy.linalg.pinv's cut-off, and the
  * scratch (doubles) that check needs: SPI_PINV_SLOTS systems at once, each
  * two m x m matrices. */
+/* Iteration limit of the FP64 iterative refinement of the duals over an
+ * FP32 factor (spi_krige_factor / spi_krige_duals with ws->l32). */
+#define SPI_IR_MAX_ITERS 12
 #define SPI_PINV_MAX_M 256
 #define SPI_PINV_SLOTS 16
 #define SPI_PINV_SCRATCH_DOUBLES (SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M)
@@ -222,6 +225,23 @@ typedef struct {
                             spi_krige_factor); NULL: Gauss-Jordan only */
     int32_t *pinv_used;  /* optional [n_sys]: 1 where that pinv replaced the
                             Gauss-Jordan inverse, else 0 */
+    float *l32;          /* optional arena of the same layout as l_arena
+                            (floats): with it, and without linv_arena,
+                            spi_krige_factor factors every system in FP32
+                            first; systems whose FP32 factor succeeds with
+                            cond <= cond_ir keep it, and spi_krige_duals
+                            solves with it by FP64 iterative refinement
+                            (residuals b - A x in FP64 with the full
+                            matrix A kept in l_arena); the others are
+                            factored in FP64 as without it */
+    int32_t *ir;         /* [n_sys] with l32: 1 where the FP32 factor is
+                            kept, else 0 */
+    int32_t *ir_iters;   /* [n_sys] with l32: refinement iterations the
+                            duals took (the largest over their
+                            right-hand sides; -1 where they did not reach
+                            FP64 accuracy in SPI_IR_MAX_ITERS) */
+    double cond_ir;      /* with l32: the largest condition estimate that
+                            keeps the FP32 factor (1e6 if 0) */
     double *gj_scratch;  /* optional, 2 * (total stations) + (2 * GA + 1) *
                             n_sys doubles: spi_krige_factor then runs the
                             exact-inverse path's Gauss-Jordan elimination
@@ -238,8 +258,11 @@ typedef struct {
  * over 8 fixed Rademacher vectors g). Under sum(lambda) = 1 the
  * weights of [[A, F], [F', 0]] equal those of the reference's
  * [[Gamma, F], [F', 0]] (Lagrange multipliers change sign).
- * Systems whose Cholesky fails or whose cond exceeds cond_max take the
- * exact-inverse path (route 1): the reference's own saddle matrix
+ * Systems whose Cholesky fails, whose cond exceeds cond_max, or (EDK)
+ * whose drift rows are linearly dependent with the unbiasedness row
+ * (F'F singular to 1e-12: their Schur complement is singular; status is
+ * then n + 1) take the exact-inverse path (route 1): the reference's own
+ * saddle matrix
  * (interp/steps.py:170-243) is inverted in place by Gauss-Jordan with
  * partial pivoting, i.e. numpy.linalg.pinv (interp/steps.py:351) without
  * its singular-value cut-off (1e-15 * s_max, numpy's default rcond), which

@@ -19,6 +19,7 @@ c_ptr = ctypes.c_void_p
 SPI_MAX_VG_COMP = 4
 SPI_MAX_DRIFT = 7
 SPI_PINV_MAX_M = 256
+SPI_IR_MAX_ITERS = 12
 SPI_PINV_SLOTS = 16
 SPI_PINV_SCRATCH_DOUBLES = SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M
 GA = SPI_MAX_DRIFT + 1
@@ -69,7 +70,8 @@ class KrigeWsT(ctypes.Structure):
                 ("g_cols", c_ptr), ("s_inv", c_ptr), ("g_colsum", c_ptr), ("linv_hi", c_ptr),
                 ("linv_lo", c_ptr), ("g_hi", c_ptr), ("g_lo", c_ptr), ("w_hi", c_ptr),
                 ("w_lo", c_ptr), ("cell_yy", c_ptr), ("tier", c_ptr), ("var_cells", c_ptr),
-                ("pinv_scratch", c_ptr), ("pinv_used", c_ptr), ("gj_scratch", c_ptr)]
+                ("pinv_scratch", c_ptr), ("pinv_used", c_ptr), ("l32", c_ptr), ("ir", c_ptr),
+                ("ir_iters", c_ptr), ("cond_ir", c_dbl), ("gj_scratch", c_ptr)]
 
 
 class OutT(ctypes.Structure):

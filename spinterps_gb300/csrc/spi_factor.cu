@@ -65,7 +65,7 @@ __device__ double block_sum(double t, double* red) {
 // 196-226); with ascending station lists the entry (i, j), i > j, is the
 // mirror of (j, i), whose distance is dist(stn[j], stn[i]).
 __global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restrict__ l_arena,
-                            double* __restrict__ shift_out) {
+                            double* __restrict__ shift_out, int full) {
   const int s = blockIdx.y;
   SysView v = sys_view(sys, s);
   const spi_vg_t vg = sys.vg[s];
@@ -77,27 +77,33 @@ __global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restr
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn;
        e += (int64_t)gridDim.x * blockDim.x) {
     int i = (int)(e / v.n), j = (int)(e - (int64_t)i * v.n);
-    if (j > i) {
+    if (j > i && !full) {
       A[e] = 0.0;
       continue;
     }
-    int si = v.idx[i], sj = v.idx[j];
+    // (i, j) and its mirror from the same distance: dists[lo, hi]
+    int si = v.idx[max(i, j)], sj = v.idx[min(i, j)];
     double d = dist_f64(dom.stn_x[sj], dom.stn_y[sj], dom.stn_x[si], dom.stn_y[si]);
     double g = vg_fill_f64(vg, d, sk, dom.min_vg_val);
     A[e] = sk ? g : __dsub_rn(sh, g);
   }
 }
 
-// Right-looking blocked Cholesky, in place on the lower triangle.
-__global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, double* __restrict__ l_arena,
-                                            int32_t* __restrict__ status) {
+// Right-looking blocked Cholesky, in place on the lower triangle, in T
+// (FP64; FP32 for the refinement path's factor). skip (optional): systems
+// with skip[s] != 0 are left alone.
+template <typename T>
+__global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, T* __restrict__ l_arena,
+                                            int32_t* __restrict__ status,
+                                            const int32_t* __restrict__ skip) {
   const int s = blockIdx.x;
+  if (skip && skip[s]) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
-  double* A = l_arena + v.moff;
-  __shared__ double D[NB][NB + 1];
-  __shared__ double Pi[64][NB + 1];
-  __shared__ double Pj[64][NB + 1];
+  T* A = l_arena + v.moff;
+  __shared__ T D[NB][NB + 1];
+  __shared__ T Pi[64][NB + 1];
+  __shared__ T Pj[64][NB + 1];
   __shared__ int fail;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) fail = 0;
@@ -111,18 +117,18 @@ __global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, double* __restri
     __syncthreads();
     if (warp == 0) {
       for (int j = 0; j < nb; ++j) {
-        double djj = D[j][j];
+        T djj = D[j][j];
         if (!(djj > 0.0)) {  // not positive, or NaN
           if (lane == 0) fail = k0 + j + 1;
           break;
         }
-        double ljj = sqrt(djj);
+        T ljj = sqrt(djj);
         __syncwarp();
         if (lane == j) D[j][j] = ljj;
         if (lane > j && lane < nb) D[lane][j] = D[lane][j] / ljj;
         __syncwarp();
         if (lane > j && lane < nb) {
-          double lij = D[lane][j];
+          T lij = D[lane][j];
           for (int c = j + 1; c <= lane; ++c) D[lane][c] -= lij * D[c][j];
         }
         __syncwarp();
@@ -136,14 +142,14 @@ __global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, double* __restri
     }
     // panel: rows below the diagonal block, A21 <- A21 L11^-T
     for (int r = k0 + nb + tid; r < n; r += FT) {
-      double x[NB];
-      double* row = A + (int64_t)r * n + k0;
+      T x[NB];
+      T* row = A + (int64_t)r * n + k0;
 #pragma unroll
       for (int j = 0; j < NB; ++j) x[j] = (j < nb) ? row[j] : 0.0;
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
         if (j < nb) {
-          double t = x[j];
+          T t = x[j];
 #pragma unroll
           for (int c = 0; c < NB; ++c)
             if (c < j) t -= x[c] * D[j][c];
@@ -170,10 +176,10 @@ __global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, double* __restri
         }
         __syncthreads();
         const int rr = (tid / 16) * 4, cc = (tid % 16) * 4;
-        double acc[4][4] = {};
+        T acc[4][4] = {};
 #pragma unroll 4
         for (int c = 0; c < NB; ++c) {
-          double a[4], b[4];
+          T a[4], b[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             a[q] = Pi[rr + q][c];
@@ -450,14 +456,15 @@ constexpr int KS = 4;
 // Y_k <- L^-1 Y_k. Blocks of 32 rows: the rows' dot products with the
 // solved part (a warp per row, lanes along the row), then the 32 x 32
 // diagonal block by one warp (a lane per row).
-__device__ void trsv_lower_multi(const double* __restrict__ L, int n, double* Y, int ldy,
+template <typename TL>
+__device__ void trsv_lower_multi(const TL* __restrict__ L, int n, double* Y, int ldy,
                                  int nk) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i0 = 0; i0 < n; i0 += 32) {
     const int nb = min(32, n - i0);
     if (i0 > 0) {
       for (int r = warp; r < nb; r += FT / 32) {
-        const double* row = L + (int64_t)(i0 + r) * n;
+        const TL* row = L + (int64_t)(i0 + r) * n;
         double acc[KS];
 #pragma unroll
         for (int k = 0; k < KS; ++k) acc[k] = 0.0;
@@ -477,14 +484,14 @@ __device__ void trsv_lower_multi(const double* __restrict__ L, int n, double* Y,
     }
     if (warp == 0) {
       double t[KS];
-      const double* Lb = L + (int64_t)(i0 + min(lane, nb - 1)) * n + i0;  // this lane's row
+      const TL* Lb = L + (int64_t)(i0 + min(lane, nb - 1)) * n + i0;  // this lane's row
       // one reciprocal per row (divisions run on the 1/64-rate FP64 pipe)
-      const double rd = 1.0 / Lb[min(lane, nb - 1)];
+      const double rd = 1.0 / (double)Lb[min(lane, nb - 1)];
 #pragma unroll
       for (int k = 0; k < KS; ++k) t[k] = (lane < nb && k < nk) ? Y[k * ldy + i0 + lane] : 0.0;
       for (int c = 0; c < nb; ++c) {
         const double rcc = __shfl_sync(0xffffffffu, rd, c);
-        const double lrc = (lane > c && lane < nb) ? Lb[c] : 0.0;
+        const double lrc = (lane > c && lane < nb) ? (double)Lb[c] : 0.0;
 #pragma unroll
         for (int k = 0; k < KS; ++k) {
           const double y = __shfl_sync(0xffffffffu, t[k], c) * rcc;
@@ -502,7 +509,8 @@ __device__ void trsv_lower_multi(const double* __restrict__ L, int n, double* Y,
 // Y_k <- L^-T Y_k. Blocks of 32 rows from the bottom: the diagonal block
 // by one warp, then every earlier entry updated by the block's solved
 // values (a thread per entry, reading the block's rows of L along them).
-__device__ void trsv_lower_t_multi(const double* __restrict__ L, int n, double* Y, int ldy,
+template <typename TL>
+__device__ void trsv_lower_t_multi(const TL* __restrict__ L, int n, double* Y, int ldy,
                                    int nk) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = (n + 31) / 32;
@@ -510,13 +518,14 @@ __device__ void trsv_lower_t_multi(const double* __restrict__ L, int n, double* 
     const int i0 = I * 32, nb = min(32, n - i0);
     if (warp == 0) {
       double t[KS];
-      const double rd = 1.0 / L[(int64_t)(i0 + min(lane, nb - 1)) * n + i0 + min(lane, nb - 1)];
+      const double rd =
+          1.0 / (double)L[(int64_t)(i0 + min(lane, nb - 1)) * n + i0 + min(lane, nb - 1)];
 #pragma unroll
       for (int k = 0; k < KS; ++k) t[k] = (lane < nb && k < nk) ? Y[k * ldy + i0 + lane] : 0.0;
       for (int c = nb - 1; c >= 0; --c) {
-        const double* Lc = L + (int64_t)(i0 + c) * n + i0;  // row c of the block
+        const TL* Lc = L + (int64_t)(i0 + c) * n + i0;  // row c of the block
         const double rcc = __shfl_sync(0xffffffffu, rd, c);
-        const double lcr = (lane < c) ? Lc[lane] : 0.0;
+        const double lcr = (lane < c) ? (double)Lc[lane] : 0.0;
 #pragma unroll
         for (int k = 0; k < KS; ++k) {
           const double y = __shfl_sync(0xffffffffu, t[k], c) * rcc;
@@ -544,6 +553,159 @@ __device__ void trsv_lower_t_multi(const double* __restrict__ L, int n, double* 
   }
 }
 
+// A^-1 applied to the kk vectors Y[k * n + i]: two triangular solves with
+// the system's FP64 factor, or, where the system kept its FP32 factor
+// (ws.ir[s]), FP64 iterative refinement over it: x = L32^-T L32^-1 b, then
+// d = L32^-T L32^-1 (b - A x) with the residual from the full FP64 matrix
+// (kept in l_arena), x += d, until max|d| <= 4 eps max|x| or
+// SPI_IR_MAX_ITERS corrections. bval(k, i): entry i of right-hand side k
+// (the Y held on entry); D: scratch of kk * n doubles. The iterations are
+// recorded in ws.ir_iters[s] (their maximum; SPI_IR_MAX_ITERS + 1 when the
+// corrections did not reach FP64 accuracy).
+template <typename BF>
+__device__ void ainv_apply(const spi_krige_ws_t& ws, int s, int n, int64_t moff, double* Y,
+                           double* D, int kk, BF bval) {
+  if (!(ws.l32 && ws.ir && ws.ir[s])) {
+    const double* L = ws.l_arena + moff;
+    trsv_lower_multi(L, n, Y, n, kk);
+    trsv_lower_t_multi(L, n, Y, n, kk);
+    return;
+  }
+  const float* L = ws.l32 + moff;
+  const double* A = ws.l_arena + moff;
+  __shared__ double rmax[2][FT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  trsv_lower_multi(L, n, Y, n, kk);
+  trsv_lower_t_multi(L, n, Y, n, kk);
+  int it = 1;
+  bool conv = false;
+  for (; it <= SPI_IR_MAX_ITERS; ++it) {
+    __syncthreads();
+    for (int i = warp; i < n; i += FT / 32) {
+      const double* row = A + (int64_t)i * n;
+      double t[KS];
+#pragma unroll
+      for (int k = 0; k < KS; ++k) t[k] = 0.0;
+      for (int j = lane; j < n; j += 32) {
+        const double a = row[j];
+#pragma unroll
+        for (int k = 0; k < KS; ++k)
+          if (k < kk) t[k] = fma(a, Y[k * n + j], t[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < KS; ++k)
+        for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+      if (lane == 0)
+        for (int k = 0; k < kk; ++k) D[k * n + i] = bval(k, i) - t[k];
+    }
+    __syncthreads();
+    trsv_lower_multi(L, n, D, n, kk);
+    trsv_lower_t_multi(L, n, D, n, kk);
+    double dm = 0.0, xm = 0.0;
+    for (int e = threadIdx.x; e < kk * n; e += FT) {
+      const double x = Y[e] + D[e];
+      Y[e] = x;
+      dm = fmax(dm, fabs(D[e]));
+      xm = fmax(xm, fabs(x));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+      xm = fmax(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+    }
+    __syncthreads();
+    if (lane == 0) {
+      rmax[0][warp] = dm;
+      rmax[1][warp] = xm;
+    }
+    __syncthreads();
+    dm = xm = 0.0;
+    for (int w = 0; w < FT / 32; ++w) {
+      dm = fmax(dm, rmax[0][w]);
+      xm = fmax(xm, rmax[1][w]);
+    }
+    if (dm <= 4.0 * 2.220446049250313e-16 * xm) {
+      conv = true;
+      break;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && ws.ir_iters)
+    atomicMax(ws.ir_iters + s, conv ? it : SPI_IR_MAX_ITERS + 1);
+}
+
+// EDK systems whose drift rows are linearly dependent with the
+// unbiasedness row (a drift constant over the stations, two proportional
+// drifts): F = [1 | drifts] is then rank deficient, the Schur complement
+// F'A^-1 F of the Cholesky path singular, and the reference's saddle
+// matrix singular, which its pinv resolves. Such systems are sent down the
+// exact-inverse path (status = n + 1): F'F's Cholesky with pivots under
+// 1e-12 of its diagonal's largest entry marks them (a <= GA rows, one
+// thread after the block sums).
+__global__ __launch_bounds__(FT) void k_drift_check(spi_domain_t dom, spi_systems_t sys,
+                                                   int32_t* __restrict__ status) {
+  const int s = blockIdx.x;
+  const int a = extra_rows(sys.kind, dom.n_drift);
+  if (a < 2 || status[s] != 0) return;
+  SysView v = sys_view(sys, s);
+  const int n = v.n;
+  __shared__ double red[FT / 32];
+  __shared__ double M[GA][GA];
+  auto fcol = [&](int k, int i) {
+    return (k == 0) ? 1.0 : dom.stn_drift[(int64_t)v.idx[i] * dom.n_drift + (k - 1)];
+  };
+  for (int k = 0; k < a; ++k)
+    for (int l = 0; l <= k; ++l) {
+      double t = 0.0;
+      for (int i = threadIdx.x; i < n; i += FT) t = fma(fcol(k, i), fcol(l, i), t);
+      t = block_sum(t, red);
+      if (threadIdx.x == 0) M[k][l] = M[l][k] = t;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double dmax = 0.0;
+    for (int k = 0; k < a; ++k) dmax = fmax(dmax, M[k][k]);
+    bool dep = !(dmax > 0.0);
+    for (int j = 0; j < a && !dep; ++j) {
+      double d = M[j][j];
+      for (int c = 0; c < j; ++c) d -= M[j][c] * M[j][c];
+      if (!(d > 1e-12 * dmax)) {
+        dep = true;
+        break;
+      }
+      const double lj = sqrt(d);
+      M[j][j] = lj;
+      for (int r = j + 1; r < a; ++r) {
+        double t = M[r][j];
+        for (int c = 0; c < j; ++c) t -= M[r][c] * M[j][c];
+        M[r][j] = t / lj;
+      }
+    }
+    if (dep) status[s] = n + 1;
+  }
+}
+
+// FP32 copy of every system's matrix (the refinement path's factor).
+__global__ void k_to_f32(spi_systems_t sys, const double* __restrict__ l_arena,
+                         float* __restrict__ l32) {
+  const int s = blockIdx.y;
+  SysView v = sys_view(sys, s);
+  const int64_t nn = (int64_t)v.n * v.n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x)
+    l32[v.moff + e] = (float)l_arena[v.moff + e];
+}
+
+// Which systems keep the FP32 factor: it succeeded with cond <= cond_ir;
+// the others' status is reset for the FP64 factorisation.
+__global__ void k_ir_gate(spi_systems_t sys, spi_krige_ws_t ws, double cond_ir) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= sys.n_sys) return;
+  const int keep = ws.status[s] == 0 && ws.cond[s] <= cond_ir;
+  ws.ir[s] = keep;
+  ws.ir_iters[s] = 0;
+  if (!keep) ws.status[s] = 0;
+}
+
 // A deterministic Rademacher sign for entry i of probe k of system s.
 __device__ __forceinline__ double probe_sign(int s, int k, int i) {
   uint32_t h = (uint32_t)i * 0x9E3779B1u ^ ((uint32_t)k * 0x85EBCA77u + (uint32_t)s * 0xC2B2AE3Du);
@@ -561,18 +723,21 @@ __device__ __forceinline__ double probe_sign(int s, int k, int i) {
 // of magnitude the routing thresholds work in). Dynamic shared memory:
 // nk x n doubles.
 constexpr int KP = 8;
+template <typename TL>
 __global__ __launch_bounds__(FT) void k_cond_est(spi_systems_t sys,
-                                                const double* __restrict__ l_arena,
+                                                const TL* __restrict__ l_arena,
                                                 const int32_t* __restrict__ status,
-                                                double* __restrict__ cond, int nk) {
+                                                double* __restrict__ cond, int nk,
+                                                const int32_t* __restrict__ skip) {
   const int s = blockIdx.x;
+  if (skip && skip[s]) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
   if (status[s] != 0) {
     if (threadIdx.x == 0) cond[s] = __longlong_as_double(0x7ff0000000000000LL);
     return;
   }
-  const double* L = l_arena + v.moff;
+  const TL* L = l_arena + v.moff;
   extern __shared__ double ysm[];
   __shared__ double red[FT / 32];
   double tot = 0.0;
@@ -593,7 +758,8 @@ __global__ __launch_bounds__(FT) void k_cond_est(spi_systems_t sys,
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < FT / 32; ++w) t += red[w];
-    cond[s] = (double)n * (L[0] * L[0]) * (t / KP);
+    const double l0 = (double)L[0];
+    cond[s] = (double)n * (l0 * l0) * (t / KP);
   }
 }
 
@@ -608,7 +774,6 @@ __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_system
   if (ws.route[s] != 0) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
-  const double* L = ws.l_arena + v.moff;
   extern __shared__ double ysm[];
   __shared__ double red[FT / 32];
   __shared__ double S[GA][GA];
@@ -628,8 +793,8 @@ __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_system
       ysm[k * n + i] = fcol(k0 + k, i);
     }
     __syncthreads();
-    trsv_lower_multi(L, n, ysm, n, kk);
-    trsv_lower_t_multi(L, n, ysm, n, kk);
+    ainv_apply(ws, s, n, v.moff, ysm, ysm + nk * n, kk,
+               [&](int k, int i) { return fcol(k0 + k, i); });
     for (int e = threadIdx.x; e < kk * n; e += FT) G[(int64_t)k0 * n + e] = ysm[e];
   }
   __syncthreads();
@@ -683,7 +848,6 @@ __global__ __launch_bounds__(FT) void k_duals_solve_steps(spi_domain_t dom, spi_
   if (sb + (int64_t)blockIdx.x * nk >= se) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
-  const double* L = ws.l_arena + v.moff;
   extern __shared__ double ysm[];
   __shared__ double red[FT / 32];
   __shared__ double Si[GA][GA];
@@ -719,8 +883,9 @@ __global__ __launch_bounds__(FT) void k_duals_solve_steps(spi_domain_t dom, spi_
         }
       __syncthreads();
     }
-    trsv_lower_multi(L, n, ysm, n, kk);
-    trsv_lower_t_multi(L, n, ysm, n, kk);
+    ainv_apply(ws, s, n, v.moff, ysm, ysm + nk * n, kk, [&](int k, int i) {
+      return vals[sys.val_off[sys.steps[q0 + k]] + i];
+    });
     for (int k = 0; k < kk; ++k) {
       const int j = sys.steps[q0 + k];
       const int64_t vo = sys.val_off[j];
@@ -933,13 +1098,21 @@ static int check_ws(const spi_krige_ws_t* ws) {
 
 // Right-hand sides per triangular-solve pass and the shared memory they
 // take (KS at most, within 200 KB).
-static int solve_smem(int max_n, int* nk, size_t* bytes) {
-  int k = (int)((200 * 1024) / ((size_t)max_n * sizeof(double)));
+// Right-hand sides per pass of the triangular-solve kernels and their
+// dynamic shared memory: nk x n doubles, twice that with the refinement's
+// correction vectors (ir).
+static int solve_smem(int max_n, int* nk, size_t* bytes, int ir = 0) {
+  const size_t per = (size_t)max_n * sizeof(double) * (ir ? 2 : 1);
+  int k = (int)((200 * 1024) / per);
   if (k > KS) k = KS;
   if (k < 1) return SPI_ERR_TOO_LARGE;
   *nk = k;
-  *bytes = (size_t)k * max_n * sizeof(double);
+  *bytes = (size_t)k * per;
   return SPI_OK;
+}
+
+static bool ir_mode(const spi_krige_ws_t* ws) {
+  return ws->l32 && !ws->linv_arena && ws->ir && ws->ir_iters;
 }
 
 extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sys,
@@ -956,21 +1129,37 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   int gx = (int)((nn + 255) / 256);
   if (gx > 64) gx = 64;
   if (gx < 1) gx = 1;
-  k_build_sys<<<dim3(gx, sys->n_sys), 256, 0, st>>>(d, sy, ws->l_arena, ws->shift);
+  const bool ir = ir_mode(ws);
+  k_build_sys<<<dim3(gx, sys->n_sys), 256, 0, st>>>(d, sy, ws->l_arena, ws->shift, ir ? 1 : 0);
   SPI_LAUNCH_CHECK();
-  k_chol<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status);
+  int nk = 0;
+  size_t ysm = 0;
+  if (!ws->linv_arena) {
+    if ((rc = solve_smem(sys->max_n, &nk, &ysm))) return rc;
+    if (ysm > 48 * 1024 &&
+        (cudaFuncSetAttribute(k_cond_est<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)ysm) != cudaSuccess ||
+         cudaFuncSetAttribute(k_cond_est<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)ysm) != cudaSuccess))
+      return SPI_ERR_CUDA;
+  }
+  if (ir) {
+    // FP32 factor first; systems that keep it skip the FP64 one
+    k_to_f32<<<dim3(gx, sys->n_sys), 256, 0, st>>>(sy, ws->l_arena, ws->l32);
+    k_chol<float><<<sys->n_sys, FT, 0, st>>>(sy, ws->l32, ws->status, nullptr);
+    k_cond_est<float><<<sys->n_sys, FT, ysm, st>>>(sy, ws->l32, ws->status, ws->cond, nk,
+                                                    nullptr);
+    k_ir_gate<<<(sys->n_sys + 255) / 256, 256, 0, st>>>(sy, *ws,
+                                                       ws->cond_ir > 0 ? ws->cond_ir : 1e6);
+    SPI_LAUNCH_CHECK();
+  }
+  k_chol<double><<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status, ir ? ws->ir : nullptr);
   SPI_LAUNCH_CHECK();
   if (ws->linv_arena) {
     k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->linv_arena, ws->status, ws->cond);
   } else {
-    int nk;
-    size_t ysm;
-    if ((rc = solve_smem(sys->max_n, &nk, &ysm))) return rc;
-    if (ysm > 48 * 1024 &&
-        cudaFuncSetAttribute(k_cond_est, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)ysm) != cudaSuccess)
-      return SPI_ERR_CUDA;
-    k_cond_est<<<sys->n_sys, FT, ysm, st>>>(sy, ws->l_arena, ws->status, ws->cond, nk);
+    k_cond_est<double><<<sys->n_sys, FT, ysm, st>>>(sy, ws->l_arena, ws->status, ws->cond, nk,
+                                                     ir ? ws->ir : nullptr);
   }
   SPI_LAUNCH_CHECK();
   size_t gsm = (size_t)(sys->max_n + GA) * (2 * sizeof(double) + sizeof(int));
@@ -979,6 +1168,10 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
       cudaFuncSetAttribute(k_gj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm) !=
           cudaSuccess)
     return SPI_ERR_CUDA;
+  if (sys->kind == SPI_KIND_EDK) {
+    k_drift_check<<<sys->n_sys, FT, 0, st>>>(d, sy, ws->status);
+    SPI_LAUNCH_CHECK();
+  }
   const int pinv_on = ws->pinv_scratch != nullptr;
   if (ws->gj_scratch) {
     if ((rc = launch_gj_multi(d, sy, *ws, cond_max, pinv_on, st))) return rc;
@@ -1014,10 +1207,11 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
   k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals);
   SPI_LAUNCH_CHECK();
   if (!ws->linv_arena) {
-    // route-0 systems without Linv: triangular solves with L
+    // route-0 systems without Linv: triangular solves with L (or FP64
+    // refinement over the FP32 factor)
     int nk;
     size_t ysm;
-    if ((rc = solve_smem(sys->max_n, &nk, &ysm))) return rc;
+    if ((rc = solve_smem(sys->max_n, &nk, &ysm, ir_mode(ws) ? 1 : 0))) return rc;
     if (ysm > 48 * 1024 &&
         cudaFuncSetAttribute(k_duals_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)ysm) != cudaSuccess)

@@ -240,7 +240,8 @@ class _KrigeBatch:
     """One chunk of kriging systems: device descriptors and workspaces."""
 
     def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
-                 want_var=False, tensor_cores=True, n_probe=0, need_linv=None, pinv=None):
+                 want_var=False, tensor_cores=True, n_probe=0, need_linv=None, pinv=None,
+                 ir=True, cond_ir=1e6):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -345,11 +346,22 @@ class _KrigeBatch:
         if self.max_m >= GJ_MULTI_MIN_M:
             self.gj = torch.empty(2 * int(stn_off[-1]) + (2 * nat.GA + 1) * len(ch),
                                   dtype=torch.float64, device=dev)
-        pv = (_ptr(pinv), _ptr(self.pinv_used), _ptr(self.gj))
-        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells), *pv)
+        # the mixed path without the OK variance's inverse factor: every
+        # system factored in FP32 first, its duals refined in FP64 where
+        # the FP32 factor holds (cond <= cond_ir), FP64 otherwise
+        self.l32 = self.ir = self.ir_iters = None
+        if precision == 1 and self.X is None and ir:
+            self.l32 = torch.empty(self.arena, dtype=torch.float32, device=dev)
+            self.ir = torch.zeros(n_sys, dtype=torch.int32, device=dev)
+            self.ir_iters = torch.zeros(n_sys, dtype=torch.int32, device=dev)
+        extra = dict(pinv_scratch=_ptr(pinv), pinv_used=_ptr(self.pinv_used),
+                     gj_scratch=_ptr(self.gj), l32=_ptr(self.l32), ir=_ptr(self.ir),
+                     ir_iters=_ptr(self.ir_iters), cond_ir=float(cond_ir))
+        self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells),
+                               **extra)
         self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None,
-                                     None, *pv)
-        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None, None, *pv)
+                                     None, **extra)
+        self.ws_probe_df = (nat.KrigeWsT(*ptrs, _ptr(self.probe_df[0]), None, None, **extra)
                             if self.probe_df else None)
         # algorithmic FLOP of the cell kernel: per (system, cell) the
         # triangular variance n(n+1), the dual columns 2na; per cell-step 2n
@@ -507,7 +519,7 @@ class InterpPlan:
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
                  cond_max=1e13, cond_split=None, tensor_cores=True, probe_cells=1024,
-                 probe_tol=2e-6, cond_df=COND_DF):
+                 probe_tol=2e-6, cond_df=COND_DF, refine=True, cond_ir=1e6):
         dev = self.dev = _require_cuda(device)
         if cond_split is None:
             # a cap under the probe; without it, the a-priori split
@@ -593,7 +605,7 @@ class InterpPlan:
                 batches = [_KrigeBatch(dev, self.dom, kind, systems, ch, data, T, val_off, beta,
                                        prec, want_var=var is not None,
                                        tensor_cores=tensor_cores, n_probe=n_probe,
-                                       pinv=self.pinv)
+                                       pinv=self.pinv, ir=refine, cond_ir=cond_ir)
                            for ch in _chunk_systems(systems, prec, arena_budget)]
                 fills = (
                     _fill_args(dev, self.single, self.single_val,
@@ -772,6 +784,20 @@ class InterpPlan:
             self.info.setdefault("exact_inverse_steps", {})[kind] = sorted(routed)
             # exact-inverse steps whose inverse is pinv's truncated one
             self.info.setdefault("pinv_steps", {})[kind] = sorted(pinv)
+            # the FP32 factor with FP64 refinement: steps and iterations
+            irs, iters = [], {}
+            for b in batches:
+                if b.ir is None:
+                    continue
+                kept = b.ir.cpu().numpy()
+                its = b.ir_iters.cpu().numpy()
+                for k, sl in enumerate(b.steps_l):
+                    if kept[k]:
+                        for j in sl:
+                            irs.append(int(j))
+                            iters[int(j)] = int(its[k])
+            self.info.setdefault("ir_steps", {})[kind] = sorted(irs)
+            self.info.setdefault("ir_iters", {})[kind] = iters
             self.info["cond"][kind] = cond
         return self.info
 
@@ -793,6 +819,10 @@ class InterpPlan:
                 # exact-inverse elimination (one kernel, or set-up + 2 per
                 # row + finish), the pinv check
                 n += 3 + (2 * b.max_m + 2 if b.gj is not None else 1) + (b.pinv is not None)
+                n += 1 if kind == "EDK" else 0  # the drift-dependence check
+                # the FP32 factor of the refinement path: copy, Cholesky,
+                # condition estimate, gate
+                n += 4 if b.l32 is not None else 0
                 n += 1 if b.X is not None else 3
                 if b.split is not None:
                     n += 2 + (b.X is not None)
@@ -888,7 +918,7 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
                  arena_budget=8 << 30, cond_max=1e13, cond_split=None, tensor_cores=True,
                  probe_cells=1024, probe_tol=2e-6, neb_sel_mthd="all", n_nebs=None,
-                 n_pies=None):
+                 n_pies=None, refine=True, cond_ir=1e6):
     """Interpolate every step onto every cell on the GPU.
 
     ``neb_sel_mthd`` 'nrst' / 'pie' (with ``n_nebs``, ``n_pies``) selects
@@ -901,8 +931,12 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
     runs on tcgen05 in 3xTF32). In the mixed path each system first runs in
     both tiers on ``probe_cells`` cells and takes the FP32 tier only where
     they agree to ``probe_tol`` of the fields' scale, and only on the
-    Cholesky path with cond <= ``cond_split``. Returns ``(fields, problem_steps)``, plus an info dict
-    (failed systems, condition estimates) when ``return_info``.
+    Cholesky path with cond <= ``cond_split``. With ``refine`` the mixed
+    path factors systems without the OK variance in FP32 and refines their
+    duals in FP64 (kept where the FP32 factor's condition estimate is at
+    most ``cond_ir``). Returns ``(fields, problem_steps)``, plus an info
+    dict (failed systems, condition estimates, tiers, refinement
+    iterations) when ``return_info``.
     """
     if neb_sel_mthd != "all":
         from .nebs import interp_steps_nebs
@@ -922,7 +956,8 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                       intrp_dtype=intrp_dtype, time_steps=time_steps, precision=precision,
                       device=device, arena_budget=arena_budget, cond_max=cond_max,
                       cond_split=cond_split, tensor_cores=tensor_cores,
-                      probe_cells=probe_cells, probe_tol=probe_tol)
+                      probe_cells=probe_cells, probe_tol=probe_tol, refine=refine,
+                      cond_ir=cond_ir)
     plan.execute()
     flds = plan.fields(numpy=return_numpy)
     prblm = plan.problem_steps()

@@ -389,3 +389,28 @@ def test_step_by_step_elimination_is_bit_identical(monkeypatch, case):
     assert any(i0["exact_inverse_steps"].values())
     for lab in f0:
         assert np.array_equal(f0[lab], f1[lab], equal_nan=True), lab
+
+
+def test_fp32_factor_with_fp64_refinement():
+    """The mixed path's FP32 factorisation with FP64 iterative refinement of
+    the duals (systems without the OK variance; EDK and SK here): every
+    well-conditioned system keeps its FP32 factor, its duals converge to
+    FP64 accuracy in a few iterations, and the fields equal those of the
+    FP64 factorisation (refine=False) to 1e-10 of the field, within the
+    mixed bar of the oracle."""
+    spi = _spi()
+    sx, sy, z, cx, cy, vgs, sd, cd = _random_case(17, n=300, t=6)
+    args = port.interp_args_for(["SK", "EDK"], est_vars=False)
+    kw = dict(stn_drifts=sd, cell_drifts=cd, min_var_thr=0.1, min_vg_val=1e-4,
+              intrp_dtype=np.float64, precision="mixed")
+    got, _, info = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, return_info=True, **kw)
+    ref64, _ = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, refine=False, **kw)
+    ora, _ = port.interp_steps(sx, sy, z, cx, cy, vgs, args, **{k: v for k, v in kw.items()
+                                                                 if k != "precision"})
+    kept = info["ir_steps"]["EDK"]
+    assert len(kept) >= 3, info["ir_steps"]
+    its = info["ir_iters"]["EDK"]
+    assert all(1 <= its[j] <= 6 for j in kept), its
+    for lab in ref64:
+        assert _err(got[lab], ref64[lab]) <= 1e-10, lab
+        assert _err(got[lab], ora[lab]) <= MIXED_TOL, lab
