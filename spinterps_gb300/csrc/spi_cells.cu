@@ -96,6 +96,9 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   };
 
   const spi_vg_t vg = A.sys.vg[s];
+  // the variogram with its reciprocal ranges (FP64 right-hand sides)
+  __shared__ VgPre vgp64;
+  if (sizeof(T) == 8 && tid == 0) vgp64.init(vg);
   // right-hand side: covariance form s - gamma on the Cholesky path, the
   // reference's gamma itself on the exact-inverse path
   const double sh = A.ws.shift[s];
@@ -106,6 +109,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
     n_ok = 0;
   }
   for (int e = tid; e < TC * GA; e += CT) qc[e] = 0.0;
+  __syncthreads();  // vgp64
 
   if (!failed) {
     // ---- 1. right-hand sides, cell-contiguous: cvT[j][cell] ----
@@ -128,7 +132,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
               best = d;
               bj = j;
             }
-            const double g = vg_fill_f64(vg, d, sk, A.dom.min_vg_val);
+            const double g = vgp64.fill(d, sk, A.dom.min_vg_val);
             v = (sk || prim) ? g : __dsub_rn(sh, g);
           }
           if (prim && live && j >= n && j < n + a) {

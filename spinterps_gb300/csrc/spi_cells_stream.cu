@@ -170,11 +170,14 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   double cx = 0.0, cy = 0.0;
   float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
   __shared__ RhsDf kd;
+  // the variogram with its reciprocal ranges (FP64 right-hand sides)
+  __shared__ VgPre vgp64;
   if constexpr (sizeof(T) == 8) {
     if (live) {
       cx = A.dom.cell_x[gc];
       cy = A.dom.cell_y[gc];
     }
+    if (tid == 0) vgp64.init(vg);
   } else {
     if (live) cp = reinterpret_cast<const float4*>(A.dom.cell_split)[gc];
     if (tid == 0) kd.init(vg, sh, A.dom.min_vg_val);
@@ -212,7 +215,12 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
     if constexpr (sizeof(T) == 8) {
       for (int j = warp; j < n; j += SNW) {
         const int st = idx[j];
-        const double c = live ? rhs_f64(A.dom, vg, sk, prim, sh, cx, cy, st) : 0.0;
+        double c = 0.0;
+        if (live) {
+          const double g = vgp64.fill(
+              dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]), sk, A.dom.min_vg_val);
+          c = (sk || prim) ? g : __dsub_rn(sh, g);
+        }
 #pragma unroll
         for (int v = 0; v < SSV; ++v)
           if (v < nv) acc[v] = fma(c, vp64[v][j], acc[v]);

