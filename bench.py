@@ -567,6 +567,10 @@ def run_ours(args):
                                     "magnitude; per_cell: |mixed - fp64| / |fp64| over cells "
                                     "above the stated floor"}
         del p64, pm
+    # variogram fitting of the workload's steps: plain vs learned warm start
+    fit = None
+    if rank == 0 and not args.no_fit:
+        fit = fit_leg(args)
     # the small configuration (150 stations, 24 steps, 200 x 200 cells):
     # launch overhead, CUDA graph, tile autotuner
     small = None
@@ -617,6 +621,7 @@ def run_ours(args):
             "fp64_path": fp64,
             "small": small,
             "large": large,
+            "fit": fit,
         }
         print(json.dumps(line))
     if world > 1:
@@ -648,7 +653,7 @@ def _cpu_fit_worker(args):
     return time.perf_counter() - t0
 
 
-def run_fit(args):
+def fit_leg(args):
     """Variogram fitting of the workload's 365 steps (the reference's fitvgs
     settings): plain GPU fit, warm-started GPU fit, CPU oracle sample, and
     the leave-one-out kriging RMSE of the fitted variograms."""
@@ -709,7 +714,12 @@ def run_fit(args):
                             "ratio": float(r_w[ok].mean() / r_p[ok].mean()),
                             "steps": int(ok.sum())},
             "cpu_baseline": cpu}
-    print(json.dumps(line))
+    return line
+
+
+def run_fit(args):
+    """The fitting leg alone, as its own JSON line."""
+    print(json.dumps(fit_leg(args)))
 
 
 def field_errors(x, y, floor_frac=1e-3):
@@ -851,6 +861,67 @@ def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
     if clk:
         out["clocks"] = clk.summary()
     return out
+
+
+def run_year(args):
+    """The large hourly configuration over its whole year: all 8760 steps
+    (4000 stations, EDK with two drifts, 2000 x 2000 cells, float32 fields,
+    learned variograms) through the public wave API
+    (spinterps_gb300.waves.interp_steps_waves), the steps in waves sized to
+    a device budget, every wave's fields copied to host memory and reduced
+    there to per-step means by the sink. Wall time of the whole call, host
+    planning and copies included."""
+    import torch
+    from spinterps_gb300 import fitvgs, synth, warmstart, waves
+    from spinterps_gb300.steps import interp_args_for
+    T = args.year_steps
+    t0 = time.perf_counter()
+    w = synth.large_edk(n_steps=T, nx=args.large_nx, ny=args.large_nx)
+    t_gen = time.perf_counter() - t0
+    pts = fitvgs.step_points(w["sx"], w["sy"], w["z"])
+    mlp = warmstart.WarmStartMLP.load()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    strs, det = warmstart.warm_fit_steps(None, None, None, mlp, points=pts, seed=1)
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    vgs = [s[-1] if s else "1.0 Nug(0.0)" for s in strs]
+    iargs = interp_args_for(["EDK"], est_vars=False)
+    C = w["cx"].size
+    means = np.full(T, np.nan)
+    n_waves = [0]
+
+    def sink(first, flds):
+        v = flds["EDK"]
+        means[first:first + v.shape[0]] = np.nanmean(v[:, ::97], axis=1)
+        n_waves[0] += 1
+
+    with Clocks(0) as clk:
+        t0 = time.perf_counter()
+        prblm, info = waves.interp_steps_waves(
+            w["sx"], w["sy"], w["z"], w["cx"], w["cy"], vgs, iargs, sink=sink,
+            budget=int(args.year_budget_gb * 2 ** 30), stn_drifts=w["stn_drift"],
+            cell_drifts=w["cell_drift"], min_vg_val=1e-4, intrp_dtype=np.float32,
+            precision="mixed")
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    fast = sum(len(i["info"].get("fp32_tier_steps", {}).get("EDK", [])) for i in info)
+    ir = sum(len(i["info"].get("ir_steps", {}).get("EDK", [])) for i in info)
+    iters = [v for i in info for v in i["info"].get("ir_iters", {}).get("EDK", {}).values()]
+    line = {"metric": METRIC, "value": T * C / wall, "unit": UNIT, "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"large_edk_4000stn_{T}steps_{args.large_nx}x{args.large_nx}",
+                       "stations": 4000, "steps": T, "cells": C, "methods": ["EDK"],
+                       "api": "waves.interp_steps_waves, fields to host per wave",
+                       "budget_gb": args.year_budget_gb},
+            "wall_s": wall, "waves": n_waves[0], "problem_steps": len(prblm),
+            "fp32_tier_steps": fast, "ir_steps": ir,
+            "ir_iterations": {str(k): int(np.sum(np.asarray(iters) == k))
+                              for k in sorted(set(iters))},
+            "plan_s": float(sum(i["plan_s"] for i in info)),
+            "field_mean_range": [float(np.nanmin(means)), float(np.nanmax(means))],
+            "fit_s": t_fit, "synthesis_s": t_gen, "clocks": clk.summary()}
+    print(json.dumps(line))
 
 
 def run_large(args):
@@ -1087,6 +1158,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-large", action="store_true",
                     help="leave the large configuration out of the default line")
+    ap.add_argument("--year", action="store_true",
+                    help="the large configuration over all its steps through the wave API")
+    ap.add_argument("--year-steps", type=int, default=8760)
+    ap.add_argument("--year-budget-gb", type=float, default=24.0)
+    ap.add_argument("--no-fit", action="store_true",
+                    help="leave variogram fitting out of the default line")
     ap.add_argument("--no-small", action="store_true",
                     help="leave the small configuration out of the default line")
     ap.add_argument("--small", action="store_true",
@@ -1123,6 +1200,9 @@ def main():
     args = ap.parse_args()
     if args.small:
         print(json.dumps(dict(small_leg(args), metric=METRIC, unit=UNIT, n_gpus=1)))
+        return
+    if args.year:
+        run_year(args)
         return
     if args.nebs:
         run_nebs(args)

@@ -93,7 +93,7 @@ def make_training_set(n_fields, seed=0, chunk=200, device="cuda"):
             np.concatenate(mk))
 
 
-def main(n_fields=3000, out=DEFAULT_WEIGHTS, epochs=300, seed=0):
+def main(n_fields=50000, out=DEFAULT_WEIGHTS, epochs=300, seed=0):
     t0 = time.time()
     F, C, Y, M = make_training_set(n_fields, seed=seed)
     t1 = time.time()
@@ -112,6 +112,6 @@ def main(n_fields=3000, out=DEFAULT_WEIGHTS, epochs=300, seed=0):
 
 
 if __name__ == "__main__":
-    n = int(sys.argv[1]) if len(sys.argv) > 1 else 3000
+    n = int(sys.argv[1]) if len(sys.argv) > 1 else 50000
     dst = sys.argv[2] if len(sys.argv) > 2 else DEFAULT_WEIGHTS
     main(n, dst)

@@ -30,13 +30,17 @@ from .steps import InterpPlan, _require_cuda
 
 def step_bytes(n_present, n_cells, n_labels, out_itemsize, krige_kinds, ok_var, mixed):
     """Device bytes one step adds to a wave: its fields, and per kriging
-    kind its system's factor arena(s) and per-cell variance buffer."""
+    kind its system's factor arena(s), per-cell variance buffer and the
+    mixed path's FP32 factor."""
     b = n_cells * n_labels * out_itemsize
     arena = (n_present + nat.GA) ** 2 * 8
     for kind in krige_kinds:
-        b += arena * (2 if (ok_var and kind == "OK") else 1)
-        if mixed and ok_var and kind == "OK":
+        var = ok_var and kind == "OK"
+        b += arena * (2 if var else 1)
+        if mixed and var:
             b += n_cells * 8
+        if mixed and not var:
+            b += arena // 2  # the FP32 factor of the refinement path
     return int(b)
 
 
