@@ -235,15 +235,21 @@ typedef struct {
                             matrix A kept in l_arena); the others are
                             factored in FP64 as without it */
     int32_t *ir;         /* [n_sys] with l32: 1 where the FP32 factor is
-                            kept, else 0 */
-    int32_t *ir_iters;   /* [n_sys] with l32: refinement iterations the
-                            duals took (the largest over their
-                            right-hand sides; -1 where they did not reach
-                            FP64 accuracy in SPI_IR_MAX_ITERS) */
+                            kept, 2 where its refinement did not converge
+                            and the system was factored and solved again in
+                            FP64, 0 where it was factored in FP64 from the
+                            start */
+    int32_t *ir_iters;   /* [n_sys] with l32: refinement corrections the
+                            duals took (the largest over their right-hand
+                            sides; bit 30 set where the componentwise
+                            backward error did not reach sqrt(n) eps in
+                            SPI_IR_MAX_ITERS) */
     double cond_ir;      /* with l32: the largest condition estimate that
-                            keeps the FP32 factor (1e6 if 0) */
-    double *gj_scratch;  /* optional, 2 * (total stations) + (2 * GA + 1) *
-                            n_sys doubles: spi_krige_factor then runs the
+                            tries the FP32 factor (1e12 if 0; the estimate
+                            overstates the condition, and systems whose
+                            refinement fails fall back to FP64) */
+    double *gj_scratch;  /* optional, 1 + 2 * (total stations) + (2 * GA +
+                            1) * n_sys doubles: spi_krige_factor then runs the
                             exact-inverse path's Gauss-Jordan elimination
                             step by step over the whole GPU (two launches per
                             step, the same arithmetic); NULL: one CTA per

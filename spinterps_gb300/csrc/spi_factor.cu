@@ -90,14 +90,14 @@ __global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restr
 }
 
 // Right-looking blocked Cholesky, in place on the lower triangle, in T
-// (FP64; FP32 for the refinement path's factor). skip (optional): systems
-// with skip[s] != 0 are left alone.
+// (FP64; FP32 for the refinement path's factor). gate (optional): only
+// systems with gate[s] == want are factored.
 template <typename T>
 __global__ __launch_bounds__(FT) void k_chol(spi_systems_t sys, T* __restrict__ l_arena,
                                             int32_t* __restrict__ status,
-                                            const int32_t* __restrict__ skip) {
+                                            const int32_t* __restrict__ gate, int want) {
   const int s = blockIdx.x;
-  if (skip && skip[s]) return;
+  if (gate && gate[s] != want) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
   T* A = l_arena + v.moff;
@@ -555,17 +555,20 @@ __device__ void trsv_lower_t_multi(const TL* __restrict__ L, int n, double* Y, i
 
 // A^-1 applied to the kk vectors Y[k * n + i]: two triangular solves with
 // the system's FP64 factor, or, where the system kept its FP32 factor
-// (ws.ir[s]), FP64 iterative refinement over it: x = L32^-T L32^-1 b, then
-// d = L32^-T L32^-1 (b - A x) with the residual from the full FP64 matrix
-// (kept in l_arena), x += d, until max|d| <= 4 eps max|x| or
-// SPI_IR_MAX_ITERS corrections. bval(k, i): entry i of right-hand side k
-// (the Y held on entry); D: scratch of kk * n doubles. The iterations are
-// recorded in ws.ir_iters[s] (their maximum; SPI_IR_MAX_ITERS + 1 when the
-// corrections did not reach FP64 accuracy).
+// (ws.ir[s] == 1), FP64 iterative refinement over it: x = L32^-T L32^-1 b,
+// then, with the residual r = b - A x of the full FP64 matrix (kept in
+// l_arena), x += L32^-T L32^-1 r until the componentwise backward error
+// max_i |r_i| / (sum_j |A_ij| |x_j| + |b_i|) is under sqrt(n) eps (the
+// FP64 solve's own level), at most SPI_IR_MAX_ITERS corrections. bval(k, i):
+// entry i of right-hand side k (the Y held on entry); D: scratch of kk * n
+// doubles. ws.ir_iters[s] records the corrections (their maximum over the
+// calls); kIrFailed is or-ed in when they did not converge, and
+// spi_krige_duals then refactors the system in FP64 and solves again.
+constexpr int kIrFailed = 0x40000000;
 template <typename BF>
 __device__ void ainv_apply(const spi_krige_ws_t& ws, int s, int n, int64_t moff, double* Y,
                            double* D, int kk, BF bval) {
-  if (!(ws.l32 && ws.ir && ws.ir[s])) {
+  if (!(ws.l32 && ws.ir && ws.ir[s] == 1)) {
     const double* L = ws.l_arena + moff;
     trsv_lower_multi(L, n, Y, n, kk);
     trsv_lower_t_multi(L, n, Y, n, kk);
@@ -573,64 +576,67 @@ __device__ void ainv_apply(const spi_krige_ws_t& ws, int s, int n, int64_t moff,
   }
   const float* L = ws.l32 + moff;
   const double* A = ws.l_arena + moff;
-  __shared__ double rmax[2][FT / 32];
+  __shared__ double rmax[FT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double tol = sqrt((double)n) * 2.220446049250313e-16;
   trsv_lower_multi(L, n, Y, n, kk);
   trsv_lower_t_multi(L, n, Y, n, kk);
-  int it = 1;
+  int it = 0;
   bool conv = false;
-  for (; it <= SPI_IR_MAX_ITERS; ++it) {
+  for (;; ++it) {
+    // D = b - A x and the componentwise backward error, a warp per row
+    double be = 0.0;
     __syncthreads();
     for (int i = warp; i < n; i += FT / 32) {
       const double* row = A + (int64_t)i * n;
-      double t[KS];
+      double t[KS], ta[KS];
 #pragma unroll
-      for (int k = 0; k < KS; ++k) t[k] = 0.0;
+      for (int k = 0; k < KS; ++k) t[k] = ta[k] = 0.0;
       for (int j = lane; j < n; j += 32) {
         const double a = row[j];
 #pragma unroll
         for (int k = 0; k < KS; ++k)
-          if (k < kk) t[k] = fma(a, Y[k * n + j], t[k]);
+          if (k < kk) {
+            const double x = Y[k * n + j];
+            t[k] = fma(a, x, t[k]);
+            ta[k] = fma(fabs(a), fabs(x), ta[k]);
+          }
       }
 #pragma unroll
       for (int k = 0; k < KS; ++k)
-        for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+        for (int o = 16; o > 0; o >>= 1) {
+          t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+          ta[k] += __shfl_xor_sync(0xffffffffu, ta[k], o);
+        }
       if (lane == 0)
-        for (int k = 0; k < kk; ++k) D[k * n + i] = bval(k, i) - t[k];
+        for (int k = 0; k < kk; ++k) {
+          const double b = bval(k, i), r = b - t[k];
+          D[k * n + i] = r;
+          const double den = ta[k] + fabs(b);
+          if (den > 0.0) be = fmax(be, fabs(r) / den);
+          else if (r != 0.0) be = __longlong_as_double(0x7ff0000000000000LL);
+        }
     }
+    for (int o = 16; o > 0; o >>= 1) be = fmax(be, __shfl_xor_sync(0xffffffffu, be, o));
     __syncthreads();
-    trsv_lower_multi(L, n, D, n, kk);
-    trsv_lower_t_multi(L, n, D, n, kk);
-    double dm = 0.0, xm = 0.0;
-    for (int e = threadIdx.x; e < kk * n; e += FT) {
-      const double x = Y[e] + D[e];
-      Y[e] = x;
-      dm = fmax(dm, fabs(D[e]));
-      xm = fmax(xm, fabs(x));
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
-      xm = fmax(xm, __shfl_xor_sync(0xffffffffu, xm, o));
-    }
+    if (lane == 0) rmax[warp] = be;
     __syncthreads();
-    if (lane == 0) {
-      rmax[0][warp] = dm;
-      rmax[1][warp] = xm;
-    }
-    __syncthreads();
-    dm = xm = 0.0;
-    for (int w = 0; w < FT / 32; ++w) {
-      dm = fmax(dm, rmax[0][w]);
-      xm = fmax(xm, rmax[1][w]);
-    }
-    if (dm <= 4.0 * 2.220446049250313e-16 * xm) {
+    be = 0.0;
+    for (int w = 0; w < FT / 32; ++w) be = fmax(be, rmax[w]);
+    if (be <= tol) {
       conv = true;
       break;
     }
+    if (it == SPI_IR_MAX_ITERS) break;
+    trsv_lower_multi(L, n, D, n, kk);
+    trsv_lower_t_multi(L, n, D, n, kk);
+    for (int e = threadIdx.x; e < kk * n; e += FT) Y[e] += D[e];
   }
   __syncthreads();
-  if (threadIdx.x == 0 && ws.ir_iters)
-    atomicMax(ws.ir_iters + s, conv ? it : SPI_IR_MAX_ITERS + 1);
+  if (threadIdx.x == 0 && ws.ir_iters) {
+    atomicMax(ws.ir_iters + s, it);
+    if (!conv) atomicOr(ws.ir_iters + s, kIrFailed);
+  }
 }
 
 // EDK systems whose drift rows are linearly dependent with the
@@ -695,6 +701,14 @@ __global__ void k_to_f32(spi_systems_t sys, const double* __restrict__ l_arena,
     l32[v.moff + e] = (float)l_arena[v.moff + e];
 }
 
+// Systems whose refinement did not converge fall back to the FP64 factor
+// (ir = 2): spi_krige_duals then factors and solves them again.
+__global__ void k_ir_fail_gate(spi_systems_t sys, spi_krige_ws_t ws) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= sys.n_sys) return;
+  if (ws.ir[s] == 1 && (ws.ir_iters[s] & kIrFailed)) ws.ir[s] = 2;
+}
+
 // Which systems keep the FP32 factor: it succeeded with cond <= cond_ir;
 // the others' status is reset for the FP64 factorisation.
 __global__ void k_ir_gate(spi_systems_t sys, spi_krige_ws_t ws, double cond_ir) {
@@ -728,9 +742,9 @@ __global__ __launch_bounds__(FT) void k_cond_est(spi_systems_t sys,
                                                 const TL* __restrict__ l_arena,
                                                 const int32_t* __restrict__ status,
                                                 double* __restrict__ cond, int nk,
-                                                const int32_t* __restrict__ skip) {
+                                                const int32_t* __restrict__ gate, int want) {
   const int s = blockIdx.x;
-  if (skip && skip[s]) return;
+  if (gate && gate[s] != want) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
   if (status[s] != 0) {
@@ -769,9 +783,11 @@ __global__ __launch_bounds__(FT) void k_cond_est(spi_systems_t sys,
 // Dynamic shared memory: nk x n doubles.
 __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_systems_t sys,
                                                    spi_krige_ws_t ws,
-                                                   const double* __restrict__ vals, int nk) {
+                                                   const double* __restrict__ vals, int nk,
+                                                   int only_fallback) {
   const int s = blockIdx.x;
   if (ws.route[s] != 0) return;
+  if (only_fallback && ws.ir[s] != 2) return;
   SysView v = sys_view(sys, s);
   const int n = v.n;
   extern __shared__ double ysm[];
@@ -841,9 +857,10 @@ __global__ __launch_bounds__(FT) void k_duals_solve(spi_domain_t dom, spi_system
 __global__ __launch_bounds__(FT) void k_duals_solve_steps(spi_domain_t dom, spi_systems_t sys,
                                                          spi_krige_ws_t ws,
                                                          const double* __restrict__ vals,
-                                                         int nk) {
+                                                         int nk, int only_fallback) {
   const int s = blockIdx.y;
   if (ws.route[s] != 0) return;
+  if (only_fallback && ws.ir[s] != 2) return;
   const int64_t sb = sys.step_off[s], se = sys.step_off[s + 1];
   if (sb + (int64_t)blockIdx.x * nk >= se) return;
   SysView v = sys_view(sys, s);
@@ -1146,20 +1163,21 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   if (ir) {
     // FP32 factor first; systems that keep it skip the FP64 one
     k_to_f32<<<dim3(gx, sys->n_sys), 256, 0, st>>>(sy, ws->l_arena, ws->l32);
-    k_chol<float><<<sys->n_sys, FT, 0, st>>>(sy, ws->l32, ws->status, nullptr);
+    k_chol<float><<<sys->n_sys, FT, 0, st>>>(sy, ws->l32, ws->status, nullptr, 0);
     k_cond_est<float><<<sys->n_sys, FT, ysm, st>>>(sy, ws->l32, ws->status, ws->cond, nk,
-                                                    nullptr);
+                                                    nullptr, 0);
     k_ir_gate<<<(sys->n_sys + 255) / 256, 256, 0, st>>>(sy, *ws,
-                                                       ws->cond_ir > 0 ? ws->cond_ir : 1e6);
+                                                       ws->cond_ir > 0 ? ws->cond_ir : 1e12);
     SPI_LAUNCH_CHECK();
   }
-  k_chol<double><<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status, ir ? ws->ir : nullptr);
+  k_chol<double><<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status, ir ? ws->ir : nullptr,
+                                            0);
   SPI_LAUNCH_CHECK();
   if (ws->linv_arena) {
     k_trinv<<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->linv_arena, ws->status, ws->cond);
   } else {
     k_cond_est<double><<<sys->n_sys, FT, ysm, st>>>(sy, ws->l_arena, ws->status, ws->cond, nk,
-                                                     ir ? ws->ir : nullptr);
+                                                     ir ? ws->ir : nullptr, 0);
   }
   SPI_LAUNCH_CHECK();
   size_t gsm = (size_t)(sys->max_n + GA) * (2 * sizeof(double) + sizeof(int));
@@ -1216,18 +1234,38 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
         cudaFuncSetAttribute(k_duals_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)ysm) != cudaSuccess)
       return SPI_ERR_CUDA;
-    k_duals_solve<<<sys->n_sys, FT, ysm, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals, nk);
-    SPI_LAUNCH_CHECK();
-    // the steps: groups of nk spread over gx CTAs per system
     if (ysm > 48 * 1024 &&
         cudaFuncSetAttribute(k_duals_solve_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)ysm) != cudaSuccess)
       return SPI_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the steps: groups of nk spread over gx CTAs per system
     int gx = (304 + sys->n_sys - 1) / sys->n_sys;
     gx = gx < 1 ? 1 : (gx > 64 ? 64 : gx);
-    k_duals_solve_steps<<<dim3(gx, sys->n_sys), FT, ysm, (cudaStream_t)stream>>>(*dom, *sys,
-                                                                               *ws, vals, nk);
-    SPI_LAUNCH_CHECK();
+    const int passes = ir_mode(ws) ? 2 : 1;
+    for (int pass = 0; pass < passes; ++pass) {
+      if (pass == 1) {
+        // systems whose refinement did not converge: FP64 factor, then
+        // their duals again
+        k_ir_fail_gate<<<(sys->n_sys + 255) / 256, 256, 0, st>>>(*sys, *ws);
+        k_chol<double><<<sys->n_sys, FT, 0, st>>>(*sys, ws->l_arena, ws->status, ws->ir, 2);
+        int nk1;
+        size_t ysm1;
+        if ((rc = solve_smem(sys->max_n, &nk1, &ysm1))) return rc;
+        if (ysm1 > 48 * 1024 &&
+            cudaFuncSetAttribute(k_cond_est<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ysm1) != cudaSuccess)
+          return SPI_ERR_CUDA;
+        k_cond_est<double><<<sys->n_sys, FT, ysm1, st>>>(*sys, ws->l_arena, ws->status,
+                                                         ws->cond, nk1, ws->ir, 2);
+        SPI_LAUNCH_CHECK();
+      }
+      k_duals_solve<<<sys->n_sys, FT, ysm, st>>>(*dom, *sys, *ws, vals, nk, pass);
+      SPI_LAUNCH_CHECK();
+      k_duals_solve_steps<<<dim3(gx, sys->n_sys), FT, ysm, st>>>(*dom, *sys, *ws, vals, nk,
+                                                                 pass);
+      SPI_LAUNCH_CHECK();
+    }
   }
   return SPI_OK;
 }

@@ -19,7 +19,10 @@
 // k_gjm_finish unscrambles the columns in reverse pivot order and sets the
 // route as k_gj does (||M||_F ||P||_F against 1e15, the pinv check's
 // candidates). No kernel waits on another CTA: the steps are ordered by
-// their launches on the stream.
+// their launches on the stream. Outside a stream capture the host reads
+// the largest pending system's row count back after the set-up and
+// launches only that many steps (a batch with no exact-inverse system
+// launches none).
 #include "spi_common.cuh"
 #include "spi_saddle.cuh"
 
@@ -49,7 +52,7 @@ __device__ __forceinline__ GjSys gj_sys(const spi_domain_t& dom, const spi_syste
   g.m = g.n + extra_rows(sys.kind, dom.n_drift);
   g.idx = sys.stn_idx + off;
   g.A = ws.l_arena + sys.mat_off[s];
-  double* sc = ws.gj_scratch + 2 * off + (int64_t)(2 * GAM + 1) * s;
+  double* sc = ws.gj_scratch + 1 + 2 * off + (int64_t)(2 * GAM + 1) * s;
   g.f = sc;
   g.piv = sc + g.m;
   g.fm = sc + 2 * g.m;
@@ -77,6 +80,9 @@ __global__ __launch_bounds__(GT) void k_gjm_setup(spi_domain_t dom, spi_systems_
   if (blockIdx.x == 0 && threadIdx.x == 0) ws.route[s] = chol ? 0 : kPending;
   if (chol) return;
   const GjSys g = gj_sys(dom, sys, ws, s);
+  // the largest pending system's rows: the host launches that many steps
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    atomicMax(reinterpret_cast<int*>(ws.gj_scratch), g.m);
   const spi_vg_t vg = sys.vg[s];
   const int sk = sys.kind == SPI_KIND_SK;
   const int64_t mm = (int64_t)g.m * g.m;
@@ -223,12 +229,28 @@ int launch_gj_multi(const spi_domain_t& dom, const spi_systems_t& sys, const spi
   const int max_m = sys.max_n + extra_rows(sys.kind, dom.n_drift);
   int gx = (int)(((int64_t)max_m * max_m + GT * 8 - 1) / (GT * 8));
   gx = gx < 1 ? 1 : (gx > 256 ? 256 : gx);
+  if (cudaMemsetAsync(ws.gj_scratch, 0, sizeof(int), st) != cudaSuccess) return SPI_ERR_CUDA;
   k_gjm_setup<<<dim3(gx, sys.n_sys), GT, 0, st>>>(dom, sys, ws, cond_max);
   SPI_LAUNCH_CHECK();
+  // Outside a stream capture the steps stop at the largest pending system
+  // (none: no step at all), read back once per batch; a captured graph
+  // keeps every step up to the batch's largest system (the kernels of a
+  // system with fewer rows, or not pending, return at once).
+  int steps = max_m;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return SPI_ERR_CUDA;
+  if (cap == cudaStreamCaptureStatusNone) {
+    int h = 0;
+    if (cudaMemcpyAsync(&h, ws.gj_scratch, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return SPI_ERR_CUDA;
+    steps = h < max_m ? h : max_m;
+  }
   // the update: about 8 rows per warp per step
   int ux = (max_m + (GT / 32) * 8 - 1) / ((GT / 32) * 8);
   ux = ux < 1 ? 1 : ux;
-  for (int k = 0; k < max_m; ++k) {
+  for (int k = 0; k < steps; ++k) {
     k_gjm_pivot<<<sys.n_sys, GT, 0, st>>>(dom, sys, ws, k);
     k_gjm_update<<<dim3(ux, sys.n_sys), GT, 0, st>>>(dom, sys, ws, k);
   }

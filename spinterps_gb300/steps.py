@@ -241,7 +241,7 @@ class _KrigeBatch:
 
     def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
                  want_var=False, tensor_cores=True, n_probe=0, need_linv=None, pinv=None,
-                 ir=True, cond_ir=1e6):
+                 ir=True, cond_ir=1e12):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -344,7 +344,7 @@ class _KrigeBatch:
         self.max_m = int(ns.max()) + self.a_rows
         self.gj = None
         if self.max_m >= GJ_MULTI_MIN_M:
-            self.gj = torch.empty(2 * int(stn_off[-1]) + (2 * nat.GA + 1) * len(ch),
+            self.gj = torch.empty(1 + 2 * int(stn_off[-1]) + (2 * nat.GA + 1) * len(ch),
                                   dtype=torch.float64, device=dev)
         # the mixed path without the OK variance's inverse factor: every
         # system factored in FP32 first, its duals refined in FP64 where
@@ -478,6 +478,17 @@ class _KrigeBatch:
                 _ptr(self.vals), ws, 1 if want_var else 0, prec, filt, float(cond_split),
                 ctypes.byref(out), tile, s))
 
+    def gj_launches(self):
+        """Kernels of the exact-inverse elimination in spi_krige_factor: one
+        (one CTA per system), or, step by step over the GPU, set-up and
+        finish plus two per row of the largest system that took the
+        exact-inverse path (read from the routes of the last run)."""
+        if self.gj is None:
+            return 1
+        route = self.route.cpu().numpy()
+        pend = self.n[route != 0]
+        return 2 + (2 * int(pend.max() + self.a_rows) if pend.size else 0)
+
     def passes(self):
         """The cell-kernel passes of run(): (precision, route filter)."""
         return [(1, 1), (0, 2)] if self.precision == 1 else [(0, 0)]
@@ -519,7 +530,7 @@ class InterpPlan:
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
                  cond_max=1e13, cond_split=None, tensor_cores=True, probe_cells=1024,
-                 probe_tol=2e-6, cond_df=COND_DF, refine=True, cond_ir=1e6):
+                 probe_tol=2e-6, cond_df=COND_DF, refine=True, cond_ir=1e12):
         dev = self.dev = _require_cuda(device)
         if cond_split is None:
             # a cap under the probe; without it, the a-priori split
@@ -785,19 +796,24 @@ class InterpPlan:
             # exact-inverse steps whose inverse is pinv's truncated one
             self.info.setdefault("pinv_steps", {})[kind] = sorted(pinv)
             # the FP32 factor with FP64 refinement: steps and iterations
-            irs, iters = [], {}
+            # (ir 1: refined over the FP32 factor; 2: refinement did not
+            # converge, factored and solved again in FP64)
+            irs, iters, back = [], {}, []
             for b in batches:
                 if b.ir is None:
                     continue
                 kept = b.ir.cpu().numpy()
                 its = b.ir_iters.cpu().numpy()
                 for k, sl in enumerate(b.steps_l):
-                    if kept[k]:
+                    if kept[k] == 1:
                         for j in sl:
                             irs.append(int(j))
-                            iters[int(j)] = int(its[k])
+                            iters[int(j)] = int(its[k] & 0xFFFF)
+                    elif kept[k] == 2:
+                        back.extend(int(j) for j in sl)
             self.info.setdefault("ir_steps", {})[kind] = sorted(irs)
             self.info.setdefault("ir_iters", {})[kind] = iters
+            self.info.setdefault("ir_fallback_steps", {})[kind] = sorted(back)
             self.info["cond"][kind] = cond
         return self.info
 
@@ -818,11 +834,14 @@ class InterpPlan:
                 # build, Cholesky, inverse or condition estimate, the
                 # exact-inverse elimination (one kernel, or set-up + 2 per
                 # row + finish), the pinv check
-                n += 3 + (2 * b.max_m + 2 if b.gj is not None else 1) + (b.pinv is not None)
+                n += 3 + b.gj_launches() + (b.pinv is not None)
                 n += 1 if kind == "EDK" else 0  # the drift-dependence check
                 # the FP32 factor of the refinement path: copy, Cholesky,
                 # condition estimate, gate
                 n += 4 if b.l32 is not None else 0
+                # the refinement's fallback pass: gate, FP64 Cholesky,
+                # condition estimate, the two dual kernels again
+                n += 5 if b.l32 is not None else 0
                 n += 1 if b.X is not None else 3
                 if b.split is not None:
                     n += 2 + (b.X is not None)
@@ -918,7 +937,7 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
                  arena_budget=8 << 30, cond_max=1e13, cond_split=None, tensor_cores=True,
                  probe_cells=1024, probe_tol=2e-6, neb_sel_mthd="all", n_nebs=None,
-                 n_pies=None, refine=True, cond_ir=1e6):
+                 n_pies=None, refine=True, cond_ir=1e12):
     """Interpolate every step onto every cell on the GPU.
 
     ``neb_sel_mthd`` 'nrst' / 'pie' (with ``n_nebs``, ``n_pies``) selects
@@ -933,8 +952,9 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
     they agree to ``probe_tol`` of the fields' scale, and only on the
     Cholesky path with cond <= ``cond_split``. With ``refine`` the mixed
     path factors systems without the OK variance in FP32 and refines their
-    duals in FP64 (kept where the FP32 factor's condition estimate is at
-    most ``cond_ir``). Returns ``(fields, problem_steps)``, plus an info
+    duals in FP64 (tried where the FP32 factor's condition estimate is at
+    most ``cond_ir``; systems whose refinement does not converge are
+    factored and solved again in FP64). Returns ``(fields, problem_steps)``, plus an info
     dict (failed systems, condition estimates, tiers, refinement
     iterations) when ``return_info``.
     """

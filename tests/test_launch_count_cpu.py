@@ -26,13 +26,15 @@ def entry_kernels(name, batch):
         # build, Cholesky, inverse or condition estimate, Gauss-Jordan (one
         # kernel, or set-up + 2 per row + finish over the GPU), and the pinv
         # check of exact-inverse systems when the batch has its scratch
-        gj = 2 * batch.max_m + 2 if batch.gj is not None else 1
+        gj = batch.gj_launches()
         # + the FP32 factor of the refinement path (copy, Cholesky,
         # condition estimate, gate)
         return (3 + gj + (batch.pinv is not None) + (4 if batch.l32 is not None else 0)
                 + (batch.kind == "EDK"))
     if name == "spi_krige_duals":
-        return 1 if batch.X is not None else 3  # + the two triangular-solve kernels
+        # + the two triangular-solve kernels, + the refinement's fallback
+        # pass (gate, Cholesky, condition estimate, both solve kernels)
+        return 1 if batch.X is not None else (3 + (5 if batch.l32 is not None else 0))
     return {"spi_split_f64": 1, "spi_krige_var_tc": 1, "spi_krige_var_df": 1,
             "spi_krige_cells": 1, "spi_krige_cells_tiled": 1, "spi_krige_tier": 1}[name]
 
@@ -144,13 +146,12 @@ def test_plan_dry_run(monkeypatch, precision):
             # step-by-step elimination with its scratch (systems >= 256 rows)
             ws, sy = a[2]._obj, a[1]._obj
             gj = 1
-            if ws.gj_scratch:
-                gj = 2 * (sy.max_n + (0 if sy.kind == 1 else 1 + a[0]._obj.n_drift
-                                      if sy.kind == 2 else 1)) + 2
+            assert not ws.gj_scratch  # small systems: one CTA each
             return (3 + gj + bool(ws.pinv_scratch) + (4 if ws.l32 and not ws.linv_arena else 0)
                     + (sy.kind == 2))
         if name == "spi_krige_duals":
-            return 1 if a[3]._obj.linv_arena else 3
+            ws = a[3]._obj
+            return 1 if ws.linv_arena else (3 + (5 if ws.l32 else 0))
         return 1
 
     for timing in (False, True):
