@@ -254,6 +254,14 @@ typedef struct {
                             step by step over the whole GPU (two launches per
                             step, the same arithmetic); NULL: one CTA per
                             system */
+    float *linv_tc;      /* Linv's three TF32 terms per system, packed by
+                            spi_krige_var_tc_pack in the tensor cores'
+                            shared-memory tile order: per block of 256 rows,
+                            per chunk of 16 columns (up to the block's last
+                            row), 3 tiles of 256 x 16 TF32 values (48 KB);
+                            required by spi_krige_var_tc */
+    const int64_t *linv_tc_off; /* [n_sys + 1]: first 48 KB chunk of each
+                            system in linv_tc (see spi_krige_var_tc_pack) */
 } spi_krige_ws_t;
 
 /* Build and factor every system of the batch in FP64.
@@ -381,12 +389,24 @@ int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n
  * (ws->tier, else route 0 and cond <= cond_split; kinds OK / EDK) on the tensor cores
  * (tcgen05, 3xTF32: Linv and the right-hand sides as TF32 hi/lo pairs,
  * FP32 accumulation in tensor memory), into ws->cell_yy [n_sys, n_cells].
- * Requires ws->linv_hi (spi_split_f64 of linv_arena) and the domain's
- * split coordinates. Replaces the variance half of
- * interp/steps.py:403-435 (var = lambda'r + mu per cell and step). */
+ * Requires ws->linv_tc (spi_krige_var_tc_pack) and the domain's split
+ * coordinates. Replaces the variance half of interp/steps.py:403-435
+ * (var = lambda'r + mu per cell and step). */
 int spi_krige_var_tc(const spi_domain_t *dom, const spi_systems_t *sys,
                      const spi_krige_ws_t *ws, double cond_split, int32_t *err_flag,
                      spi_stream_t stream);
+
+/* Pack Linv (ws->linv_hi / linv_lo, spi_split_f64 of linv_arena) of every
+ * route-0 system into ws->linv_tc for spi_krige_var_tc: Linv = b0 + b1 + b2
+ * in TF32 terms (b0 the TF32 rounding of hi, b1 of the remainder plus lo,
+ * b2 what is left), each 256-row block's rows 0..255 by 16-column chunks
+ * up to the block's last row, each chunk 3 tiles of 256 x 16 values in the
+ * no-swizzle K-major core-matrix order the MMA reads (one bulk copy per
+ * chunk). System s's chunks start at chunk ws->linv_tc_off[s]; a system
+ * of n stations has sum over blocks b of ceil(min(n, 256 (b + 1)) / 16)
+ * chunks. */
+int spi_krige_var_tc_pack(const spi_systems_t *sys, const spi_krige_ws_t *ws,
+                          spi_stream_t stream);
 
 /* The same term |Linv c|^2 in double-float on the FP32 pipe (every product
  * split by FMA, sums by TwoSum: ~1e-9 of the sill), into ws->cell_yy, for

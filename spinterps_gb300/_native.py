@@ -71,7 +71,8 @@ class KrigeWsT(ctypes.Structure):
                 ("linv_lo", c_ptr), ("g_hi", c_ptr), ("g_lo", c_ptr), ("w_hi", c_ptr),
                 ("w_lo", c_ptr), ("cell_yy", c_ptr), ("tier", c_ptr), ("var_cells", c_ptr),
                 ("pinv_scratch", c_ptr), ("pinv_used", c_ptr), ("l32", c_ptr), ("ir", c_ptr),
-                ("ir_iters", c_ptr), ("cond_ir", c_dbl), ("gj_scratch", c_ptr)]
+                ("ir_iters", c_ptr), ("cond_ir", c_dbl), ("gj_scratch", c_ptr),
+                ("linv_tc", c_ptr), ("linv_tc_off", c_ptr)]
 
 
 class OutT(ctypes.Structure):
@@ -107,6 +108,7 @@ _SIGS = {
     "spi_krige_tier": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_i64, c_ptr, c_ptr,
                        c_ptr, c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr,
                        c_ptr],
+    "spi_krige_var_tc_pack": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_ptr],
     "spi_krige_var_df": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],
     "spi_krige_var_tc": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),

@@ -10,20 +10,29 @@
 // One CTA = 128 cells x 256 threads. The accumulator D [128 cells x 256
 // rows of Linv] lives in tensor memory (TMEM lane = cell, column = row), so
 // each lane squares and sums its own row of D. Rows of Linv go in blocks of
-// 256 (the MMA's N), the stations (K) in chunks of 16: per chunk all
-// threads stage A = the right-hand sides (128 x 16, generated in
-// double-float by rhs_df) and B = Linv's rows (256 x 16, triangular)
-// in shared memory in the no-swizzle K-major layout (8-row x 16-byte core
-// matrices), A as two TF32 terms (a0 + a1, ~22 bits), Linv as three
-// (b0 + b1 + b2, ~33 bits: its rounding, amplified by the cancellation in
-// Linv c, dominates the variance's error). One thread then issues 2
-// K-steps x 5 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 + a1 b1, FP32
-// accumulation in TMEM) and commits them to an mbarrier that every thread
-// waits on (with an iteration limit: on expiry the kernel raises err_flag,
-// waits once more, with the same limit, for the MMAs in flight, frees its
-// TMEM and returns). Squares are summed in double-float (FP32 pairs: the FP64
-// pipe is 1/64 of FP32 on GB300); the mixed path's probe checks every
-// system's variance against the FP64 kernel.
+// 256 (the MMA's N), the stations (K) in chunks of 16, in a two-stage
+// shared-memory ring:
+//   - B, Linv's rows (256 x 16, triangular) as three TF32 terms (b0 + b1 +
+//     b2, ~33 bits: Linv's rounding, amplified by the cancellation in
+//     Linv c, dominates the variance's error), is packed once per system in
+//     the MMA's tile order (spi_krige_var_tc_pack) and arrives by one bulk
+//     copy (cp.async.bulk, 48 KB) per chunk, issued by one thread and
+//     counted on an mbarrier;
+//   - A, the cells' right-hand sides (128 x 16), is generated by all
+//     threads in double-float (rhs_df) and stored as two TF32 terms (a0 +
+//     a1, ~22 bits), in the no-swizzle K-major layout (8-row x 16-byte core
+//     matrices).
+// One thread issues the chunk's 2 K-steps x 5 MMAs (a0 b0 + a0 b1 + a1 b0 +
+// a0 b2 + a1 b1, FP32 accumulation in TMEM) and commits them to the
+// stage's mbarrier, then every thread goes on to the next chunk: the
+// right-hand sides of chunk c + 1 are generated while chunk c's MMAs run,
+// and a stage is refilled only after its previous MMAs completed. Every
+// wait is bounded: on expiry the kernel raises err_flag, drains the MMAs in
+// flight on a best-effort basis (one more bounded wait), frees its TMEM and
+// returns; the probe's tier choice (spi_krige_tier) then keeps every system
+// in FP64 and the host raises. Squares are summed in double-float (FP32
+// pairs: the FP64 pipe is 1/64 of FP32 on GB300); the mixed path's probe
+// checks every system's variance against the FP64 kernel.
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
 
@@ -35,9 +44,11 @@ constexpr int VT_KC = 16;   // stations per staged chunk
 constexpr int VT_T = 256;   // threads
 constexpr long VT_SPIN = 1L << 26;   // mbarrier polls before giving up
 
-constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;
-constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;
-constexpr size_t VT_SMEM = 2 * VT_A_BYTES + 3 * VT_B_BYTES;
+constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;       // one TF32 term of A
+constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;       // one TF32 term of B
+constexpr size_t VT_STAGE = 2 * VT_A_BYTES + 3 * VT_B_BYTES;  // A (2 terms), B (3 terms)
+constexpr size_t VT_SMEM = 2 * VT_STAGE;                      // two stages
+constexpr int VT_CHUNK_FLOATS = (int)(3 * VT_B_BYTES / 4);    // one packed chunk of B
 
 struct VarTcArgs {
   spi_domain_t dom;
@@ -101,6 +112,24 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity
   return done != 0;
 }
 
+// Chunks of 16 columns of B in the 256-row block starting at row rb.
+__device__ __forceinline__ int vt_chunks(int n, int rb) { return (min(n, rb + VT_N) + VT_KC - 1) / VT_KC; }
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
+}
+
+// One thread: B of chunk (rb, kc) by one bulk copy into the stage, counted
+// on the stage's mbarrier (expect_tx of the copy's bytes).
+__device__ __forceinline__ void vt_load_b(uint32_t dst, const float* src, uint32_t mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
+               "r"((uint32_t)(3 * VT_B_BYTES)));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"((uint32_t)(3 * VT_B_BYTES)), "r"(mbar)
+      : "memory");
+}
+
 __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const int s = blockIdx.y;
   const int64_t C = A.dom.n_cells;
@@ -112,22 +141,17 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const int64_t soff = A.sys.stn_off[s];
   const int n = (int)(A.sys.stn_off[s + 1] - soff);
   const int32_t* idx = A.sys.stn_idx + soff;
-  const int64_t moff = A.sys.mat_off[s];
   const spi_vg_t vg = A.sys.vg[s];
   const double sh = A.ws.shift[s];
-  const float* Lh = A.ws.linv_hi + moff;
-  const float* Ll = A.ws.linv_lo + moff;
-
+  const float* pk = A.ws.linv_tc + (int64_t)A.ws.linv_tc_off[s] * VT_CHUNK_FLOATS;
   extern __shared__ __align__(1024) unsigned char smv[];
-  unsigned char* sAh = smv;
-  unsigned char* sAl = sAh + VT_A_BYTES;
-  unsigned char* sB0 = sAl + VT_A_BYTES;
-  unsigned char* sB1 = sB0 + VT_B_BYTES;
-  unsigned char* sB2 = sB1 + VT_B_BYTES;
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t bbar[2];   // B of a stage arrived
+  __shared__ __align__(8) uint64_t mbar[2];   // the stage's MMAs completed
   __shared__ uint32_t tbase;
   __shared__ int fail;
   __shared__ double half_yy[VT_M];
+  auto stage_a = [&](int st) { return smv + st * VT_STAGE; };
+  auto stage_b = [&](int st) { return smv + st * VT_STAGE + 2 * VT_A_BYTES; };
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) {
@@ -138,7 +162,10 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   }
   if (tid == 0) {
     fail = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
+    for (int q = 0; q < 2; ++q) {
+      mbar_init(smem_u32(&bbar[q]), 1);
+      mbar_init(smem_u32(&mbar[q]), 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -163,18 +190,37 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   // epilogue roles: TMEM lanes of warp % 4, column half warp / 4
   const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
   df yy = {0.f, 0.f};  // sum of squares, double-float (no FP64 pipe per row)
-  uint32_t phase = 0;
-
-  for (int rb = 0; rb < n; rb += VT_N) {
-    const int kend = min(n, rb + VT_N);
-    for (int k0 = 0; k0 < kend; k0 += VT_KC) {
+  // g: chunks issued so far (over every row block); stage g & 1 holds
+  // chunk g, and its mbarriers complete once per use: phase parity
+  // (g >> 1) & 1. seen: chunks whose MMAs every thread has seen complete.
+  int g = 0, seen = 0;
+  auto wait_mma = [&](int upto) {  // MMAs of chunks < upto complete
+    while (seen < upto && !fail) {
+      if (!mbar_wait_bounded(smem_u32(&mbar[seen & 1]), (uint32_t)((seen >> 1) & 1)))
+        atomicExch(&fail, 1);
+      ++seen;
+    }
+  };
+  int chunk0 = 0;  // chunks of B of the row blocks before this one
+  for (int rb = 0; rb < n && !fail; rb += VT_N) {
+    const int nc = vt_chunks(n, rb);
+    for (int kc = 0; kc < nc; ++kc, ++g) {
+      const int st = g & 1;
+      // the stage's previous chunk (g - 2) must be consumed before refill
+      wait_mma(g - 1);
+      __syncthreads();
+      if (fail) break;
+      unsigned char* sAh = stage_a(st);
+      unsigned char* sAl = sAh + VT_A_BYTES;
+      if (tid == 0)
+        vt_load_b(smem_u32(stage_b(st)), pk + (int64_t)(chunk0 + kc) * VT_CHUNK_FLOATS,
+                  smem_u32(&bbar[st]));
+      const int k0 = kc * VT_KC;
 #pragma unroll 4
       for (int q = 0; q < VT_KC / 2; ++q) {
         const int kk = khalf * (VT_KC / 2) + q, j = k0 + kk;
         df c = {0.f, 0.f};
-        if (live && j < n) {
-          c = rhs_df(A.dom, vgp, kd, 0, sh, cp, sp4[idx[j]], gc, idx + j);
-        }
+        if (live && j < n) c = rhs_df(A.dom, vgp, kd, 0, sh, cp, sp4[idx[j]], gc, idx + j);
         float h, l;
         tf32_split(c.h, h, l);
         l += c.l;
@@ -182,55 +228,41 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
         *reinterpret_cast<float*>(sAh + o) = h;
         *reinterpret_cast<float*>(sAl + o) = l;
       }
-#pragma unroll 4
-      for (int i = 0; i < VT_N * VT_KC / VT_T; ++i) {
-        const int e = tid + VT_T * i, r = e / VT_KC, k = e % VT_KC;
-        const int row = rb + r, col = k0 + k;
-        float vh = 0.f, vl = 0.f;
-        if (row < n && col <= row) {
-          vh = Lh[(int64_t)row * n + col];
-          vl = Ll[(int64_t)row * n + col];
-        }
-        // Linv in three TF32 terms (~33 bits): its rounding, amplified by
-        // the cancellation in Linv c, dominates the variance's error
-        const float b0 = tf32_rn(vh);
-        const float r1 = (vh - b0) + vl;
-        const float b1 = tf32_rn(r1);
-        const int o = tile_off(VT_N, r, k);
-        *reinterpret_cast<float*>(sB0 + o) = b0;
-        *reinterpret_cast<float*>(sB1 + o) = b1;
-        *reinterpret_cast<float*>(sB2 + o) = r1 - b1;
-      }
       asm volatile("fence.proxy.async.shared::cta;");
       __syncthreads();
       if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (!mbar_wait_bounded(smem_u32(&bbar[st]), (uint32_t)((g >> 1) & 1))) {
+          atomicExch(&fail, 1);
+        } else {
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t sB0 = smem_u32(stage_b(st));
 #pragma unroll
-        for (int ks = 0; ks < VT_KC / 8; ++ks) {
-          const uint32_t ao = 2 * ks * (VT_M * 16), bo = 2 * ks * (VT_N * 16);
-          const uint64_t ah = umma_desc(smem_u32(sAh) + ao, VT_M * 16, 128);
-          const uint64_t al = umma_desc(smem_u32(sAl) + ao, VT_M * 16, 128);
-          const uint64_t b0 = umma_desc(smem_u32(sB0) + bo, VT_N * 16, 128);
-          const uint64_t b1 = umma_desc(smem_u32(sB1) + bo, VT_N * 16, 128);
-          const uint64_t b2 = umma_desc(smem_u32(sB2) + bo, VT_N * 16, 128);
-          mma_tf32(tmem, ah, b0, idesc, (k0 > 0 || ks > 0) ? 1u : 0u);
-          mma_tf32(tmem, ah, b1, idesc, 1u);
-          mma_tf32(tmem, al, b0, idesc, 1u);
-          mma_tf32(tmem, ah, b2, idesc, 1u);
-          mma_tf32(tmem, al, b1, idesc, 1u);
+          for (int ks = 0; ks < VT_KC / 8; ++ks) {
+            const uint32_t ao = 2 * ks * (VT_M * 16), bo = 2 * ks * (VT_N * 16);
+            const uint64_t ah = umma_desc(smem_u32(sAh) + ao, VT_M * 16, 128);
+            const uint64_t al = umma_desc(smem_u32(sAl) + ao, VT_M * 16, 128);
+            const uint64_t b0 = umma_desc(sB0 + bo, VT_N * 16, 128);
+            const uint64_t b1 = umma_desc(sB0 + (uint32_t)VT_B_BYTES + bo, VT_N * 16, 128);
+            const uint64_t b2 = umma_desc(sB0 + 2 * (uint32_t)VT_B_BYTES + bo, VT_N * 16, 128);
+            mma_tf32(tmem, ah, b0, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+            mma_tf32(tmem, ah, b1, idesc, 1u);
+            mma_tf32(tmem, al, b0, idesc, 1u);
+            mma_tf32(tmem, ah, b2, idesc, 1u);
+            mma_tf32(tmem, al, b1, idesc, 1u);
+          }
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_u32(&mbar)));
+                smem_u32(&mbar[st])));
       }
-      if (!mbar_wait_bounded(smem_u32(&mbar), phase)) atomicExch(&fail, 1);
-      phase ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      __syncthreads();
-      if (fail) break;
     }
+    chunk0 += nc;
+    // this block's MMAs complete, then its rows: each lane's 128 columns
+    // of its half
+    wait_mma(g);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    __syncthreads();
     if (fail) break;
-    // this block's rows: each lane's 128 columns of its half
 #pragma unroll
     for (int cc = 0; cc < 4; ++cc) {
       uint32_t r[32];
@@ -260,10 +292,14 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
     __syncthreads();
   }
   if (fail) {
-    // the timed-out MMAs may still be writing tensor memory: wait for their
-    // commit once more, with the same limit, before the columns are freed
-    mbar_wait_bounded(smem_u32(&mbar), phase ^ 1u);
+    // best-effort drain: the MMAs and bulk copies in flight may still be
+    // writing; wait once more, with the same limit, for every stage's last
+    // commit before the columns are freed
+    if (tid == 0)
+      for (int q = seen; q < g; ++q)
+        mbar_wait_bounded(smem_u32(&mbar[q & 1]), (uint32_t)((q >> 1) & 1));
     asm volatile("tcgen05.fence::after_thread_sync;");
+    __syncthreads();
   }
   const double yy64 = (double)yy.h + (double)yy.l;
   if (e_half == 1) half_yy[e_cell] = yy64;
@@ -278,6 +314,45 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(VT_N));
 }
 
+// Linv's TF32 terms of chunk (blockIdx.x) of system blockIdx.y in the tile
+// order k_var_tc reads (see spi_krige_var_tc_pack).
+__global__ __launch_bounds__(VT_T) void k_var_tc_pack(spi_systems_t sys, spi_krige_ws_t ws) {
+  const int s = blockIdx.y;
+  if (ws.route[s] != 0) return;
+  const int64_t soff = sys.stn_off[s];
+  const int n = (int)(sys.stn_off[s + 1] - soff);
+  // the chunk's row block and column chunk
+  int t = blockIdx.x, rb = 0;
+  while (rb < n && t >= vt_chunks(n, rb)) {
+    t -= vt_chunks(n, rb);
+    rb += VT_N;
+  }
+  if (rb >= n) return;
+  const int k0 = t * VT_KC;
+  const int64_t moff = sys.mat_off[s];
+  const float* Lh = ws.linv_hi + moff;
+  const float* Ll = ws.linv_lo + moff;
+  float* dst = ws.linv_tc + (ws.linv_tc_off[s] + blockIdx.x) * (int64_t)VT_CHUNK_FLOATS;
+  unsigned char* d0 = reinterpret_cast<unsigned char*>(dst);
+  for (int i = 0; i < VT_N * VT_KC / VT_T; ++i) {
+    const int e = threadIdx.x + VT_T * i, r = e / VT_KC, k = e % VT_KC;
+    const int row = rb + r, col = k0 + k;
+    float vh = 0.f, vl = 0.f;
+    if (row < n && col <= row) {
+      vh = Lh[(int64_t)row * n + col];
+      vl = Ll[(int64_t)row * n + col];
+    }
+    // Linv in three TF32 terms (~33 bits)
+    const float b0 = tf32_rn(vh);
+    const float r1 = (vh - b0) + vl;
+    const float b1 = tf32_rn(r1);
+    const int o = tile_off(VT_N, r, k);
+    *reinterpret_cast<float*>(d0 + o) = b0;
+    *reinterpret_cast<float*>(d0 + VT_B_BYTES + o) = b1;
+    *reinterpret_cast<float*>(d0 + 2 * VT_B_BYTES + o) = r1 - b1;
+  }
+}
+
 }  // namespace spi
 
 using namespace spi;
@@ -288,9 +363,9 @@ extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sy
   if (!dom || !sys || !ws || !err_flag) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (sys->n_sys == 0 || dom->n_cells == 0) return SPI_OK;
-  if (!ws->cell_yy || !ws->linv_hi || !ws->route || !ws->cond || !ws->shift ||
-      !dom->cell_split || !dom->stn_split || !sys->vg || !sys->stn_off || !sys->stn_idx ||
-      !sys->mat_off)
+  if (!ws->cell_yy || !ws->linv_tc || !ws->linv_tc_off || !ws->route || !ws->cond ||
+      !ws->shift || !dom->cell_split || !dom->stn_split || !sys->vg || !sys->stn_off ||
+      !sys->stn_idx || !sys->mat_off)
     return SPI_ERR_ARG;
   const int64_t tiles = (dom->n_cells + VT_M - 1) / VT_M;
   if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
@@ -300,6 +375,26 @@ extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sy
   VarTcArgs A{*dom, *sys, *ws, cond_split, err_flag};
   dim3 grid((unsigned)tiles, (unsigned)sys->n_sys);
   k_var_tc<<<grid, VT_T, VT_SMEM, (cudaStream_t)stream>>>(A);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
+
+extern "C" int spi_krige_var_tc_pack(const spi_systems_t* sys, const spi_krige_ws_t* ws,
+                                     spi_stream_t stream) {
+  if (!sys || !ws) return SPI_ERR_ARG;
+  if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
+  if (sys->n_sys == 0) return SPI_OK;
+  if (!ws->linv_hi || !ws->linv_lo || !ws->linv_tc || !ws->linv_tc_off || !ws->route ||
+      !sys->stn_off || !sys->mat_off || sys->max_n < 1)
+    return SPI_ERR_ARG;
+  // chunks of the largest system
+  int most = 0;
+  for (int rb = 0; rb < sys->max_n; rb += VT_N) {
+    const int e = sys->max_n < rb + VT_N ? sys->max_n : rb + VT_N;
+    most += (e + VT_KC - 1) / VT_KC;
+  }
+  dim3 grid((unsigned)most, (unsigned)sys->n_sys);
+  k_var_tc_pack<<<grid, VT_T, 0, (cudaStream_t)stream>>>(*sys, *ws);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

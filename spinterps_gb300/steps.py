@@ -305,9 +305,18 @@ class _KrigeBatch:
         # the OK variance)
         self.yy = None
         self.tc_err = None
+        self.linv_tc = self.linv_tc_off = None
         if precision == 1 and want_var and kind == "OK" and tensor_cores:
             self.yy = torch.empty(len(ch) * dom.C, dtype=torch.float64, device=dev)
             self.tc_err = torch.zeros(1, dtype=torch.int32, device=dev)
+            # Linv's TF32 terms in the tensor cores' tile order: per system,
+            # per 256-row block, 16-column chunks up to the block's last row,
+            # 48 KB each (spi_krige_var_tc_pack)
+            chunks = np.array([sum((min(int(n), rb + 256) + 15) // 16
+                                   for rb in range(0, int(n), 256)) for n in ns], dtype=np.int64)
+            off = np.concatenate([[0], np.cumsum(chunks)]).astype(np.int64)
+            self.linv_tc = torch.empty(int(off[-1]) * 12288, dtype=torch.float32, device=dev)
+            self.linv_tc_off = torch.as_tensor(off, device=dev)
         # the probe (precision 1): both tiers on a few cells decide each
         # system's tier (spi_krige_tier)
         self.tier = self.probe = self.probe_df = None
@@ -356,7 +365,8 @@ class _KrigeBatch:
             self.ir_iters = torch.zeros(n_sys, dtype=torch.int32, device=dev)
         extra = dict(pinv_scratch=_ptr(pinv), pinv_used=_ptr(self.pinv_used),
                      gj_scratch=_ptr(self.gj), l32=_ptr(self.l32), ir=_ptr(self.ir),
-                     ir_iters=_ptr(self.ir_iters), cond_ir=float(cond_ir))
+                     ir_iters=_ptr(self.ir_iters), cond_ir=float(cond_ir),
+                linv_tc=_ptr(self.linv_tc), linv_tc_off=_ptr(self.linv_tc_off))
         self.ws = nat.KrigeWsT(*ptrs, _ptr(self.yy), _ptr(self.tier), _ptr(self.var_cells),
                                **extra)
         self.ws_probe = nat.KrigeWsT(*ptrs, _ptr(self.probe[4]) if self.probe else None, None,
@@ -430,6 +440,8 @@ class _KrigeBatch:
             xh, xl, gh, gl, wh, wl = self.split
             if self.X is not None:
                 nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
+                if self.linv_tc is not None:
+                    nat.call("spi_krige_var_tc_pack", ctypes.byref(self.sy), ws, s)
             nat.call("spi_split_f64", _ptr(self.g_cols), _ptr(gh), _ptr(gl), self.g_cols.numel(), s)
             nat.call("spi_split_f64", _ptr(self.w_hat), _ptr(wh), _ptr(wl), self.w_hat.numel(), s)
         if self.probe is not None and probe is not None:
@@ -844,7 +856,7 @@ class InterpPlan:
                 n += 5 if b.l32 is not None else 0
                 n += 1 if b.X is not None else 3
                 if b.split is not None:
-                    n += 2 + (b.X is not None)
+                    n += 2 + (b.X is not None) + (b.linv_tc is not None)
                 if b.probe is not None and self.pdom is not None:
                     n += (b.probe[4] is not None and want_var) + 2 + 1
                     n += 2 if (b.probe_df is not None and want_var) else 0

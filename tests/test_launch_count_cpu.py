@@ -36,7 +36,8 @@ def entry_kernels(name, batch):
         # pass (gate, Cholesky, condition estimate, both solve kernels)
         return 1 if batch.X is not None else (3 + (5 if batch.l32 is not None else 0))
     return {"spi_split_f64": 1, "spi_krige_var_tc": 1, "spi_krige_var_df": 1,
-            "spi_krige_cells": 1, "spi_krige_cells_tiled": 1, "spi_krige_tier": 1}[name]
+            "spi_krige_cells": 1, "spi_krige_cells_tiled": 1, "spi_krige_tier": 1,
+            "spi_krige_var_tc_pack": 1}[name]
 
 
 def make_batch(kind, precision, want_var, n_probe, tensor_cores=True):
