@@ -349,7 +349,7 @@ def measured_peaks():
 # bf16 tensor pipe; the CUDA-core FP32 / FP64 FMA rates measured here
 # (fma_peak_tflops).
 KERNEL_BOUND = {
-    "var_tc": ("tensor", "spi::k_var_tc (tcgen05 3xTF32 OK-variance contraction)"),
+    "var_tc": ("tensor", "spi::k_var_tc (tcgen05 TF32 OK-variance contraction, 5 MMAs per product)"),
     "var_df": ("fp32", "spi::k_var_df (double-float OK-variance contraction, FP32 pipe)"),
     "cells_fp32": ("fp32", "spi::k_krige_cells<float> (FP32 tier: estimates, sum check)"),
     "cells_fp64": ("fp64", "spi::k_krige_cells<double> (FP64 tier: ill-conditioned and "
@@ -394,7 +394,7 @@ def roofline_for(name, k):
     bf16, hbm, src = measured_peaks()
     bound, kernel = KERNEL_BOUND[name]
     if bound == "tensor":
-        peak, psrc = bf16, src + " (bf16 dense; the kernel runs 3 TF32 MMAs per product)"
+        peak, psrc = bf16, src + " (bf16 dense; the kernel runs 5 TF32 MMAs per product: a0b0 + a0b1 + a1b0 + a0b2 + a1b1)"
     elif bound == "fp64":
         peak, psrc = fma_peak_tflops(True), "measured FP64 FMA rate (spi_peak_fma, bench.py)"
     else:
@@ -741,6 +741,18 @@ def field_errors(x, y, floor_frac=1e-3):
                          "rms": float(rel.pow(2).mean().sqrt()) if rel.numel() else None}}
 
 
+def refinement_summary(info, kind):
+    """The FP32 factor + FP64 refinement path of a plan's ``collect_info``:
+    steps refined over the FP32 factor, steps whose refinement did not
+    converge (solved again over an FP64 factor), and the correction counts
+    of the refined steps."""
+    its = list(info.get("ir_iters", {}).get(kind, {}).values())
+    return {"steps": len(info.get("ir_steps", {}).get(kind, [])),
+            "fp64_fallback_steps": len(info.get("ir_fallback_steps", {}).get(kind, [])),
+            "iterations": ({"min": int(min(its)), "median": float(np.median(its)),
+                            "max": int(max(its))} if its else None)}
+
+
 def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
     """The large hourly EDK configuration on one wave of steps: 4000
     stations in a 500 km box, per-station missingness U(0.05, 0.5), two
@@ -807,6 +819,7 @@ def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
     cond = np.array(list(info["cond"]["EDK"].values()))
     n_fast = len(info.get("fp32_tier_steps", {}).get("EDK", []))
     n_cap = int(np.sum(cond <= pm.cond_split))
+    refinement = refinement_summary(info, "EDK")
     sub = np.arange(0, T, fp64_every)
     fm = pm.flds["EDK"][torch.as_tensor(sub, device=pm.flds["EDK"].device)].clone()
     del pm
@@ -855,6 +868,7 @@ def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
            "kernels": kernels, "roofline": roofline_for(dom_k, kernels[dom_k]),
            "tiers": {"fp32": n_fast, "fp64": int(cond.size - n_fast), "cond_under_cap": n_cap,
                      "cond_median": float(np.median(cond)), "cond_max": float(cond.max())},
+           "refinement": refinement,
            "fit": {"seconds": t_fit, "fallback_steps": len(det["_fallback_steps"]),
                    "de_ms": det["_de_ms"], "ms": det["_ms"]},
            "synthesis_s": t_gen}
@@ -984,7 +998,8 @@ def run_stress(args):
                                   "rms": float(dd.pow(2).mean().sqrt() / sc)},
             "tiers": {"fp32_steps": len(info.get("fp32_tier_steps", {}).get("EDK", [])),
                       "fp64_steps": T - len(info.get("fp32_tier_steps", {}).get("EDK", [])),
-                      "cond_min": float(cond.min()), "cond_max": float(cond.max())}}
+                      "cond_min": float(cond.min()), "cond_max": float(cond.max())},
+            "refinement": refinement_summary(info, "EDK")}
     print(json.dumps(line))
 
 

@@ -387,8 +387,9 @@ int spi_krige_tier(const spi_systems_t *sys, const spi_krige_ws_t *ws, int64_t n
 
 /* The OK variance term |Linv c|^2 of every cell of the FP32-tier systems
  * (ws->tier, else route 0 and cond <= cond_split; kinds OK / EDK) on the tensor cores
- * (tcgen05, 3xTF32: Linv and the right-hand sides as TF32 hi/lo pairs,
- * FP32 accumulation in tensor memory), into ws->cell_yy [n_sys, n_cells].
+ * (tcgen05 kind::tf32: Linv as three TF32 terms b0 + b1 + b2, the right-hand
+ * sides as two a0 + a1, five MMAs per product a0b0 + a0b1 + a1b0 + a0b2 +
+ * a1b1, FP32 accumulation in tensor memory), into ws->cell_yy [n_sys, n_cells].
  * Requires ws->linv_tc (spi_krige_var_tc_pack) and the domain's split
  * coordinates. Replaces the variance half of interp/steps.py:403-435
  * (var = lambda'r + mu per cell and step). */

@@ -24,11 +24,17 @@ step engine's:
 Differences, by design:
 - The reference's ``numpy.linalg.pinv`` is replaced by a Gauss-Jordan
   inverse on the GPU. This is the same matrix whenever pinv's cut-off
-  (singular values below m * eps * the largest) removes nothing, which is
-  certain while ||A||_F ||A^-1||_F <= 1 / (m eps).
+  (numpy's default rcond: singular values up to 1e-15 times the largest
+  are dropped) removes nothing, which is certain while
+  ||A||_F ||A^-1||_F <= 1e15.
 - Above that bound, for example with duplicated stations, the matrix takes
-  ``torch.linalg.pinv``: an SVD pseudo-inverse on the GPU with numpy's
-  default cut-off. ``pinv_route`` on the object records which was used.
+  ``torch.linalg.pinv``: an SVD pseudo-inverse on the GPU with torch's
+  default cut-off, m * eps times the largest singular value. An exactly
+  singular matrix's null singular values come out of an SVD as rounding
+  noise of about eps to 16 eps times the largest, on either side of
+  numpy's 1e-15 depending on the LAPACK build; the wider cut-off drops
+  them on every platform. ``pinv_route`` on the object records which
+  inverse was used.
 - ``krige()`` runs once per object. A second call on the reference's
   object appends the components again and adds onto the old matrix, which
   kriges a different system, so here a second call raises RuntimeError.
@@ -48,6 +54,9 @@ from .steps import _require_cuda
 
 _CODES = {b"Rng": 0, b"Nug": 1, b"Sph": 2, b"Exp": 3, b"Lin": 4, b"Gau": 5, b"Pow": 6,
           b"Hol": 7}
+# ||A||_F ||A^-1||_F bound under which numpy.linalg.pinv (rcond 1e-15)
+# drops no singular value: the Gauss-Jordan inverse is its matrix
+PINV_COND = 1e15
 
 
 def parse_model(model):
@@ -117,7 +126,7 @@ def krige_points(kind, xi, yi, zi, xk, yk, model, si=None, sk=None, ixi=None, wa
              ctypes.byref(vg), _ptr(in_dists), _ptr(lhs), _ptr(inv), _ptr(status), _ptr(cond),
              st)
     route = "gj"
-    if int(status.item()) or not float(cond.item()) * m * np.finfo(np.float64).eps <= 1.0:
+    if int(status.item()) or not float(cond.item()) <= PINV_COND:
         inv = torch.linalg.pinv(lhs).contiguous()
         route = "pinv"
     rhss = torch.empty((n_out, m), **f64)

@@ -597,7 +597,7 @@ class InterpPlan:
                      if v is not None]
             var_scale = max(sills) if sills else 1.0
             # variances get 2.5x the estimates' tolerance (still 2x under the
-            # 1e-5 bar): the tensor-core 3xTF32 term carries ~2e-6 of the sill
+            # 1e-5 bar): the tensor-core TF32-split term carries ~2e-6 of the sill
             self.probe_args = (self.pdom, probe_tol * est_scale, 2.5 * probe_tol * var_scale)
         # scratch of the pinv check of exact-inverse systems (spi_krige_factor)
         self.pinv = (torch.empty(nat.SPI_PINV_SCRATCH_DOUBLES, dtype=torch.float64, device=dev)
@@ -959,7 +959,7 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
     (see the module docstring). ``precision`` is "fp64" (plain FP64) or
     "mixed" (FP32 right-hand sides and contractions over the FP64
     factorisation; with ``tensor_cores`` the OK variance of the FP32 tier
-    runs on tcgen05 in 3xTF32). In the mixed path each system first runs in
+    runs on tcgen05 as split TF32 products). In the mixed path each system first runs in
     both tiers on ``probe_cells`` cells and takes the FP32 tier only where
     they agree to ``probe_tol`` of the fields' scale, and only on the
     Cholesky path with cond <= ``cond_split``. With ``refine`` the mixed
