@@ -67,6 +67,11 @@ int spi_check_full_nuggetness(const char *vg_str, double min_vg_val, int32_t *ou
 /* Library version string. */
 const char *spi_version(void);
 
+/* The CUDA error behind the calling thread's last SPI_ERR_CUDA status, as
+ * "name: description" (cudaGetErrorName / cudaGetErrorString), else the
+ * runtime's pending error; "" when there is none. Reading it clears it. */
+const char *spi_cuda_error(void);
+
 /* ---- drop-ins for the reference's Cython kernels (all device arrays) ---- */
 
 /* Replaces fill_dists_2d_mat (cyth/interpmthds.pyx:123-143):

@@ -41,9 +41,11 @@ SPI_ERR_TOO_LARGE = 5
 
 
 class SpiError(RuntimeError):
-    def __init__(self, fn, code):
-        super().__init__(f"{fn} returned {STATUS.get(code, code)}")
+    def __init__(self, fn, code, detail=""):
+        msg = f"{fn} returned {STATUS.get(code, code)}"
+        super().__init__(f"{msg} ({detail})" if detail else msg)
         self.code = code
+        self.detail = detail
 
 
 class VgT(ctypes.Structure):
@@ -148,7 +150,7 @@ _SIGS = {
 }
 
 # every entry point the header declares (checked by the CPU tests)
-EXPORTS = sorted(list(_SIGS) + ["spi_version", "spi_mlp_n_params"])
+EXPORTS = sorted(list(_SIGS) + ["spi_version", "spi_cuda_error", "spi_mlp_n_params"])
 
 _lib = None
 _lock = threading.Lock()
@@ -171,6 +173,8 @@ def load(path=LIB_PATH):
             fn.restype = ctypes.c_int
         lib.spi_version.restype = ctypes.c_char_p
         lib.spi_version.argtypes = []
+        lib.spi_cuda_error.restype = ctypes.c_char_p
+        lib.spi_cuda_error.argtypes = []
         lib.spi_mlp_n_params.restype = c_i64
         lib.spi_mlp_n_params.argtypes = [c_i32, c_i32, c_i32, c_i32]
         _lib = lib
@@ -185,5 +189,8 @@ def call(name, *args):
     """Call an entry point; raise SpiError on a non-zero status."""
     rc = getattr(lib(), name)(*args)
     if rc != 0:
-        raise SpiError(name, rc)
+        detail = ""
+        if STATUS.get(rc) == "SPI_ERR_CUDA":
+            detail = (lib().spi_cuda_error() or b"").decode(errors="replace")
+        raise SpiError(name, rc, detail)
     return rc

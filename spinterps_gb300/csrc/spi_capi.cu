@@ -1,7 +1,10 @@
 // Host-side entry points of the C ABI: variogram string parsing and the
 // nugget-only check. Pure C++ (no device code); errors are status codes.
+#include <cuda_runtime.h>
+
 #include <cctype>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -160,3 +163,18 @@ extern "C" int spi_check_full_nuggetness(const char* vg_str, double min_vg_val, 
 }
 
 extern "C" const char* spi_version(void) { return "spinterps_gb300 0.1 (sm_103a)"; }
+
+namespace spi {
+static thread_local cudaError_t g_cuda_error = cudaSuccess;
+void record_cuda_error(cudaError_t e) { g_cuda_error = e; }
+}  // namespace spi
+
+extern "C" const char* spi_cuda_error(void) {
+  static thread_local char buf[256];
+  cudaError_t e = spi::g_cuda_error;
+  spi::g_cuda_error = cudaSuccess;
+  if (e == cudaSuccess) e = cudaPeekAtLastError();
+  if (e == cudaSuccess) return "";
+  std::snprintf(buf, sizeof(buf), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+  return buf;
+}

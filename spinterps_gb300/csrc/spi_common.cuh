@@ -246,9 +246,17 @@ __device__ __forceinline__ double clip_est(double v, const spi_out_t &o) {
 
 }  // namespace spi
 
+namespace spi {
+// Keeps the CUDA error behind an SPI_ERR_CUDA status for spi_cuda_error.
+void record_cuda_error(cudaError_t e);
+}  // namespace spi
+
 // Launch check used by every entry point.
 #define SPI_LAUNCH_CHECK()                                      \
   do {                                                          \
     cudaError_t _e = cudaGetLastError();                        \
-    if (_e != cudaSuccess) return SPI_ERR_CUDA;                 \
+    if (_e != cudaSuccess) {                                    \
+      spi::record_cuda_error(_e);                               \
+      return SPI_ERR_CUDA;                                      \
+    }                                                           \
   } while (0)
