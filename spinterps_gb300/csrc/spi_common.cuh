@@ -249,6 +249,16 @@ __device__ __forceinline__ double clip_est(double v, const spi_out_t &o) {
 namespace spi {
 // Keeps the CUDA error behind an SPI_ERR_CUDA status for spi_cuda_error.
 void record_cuda_error(cudaError_t e);
+
+// Opts a kernel into `bytes` of dynamic shared memory. A launch needs the
+// opt-in once its static plus dynamic shared memory passes 48 KB, so a
+// dynamic request just under 48 KB already needs it when the kernel has
+// static arrays; it is set for every request.
+template <typename K>
+inline bool smem_opt_in(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes) == cudaSuccess;
+}
 }  // namespace spi
 
 // Launch check used by every entry point.

@@ -1153,11 +1153,7 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   size_t ysm = 0;
   if (!ws->linv_arena) {
     if ((rc = solve_smem(sys->max_n, &nk, &ysm))) return rc;
-    if (ysm > 48 * 1024 &&
-        (cudaFuncSetAttribute(k_cond_est<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)ysm) != cudaSuccess ||
-         cudaFuncSetAttribute(k_cond_est<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)ysm) != cudaSuccess))
+    if (!smem_opt_in(k_cond_est<double>, ysm) || !smem_opt_in(k_cond_est<float>, ysm))
       return SPI_ERR_CUDA;
   }
   if (ir) {
@@ -1182,10 +1178,7 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
   SPI_LAUNCH_CHECK();
   size_t gsm = (size_t)(sys->max_n + GA) * (2 * sizeof(double) + sizeof(int));
   if (gsm > 200 * 1024) return SPI_ERR_TOO_LARGE;
-  if (gsm > 48 * 1024 &&
-      cudaFuncSetAttribute(k_gj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm) !=
-          cudaSuccess)
-    return SPI_ERR_CUDA;
+  if (!smem_opt_in(k_gj, gsm)) return SPI_ERR_CUDA;
   if (sys->kind == SPI_KIND_EDK) {
     k_drift_check<<<sys->n_sys, FT, 0, st>>>(d, sy, ws->status);
     SPI_LAUNCH_CHECK();
@@ -1217,11 +1210,7 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
   if (!vals) return SPI_ERR_ARG;
   size_t smem = (size_t)3 * (sys->max_n + GA) * sizeof(double);
   if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
-  if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(k_duals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return SPI_ERR_CUDA;
-  }
+  if (!smem_opt_in(k_duals, smem)) return SPI_ERR_CUDA;
   k_duals<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, vals);
   SPI_LAUNCH_CHECK();
   if (!ws->linv_arena) {
@@ -1230,13 +1219,7 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
     int nk;
     size_t ysm;
     if ((rc = solve_smem(sys->max_n, &nk, &ysm, ir_mode(ws) ? 1 : 0))) return rc;
-    if (ysm > 48 * 1024 &&
-        cudaFuncSetAttribute(k_duals_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)ysm) != cudaSuccess)
-      return SPI_ERR_CUDA;
-    if (ysm > 48 * 1024 &&
-        cudaFuncSetAttribute(k_duals_solve_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)ysm) != cudaSuccess)
+    if (!smem_opt_in(k_duals_solve, ysm) || !smem_opt_in(k_duals_solve_steps, ysm))
       return SPI_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
     // the steps: groups of nk spread over gx CTAs per system
@@ -1252,10 +1235,7 @@ extern "C" int spi_krige_duals(const spi_domain_t* dom, const spi_systems_t* sys
         int nk1;
         size_t ysm1;
         if ((rc = solve_smem(sys->max_n, &nk1, &ysm1))) return rc;
-        if (ysm1 > 48 * 1024 &&
-            cudaFuncSetAttribute(k_cond_est<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)ysm1) != cudaSuccess)
-          return SPI_ERR_CUDA;
+        if (!smem_opt_in(k_cond_est<double>, ysm1)) return SPI_ERR_CUDA;
         k_cond_est<double><<<sys->n_sys, FT, ysm1, st>>>(*sys, ws->l_arena, ws->status,
                                                          ws->cond, nk1, ws->ir, 2);
         SPI_LAUNCH_CHECK();
@@ -1279,10 +1259,7 @@ extern "C" int spi_krige_loo(const spi_domain_t* dom, const spi_systems_t* sys,
   if (!resid || !ws->linv_arena) return SPI_ERR_ARG;
   size_t smem = (size_t)sys->max_n * sizeof(double);
   if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_loo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess)
-    return SPI_ERR_CUDA;
+  if (!smem_opt_in(k_loo, smem)) return SPI_ERR_CUDA;
   k_loo<<<sys->n_sys, FT, smem, (cudaStream_t)stream>>>(*dom, *sys, *ws, resid);
   SPI_LAUNCH_CHECK();
   return SPI_OK;

@@ -264,10 +264,7 @@ extern "C" int spi_legacy_system(int32_t kind, const double* xi, const double* y
   const int64_t m = (int64_t)n + (sk ? 0 : 1 + n_drift);
   const size_t smem = (size_t)m * (2 * sizeof(double) + sizeof(int));
   if (smem > 200 * 1024) return SPI_ERR_TOO_LARGE;
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(spi::k_leg_system, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
-    return SPI_ERR_CUDA;
+  if (!spi::smem_opt_in(spi::k_leg_system, smem)) return SPI_ERR_CUDA;
   spi::k_leg_system<<<1, spi::LT, smem, (cudaStream_t)stream>>>(sk, xi, yi, n, si, n_drift, *vg,
                                                                 in_dists, lhs, lhs_inv, status,
                                                                 cond);

@@ -298,16 +298,10 @@ extern "C" int spi_local_cells(const spi_domain_t* dom, int32_t kind, int32_t k,
   if (blocks > 152 * 64) blocks = 152 * 64;
   cudaStream_t st = (cudaStream_t)stream;
   if (out->out_f64) {
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(spi::k_local<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
-      return SPI_ERR_CUDA;
+    if (!spi::smem_opt_in(spi::k_local<double>, smem)) return SPI_ERR_CUDA;
     spi::k_local<double><<<(unsigned)blocks, 32 * warps, smem, st>>>(A);
   } else {
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(spi::k_local<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
-      return SPI_ERR_CUDA;
+    if (!spi::smem_opt_in(spi::k_local<float>, smem)) return SPI_ERR_CUDA;
     spi::k_local<float><<<(unsigned)blocks, 32 * warps, smem, st>>>(A);
   }
   SPI_LAUNCH_CHECK();
