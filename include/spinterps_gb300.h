@@ -178,6 +178,11 @@ typedef struct {
  * FP32 factor (spi_krige_factor / spi_krige_duals with ws->l32). */
 #define SPI_IR_MAX_ITERS 12
 #define SPI_PINV_MAX_M 256
+/* spi_krige_var_tc's packed chunks: 8 columns of Linv (the tensor cores'
+ * K-step) as 3 TF32 tiles of 256 x 8, then the 8 stations' split
+ * coordinates (float4 each) */
+#define SPI_VAR_TC_KC 8
+#define SPI_VAR_TC_CHUNK_FLOATS (3 * 256 * SPI_VAR_TC_KC + 4 * SPI_VAR_TC_KC)
 #define SPI_PINV_SLOTS 16
 #define SPI_PINV_SCRATCH_DOUBLES (SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M)
 
@@ -262,10 +267,12 @@ typedef struct {
     float *linv_tc;      /* Linv's three TF32 terms per system, packed by
                             spi_krige_var_tc_pack in the tensor cores'
                             shared-memory tile order: per block of 256 rows,
-                            per chunk of 16 columns (up to the block's last
-                            row), 3 tiles of 256 x 16 TF32 values (48 KB);
-                            required by spi_krige_var_tc */
-    const int64_t *linv_tc_off; /* [n_sys + 1]: first 48 KB chunk of each
+                            per chunk of SPI_VAR_TC_KC columns (up to the
+                            block's last row), 3 tiles of 256 x 8 TF32
+                            values and the chunk's stations
+                            (SPI_VAR_TC_CHUNK_FLOATS floats, 16-byte
+                            aligned); required by spi_krige_var_tc */
+    const int64_t *linv_tc_off; /* [n_sys + 1]: first packed chunk of each
                             system in linv_tc (see spi_krige_var_tc_pack) */
 } spi_krige_ws_t;
 
@@ -405,14 +412,15 @@ int spi_krige_var_tc(const spi_domain_t *dom, const spi_systems_t *sys,
 /* Pack Linv (ws->linv_hi / linv_lo, spi_split_f64 of linv_arena) of every
  * route-0 system into ws->linv_tc for spi_krige_var_tc: Linv = b0 + b1 + b2
  * in TF32 terms (b0 the TF32 rounding of hi, b1 of the remainder plus lo,
- * b2 what is left), each 256-row block's rows 0..255 by 16-column chunks
- * up to the block's last row, each chunk 3 tiles of 256 x 16 values in the
- * no-swizzle K-major core-matrix order the MMA reads (one bulk copy per
- * chunk). System s's chunks start at chunk ws->linv_tc_off[s]; a system
- * of n stations has sum over blocks b of ceil(min(n, 256 (b + 1)) / 16)
- * chunks. */
-int spi_krige_var_tc_pack(const spi_systems_t *sys, const spi_krige_ws_t *ws,
-                          spi_stream_t stream);
+ * b2 what is left), each 256-row block's rows 0..255 by chunks of
+ * SPI_VAR_TC_KC columns up to the block's last row, each chunk 3 tiles of
+ * 256 x 8 values in the no-swizzle K-major core-matrix order the MMA reads,
+ * followed by the chunk's stations' split coordinates (dom->stn_split; one
+ * bulk copy per chunk). System s's chunks start at chunk
+ * ws->linv_tc_off[s]; a system of n stations has sum over blocks b of
+ * ceil(min(n, 256 (b + 1)) / 8) chunks. */
+int spi_krige_var_tc_pack(const spi_domain_t *dom, const spi_systems_t *sys,
+                          const spi_krige_ws_t *ws, spi_stream_t stream);
 
 /* The same term |Linv c|^2 in double-float on the FP32 pipe (every product
  * split by FMA, sums by TwoSum: ~1e-9 of the sill), into ws->cell_yy, for

@@ -19,6 +19,8 @@ c_ptr = ctypes.c_void_p
 SPI_MAX_VG_COMP = 4
 SPI_MAX_DRIFT = 7
 SPI_PINV_MAX_M = 256
+SPI_VAR_TC_KC = 8
+SPI_VAR_TC_CHUNK_FLOATS = 3 * 256 * SPI_VAR_TC_KC + 4 * SPI_VAR_TC_KC
 SPI_IR_MAX_ITERS = 12
 SPI_PINV_SLOTS = 16
 SPI_PINV_SCRATCH_DOUBLES = SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M
@@ -110,7 +112,8 @@ _SIGS = {
     "spi_krige_tier": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_i64, c_ptr, c_ptr,
                        c_ptr, c_ptr, c_ptr, c_dbl, c_dbl, c_dbl, c_dbl, c_ptr, c_ptr, c_ptr,
                        c_ptr],
-    "spi_krige_var_tc_pack": [ctypes.POINTER(SystemsT), ctypes.POINTER(KrigeWsT), c_ptr],
+    "spi_krige_var_tc_pack": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
+                              ctypes.POINTER(KrigeWsT), c_ptr],
     "spi_krige_var_df": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),
                          ctypes.POINTER(KrigeWsT), c_dbl, c_ptr],
     "spi_krige_var_tc": [ctypes.POINTER(DomainT), ctypes.POINTER(SystemsT),

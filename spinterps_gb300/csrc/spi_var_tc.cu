@@ -7,32 +7,35 @@
 // (n^2 flops per cell, shared by every step of the system; the rest of the
 // variance formula is in the cell kernel's FP64 epilogue).
 //
-// One CTA = 128 cells x 256 threads. The accumulator D [128 cells x 256
-// rows of Linv] lives in tensor memory (TMEM lane = cell, column = row), so
-// each lane squares and sums its own row of D. Rows of Linv go in blocks of
-// 256 (the MMA's N), the stations (K) in chunks of 16, in a two-stage
-// shared-memory ring:
-//   - B, Linv's rows (256 x 16, triangular) as three TF32 terms (b0 + b1 +
+// One CTA = 128 cells x 256 threads, two CTAs per SM (each holds 256 of the
+// SM's 512 tensor-memory columns). The accumulator D [128 cells x 256 rows
+// of Linv] lives in TMEM (lane = cell, column = row), so each lane squares
+// and sums its own row of D. Rows of Linv go in blocks of 256 (the MMA's
+// N), the stations (K) in chunks of 8, through a three-stage shared-memory
+// ring:
+//   - B, Linv's rows (256 x 8, triangular) as three TF32 terms (b0 + b1 +
 //     b2, ~33 bits: Linv's rounding, amplified by the cancellation in
-//     Linv c, dominates the variance's error), is packed once per system in
-//     the MMA's tile order (spi_krige_var_tc_pack) and arrives by one bulk
-//     copy (cp.async.bulk, 48 KB) per chunk, issued by one thread and
-//     counted on an mbarrier;
-//   - A, the cells' right-hand sides (128 x 16), is generated by all
-//     threads in double-float (rhs_df) and stored as two TF32 terms (a0 +
-//     a1, ~22 bits), in the no-swizzle K-major layout (8-row x 16-byte core
-//     matrices).
-// One thread issues the chunk's 2 K-steps x 5 MMAs (a0 b0 + a0 b1 + a1 b0 +
-// a0 b2 + a1 b1, FP32 accumulation in TMEM) and commits them to the
-// stage's mbarrier, then every thread goes on to the next chunk: the
-// right-hand sides of chunk c + 1 are generated while chunk c's MMAs run,
-// and a stage is refilled only after its previous MMAs completed. Every
-// wait is bounded: on expiry the kernel raises err_flag, drains the MMAs in
-// flight on a best-effort basis (one more bounded wait), frees its TMEM and
-// returns; the probe's tier choice (spi_krige_tier) then keeps every system
-// in FP64 and the host raises. Squares are summed in double-float (FP32
-// pairs: the FP64 pipe is 1/64 of FP32 on GB300); the mixed path's probe
-// checks every system's variance against the FP64 kernel.
+//     Linv c, dominates the variance's error), and the chunk's 8 stations'
+//     split coordinates, are packed once per system in the MMA's tile
+//     order (spi_krige_var_tc_pack) and arrive by one bulk copy
+//     (cp.async.bulk, 24 KB) per chunk, issued one chunk ahead by one
+//     thread and counted on the stage's mbarrier;
+//   - A, the cells' right-hand sides (128 x 8), is generated by all threads
+//     in double-float (rhs_df, or rhs_df_single for a one-structure
+//     variogram) from the stations in shared memory and stored as two TF32
+//     terms (a0 + a1, ~22 bits), in the no-swizzle K-major layout (8-row x
+//     16-byte core matrices).
+// One thread issues the chunk's 5 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 +
+// a1 b1, K = 8, FP32 accumulation in TMEM) and commits them to the stage's
+// mbarrier; the threads go on to the next chunk while they run, and a stage
+// is refilled only after the MMAs that read it completed. Every wait is
+// bounded: on expiry the kernel raises err_flag, drains the copies and MMAs
+// in flight on a best-effort basis (one more bounded wait each), frees its
+// TMEM and returns; the probe's tier choice (spi_krige_tier) then keeps
+// every system in FP64 and the host raises. Squares are summed in
+// double-float (FP32 pairs: the FP64 pipe is 1/64 of FP32 on GB300); the
+// mixed path's probe checks every system's variance against the FP64
+// kernel.
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
 
@@ -40,15 +43,21 @@ namespace spi {
 
 constexpr int VT_M = 128;   // cells per CTA (MMA M, TMEM lanes)
 constexpr int VT_N = 256;   // Linv rows per block (MMA N, TMEM columns)
-constexpr int VT_KC = 16;   // stations per staged chunk
+constexpr int VT_KC = SPI_VAR_TC_KC;  // stations per chunk (one MMA K-step)
 constexpr int VT_T = 256;   // threads
+constexpr int VT_NST = 3;   // ring stages
 constexpr long VT_SPIN = 1L << 26;   // mbarrier polls before giving up
 
 constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;       // one TF32 term of A
 constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;       // one TF32 term of B
-constexpr size_t VT_STAGE = 2 * VT_A_BYTES + 3 * VT_B_BYTES;  // A (2 terms), B (3 terms)
-constexpr size_t VT_SMEM = 2 * VT_STAGE;                      // two stages
-constexpr int VT_CHUNK_FLOATS = (int)(3 * VT_B_BYTES / 4);    // one packed chunk of B
+constexpr size_t VT_S_BYTES = (size_t)VT_KC * 16;             // the chunk's stations (float4)
+constexpr size_t VT_CHUNK_BYTES = 3 * VT_B_BYTES + VT_S_BYTES;  // one packed chunk
+constexpr size_t VT_STAGE = 2 * VT_A_BYTES + VT_CHUNK_BYTES;  // A (2 terms), the chunk
+constexpr size_t VT_SMEM = VT_NST * VT_STAGE;
+constexpr int VT_CHUNK_FLOATS = (int)(VT_CHUNK_BYTES / 4);
+static_assert(VT_CHUNK_FLOATS == SPI_VAR_TC_CHUNK_FLOATS, "packed chunk size");
+static_assert(VT_KC == 8, "one MMA K-step (TF32: K = 8) per chunk");
+static_assert(VT_STAGE % 16 == 0 && VT_CHUNK_BYTES % 16 == 0, "bulk copies: 16-byte units");
 
 struct VarTcArgs {
   spi_domain_t dom;
@@ -119,18 +128,46 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
 }
 
-// One thread: B of chunk (rb, kc) by one bulk copy into the stage, counted
-// on the stage's mbarrier (expect_tx of the copy's bytes).
-__device__ __forceinline__ void vt_load_b(uint32_t dst, const float* src, uint32_t mbar) {
+// One thread: packed chunk (B and its stations) by one bulk copy into the
+// stage, counted on the stage's mbarrier (expect_tx of the copy's bytes).
+__device__ __forceinline__ void vt_load(uint32_t dst, const float* src, uint32_t mbar) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
-               "r"((uint32_t)(3 * VT_B_BYTES)));
+               "r"((uint32_t)VT_CHUNK_BYTES));
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"((uint32_t)(3 * VT_B_BYTES)), "r"(mbar)
+      "l"(src), "r"((uint32_t)VT_CHUNK_BYTES), "r"(mbar)
       : "memory");
 }
 
-__global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
+// The chunk's right-hand sides of one thread: cell a_cell, stations
+// k0 + kb .. k0 + kb + 3 (coordinates from the stage), as two TF32 terms
+// into the A tiles. CODE: the single structure's model, or -1 (rhs_df).
+template <int CODE>
+__device__ __forceinline__ void vt_gen(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                       const RhsDf& kd, double sh, float4 cp, bool live,
+                                       int64_t gc, const int32_t* idx, int n, int k0, int kb,
+                                       int a_cell, const float4* ssp, unsigned char* sAh,
+                                       unsigned char* sAl) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int kk = kb + q, j = k0 + kk;
+    df c = {0.f, 0.f};
+    if (live && j < n) {
+      if constexpr (CODE < 0)
+        c = rhs_df(dom, vgp, kd, 0, sh, cp, ssp[kk], gc, idx + j);
+      else
+        c = rhs_df_single<CODE>(dom, vgp, kd, 0, sh, cp, ssp[kk], gc, idx + j);
+    }
+    float h, l;
+    tf32_split(c.h, h, l);
+    l += c.l;
+    const int o = tile_off(VT_M, a_cell, kk);
+    *reinterpret_cast<float*>(sAh + o) = h;
+    *reinterpret_cast<float*>(sAl + o) = l;
+  }
+}
+
+__global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
   const int s = blockIdx.y;
   const int64_t C = A.dom.n_cells;
   const int64_t c0 = (int64_t)blockIdx.x * VT_M;
@@ -145,13 +182,12 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   const double sh = A.ws.shift[s];
   const float* pk = A.ws.linv_tc + (int64_t)A.ws.linv_tc_off[s] * VT_CHUNK_FLOATS;
   extern __shared__ __align__(1024) unsigned char smv[];
-  __shared__ __align__(8) uint64_t bbar[2];   // B of a stage arrived
-  __shared__ __align__(8) uint64_t mbar[2];   // the stage's MMAs completed
+  __shared__ __align__(8) uint64_t bbar[VT_NST];   // the stage's chunk arrived
+  __shared__ __align__(8) uint64_t mbar[VT_NST];   // the stage's MMAs completed
   __shared__ uint32_t tbase;
   __shared__ int fail;
   __shared__ double half_yy[VT_M];
-  auto stage_a = [&](int st) { return smv + st * VT_STAGE; };
-  auto stage_b = [&](int st) { return smv + st * VT_STAGE + 2 * VT_A_BYTES; };
+  auto stage = [&](int st) { return smv + st * VT_STAGE; };
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) {
@@ -160,13 +196,15 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
                  "r"(VT_N));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  __shared__ RhsDf kd;
   if (tid == 0) {
     fail = 0;
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < VT_NST; ++q) {
       mbar_init(smem_u32(&bbar[q]), 1);
       mbar_init(smem_u32(&mbar[q]), 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;");
+    kd.init(vg, sh, A.dom.min_vg_val);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -175,88 +213,98 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
   // kind::tf32, D FP32, A/B TF32 K-major, N = 256, M = 128
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(VT_N >> 3) << 17) |
                          ((uint32_t)(VT_M >> 4) << 24);
+  // the single structure's model, uniform over the CTA (-1: general form)
+  const int scode = (kd.exact && kd.single >= 0) ? kd.code[kd.single] : -1;
 
-  // staging roles: A = cell (tid % 128), stations [khalf * KC/2, +KC/2) of a chunk
-  const int a_cell = tid & (VT_M - 1), khalf = tid >> 7;
+  // staging roles: A = cell (tid % 128), stations [kb, kb + 4) of a chunk
+  const int a_cell = tid & (VT_M - 1), kb = (tid >> 7) * 4;
   const int64_t gc = c0 + a_cell;
   const bool live = gc < C;
   const float4 cp = live ? reinterpret_cast<const float4*>(A.dom.cell_split)[gc]
                          : make_float4(0.f, 0.f, 0.f, 0.f);
-  __shared__ RhsDf kd;
-  if (tid == 0) kd.init(vg, sh, A.dom.min_vg_val);
-  __syncthreads();
   const spi_vg_t* vgp = A.sys.vg + s;
-  const float4* sp4 = reinterpret_cast<const float4*>(A.dom.stn_split);
   // epilogue roles: TMEM lanes of warp % 4, column half warp / 4
   const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
   df yy = {0.f, 0.f};  // sum of squares, double-float (no FP64 pipe per row)
-  // g: chunks issued so far (over every row block); stage g & 1 holds
-  // chunk g, and its mbarriers complete once per use: phase parity
-  // (g >> 1) & 1. seen: chunks whose MMAs every thread has seen complete.
-  int g = 0, seen = 0;
+  int total = 0;  // the system's chunks over all row blocks
+  for (int rb = 0; rb < n; rb += VT_N) total += vt_chunks(n, rb);
+  // chunk g sits in stage g % 3; each of a stage's mbarriers completes once
+  // per use, so chunk g's phase parity is (g / 3) & 1. seen: chunks whose
+  // MMAs this thread has seen complete; issued: chunks whose copy thread 0
+  // has started (one ahead of the chunk being generated).
+  int g = 0, seen = 0, issued = 0;
   auto wait_mma = [&](int upto) {  // MMAs of chunks < upto complete
     while (seen < upto && !fail) {
-      if (!mbar_wait_bounded(smem_u32(&mbar[seen & 1]), (uint32_t)((seen >> 1) & 1)))
+      if (!mbar_wait_bounded(smem_u32(&mbar[seen % VT_NST]), (uint32_t)((seen / VT_NST) & 1)))
         atomicExch(&fail, 1);
       ++seen;
     }
   };
-  int chunk0 = 0;  // chunks of B of the row blocks before this one
+  if (tid == 0 && total > 0) {
+    vt_load(smem_u32(stage(0) + 2 * VT_A_BYTES), pk, smem_u32(&bbar[0]));
+    issued = 1;
+  }
   for (int rb = 0; rb < n && !fail; rb += VT_N) {
     const int nc = vt_chunks(n, rb);
     for (int kc = 0; kc < nc; ++kc, ++g) {
-      const int st = g & 1;
-      // the stage's previous chunk (g - 2) must be consumed before refill
+      const int st = g % VT_NST;
+      // chunk g + 1 refills the stage of chunk g - 2: its MMAs must be done
       wait_mma(g - 1);
       __syncthreads();
       if (fail) break;
-      unsigned char* sAh = stage_a(st);
+      if (tid == 0 && g + 1 < total) {
+        vt_load(smem_u32(stage((g + 1) % VT_NST) + 2 * VT_A_BYTES),
+                pk + (int64_t)(g + 1) * VT_CHUNK_FLOATS, smem_u32(&bbar[(g + 1) % VT_NST]));
+        issued = g + 2;
+      }
+      unsigned char* sAh = stage(st);
       unsigned char* sAl = sAh + VT_A_BYTES;
-      if (tid == 0)
-        vt_load_b(smem_u32(stage_b(st)), pk + (int64_t)(chunk0 + kc) * VT_CHUNK_FLOATS,
-                  smem_u32(&bbar[st]));
+      unsigned char* sB = sAh + 2 * VT_A_BYTES;
+      const float4* ssp = reinterpret_cast<const float4*>(sB + 3 * VT_B_BYTES);
+      // chunk g's B and stations (on expiry the stage holds garbage: the
+      // right-hand sides below stay in shared memory and the MMAs are not
+      // issued)
+      if (!mbar_wait_bounded(smem_u32(&bbar[st]), (uint32_t)((g / VT_NST) & 1)))
+        atomicExch(&fail, 1);
       const int k0 = kc * VT_KC;
-#pragma unroll 4
-      for (int q = 0; q < VT_KC / 2; ++q) {
-        const int kk = khalf * (VT_KC / 2) + q, j = k0 + kk;
-        df c = {0.f, 0.f};
-        if (live && j < n) c = rhs_df(A.dom, vgp, kd, 0, sh, cp, sp4[idx[j]], gc, idx + j);
-        float h, l;
-        tf32_split(c.h, h, l);
-        l += c.l;
-        const int o = tile_off(VT_M, a_cell, kk);
-        *reinterpret_cast<float*>(sAh + o) = h;
-        *reinterpret_cast<float*>(sAl + o) = l;
+      switch (scode) {
+        case SPI_VG_EXP:
+          vt_gen<SPI_VG_EXP>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh,
+                             sAl);
+          break;
+        case SPI_VG_GAU:
+          vt_gen<SPI_VG_GAU>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh,
+                             sAl);
+          break;
+        case SPI_VG_SPH:
+          vt_gen<SPI_VG_SPH>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh,
+                             sAl);
+          break;
+        default:
+          vt_gen<-1>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh, sAl);
       }
       asm volatile("fence.proxy.async.shared::cta;");
       __syncthreads();
       if (tid == 0) {
-        if (!mbar_wait_bounded(smem_u32(&bbar[st]), (uint32_t)((g >> 1) & 1))) {
-          atomicExch(&fail, 1);
-        } else {
+        if (!fail) {
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t sB0 = smem_u32(stage_b(st));
-#pragma unroll
-          for (int ks = 0; ks < VT_KC / 8; ++ks) {
-            const uint32_t ao = 2 * ks * (VT_M * 16), bo = 2 * ks * (VT_N * 16);
-            const uint64_t ah = umma_desc(smem_u32(sAh) + ao, VT_M * 16, 128);
-            const uint64_t al = umma_desc(smem_u32(sAl) + ao, VT_M * 16, 128);
-            const uint64_t b0 = umma_desc(sB0 + bo, VT_N * 16, 128);
-            const uint64_t b1 = umma_desc(sB0 + (uint32_t)VT_B_BYTES + bo, VT_N * 16, 128);
-            const uint64_t b2 = umma_desc(sB0 + 2 * (uint32_t)VT_B_BYTES + bo, VT_N * 16, 128);
-            mma_tf32(tmem, ah, b0, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
-            mma_tf32(tmem, ah, b1, idesc, 1u);
-            mma_tf32(tmem, al, b0, idesc, 1u);
-            mma_tf32(tmem, ah, b2, idesc, 1u);
-            mma_tf32(tmem, al, b1, idesc, 1u);
-          }
+          const uint64_t ah = umma_desc(smem_u32(sAh), VT_M * 16, 128);
+          const uint64_t al = umma_desc(smem_u32(sAl), VT_M * 16, 128);
+          const uint32_t b = smem_u32(sB);
+          const uint64_t b0 = umma_desc(b, VT_N * 16, 128);
+          const uint64_t b1 = umma_desc(b + (uint32_t)VT_B_BYTES, VT_N * 16, 128);
+          const uint64_t b2 = umma_desc(b + 2 * (uint32_t)VT_B_BYTES, VT_N * 16, 128);
+          mma_tf32(tmem, ah, b0, idesc, kc > 0 ? 1u : 0u);
+          mma_tf32(tmem, ah, b1, idesc, 1u);
+          mma_tf32(tmem, al, b0, idesc, 1u);
+          mma_tf32(tmem, ah, b2, idesc, 1u);
+          mma_tf32(tmem, al, b1, idesc, 1u);
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 smem_u32(&mbar[st])));
       }
     }
-    chunk0 += nc;
     // this block's MMAs complete, then its rows: each lane's 128 columns
     // of its half
     wait_mma(g);
@@ -292,12 +340,16 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
     __syncthreads();
   }
   if (fail) {
-    // best-effort drain: the MMAs and bulk copies in flight may still be
-    // writing; wait once more, with the same limit, for every stage's last
-    // commit before the columns are freed
-    if (tid == 0)
+    // best-effort drain: copies and MMAs in flight may still be writing;
+    // wait once more, with the same limit, for every copy started and every
+    // stage's last commit before the columns are freed
+    if (tid == 0) {
+      // the copies of chunks g - 1 (its wait may have expired) and later
+      for (int q = g > 0 ? g - 1 : 0; q < issued; ++q)
+        mbar_wait_bounded(smem_u32(&bbar[q % VT_NST]), (uint32_t)((q / VT_NST) & 1));
       for (int q = seen; q < g; ++q)
-        mbar_wait_bounded(smem_u32(&mbar[q & 1]), (uint32_t)((q >> 1) & 1));
+        mbar_wait_bounded(smem_u32(&mbar[q % VT_NST]), (uint32_t)((q / VT_NST) & 1));
+    }
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();
   }
@@ -314,9 +366,11 @@ __global__ __launch_bounds__(VT_T) void k_var_tc(VarTcArgs A) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(VT_N));
 }
 
-// Linv's TF32 terms of chunk (blockIdx.x) of system blockIdx.y in the tile
-// order k_var_tc reads (see spi_krige_var_tc_pack).
-__global__ __launch_bounds__(VT_T) void k_var_tc_pack(spi_systems_t sys, spi_krige_ws_t ws) {
+// Linv's TF32 terms of chunk (blockIdx.x) of system blockIdx.y, and its
+// stations' split coordinates, in the order k_var_tc reads them (see
+// spi_krige_var_tc_pack).
+__global__ __launch_bounds__(VT_T) void k_var_tc_pack(spi_domain_t dom, spi_systems_t sys,
+                                                      spi_krige_ws_t ws) {
   const int s = blockIdx.y;
   if (ws.route[s] != 0) return;
   const int64_t soff = sys.stn_off[s];
@@ -351,6 +405,12 @@ __global__ __launch_bounds__(VT_T) void k_var_tc_pack(spi_systems_t sys, spi_kri
     *reinterpret_cast<float*>(d0 + VT_B_BYTES + o) = b1;
     *reinterpret_cast<float*>(d0 + 2 * VT_B_BYTES + o) = r1 - b1;
   }
+  if (threadIdx.x < VT_KC) {
+    const int j = k0 + threadIdx.x;
+    reinterpret_cast<float4*>(d0 + 3 * VT_B_BYTES)[threadIdx.x] =
+        j < n ? reinterpret_cast<const float4*>(dom.stn_split)[sys.stn_idx[soff + j]]
+              : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
 }
 
 }  // namespace spi
@@ -369,9 +429,8 @@ extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sy
     return SPI_ERR_ARG;
   const int64_t tiles = (dom->n_cells + VT_M - 1) / VT_M;
   if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
-  if (cudaFuncSetAttribute(k_var_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)VT_SMEM) != cudaSuccess)
-    return SPI_ERR_CUDA;
+  if (reinterpret_cast<uintptr_t>(ws->linv_tc) & 15) return SPI_ERR_ARG;
+  if (!smem_opt_in(k_var_tc, VT_SMEM)) return SPI_ERR_CUDA;
   VarTcArgs A{*dom, *sys, *ws, cond_split, err_flag};
   dim3 grid((unsigned)tiles, (unsigned)sys->n_sys);
   k_var_tc<<<grid, VT_T, VT_SMEM, (cudaStream_t)stream>>>(A);
@@ -379,13 +438,16 @@ extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sy
   return SPI_OK;
 }
 
-extern "C" int spi_krige_var_tc_pack(const spi_systems_t* sys, const spi_krige_ws_t* ws,
-                                     spi_stream_t stream) {
-  if (!sys || !ws) return SPI_ERR_ARG;
+extern "C" int spi_krige_var_tc_pack(const spi_domain_t* dom, const spi_systems_t* sys,
+                                     const spi_krige_ws_t* ws, spi_stream_t stream) {
+  if (!dom || !sys || !ws) return SPI_ERR_ARG;
   if (sys->n_sys < 0 || sys->n_sys > 65535) return SPI_ERR_TOO_LARGE;
   if (sys->n_sys == 0) return SPI_OK;
   if (!ws->linv_hi || !ws->linv_lo || !ws->linv_tc || !ws->linv_tc_off || !ws->route ||
-      !sys->stn_off || !sys->mat_off || sys->max_n < 1)
+      !sys->stn_off || !sys->stn_idx || !sys->mat_off || !dom->stn_split || sys->max_n < 1)
+    return SPI_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(ws->linv_tc) & 15) ||
+      (reinterpret_cast<uintptr_t>(dom->stn_split) & 15))
     return SPI_ERR_ARG;
   // chunks of the largest system
   int most = 0;
@@ -394,7 +456,7 @@ extern "C" int spi_krige_var_tc_pack(const spi_systems_t* sys, const spi_krige_w
     most += (e + VT_KC - 1) / VT_KC;
   }
   dim3 grid((unsigned)most, (unsigned)sys->n_sys);
-  k_var_tc_pack<<<grid, VT_T, 0, (cudaStream_t)stream>>>(*sys, *ws);
+  k_var_tc_pack<<<grid, VT_T, 0, (cudaStream_t)stream>>>(*dom, *sys, *ws);
   SPI_LAUNCH_CHECK();
   return SPI_OK;
 }

@@ -310,12 +310,14 @@ class _KrigeBatch:
             self.yy = torch.empty(len(ch) * dom.C, dtype=torch.float64, device=dev)
             self.tc_err = torch.zeros(1, dtype=torch.int32, device=dev)
             # Linv's TF32 terms in the tensor cores' tile order: per system,
-            # per 256-row block, 16-column chunks up to the block's last row,
-            # 48 KB each (spi_krige_var_tc_pack)
-            chunks = np.array([sum((min(int(n), rb + 256) + 15) // 16
+            # per 256-row block, 8-column chunks up to the block's last row,
+            # each with its stations' coordinates (spi_krige_var_tc_pack)
+            kc = nat.SPI_VAR_TC_KC
+            chunks = np.array([sum((min(int(n), rb + 256) + kc - 1) // kc
                                    for rb in range(0, int(n), 256)) for n in ns], dtype=np.int64)
             off = np.concatenate([[0], np.cumsum(chunks)]).astype(np.int64)
-            self.linv_tc = torch.empty(int(off[-1]) * 12288, dtype=torch.float32, device=dev)
+            self.linv_tc = torch.empty(int(off[-1]) * nat.SPI_VAR_TC_CHUNK_FLOATS,
+                                       dtype=torch.float32, device=dev)
             self.linv_tc_off = torch.as_tensor(off, device=dev)
         # the probe (precision 1): both tiers on a few cells decide each
         # system's tier (spi_krige_tier)
@@ -441,7 +443,8 @@ class _KrigeBatch:
             if self.X is not None:
                 nat.call("spi_split_f64", _ptr(self.X), _ptr(xh), _ptr(xl), self.arena, s)
                 if self.linv_tc is not None:
-                    nat.call("spi_krige_var_tc_pack", ctypes.byref(self.sy), ws, s)
+                    nat.call("spi_krige_var_tc_pack", ctypes.byref(dom.st), ctypes.byref(self.sy),
+                             ws, s)
             nat.call("spi_split_f64", _ptr(self.g_cols), _ptr(gh), _ptr(gl), self.g_cols.numel(), s)
             nat.call("spi_split_f64", _ptr(self.w_hat), _ptr(wh), _ptr(wl), self.w_hat.numel(), s)
         if self.probe is not None and probe is not None:

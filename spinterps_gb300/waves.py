@@ -38,7 +38,12 @@ def step_bytes(n_present, n_cells, n_labels, out_itemsize, krige_kinds, ok_var, 
         var = ok_var and kind == "OK"
         b += arena * (2 if var else 1)
         if mixed and var:
-            b += n_cells * 8
+            # the tensor-core variance: per-cell |Linv c|^2, Linv's FP32
+            # hi / lo copies and its packed TF32 terms
+            kc = nat.SPI_VAR_TC_KC
+            chunks = sum((min(n_present, rb + 256) + kc - 1) // kc
+                         for rb in range(0, n_present, 256))
+            b += n_cells * 8 + arena + chunks * nat.SPI_VAR_TC_CHUNK_FLOATS * 4
         if mixed and not var:
             b += arena // 2  # the FP32 factor of the refinement path
     return int(b)
