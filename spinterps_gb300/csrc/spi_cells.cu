@@ -119,20 +119,25 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       const bool live = gc < C;
       if constexpr (sizeof(T) == 8) {
         const double cx = live ? A.dom.cell_x[gc] : 0.0, cy = live ? A.dom.cell_y[gc] : 0.0;
-        // the nearest station of the cell comes with its distances (the
-        // same FP64 distances as nnb_f64_warp: first index of the minimum)
+        // the nearest station of the cell comes with its squared distances:
+        // the first index of the smallest dist_f64 (as nnb_f64_warp). The
+        // root is monotone, so a smaller square never has a larger root,
+        // and squares more than 2^-50 apart (relative) never share one;
+        // closer pairs compare their roots (a later index wins only with a
+        // strictly smaller root)
         double best = __longlong_as_double(0x7ff0000000000000LL);
         int bj = 0x7fffffff;
         for (int j = jg; j < npad; j += njg) {
           double v = 0.0;
           if (live && j < n) {
             const int st = idx[j];
-            const double d = dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
-            if (d < best) {
-              best = d;
+            const double d2 = dist2_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]);
+            if (d2 < best &&
+                (best - d2 > 0x1p-50 * best || __dsqrt_rn(d2) < __dsqrt_rn(best))) {
+              best = d2;
               bj = j;
             }
-            const double g = vgp64.fill(d, sk, A.dom.min_vg_val);
+            const double g = vgp64.fill_d2(d2, sk, A.dom.min_vg_val);
             v = (sk || prim) ? g : __dsub_rn(sh, g);
           }
           if (prim && live && j >= n && j < n + a) {
@@ -144,7 +149,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
         // per cell, the minimum over the thread groups (Bs is free until
         // the contractions below)
         double* bd = reinterpret_cast<double*>(Bs);
-        bd[jg * TC + cell] = best;
+        bd[jg * TC + cell] = __dsqrt_rn(best);
         bd[CT + jg * TC + cell] = (double)bj;
         __syncthreads();
         if (tid < TC) {

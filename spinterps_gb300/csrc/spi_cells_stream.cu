@@ -217,8 +217,8 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
         const int st = idx[j];
         double c = 0.0;
         if (live) {
-          const double g = vgp64.fill(
-              dist_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]), sk, A.dom.min_vg_val);
+          const double g = vgp64.fill_d2(
+              dist2_f64(cx, cy, A.dom.stn_x[st], A.dom.stn_y[st]), sk, A.dom.min_vg_val);
           c = (sk || prim) ? g : __dsub_rn(sh, g);
         }
 #pragma unroll
@@ -317,7 +317,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
         // SK's FP32 sum(lambda) within its rounding bound of the check's
         // boundary: decided in FP64 (as k_krige_cells)
         if (sizeof(T) == 4 && sk && g < C &&
-            near_isclose_boundary(sl, kSumLambdaRelErr * q[1])) {
+            near_isclose_boundary(sl, kSumLambdaRelErrDf * q[1])) {
           ok = 2;
           atomicOr(&any_chk, 1);
         }

@@ -23,6 +23,13 @@ __device__ __forceinline__ double dist_f64(double x1, double y1, double x2, doub
   return __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
 }
 
+// The squared distance under dist_f64's root (the same rounded operations).
+__device__ __forceinline__ double dist2_f64(double x1, double y1, double x2, double y2) {
+  double dx = __dsub_rn(x1, x2);
+  double dy = __dsub_rn(y1, y2);
+  return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+}
+
 // Variogram models of cyth/interpmthds.pyx:38-84 in FP64, same operation
 // order, separately rounded.
 __device__ __forceinline__ double vg_eval_f64(int code, double h, double r, double s) {
@@ -155,12 +162,21 @@ __device__ __forceinline__ double div_rcp(double x, double d, double dinv) {
 // memory), for the FP64 cell kernels' right-hand sides: the same
 // operations in the same order as vg_fill_f64, each division by a range
 // made by div_rcp.
+//
+// fill_d2 takes the squared distance instead: where every structure is
+// Gaussian (plus nuggets) the root is never taken and h^2 is the squared
+// distance itself, within an ulp of the reference's (h^0.5)^2 (the cell
+// kernels' bar is 1e-9; the drop-in builders keep the reference's form).
 struct VgPre {
   spi_vg_t vg;
   double r2[SPI_MAX_VG_COMP], r3x2[SPI_MAX_VG_COMP];
   double rinv[SPI_MAX_VG_COMP], r2inv[SPI_MAX_VG_COMP], r3x2inv[SPI_MAX_VG_COMP];
+  int need_h;  // a structure other than Gau / Nug needs the distance itself
   __device__ void init(const spi_vg_t& v) {
     vg = v;
+    need_h = 0;
+    for (int c = 0; c < v.n_comp; ++c)
+      if (v.code[c] != SPI_VG_GAU && v.code[c] != SPI_VG_NUG) need_h = 1;
     for (int c = 0; c < SPI_MAX_VG_COMP; ++c) {
       const double r = v.range[c];
       r2[c] = __dmul_rn(r, r);
@@ -170,7 +186,8 @@ struct VgPre {
       r3x2inv[c] = __drcp_rn(r3x2[c]);
     }
   }
-  __device__ __forceinline__ double eval(int c, double h) const {
+  // h2: h^2 (RN(h h), or the squared distance when no structure needs h)
+  __device__ __forceinline__ double eval(int c, double h, double h2) const {
     const double r = vg.range[c], s = vg.sill[c];
     switch (vg.code[c]) {
       case SPI_VG_RNG:
@@ -189,17 +206,25 @@ struct VgPre {
         if (h > r) return s;
         return __dmul_rn(s, div_rcp(h, r, rinv[c]));
       case SPI_VG_GAU:
-        return __dmul_rn(
-            s, __dsub_rn(1.0, exp(__dmul_rn(-3.0, div_rcp(__dmul_rn(h, h), r2[c], r2inv[c])))));
+        return __dmul_rn(s, __dsub_rn(1.0, exp(__dmul_rn(-3.0, div_rcp(h2, r2[c], r2inv[c])))));
       default:
         return vg_eval_f64(vg.code[c], h, r, s);
     }
   }
   // vg_fill_f64 of the same entry
   __device__ __forceinline__ double fill(double h, int covar, double min_vg_val) const {
+    return fill_hh(h, __dmul_rn(h, h), covar, min_vg_val);
+  }
+  // the same from the squared distance d2 (dist2_f64)
+  __device__ __forceinline__ double fill_d2(double d2, int covar, double min_vg_val) const {
+    if (need_h) return fill(__dsqrt_rn(d2), covar, min_vg_val);
+    return fill_hh(0.0, d2, covar, min_vg_val);
+  }
+  __device__ __forceinline__ double fill_hh(double h, double h2, int covar,
+                                            double min_vg_val) const {
     double acc = 0.0;
     for (int c = 0; c < vg.n_comp; ++c) {
-      const double g = eval(c, h);
+      const double g = eval(c, h, h2);
       const double t = covar ? __dsub_rn(vg.sill[c], g) : g;
       acc = __dadd_rn(acc, t);
     }

@@ -317,8 +317,15 @@ __device__ __forceinline__ df rhs_df_single(const spi_domain_t& dom, const spi_v
 
 // Rounding bound of an FP32-tier sum(lambda), relative to sum |u_i| c_i:
 // entries ~1e-6 (FP32 exp, double-float distance), hi/lo products, and
-// FP32 partial sums of 128 terms (up to ~8e-6 in the worst case).
+// FP32 partial sums of 128 terms (up to ~8e-6 in the worst case). The
+// shared-memory kernel's FP32 right-hand sides (k_krige_cells<float>).
 constexpr double kSumLambdaRelErr = 1e-5;
+// The same for the streamed kernel, whose sum check (SK: every dual
+// column) takes double-float entries (rhs_df: ~1e-9 relative at most, its
+// exp 6e-11), hi/lo weights (2^-48) and double-float sums flushed to FP64
+// every 256 terms (~1e-12 of the sum of magnitudes): 1e-9, bounded here
+// with a factor 100 to spare.
+constexpr double kSumLambdaRelErrDf = 1e-7;
 
 // SK's sum(lambda) = u'c of one cell in FP64 (u = the system's first dual
 // column), lanes over stations, for cells whose FP32 value is too close to
