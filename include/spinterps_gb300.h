@@ -134,6 +134,10 @@ typedef struct {
      * [n][4] = (x_hi, x_lo, y_hi, y_lo), 16-byte aligned; made by
      * spi_split_coords and required only by the precision-1 kernels. */
     const float *stn_split, *cell_split;
+    /* the res of spi_split_coords (the heads' grid), or 0 when unknown:
+     * with it the precision-1 kernels take a failed cell's nearest station
+     * from their own squared distances wherever those decide it */
+    double split_res;
 } spi_domain_t;
 
 /* out[i] = (x_hi, x_lo, y_hi, y_lo) with x_hi = (x[i] - ox) rounded to a

@@ -59,7 +59,8 @@ class DomainT(ctypes.Structure):
     _fields_ = [("n_stns", c_i64), ("stn_x", c_ptr), ("stn_y", c_ptr),
                 ("n_cells", c_i64), ("cell_x", c_ptr), ("cell_y", c_ptr),
                 ("n_drift", c_i32), ("stn_drift", c_ptr), ("cell_drift", c_ptr),
-                ("min_vg_val", c_dbl), ("stn_split", c_ptr), ("cell_split", c_ptr)]
+                ("min_vg_val", c_dbl), ("stn_split", c_ptr), ("cell_split", c_ptr),
+                ("split_res", c_dbl)]
 
 
 class SystemsT(ctypes.Structure):

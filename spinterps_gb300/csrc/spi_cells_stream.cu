@@ -40,14 +40,17 @@ __device__ __forceinline__ void stream_chunk(const CellsArgs& A, const spi_vg_t*
                                              const float4* s_sp, const float2 (*s_w)[SCH],
                                              int nj, int warp, int nv, int v0, int plain_duals,
                                              float (&ph)[SSV], float (&pl)[SSV],
-                                             double (&acc)[SSV], int& cnt) {
+                                             double (&acc)[SSV], int& cnt, NearDf& nf,
+                                             bool track, int j0, float esp) {
   for (int jj = warp; jj < nj; jj += SNW) {
     df c = {0.f, 0.f};
     if (live) {
+      const df d2 = df_dist2(cp, s_sp[jj]);
+      if (track) nf.add(d2, j0 + jj, esp);
       if constexpr (CODE < 0)
-        c = rhs_df(A.dom, vgp, kd, sk, sh, cp, s_sp[jj], gc, idxc + jj);
+        c = rhs_df_d2(A.dom, vgp, kd, sk, sh, d2, gc, idxc + jj);
       else
-        c = rhs_df_single<CODE>(A.dom, vgp, kd, sk, sh, cp, s_sp[jj], gc, idxc + jj);
+        c = rhs_df_single_d2<CODE>(A.dom, vgp, kd, sk, sh, d2, gc, idxc + jj);
     }
 #pragma unroll
     for (int v = 0; v < SSV; ++v)
@@ -117,6 +120,14 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   __shared__ int any_chk;
   __shared__ float4 s_sp[sizeof(T) == 4 ? SCH : 1];
   __shared__ float2 s_w[SSV][sizeof(T) == 4 ? SCH : 1];
+  // the FP32 tier's nearest-station candidates per station group (warp),
+  // from the first pass's right-hand sides, and the cells they leave
+  // ambiguous
+  __shared__ NearDf s_nf[sizeof(T) == 4 ? SNW : 1][STC];
+  __shared__ int namb[STC];
+  const bool fuse_nnb = sizeof(T) == 4 && A.dom.split_res > 0.0;
+  const float esp = (float)(A.dom.split_res * 0x1p-24);
+  bool nf_ready = false;
 
   const int64_t gc = c0 + lane;
   const bool live = gc < C;
@@ -144,15 +155,35 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
     est_out[row * C + g] = cast_out<OutT>(clip_est(e, A.out));
     if (var_out) var_outp[row * C + g] = cast_out<OutT>(okf[cell] ? cvar[cell] : 0.0);
   };
+  // the nearest station of every cell that failed the sum check: from the
+  // right-hand sides' squared distances where they decide it, else (and
+  // without them) the exact FP64 search
   auto nearest = [&]() {
     __syncthreads();
-    if (any_bad)
+    if (any_bad) {
+      if (tid < STC) {
+        int amb = 1;
+        if constexpr (sizeof(T) == 4) {
+          if (nf_ready) {
+            NearDf m = s_nf[0][tid];
+#pragma unroll
+            for (int w = 1; w < SNW; ++w) m.merge(s_nf[w][tid]);
+            if (!m.amb && m.bj >= 0) {
+              nnb[tid] = m.bj;
+              amb = 0;
+            }
+          }
+        }
+        namb[tid] = amb;
+      }
+      __syncthreads();
       for (int cell = warp; cell < STC; cell += SNW) {
         const int64_t g = c0 + cell;
-        if (g >= C || okf[cell]) continue;
+        if (g >= C || okf[cell] || !namb[cell]) continue;
         const int j = nnb_f64_warp(A.dom, idx, n, A.dom.cell_x[g], A.dom.cell_y[g]);
         if (lane == 0) nnb[cell] = j;
       }
+    }
     __syncthreads();
   };
 
@@ -231,6 +262,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
 #pragma unroll
       for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
       int cnt = 0;
+      NearDf nf;
+      nf.init();
+      const bool track = fuse_nnb && v0 == 0;
       // stations in chunks staged in shared memory: split coordinates and
       // the vectors' hi/lo pairs, read by every warp at a shared index
       for (int j0 = 0; j0 < n; j0 += SCH) {
@@ -249,27 +283,31 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
         switch (scode) {
           case SPI_VG_EXP:
             stream_chunk<SPI_VG_EXP>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
             break;
           case SPI_VG_GAU:
             stream_chunk<SPI_VG_GAU>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
             break;
           case SPI_VG_SPH:
             stream_chunk<SPI_VG_SPH>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
             break;
           case SPI_VG_LIN:
             stream_chunk<SPI_VG_LIN>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt);
+                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
             break;
           default:
             stream_chunk<-1>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp, nv, v0,
-                             plain_duals, ph, pl, acc, cnt);
+                             plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
         }
       }
 #pragma unroll
       for (int v = 0; v < SSV; ++v) acc[v] += (double)ph[v] + (double)pl[v];
+      if (track) {
+        s_nf[warp][lane] = nf;  // read after the reduction's barriers
+        nf_ready = true;
+      }
     }
 #pragma unroll
     for (int v = 0; v < SSV; ++v) red[warp][v][lane] = acc[v];

@@ -258,12 +258,13 @@ __device__ __forceinline__ df rhs_df_cut(const spi_domain_t& dom, const spi_vg_t
 // min_vg_val zeroing); entries within 1e-6 of the cut, and variograms with
 // components that have no double-float form here (Pow, Hol, Rng), take
 // rhs_f64 itself.
-__device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vgp, const RhsDf& k,
-                                     int sk, double sh, float4 cp, float4 sp, int64_t gc,
-                                     const int32_t* stp) {
+// d2: the squared distance df_dist2(cp, sp) (rhs_df_d2: computed by the
+// caller).
+__device__ __forceinline__ df rhs_df_d2(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                        const RhsDf& k, int sk, double sh, df d2, int64_t gc,
+                                        const int32_t* stp) {
   if (!k.exact)
     return df_from(rhs_f64(dom, *vgp, sk, false, sh, dom.cell_x[gc], dom.cell_y[gc], *stp));
-  const df d2 = df_dist2(cp, sp);
   const df d = df_sqrt(d2);
   df c = {0.f, 0.f};
   if (k.single >= 0) {
@@ -281,15 +282,20 @@ __device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vg
   return rhs_df_cut(dom, vgp, k, sk, sh, gc, stp, c);
 }
 
+__device__ __forceinline__ df rhs_df(const spi_domain_t& dom, const spi_vg_t* vgp, const RhsDf& k,
+                                     int sk, double sh, float4 cp, float4 sp, int64_t gc,
+                                     const int32_t* stp) {
+  return rhs_df_d2(dom, vgp, k, sk, sh, k.exact ? df_dist2(cp, sp) : df{0.f, 0.f}, gc, stp);
+}
+
 // rhs_df for a variogram with one structure (plus nuggets) of the
 // compile-time model CODE (Exp, Gau, Sph or Lin; k.single indexes it): no
-// model switch per entry, and no square root for Gau.
+// model switch per entry, and no square root for Gau. d2 as rhs_df_d2.
 template <int CODE>
-__device__ __forceinline__ df rhs_df_single(const spi_domain_t& dom, const spi_vg_t* vgp,
-                                            const RhsDf& k, int sk, double sh, float4 cp,
-                                            float4 sp, int64_t gc, const int32_t* stp) {
+__device__ __forceinline__ df rhs_df_single_d2(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                               const RhsDf& k, int sk, double sh, df d2,
+                                               int64_t gc, const int32_t* stp) {
   const int q = k.single;
-  const df d2 = df_dist2(cp, sp);
   df rho;
   if constexpr (CODE == SPI_VG_GAU) {
     rho = df_exp(df_mul(d2, k.k2[q]));
@@ -314,6 +320,75 @@ __device__ __forceinline__ df rhs_df_single(const spi_domain_t& dom, const spi_v
   }
   return rhs_df_cut(dom, vgp, k, sk, sh, gc, stp, df_mul(k.sill[q], rho));
 }
+
+template <int CODE>
+__device__ __forceinline__ df rhs_df_single(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                            const RhsDf& k, int sk, double sh, float4 cp,
+                                            float4 sp, int64_t gc, const int32_t* stp) {
+  return rhs_df_single_d2<CODE>(dom, vgp, k, sk, sh, df_dist2(cp, sp), gc, stp);
+}
+
+// The nearest station of a cell from the double-float squared distances of
+// its right-hand sides (the FP32 tier), for the cells whose sum check fails:
+// the smallest d2 and its index, and whether another station lies within
+// the tolerance of it, where the double-float order may differ from the
+// FP64 order of dist_f64 (those cells take the exact FP64 search). The
+// split coordinates are exact to e = split_res 2^-24 per difference, so a
+// squared distance d2 = h^2 is within 2.83 h e + 2 e^2 of the FP64 one;
+// the tolerance is four times that, plus 1e-6 d2.
+struct NearDf {
+  float bh, bl;  // the smallest d2 so far
+  float tol;     // its tolerance
+  int bj;        // its station index (-1: none yet)
+  int amb;       // a station within tol of it
+  __device__ __forceinline__ void init() {
+    bh = bl = tol = 0.f;
+    bj = -1;
+    amb = 0;
+  }
+  __device__ __forceinline__ static float tol_of(float d2, float e) {
+    return 4.f * (2.83f * sqrtf(d2) * e + 2.f * e * e) + 1e-6f * d2;
+  }
+  // stations visited in increasing index order; (bh, bl) stays the running
+  // minimum, so a new minimum more than tol below it is more than tol
+  // below every station seen
+  __device__ __forceinline__ void add(df d2, int j, float e) {
+    if (bj < 0) {
+      bh = d2.h;
+      bl = d2.l;
+      bj = j;
+      tol = tol_of(d2.h, e);
+      return;
+    }
+    const float dd = (d2.h - bh) + (d2.l - bl);
+    if (dd <= tol) {
+      if (dd >= -tol) amb = 1;
+      else amb = 0;
+      if (dd < 0.f) {
+        bh = d2.h;
+        bl = d2.l;
+        bj = j;
+        tol = tol_of(d2.h, e);
+      }
+    }
+  }
+  // merge another station group's result
+  __device__ __forceinline__ void merge(const NearDf& o) {
+    if (o.bj < 0) return;
+    if (bj < 0) {
+      *this = o;
+      return;
+    }
+    const float dd = (o.bh - bh) + (o.bl - bl);
+    const float t = fmaxf(tol, o.tol);
+    if (dd < -t) {
+      *this = o;
+    } else if (dd <= t) {
+      if (dd < 0.f) *this = o;
+      amb = 1;
+    }
+  }
+};
 
 // Rounding bound of an FP32-tier sum(lambda), relative to sum |u_i| c_i:
 // entries ~1e-6 (FP32 exp, double-float distance), hi/lo products, and

@@ -191,6 +191,7 @@ class _Domain:
             if k > nat.SPI_MAX_DRIFT:
                 raise ValueError(f"at most {nat.SPI_MAX_DRIFT} drifts")
         self.ssplit = self.csplit = None
+        res = 0.0
         if precision == 1:
             ox = float(min(self.sx.min().item(), self.cx.min().item()))
             oy = float(min(self.sy.min().item(), self.cy.min().item()))
@@ -206,7 +207,7 @@ class _Domain:
                      _ptr(self.csplit), _stream())
         self.st = nat.DomainT(self.N, _ptr(self.sx), _ptr(self.sy), self.C, _ptr(self.cx),
                               _ptr(self.cy), k, _ptr(self.sd), _ptr(self.cd), float(min_vg_val),
-                              _ptr(self.ssplit), _ptr(self.csplit))
+                              _ptr(self.ssplit), _ptr(self.csplit), float(res))
 
 
 class _DomainView:
@@ -222,7 +223,7 @@ class _DomainView:
         d = dom.st
         self.st = nat.DomainT(d.n_stns, d.stn_x, d.stn_y, self.C, _ptr(self.cx), _ptr(self.cy),
                               d.n_drift, d.stn_drift, _ptr(self.cd), d.min_vg_val, d.stn_split,
-                              _ptr(self.csplit))
+                              _ptr(self.csplit), d.split_res)
 
 
 def _out_struct(est, var, min_var_cut, max_var_cut):

@@ -46,7 +46,8 @@ int main(void) {
   printf("spi_krige_ws_t %zu\n", sizeof(spi_krige_ws_t));
   P(spi_krige_ws_t, cell_yy) P(spi_krige_ws_t, tier)
   P(spi_vg_t, sill) P(spi_vg_t, range) P(spi_domain_t, n_drift) P(spi_domain_t, min_vg_val)
-  P(spi_domain_t, stn_split) P(spi_domain_t, cell_split) P(spi_systems_t, max_n)
+  P(spi_domain_t, stn_split) P(spi_domain_t, cell_split) P(spi_domain_t, split_res)
+  P(spi_systems_t, max_n)
   P(spi_systems_t, out_row) P(spi_out_t, clip_min) P(spi_out_t, clip_max)
   return 0;
 }''')
@@ -67,6 +68,7 @@ int main(void) {
     assert int(got["spi_domain_t.min_vg_val"]) == nat.DomainT.min_vg_val.offset
     assert int(got["spi_domain_t.stn_split"]) == nat.DomainT.stn_split.offset
     assert int(got["spi_domain_t.cell_split"]) == nat.DomainT.cell_split.offset
+    assert int(got["spi_domain_t.split_res"]) == nat.DomainT.split_res.offset
     assert int(got["spi_systems_t.max_n"]) == nat.SystemsT.max_n.offset
     assert int(got["spi_systems_t.out_row"]) == nat.SystemsT.out_row.offset
     assert int(got["spi_out_t.clip_min"]) == nat.OutT.clip_min.offset
