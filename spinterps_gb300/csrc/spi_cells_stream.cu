@@ -264,7 +264,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
       int cnt = 0;
       NearDf nf;
       nf.init();
-      const bool track = fuse_nnb && v0 == 0;
+      // (OK / EDK on the Cholesky path pass the sum check on every cell:
+      // their sum(lambda) is 1 up to rounding whatever the right-hand side)
+      const bool track = fuse_nnb && v0 == 0 && sk;
       // stations in chunks staged in shared memory: split coordinates and
       // the vectors' hi/lo pairs, read by every warp at a shared index
       for (int j0 = 0; j0 < n; j0 += SCH) {
