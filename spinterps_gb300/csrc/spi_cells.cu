@@ -296,16 +296,17 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
       }
     }
     // ---- 4b. exact-inverse path, OK variance of the cells that pass the
-    // check: lambda = P r, var = lambda'r + lambda_n, for the passing
-    // cells only (numerically singular systems: the sum check passes on
-    // ~1% of cells), one cell at a time, a warp per row of P: m^2 FMAs per
-    // passing cell, FP64-bound (P streams from L2). Systems too large for
-    // the cell's r in the staging buffer take wide passes over P's rows
-    // for the whole tile; skipped when no cell of the tile passes ----
+    // check: lambda = P r, var = lambda'r + lambda_n. A few passing cells
+    // (numerically singular systems: the sum check passes on ~1% of
+    // cells) take lambda = P r one cell at a time, a warp per row of P
+    // (latency-bound: P streams from L2 for each cell, about 3x the time
+    // per FMA of a wide pass); tiles where more than a quarter pass take
+    // wide passes over P's rows for the whole tile; skipped when no cell
+    // of the tile passes ----
     __syncthreads();
     if constexpr (sizeof(T) == 8) {
       const int m_prim = n + a;
-      if (prim && A.want_var && !sk && any_ok && m_prim <= KC * BSTR) {
+      if (prim && A.want_var && !sk && any_ok && n_ok <= TC / 4 && m_prim <= KC * BSTR) {
         const int m = m_prim;
         if (tid == 0 && A.ws.var_cells) atomicAdd(A.ws.var_cells + s, n_ok);
         double* rv = reinterpret_cast<double*>(Bs);  // [m] the cell's r

@@ -22,12 +22,13 @@
 //     thread and counted on the stage's mbarrier;
 //   - A, the cells' right-hand sides (128 x 8), is generated by all threads
 //     in double-float (rhs_df, or rhs_df_single for a one-structure
-//     variogram) from the stations in shared memory and stored as three
-//     TF32 terms (a0 + a1 + a2, ~33 bits), in the no-swizzle K-major layout
-//     (8-row x 16-byte core matrices).
-// One thread issues the chunk's 6 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 +
-// a1 b1 + a2 b0, K = 8, FP32 accumulation in TMEM: the terms left out are
-// ~2^-33 of the product) and commits them to the stage's
+//     variogram) from the stations in shared memory and stored as two TF32
+//     terms (a0 + a1, ~22 bits), in the no-swizzle K-major layout (8-row x
+//     16-byte core matrices). A third term (a2 b0, a sixth MMA) leaves the
+//     probe's variance discrepancies unchanged: the FP32 accumulation in
+//     TMEM, not A's split, bounds this kernel's accuracy.
+// One thread issues the chunk's 5 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 +
+// a1 b1, K = 8, FP32 accumulation in TMEM) and commits them to the stage's
 // mbarrier; the threads go on to the next chunk while they run, and a stage
 // is refilled only after the MMAs that read it completed. Every wait is
 // bounded: on expiry the kernel raises err_flag, drains the copies and MMAs
@@ -53,7 +54,7 @@ constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;       // one TF32 term o
 constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;       // one TF32 term of B
 constexpr size_t VT_S_BYTES = (size_t)VT_KC * 16;             // the chunk's stations (float4)
 constexpr size_t VT_CHUNK_BYTES = 3 * VT_B_BYTES + VT_S_BYTES;  // one packed chunk
-constexpr size_t VT_STAGE = 3 * VT_A_BYTES + VT_CHUNK_BYTES;  // A (3 terms), the chunk
+constexpr size_t VT_STAGE = 2 * VT_A_BYTES + VT_CHUNK_BYTES;  // A (2 terms), the chunk
 constexpr size_t VT_SMEM = VT_NST * VT_STAGE;
 constexpr int VT_CHUNK_FLOATS = (int)(VT_CHUNK_BYTES / 4);
 static_assert(VT_CHUNK_FLOATS == SPI_VAR_TC_CHUNK_FLOATS, "packed chunk size");
@@ -88,11 +89,17 @@ __device__ __forceinline__ int tile_off(int R, int row, int k) {
   return (k >> 2) * (R * 16) + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4;
 }
 
-// TF32 keeps the top 19 bits of an FP32 value: x rounded to those bits
-// (half away from zero on the magnitude); the remainder x - tf32_rn(x) is
-// exact in FP32 and at most 2^-11 |x|.
 __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// TF32 keeps the top 19 bits of an FP32 value: hi = x rounded to those
+// bits (half away from zero on the magnitude), lo = the exact remainder
+// (|lo| <= 2^-11 |x|), itself truncated by the tensor core. Rounding the
+// head rather than truncating it halves lo and the split's error.
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+  lo = x - hi;
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
@@ -135,14 +142,14 @@ __device__ __forceinline__ void vt_load(uint32_t dst, const float* src, uint32_t
 }
 
 // The chunk's right-hand sides of one thread: cell a_cell, stations
-// k0 + kb .. k0 + kb + 3 (coordinates from the stage), as three TF32 terms
-// into the A tiles (sA, + VT_A_BYTES, + 2 VT_A_BYTES). CODE: the single
-// structure's model, or -1 (rhs_df).
+// k0 + kb .. k0 + kb + 3 (coordinates from the stage), as two TF32 terms
+// into the A tiles. CODE: the single structure's model, or -1 (rhs_df).
 template <int CODE>
 __device__ __forceinline__ void vt_gen(const spi_domain_t& dom, const spi_vg_t* vgp,
                                        const RhsDf& kd, double sh, float4 cp, bool live,
                                        int64_t gc, const int32_t* idx, int n, int k0, int kb,
-                                       int a_cell, const float4* ssp, unsigned char* sA) {
+                                       int a_cell, const float4* ssp, unsigned char* sAh,
+                                       unsigned char* sAl) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int kk = kb + q, j = k0 + kk;
@@ -153,15 +160,12 @@ __device__ __forceinline__ void vt_gen(const spi_domain_t& dom, const spi_vg_t* 
       else
         c = rhs_df_single<CODE>(dom, vgp, kd, 0, sh, cp, ssp[kk], gc, idx + j);
     }
-    // c = a0 + a1 + a2: a0 the TF32 rounding of the head, a1 of the
-    // remainder (head's rest plus the tail, exact in FP32), a2 what is left
-    const float a0 = tf32_rn(c.h);
-    const float r1 = (c.h - a0) + c.l;
-    const float a1 = tf32_rn(r1);
+    float h, l;
+    tf32_split(c.h, h, l);
+    l += c.l;
     const int o = tile_off(VT_M, a_cell, kk);
-    *reinterpret_cast<float*>(sA + o) = a0;
-    *reinterpret_cast<float*>(sA + VT_A_BYTES + o) = a1;
-    *reinterpret_cast<float*>(sA + 2 * VT_A_BYTES + o) = r1 - a1;
+    *reinterpret_cast<float*>(sAh + o) = h;
+    *reinterpret_cast<float*>(sAl + o) = l;
   }
 }
 
@@ -239,7 +243,7 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
     }
   };
   if (tid == 0 && total > 0) {
-    vt_load(smem_u32(stage(0) + 3 * VT_A_BYTES), pk, smem_u32(&bbar[0]));
+    vt_load(smem_u32(stage(0) + 2 * VT_A_BYTES), pk, smem_u32(&bbar[0]));
     issued = 1;
   }
   for (int rb = 0; rb < n && !fail; rb += VT_N) {
@@ -251,12 +255,13 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
       __syncthreads();
       if (fail) break;
       if (tid == 0 && g + 1 < total) {
-        vt_load(smem_u32(stage((g + 1) % VT_NST) + 3 * VT_A_BYTES),
+        vt_load(smem_u32(stage((g + 1) % VT_NST) + 2 * VT_A_BYTES),
                 pk + (int64_t)(g + 1) * VT_CHUNK_FLOATS, smem_u32(&bbar[(g + 1) % VT_NST]));
         issued = g + 2;
       }
-      unsigned char* sA = stage(st);
-      unsigned char* sB = sA + 3 * VT_A_BYTES;
+      unsigned char* sAh = stage(st);
+      unsigned char* sAl = sAh + VT_A_BYTES;
+      unsigned char* sB = sAh + 2 * VT_A_BYTES;
       const float4* ssp = reinterpret_cast<const float4*>(sB + 3 * VT_B_BYTES);
       // chunk g's B and stations (on expiry the stage holds garbage: the
       // right-hand sides below stay in shared memory and the MMAs are not
@@ -266,36 +271,36 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
       const int k0 = kc * VT_KC;
       switch (scode) {
         case SPI_VG_EXP:
-          vt_gen<SPI_VG_EXP>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sA);
+          vt_gen<SPI_VG_EXP>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh,
+                             sAl);
           break;
         case SPI_VG_GAU:
-          vt_gen<SPI_VG_GAU>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sA);
+          vt_gen<SPI_VG_GAU>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh,
+                             sAl);
           break;
         case SPI_VG_SPH:
-          vt_gen<SPI_VG_SPH>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sA);
+          vt_gen<SPI_VG_SPH>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh,
+                             sAl);
           break;
         default:
-          vt_gen<-1>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sA);
+          vt_gen<-1>(A.dom, vgp, kd, sh, cp, live, gc, idx, n, k0, kb, a_cell, ssp, sAh, sAl);
       }
       asm volatile("fence.proxy.async.shared::cta;");
       __syncthreads();
       if (tid == 0) {
         if (!fail) {
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t a = smem_u32(sA);
-          const uint64_t a0 = umma_desc(a, VT_M * 16, 128);
-          const uint64_t a1 = umma_desc(a + (uint32_t)VT_A_BYTES, VT_M * 16, 128);
-          const uint64_t a2 = umma_desc(a + 2 * (uint32_t)VT_A_BYTES, VT_M * 16, 128);
+          const uint64_t ah = umma_desc(smem_u32(sAh), VT_M * 16, 128);
+          const uint64_t al = umma_desc(smem_u32(sAl), VT_M * 16, 128);
           const uint32_t b = smem_u32(sB);
           const uint64_t b0 = umma_desc(b, VT_N * 16, 128);
           const uint64_t b1 = umma_desc(b + (uint32_t)VT_B_BYTES, VT_N * 16, 128);
           const uint64_t b2 = umma_desc(b + 2 * (uint32_t)VT_B_BYTES, VT_N * 16, 128);
-          mma_tf32(tmem, a0, b0, idesc, kc > 0 ? 1u : 0u);
-          mma_tf32(tmem, a0, b1, idesc, 1u);
-          mma_tf32(tmem, a1, b0, idesc, 1u);
-          mma_tf32(tmem, a0, b2, idesc, 1u);
-          mma_tf32(tmem, a1, b1, idesc, 1u);
-          mma_tf32(tmem, a2, b0, idesc, 1u);
+          mma_tf32(tmem, ah, b0, idesc, kc > 0 ? 1u : 0u);
+          mma_tf32(tmem, ah, b1, idesc, 1u);
+          mma_tf32(tmem, al, b0, idesc, 1u);
+          mma_tf32(tmem, ah, b2, idesc, 1u);
+          mma_tf32(tmem, al, b1, idesc, 1u);
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -428,7 +433,7 @@ extern "C" int spi_krige_var_tc(const spi_domain_t* dom, const spi_systems_t* sy
   if (tiles > 0x7fffffff) return SPI_ERR_TOO_LARGE;
   if (reinterpret_cast<uintptr_t>(ws->linv_tc) & 15) return SPI_ERR_ARG;
   if (!smem_opt_in(k_var_tc, VT_SMEM)) return SPI_ERR_CUDA;
-  // two CTAs per SM need (nearly) all of its shared memory
+  // two CTAs per SM need most of its shared memory
   if (cudaFuncSetAttribute(k_var_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100) !=
       cudaSuccess)
     return SPI_ERR_CUDA;
