@@ -30,11 +30,12 @@ template <typename T, int TC, bool W>
 __device__ __forceinline__ void contract(const T* cvT, T* Bs, const double* const* vp64,
                                          const float* const* vph, const float* const* vpl,
                                          int nv, int jmax, int nload,
-                                         double (&out)[Layout<TC, W>::CPT][Layout<TC, W>::VPT]) {
+                                         double (&out)[Layout<TC, W>::CPT][Layout<TC, W>::VPT],
+                                         int jmin = 0) {
   if constexpr (sizeof(T) == 8)
-    tile_contract<T, TC, W>(cvT, Bs, PtrLoader64{vp64}, nv, jmax, nload, out);
+    tile_contract<T, TC, W>(cvT, Bs, PtrLoader64{vp64}, nv, jmax, nload, out, jmin);
   else
-    tile_contract<T, TC, W>(cvT, Bs, PtrLoader32{vph, vpl}, nv, jmax, nload, out);
+    tile_contract<T, TC, W>(cvT, Bs, PtrLoader32{vph, vpl}, nv, jmax, nload, out, jmin);
 }
 
 template <typename T, int TC, typename OutT>
@@ -334,20 +335,34 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
           }
         }
       } else if (prim && A.want_var && !sk && any_ok) {
+        // the whole tile, as the symmetric quadratic form over P's block
+        // upper triangle: with r' = r + e_n / 2 (r_n = 1, the unbiasedness
+        // row), var = r'P r' - P_nn / 4, and per block of VB rows i
+        // r'P r' gathers r'_i (D_i + 2 U_i): D over the block's own
+        // columns, U over the columns right of it (about m^2 / 2 FMAs per
+        // cell instead of m^2)
         const int m = m_prim;
         // cells whose tile ran this pass (the FLOP count of the roofline)
         if (tid == 0 && A.ws.var_cells)
           atomicAdd(A.ws.var_cells + s, (int)min((int64_t)TC, C - c0));
+        __syncthreads();
+        for (int cell = tid; cell < TC; cell += CT) cvT[(int64_t)n * TC + cell] = 1.5;
         double vpart[CPT];
 #pragma unroll
         for (int c = 0; c < CPT; ++c) vpart[c] = 0.0;
         const int cg = tid % 16, rg = tid / 16;
         for (int r0 = 0; r0 < m; r0 += VB) {
+          const int r1 = min(m, r0 + VB);
           __syncthreads();
           for (int v = tid; v < VB; v += CT)
             setv(v, A.ws.l_arena, nullptr, nullptr, moff + (int64_t)(r0 + v) * m, r0 + v < m);
-          double acc[CPT][4];
-          contract<T, TC, true>(cvT, Bs, vp64, vph, vpl, min(VB, m - r0), m, m, acc);
+          double dg[CPT][4], up[CPT][4];
+          contract<T, TC, true>(cvT, Bs, vp64, vph, vpl, r1 - r0, r1, m, dg, r0);
+#pragma unroll
+          for (int c = 0; c < CPT; ++c)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) up[c][r] = 0.0;
+          if (r1 < m) contract<T, TC, true>(cvT, Bs, vp64, vph, vpl, r1 - r0, m, m, up, r1);
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
             const int row = r0 + rg * 4 + r;
@@ -355,19 +370,21 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
 #pragma unroll
             for (int c = 0; c < CPT; ++c) {
               const int cell = cg * CPT + c;
-              vpart[c] += acc[c][r] * (double)cvT[(int64_t)row * TC + cell];
-              if (row == n) vpart[c] += acc[c][r];
+              vpart[c] += (double)cvT[(int64_t)row * TC + cell] * (dg[c][r] + 2.0 * up[c][r]);
             }
           }
         }
         __syncthreads();
 #pragma unroll
         for (int c = 0; c < CPT; ++c) red[rg * TC + cg * CPT + c] = vpart[c];
+        for (int cell = tid; cell < TC; cell += CT)
+          cvT[(int64_t)n * TC + cell] = c0 + cell < C ? 1.0 : 0.0;
         __syncthreads();
+        const double pnn = A.ws.l_arena[moff + (int64_t)n * m + n];
         for (int cell = tid; cell < TC; cell += CT) {
           double vv = 0.0;
           for (int g = 0; g < 16; ++g) vv += red[g * TC + cell];
-          if (okf[cell]) cvar[cell] = vv;
+          if (okf[cell]) cvar[cell] = vv - 0.25 * pnn;
         }
       }
     }

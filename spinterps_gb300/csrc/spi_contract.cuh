@@ -1,6 +1,7 @@
 // Shared-memory-tiled contraction used by the cell kernels.
 //
-// out[c][r] = sum_{j < jmax} cvT[j][cell(c)] * B_{vec(r)}[j]
+// out[c][r] = sum_{jmin <= j < jmax} cvT[j][cell(c)] * B_{vec(r)}[j]
+// (jmin a multiple of KC, 0 by default)
 // cvT [npad][TC] holds TC cells' right-hand sides (or weights),
 // cell-contiguous; B_v[j] comes from a loader functor. 256 threads, in two
 // layouts:
@@ -71,7 +72,8 @@ struct Layout {
 template <typename T, int TC, bool W, typename Loader>
 __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __restrict__ Bs,
                                               const Loader& ld, int nv, int jmax, int n,
-                                              double (&out)[Layout<TC, W>::CPT][Layout<TC, W>::VPT]) {
+                                              double (&out)[Layout<TC, W>::CPT][Layout<TC, W>::VPT],
+                                              int jmin = 0) {
   using LY = Layout<TC, W>;
   constexpr int CPT = LY::CPT, VPT = LY::VPT, NV = LY::NV;
   const int tid = threadIdx.x, cg = tid % LY::NCG, rg = tid / LY::NCG;
@@ -80,7 +82,7 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
 #pragma unroll
     for (int r = 0; r < VPT; ++r) out[c][r] = 0.0;
   if constexpr (sizeof(T) == 8) {
-    for (int k0 = 0; k0 < jmax; k0 += KC) {
+    for (int k0 = jmin; k0 < jmax; k0 += KC) {
       __syncthreads();
       for (int e = tid; e < NV * KC; e += CT) {
         int v = e / KC, jj = e % KC;
@@ -114,7 +116,7 @@ __device__ __forceinline__ void tile_contract(const T* __restrict__ cvT, T* __re
 #pragma unroll
       for (int r = 0; r < VPT; ++r) acc[c][r] = 0.f;
     int chunk = 0;
-    for (int k0 = 0; k0 < jmax; k0 += KC, ++chunk) {
+    for (int k0 = jmin; k0 < jmax; k0 += KC, ++chunk) {
       __syncthreads();
       for (int e = tid; e < NV * KC; e += CT) {
         int v = e / KC, jj = e % KC;
