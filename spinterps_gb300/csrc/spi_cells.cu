@@ -50,7 +50,7 @@ __global__ __launch_bounds__(CT) void k_krige_cells(CellsArgs A, int npad) {
   const int route = A.ws.route[s];
   {
     // filter 1: well-conditioned Cholesky systems; filter 2: all others
-    const bool fast = fp32_tier(A.ws, s, A.cond_split);
+    const bool fast = fp32_tier(A.ws, s, A.cond_split, A.sys.kind == SPI_KIND_SK);
     if ((A.route_filter == 1 && !fast) || (A.route_filter == 2 && fast)) return;
   }
   const bool prim = route == 1;   // exact-inverse path: primal formulas
@@ -662,9 +662,9 @@ __global__ __launch_bounds__(256) void k_tier(spi_systems_t sys, spi_krige_ws_t 
   __shared__ double red[3][256];
   // a timed-out tensor-core wait (spi_krige_var_tc) leaves var32 partly
   // unwritten: every system then stays in FP64
-  const bool route0 = ws.route[s] == 0 && !(tc_err && *tc_err);
-  const bool cand = route0 && ws.cond[s] <= cap;
-  const bool cand_d = route0 && v32d != nullptr && ws.cond[s] <= cap_d;
+  const bool fr = fp32_route(ws.route[s], sys.kind == SPI_KIND_SK) && !(tc_err && *tc_err);
+  const bool cand = fr && ws.cond[s] <= cap;
+  const bool cand_d = fr && v32d != nullptr && ws.cond[s] <= cap_d;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
   auto gap = [&](double a, double r) {
     return isnan(a) != isnan(r) ? inf : (isnan(a) ? 0.0 : fabs(a - r));

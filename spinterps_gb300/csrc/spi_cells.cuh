@@ -43,11 +43,23 @@ __device__ inline int nnb_f64_warp(const spi_domain_t& dom, const int32_t* idx, 
   return bj == 0x7fffffff ? 0 : bj;
 }
 
+// Systems an FP32 tier can take: the Cholesky path, and SK on the
+// exact-inverse path (its weights lambda = P c contract the same
+// covariances against the dual vectors P 1 and P z; the min_vg_val cut
+// makes SK matrices indefinite, so Cholesky fails on many well-conditioned
+// ones). OK / EDK keep the exact-inverse path in FP64: there it holds the
+// numerically singular systems, whose answers only the same FP64
+// arithmetic reproduces.
+__device__ __forceinline__ bool fp32_route(int route, int sk) {
+  return route == 0 || (sk && route == 1);
+}
+
 // The FP32 tier of the precision-1 kernels: the probe's verdict when there
-// is one (spi_krige_tier), else the Cholesky path under cond_split.
-__device__ __forceinline__ bool fp32_tier(const spi_krige_ws_t& ws, int s, double cond_split) {
+// is one (spi_krige_tier), else an FP32-capable route under cond_split.
+__device__ __forceinline__ bool fp32_tier(const spi_krige_ws_t& ws, int s, double cond_split,
+                                          int sk) {
   if (ws.tier) return ws.tier[s] != 0;
-  return ws.route[s] == 0 && ws.cond[s] <= cond_split;
+  return fp32_route(ws.route[s], sk) && ws.cond[s] <= cond_split;
 }
 
 // Host-side dispatch of the streamed kernel (spi_cells_stream.cu): systems

@@ -85,7 +85,7 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   if (c0 >= C) return;
   const int route = A.ws.route[s];
   {
-    const bool fast = fp32_tier(A.ws, s, A.cond_split);
+    const bool fast = fp32_tier(A.ws, s, A.cond_split, A.sys.kind == SPI_KIND_SK);
     if ((A.route_filter == 1 && !fast) || (A.route_filter == 2 && fast)) return;
   }
   const bool prim = route == 1;
@@ -95,7 +95,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   const int32_t* idx = A.sys.stn_idx + soff;
   const int sk = A.sys.kind == SPI_KIND_SK;
   const int a = sk ? 1 : extra_rows(A.sys.kind, A.dom.n_drift);
-  const int ndual = prim ? 1 : ((sk && sizeof(T) == 4) ? 2 : a);
+  // (SK in an FP32 tier adds |u|, the bound of its sum check's rounding,
+  // on either route)
+  const int ndual = (sk && sizeof(T) == 4) ? 2 : (prim ? 1 : a);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t st0 = A.sys.step_off[s];
   const int nsteps = (int)(A.sys.step_off[s + 1] - st0);

@@ -957,6 +957,10 @@ __global__ __launch_bounds__(FT) void k_duals(spi_domain_t dom, spi_systems_t sy
     matvec_rows(P, m, n, va, vb);
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) G[i] = vb[i];
+    // SK: |u| as a second column, as on the Cholesky path (the FP32 tier's
+    // bound of its sum check's rounding)
+    if (sk)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) G[n + i] = fabs(vb[i]);
     if (threadIdx.x < GA)
       ws.g_colsum[(int64_t)s * GA + threadIdx.x] = (threadIdx.x < ar) ? vb[n + threadIdx.x] : 0.0;
     for (int64_t si = sys.step_off[s]; si < sys.step_off[s + 1]; ++si) {

@@ -176,7 +176,7 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
   if (c0 >= C) return;
   if (A.sys.kind == SPI_KIND_SK) return;
   // tier 1 only (tier 2 takes its variance from spi_var_df.cu)
-  if (A.ws.tier ? A.ws.tier[s] != 1 : !fp32_tier(A.ws, s, A.cond_split)) return;
+  if (A.ws.tier ? A.ws.tier[s] != 1 : !fp32_tier(A.ws, s, A.cond_split, 0)) return;
   const int64_t soff = A.sys.stn_off[s];
   const int n = (int)(A.sys.stn_off[s + 1] - soff);
   const int32_t* idx = A.sys.stn_idx + soff;
