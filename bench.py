@@ -820,6 +820,7 @@ def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
     n_fast = len(info.get("fp32_tier_steps", {}).get("EDK", []))
     n_cap = int(np.sum(cond <= pm.cond_split))
     refinement = refinement_summary(info, "EDK")
+    failed = sorted(info.get("failed_steps", {}).get("EDK", []))
     sub = np.arange(0, T, fp64_every)
     fm = pm.flds["EDK"][torch.as_tensor(sub, device=pm.flds["EDK"].device)].clone()
     del pm
@@ -869,6 +870,9 @@ def large_leg(args, reps, fp64_every=1, e2e=False, clocks=True):
            "tiers": {"fp32": n_fast, "fp64": int(cond.size - n_fast), "cond_under_cap": n_cap,
                      "cond_median": float(np.median(cond)), "cond_max": float(cond.max())},
            "refinement": refinement,
+           # singular systems above the pinv check's size: nearest station
+           "singular_steps_nnb": {"count": len(failed), "steps": failed[:8],
+                                  "vgs": [vgs[j] for j in failed[:8]]},
            "fit": {"seconds": t_fit, "fallback_steps": len(det["_fallback_steps"]),
                    "de_ms": det["_de_ms"], "ms": det["_ms"]},
            "synthesis_s": t_gen}
