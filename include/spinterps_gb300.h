@@ -257,9 +257,9 @@ typedef struct {
                             duals took (the largest over their right-hand
                             sides; bit 30 set where the componentwise
                             backward error did not reach sqrt(n) eps in
-                            SPI_IR_MAX_ITERS) */
+                            SPI_IR_MAX_ITERS, or stopped halving) */
     double cond_ir;      /* with l32: the largest condition estimate that
-                            tries the FP32 factor (1e12 if 0; the estimate
+                            tries the FP32 factor (1e10 if 0; the estimate
                             overstates the condition, and systems whose
                             refinement fails fall back to FP64) */
     double *gj_scratch;  /* optional, 1 + 2 * (total stations) + (2 * GA +

@@ -17,6 +17,8 @@
 // double-float and flushed to FP64 every 256 terms: the estimate's error is
 // sum_i dc_i w_i, which large dual weights amplify. With ws.cell_yy (the
 // tensor-core |Linv c|^2) the FP32 tier also writes the OK variance.
+#include <type_traits>
+
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
 
@@ -33,7 +35,7 @@ constexpr int SCH = 256; // stations per shared-memory chunk (FP32 tier)
 // by the FMA error, the cross terms, TwoSum into a double-float partial,
 // flushed to FP64 every 256 terms. Dual columns that feed only the sum
 // check (v0 + v < plain_duals) take a plain FP32 product.
-template <int CODE>
+template <int CODE, bool TRACK>
 __device__ __forceinline__ void stream_chunk(const CellsArgs& A, const spi_vg_t* vgp,
                                              const RhsDf& kd, int sk, double sh, float4 cp,
                                              bool live, int64_t gc, const int32_t* idxc,
@@ -41,12 +43,12 @@ __device__ __forceinline__ void stream_chunk(const CellsArgs& A, const spi_vg_t*
                                              int nj, int warp, int nv, int v0, int plain_duals,
                                              float (&ph)[SSV], float (&pl)[SSV],
                                              double (&acc)[SSV], int& cnt, NearDf& nf,
-                                             bool track, int j0, float esp) {
+                                             int j0, float esp) {
   for (int jj = warp; jj < nj; jj += SNW) {
     df c = {0.f, 0.f};
     if (live) {
       const df d2 = df_dist2(cp, s_sp[jj]);
-      if (track) nf.add(d2, j0 + jj, esp);
+      if constexpr (TRACK) nf.add(d2, j0 + jj, esp);
       if constexpr (CODE < 0)
         c = rhs_df_d2(A.dom, vgp, kd, sk, sh, d2, gc, idxc + jj);
       else
@@ -284,27 +286,40 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
         // the single structure's model, uniform over the CTA
         const int scode = (kd.exact && kd.single >= 0) ? kd.code[kd.single] : -1;
         const int32_t* idxc = idx + j0;
-        switch (scode) {
-          case SPI_VG_EXP:
-            stream_chunk<SPI_VG_EXP>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
-            break;
-          case SPI_VG_GAU:
-            stream_chunk<SPI_VG_GAU>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
-            break;
-          case SPI_VG_SPH:
-            stream_chunk<SPI_VG_SPH>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
-            break;
-          case SPI_VG_LIN:
-            stream_chunk<SPI_VG_LIN>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp,
-                                     nv, v0, plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
-            break;
-          default:
-            stream_chunk<-1>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp, nv, v0,
-                             plain_duals, ph, pl, acc, cnt, nf, track, j0, esp);
-        }
+        // the nearest-station tracking as a compile-time choice: kernels
+        // that never need it carry none of its state through the loop
+        auto chunk = [&](auto trk) {
+          constexpr bool TR = decltype(trk)::value;
+          switch (scode) {
+            case SPI_VG_EXP:
+              stream_chunk<SPI_VG_EXP, TR>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj,
+                                           warp, nv, v0, plain_duals, ph, pl, acc, cnt, nf, j0,
+                                           esp);
+              break;
+            case SPI_VG_GAU:
+              stream_chunk<SPI_VG_GAU, TR>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj,
+                                           warp, nv, v0, plain_duals, ph, pl, acc, cnt, nf, j0,
+                                           esp);
+              break;
+            case SPI_VG_SPH:
+              stream_chunk<SPI_VG_SPH, TR>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj,
+                                           warp, nv, v0, plain_duals, ph, pl, acc, cnt, nf, j0,
+                                           esp);
+              break;
+            case SPI_VG_LIN:
+              stream_chunk<SPI_VG_LIN, TR>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj,
+                                           warp, nv, v0, plain_duals, ph, pl, acc, cnt, nf, j0,
+                                           esp);
+              break;
+            default:
+              stream_chunk<-1, TR>(A, vgp, kd, sk, sh, cp, live, gc, idxc, s_sp, s_w, nj, warp, nv,
+                                   v0, plain_duals, ph, pl, acc, cnt, nf, j0, esp);
+          }
+        };
+        if (track)
+          chunk(std::true_type{});
+        else
+          chunk(std::false_type{});
       }
 #pragma unroll
       for (int v = 0; v < SSV; ++v) acc[v] += (double)ph[v] + (double)pl[v];

@@ -583,6 +583,7 @@ __device__ void ainv_apply(const spi_krige_ws_t& ws, int s, int n, int64_t moff,
   trsv_lower_t_multi(L, n, Y, n, kk);
   int it = 0;
   bool conv = false;
+  double prev = __longlong_as_double(0x7ff0000000000000LL);
   for (;; ++it) {
     // D = b - A x and the componentwise backward error, a warp per row
     double be = 0.0;
@@ -627,7 +628,12 @@ __device__ void ainv_apply(const spi_krige_ws_t& ws, int s, int n, int64_t moff,
       conv = true;
       break;
     }
-    if (it == SPI_IR_MAX_ITERS) break;
+    // a factor too far from A (cond x the FP32 rounding near 1 or above)
+    // makes no progress: stop once a correction fails to halve the
+    // backward error (a converging refinement shrinks it by orders of
+    // magnitude per step)
+    if (it == SPI_IR_MAX_ITERS || !(be < 0.5 * prev)) break;
+    prev = be;
     trsv_lower_multi(L, n, D, n, kk);
     trsv_lower_t_multi(L, n, D, n, kk);
     for (int e = threadIdx.x; e < kk * n; e += FT) Y[e] += D[e];
@@ -1167,7 +1173,7 @@ extern "C" int spi_krige_factor(const spi_domain_t* dom, const spi_systems_t* sy
     k_cond_est<float><<<sys->n_sys, FT, ysm, st>>>(sy, ws->l32, ws->status, ws->cond, nk,
                                                     nullptr, 0);
     k_ir_gate<<<(sys->n_sys + 255) / 256, 256, 0, st>>>(sy, *ws,
-                                                       ws->cond_ir > 0 ? ws->cond_ir : 1e12);
+                                                       ws->cond_ir > 0 ? ws->cond_ir : 1e10);
     SPI_LAUNCH_CHECK();
   }
   k_chol<double><<<sys->n_sys, FT, 0, st>>>(sy, ws->l_arena, ws->status, ir ? ws->ir : nullptr,

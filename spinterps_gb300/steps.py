@@ -242,7 +242,7 @@ class _KrigeBatch:
 
     def __init__(self, dev, dom, kind, systems, ch, data, T, val_off, beta, precision,
                  want_var=False, tensor_cores=True, n_probe=0, need_linv=None, pinv=None,
-                 ir=True, cond_ir=1e12):
+                 ir=True, cond_ir=1e10):
         self.ch = ch
         self.kind = kind
         self.precision = precision
@@ -546,7 +546,7 @@ class InterpPlan:
                  min_var_cut=None, max_var_cut=None, min_vg_val=0.0, intrp_dtype=np.float32,
                  time_steps=None, precision="fp64", device="cuda", arena_budget=8 << 30,
                  cond_max=1e13, cond_split=None, tensor_cores=True, probe_cells=1024,
-                 probe_tol=2e-6, cond_df=COND_DF, refine=True, cond_ir=1e12):
+                 probe_tol=2e-6, cond_df=COND_DF, refine=True, cond_ir=1e10):
         dev = self.dev = _require_cuda(device)
         if cond_split is None:
             # a cap under the probe; without it, the a-priori split
@@ -953,7 +953,7 @@ def interp_steps(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, est_va
                  precision="fp64", device="cuda", return_numpy=True, return_info=False,
                  arena_budget=8 << 30, cond_max=1e13, cond_split=None, tensor_cores=True,
                  probe_cells=1024, probe_tol=2e-6, neb_sel_mthd="all", n_nebs=None,
-                 n_pies=None, refine=True, cond_ir=1e12):
+                 n_pies=None, refine=True, cond_ir=1e10):
     """Interpolate every step onto every cell on the GPU.
 
     ``neb_sel_mthd`` 'nrst' / 'pie' (with ``n_nebs``, ``n_pies``) selects
