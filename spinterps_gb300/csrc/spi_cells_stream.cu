@@ -124,10 +124,11 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
   __shared__ int any_chk;
   __shared__ float4 s_sp[sizeof(T) == 4 ? SCH : 1];
   __shared__ float2 s_w[SSV][sizeof(T) == 4 ? SCH : 1];
-  // the FP32 tier's nearest-station candidates per station group (warp),
-  // from the first pass's right-hand sides, and the cells they leave
-  // ambiguous
-  __shared__ NearDf s_nf[sizeof(T) == 4 ? SNW : 1][STC];
+  // the FP32 tier's nearest-station candidates per station group (warp)
+  // and cell, from the first pass's right-hand sides (written over red once
+  // the pass's sums are reduced), and the cells they leave ambiguous
+  NearDf* s_nf = reinterpret_cast<NearDf*>(&red[0][0][0]);
+  static_assert(sizeof(NearDf) * SNW * STC <= sizeof(red), "candidates fit in red");
   __shared__ int namb[STC];
   const bool fuse_nnb = sizeof(T) == 4 && A.dom.split_res > 0.0;
   const float esp = (float)(A.dom.split_res * 0x1p-24);
@@ -169,9 +170,9 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
         int amb = 1;
         if constexpr (sizeof(T) == 4) {
           if (nf_ready) {
-            NearDf m = s_nf[0][tid];
+            NearDf m = s_nf[tid];
 #pragma unroll
-            for (int w = 1; w < SNW; ++w) m.merge(s_nf[w][tid]);
+            for (int w = 1; w < SNW; ++w) m.merge(s_nf[w * STC + tid]);
             if (!m.amb && m.bj >= 0) {
               nnb[tid] = m.bj;
               amb = 0;
@@ -247,6 +248,11 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
     double acc[SSV];
 #pragma unroll
     for (int v = 0; v < SSV; ++v) acc[v] = 0.0;
+    // (OK / EDK on the Cholesky path pass the sum check on every cell:
+    // their sum(lambda) is 1 up to rounding whatever the right-hand side)
+    const bool track = sizeof(T) == 4 && fuse_nnb && v0 == 0 && sk;
+    NearDf nf;
+    nf.init();
     if constexpr (sizeof(T) == 8) {
       for (int j = warp; j < n; j += SNW) {
         const int st = idx[j];
@@ -266,11 +272,6 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
 #pragma unroll
       for (int v = 0; v < SSV; ++v) ph[v] = pl[v] = 0.f;
       int cnt = 0;
-      NearDf nf;
-      nf.init();
-      // (OK / EDK on the Cholesky path pass the sum check on every cell:
-      // their sum(lambda) is 1 up to rounding whatever the right-hand side)
-      const bool track = fuse_nnb && v0 == 0 && sk;
       // stations in chunks staged in shared memory: split coordinates and
       // the vectors' hi/lo pairs, read by every warp at a shared index
       for (int j0 = 0; j0 < n; j0 += SCH) {
@@ -323,10 +324,6 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
       }
 #pragma unroll
       for (int v = 0; v < SSV; ++v) acc[v] += (double)ph[v] + (double)pl[v];
-      if (track) {
-        s_nf[warp][lane] = nf;  // read after the reduction's barriers
-        nf_ready = true;
-      }
     }
 #pragma unroll
     for (int v = 0; v < SSV; ++v) red[warp][v][lane] = acc[v];
@@ -339,6 +336,10 @@ __global__ __launch_bounds__(STC * SNW, 2) void k_krige_cells_stream(CellsArgs A
       vres[v][cell] = t;
     }
     __syncthreads();
+    if (track) {
+      s_nf[warp * STC + lane] = nf;  // red is free again
+      nf_ready = true;
+    }
     if (v0 == 0) {
       // the sum check of every cell, from the dual columns (all in pass 0)
       if (tid == 0) any_bad = any_chk = 0;
