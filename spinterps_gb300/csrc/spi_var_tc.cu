@@ -21,10 +21,10 @@
 //     (cp.async.bulk, 24 KB) per chunk, issued one chunk ahead by one
 //     thread and counted on the stage's mbarrier;
 //   - A, the cells' right-hand sides (128 x 8), is generated by all threads
-//     in double-float (rhs_df, or rhs_df_single for a one-structure
-//     variogram) from the stations in shared memory and stored as two TF32
-//     terms (a0 + a1, ~22 bits), in the no-swizzle K-major layout (8-row x
-//     16-byte core matrices). A third term (a2 b0, a sixth MMA) leaves the
+//     in FP32 (vt_rhs_f32 for a one-structure variogram, else the head of
+//     the double-float rhs_df) from the stations in shared memory and
+//     stored as two TF32 terms (a0 + a1, ~22 bits), in the no-swizzle
+//     K-major layout (8-row x 16-byte core matrices). A third term (a2 b0, a sixth MMA) leaves the
 //     probe's variance discrepancies unchanged: the FP32 accumulation in
 //     TMEM, not A's split, bounds this kernel's accuracy.
 // One thread issues the chunk's 5 MMAs (a0 b0 + a0 b1 + a1 b0 + a0 b2 +
@@ -141,9 +141,47 @@ __device__ __forceinline__ void vt_load(uint32_t dst, const float* src, uint32_t
       : "memory");
 }
 
+// One FP32 right-hand side of a single-structure variogram (CODE: Exp, Gau
+// or Sph; kd.single indexes it) for the tensor-core variance. A keeps 22
+// bits (two TF32 terms), so an FP32 entry (the distance from the split
+// coordinates, the model in FP32 with the hardware exp: a few 1e-7
+// relative) costs the variance little beside the split and the FP32
+// accumulation in TMEM, at under half the instructions of the double-float
+// entry. The min_vg_val cut as rhs_df_cut, with a band wide enough for
+// FP32 (1e-6 of the cut and of the total sill): entries within it take
+// rhs_f64.
+template <int CODE>
+__device__ __forceinline__ float vt_rhs_f32(const spi_domain_t& dom, const spi_vg_t* vgp,
+                                            const RhsDf& kd, double sh, float4 cp, float4 sp,
+                                            int64_t gc, const int32_t* stp) {
+  const float dx = (cp.x - sp.x) + (cp.y - sp.y);
+  const float dy = (cp.z - sp.z) + (cp.w - sp.w);
+  const float d2 = __fmaf_rn(dx, dx, dy * dy);
+  const int q = kd.single;
+  float rho;
+  if constexpr (CODE == SPI_VG_GAU) {
+    rho = __expf(d2 * kd.k2[q].h);
+  } else if constexpr (CODE == SPI_VG_EXP) {
+    rho = __expf(sqrtf(d2) * kd.k1[q].h);
+  } else {
+    const float t = sqrtf(d2) * kd.inv_r[q].h;  // h / r
+    const float u = 1.0f - t;
+    rho = t < 1.0f ? u * u * (1.0f + 0.5f * t) : 0.0f;
+  }
+  const float c = kd.sill[q].h * rho;
+  if (kd.mvv > 0.f && !kd.nug_clear) {
+    const float gap = (kd.shift.h - c) - kd.mvv;  // gamma against the cut
+    if (fabsf(gap) <= 1e-6f * (kd.mvv + kd.shift.h))
+      return (float)rhs_f64(dom, *vgp, 0, false, sh, dom.cell_x[gc], dom.cell_y[gc], *stp);
+    if (gap <= 0.f) return kd.shift.h;
+  }
+  return c;
+}
+
 // The chunk's right-hand sides of one thread: cell a_cell, stations
 // k0 + kb .. k0 + kb + 3 (coordinates from the stage), as two TF32 terms
-// into the A tiles. CODE: the single structure's model, or -1 (rhs_df).
+// into the A tiles. CODE: the single structure's model (vt_rhs_f32), or -1
+// (the general double-float rhs_df, its head).
 template <int CODE>
 __device__ __forceinline__ void vt_gen(const spi_domain_t& dom, const spi_vg_t* vgp,
                                        const RhsDf& kd, double sh, float4 cp, bool live,
@@ -153,16 +191,15 @@ __device__ __forceinline__ void vt_gen(const spi_domain_t& dom, const spi_vg_t* 
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int kk = kb + q, j = k0 + kk;
-    df c = {0.f, 0.f};
+    float c = 0.f;
     if (live && j < n) {
       if constexpr (CODE < 0)
-        c = rhs_df(dom, vgp, kd, 0, sh, cp, ssp[kk], gc, idx + j);
+        c = rhs_df(dom, vgp, kd, 0, sh, cp, ssp[kk], gc, idx + j).h;
       else
-        c = rhs_df_single<CODE>(dom, vgp, kd, 0, sh, cp, ssp[kk], gc, idx + j);
+        c = vt_rhs_f32<CODE>(dom, vgp, kd, sh, cp, ssp[kk], gc, idx + j);
     }
     float h, l;
-    tf32_split(c.h, h, l);
-    l += c.l;
+    tf32_split(c, h, l);
     const int o = tile_off(VT_M, a_cell, kk);
     *reinterpret_cast<float*>(sAh + o) = h;
     *reinterpret_cast<float*>(sAl + o) = l;
