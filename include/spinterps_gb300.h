@@ -726,6 +726,18 @@ int spi_legacy_points(int32_t kind, const double *xi, const double *yi, const do
                       double *lambdas, double *mus, double *zk, double *est, double *ik,
                       spi_stream_t stream);
 
+/* The pseudo-inverse P of a symmetric m x m matrix M (device arrays,
+ * row-major, m <= SPI_PINV_MAX_M), for the single-neighbourhood classes'
+ * numpy.linalg.pinv (cyth/interpmthds.pyx:335, 445, 559) where their
+ * Gauss-Jordan inverse may differ from it: a cyclic Jacobi
+ * eigen-decomposition of (M + M') / 2 in FP64 on one CTA (the singular
+ * values of a symmetric matrix are its |eigenvalues|), eigenvalues with
+ * |lambda| <= rtol max |lambda| dropped. scratch: 2 m^2 doubles. *status
+ * (device): the number of eigenvalues dropped, or -1 when the sweeps did
+ * not converge (P is then not to be used). */
+int spi_sym_pinv(const double *M, int32_t m, double rtol, double *P, double *scratch,
+                 int32_t *status, spi_stream_t stream);
+
 /* ---- measurement ------------------------------------------------------ */
 
 /* No counterpart in the reference: a CUDA-core FMA throughput kernel (FP64

@@ -151,6 +151,7 @@ _SIGS = {
     "spi_legacy_points": [c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_i64,
                           c_i32, ctypes.POINTER(VgT), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                           c_ptr, c_ptr],
+    "spi_sym_pinv": [c_ptr, c_i32, c_dbl, c_ptr, c_ptr, c_ptr, c_ptr],
 }
 
 # every entry point the header declares (checked by the CPU tests)

@@ -77,12 +77,111 @@ __device__ __forceinline__ void round_pair(int r, int k, int mm, int& p, int& q)
   }
 }
 
+// Shared arrays of one CTA's Jacobi sweeps.
+struct JacobiSmem {
+  double red[PT / 32];
+  double rc[SPI_PINV_MAX_M / 2], rs[SPI_PINV_MAX_M / 2];
+  int rp[SPI_PINV_MAX_M / 2], rq[SPI_PINV_MAX_M / 2];
+  double lam_inv[SPI_PINV_MAX_M];
+};
+
+// Diagonalises the symmetric W (m x m, row-major, global scratch) by
+// cyclic Jacobi rotations, accumulating them in V (V = I on entry): on
+// return W holds the eigenvalues on its diagonal, V the eigenvectors as
+// columns. fm: ||W||_F^2. Whether the sweeps converged (the off-diagonal
+// norm at its rounding floor) within kSweeps.
+__device__ bool jacobi_sweeps(double* W, double* V, int m, double fm, JacobiSmem& sm) {
+  const int tid = threadIdx.x;
+  const int mm = m + (m & 1);
+  double prev = __longlong_as_double(0x7ff0000000000000LL);
+  for (int sweep = 0; sweep < kSweeps; ++sweep) {
+    double off2 = 0.0;
+    for (int e = tid; e < m * m; e += PT) {
+      const int i = e / m, j = e - i * m;
+      if (i != j) off2 += W[e] * W[e];
+    }
+    off2 = cta_sum(off2, sm.red);
+    // converged: each off-diagonal entry at the rounding level of its
+    // rotations (~eps times its row's diagonal), or stalled there
+    if (off2 <= 8.0 * m * kEps * kEps * fm || (off2 <= 1e-24 * fm && off2 > 0.25 * prev))
+      return true;
+    prev = off2;
+    for (int r = 0; r < mm - 1; ++r) {
+      // the round's rotations
+      if (tid < mm / 2) {
+        int p, q;
+        round_pair(r, tid, mm, p, q);
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double c = 1.0, sn = 0.0;
+        if (q < m) {
+          const double apq = W[p * m + q];
+          if (apq != 0.0) {
+            const double app = W[p * m + p], aqq = W[q * m + q];
+            const double th = (aqq - app) / (2.0 * apq);
+            double t;
+            if (fabs(th) > 1e150)
+              t = 0.5 / th;
+            else
+              t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            sn = t * c;
+          }
+        }
+        sm.rp[tid] = p;
+        sm.rq[tid] = q;
+        sm.rc[tid] = c;
+        sm.rs[tid] = sn;
+      }
+      __syncthreads();
+      // rows p, q of W (W <- J' W)
+      for (int e = tid; e < (mm / 2) * m; e += PT) {
+        const int k = e / m, j = e - k * m;
+        const int p = sm.rp[k], q = sm.rq[k];
+        if (q >= m || sm.rs[k] == 0.0) continue;
+        const double c = sm.rc[k], sn = sm.rs[k];
+        const double wp = W[p * m + j], wq = W[q * m + j];
+        W[p * m + j] = c * wp - sn * wq;
+        W[q * m + j] = sn * wp + c * wq;
+      }
+      __syncthreads();
+      // columns p, q of W and V (W <- W J, V <- V J)
+      for (int e = tid; e < m * (mm / 2); e += PT) {
+        const int i = e / (mm / 2), k = e - i * (mm / 2);
+        const int p = sm.rp[k], q = sm.rq[k];
+        if (q >= m || sm.rs[k] == 0.0) continue;
+        const double c = sm.rc[k], sn = sm.rs[k];
+        const double wp = W[i * m + p], wq = W[i * m + q];
+        W[i * m + p] = c * wp - sn * wq;
+        W[i * m + q] = sn * wp + c * wq;
+        const double vp = V[i * m + p], vq = V[i * m + q];
+        V[i * m + p] = c * vp - sn * vq;
+        V[i * m + q] = sn * vp + c * vq;
+      }
+      __syncthreads();
+    }
+  }
+  return false;
+}
+
+// P = V diag(lam_inv) V' (row-major m x m).
+__device__ void pinv_assemble(const double* V, const double* lam_inv, int m, double* P) {
+  for (int e = threadIdx.x; e < m * m; e += PT) {
+    const int i = e / m, j = e - i * m;
+    const double* vi = V + i * m;
+    const double* vj = V + j * m;
+    double t = 0.0;
+    for (int k = 0; k < m; ++k) t = fma(vi[k] * lam_inv[k], vj[k], t);
+    P[e] = t;
+  }
+}
+
 __global__ __launch_bounds__(PT) void k_pinv(spi_domain_t dom, spi_systems_t sys,
                                              spi_krige_ws_t ws) {
-  __shared__ double red[PT / 32];
-  __shared__ double rc[SPI_PINV_MAX_M / 2], rs[SPI_PINV_MAX_M / 2];
-  __shared__ int rp[SPI_PINV_MAX_M / 2], rq[SPI_PINV_MAX_M / 2];
-  __shared__ double lam_inv[SPI_PINV_MAX_M];
+  __shared__ JacobiSmem sm;
   const int tid = threadIdx.x;
   double* W = ws.pinv_scratch + (size_t)blockIdx.x * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M;
   double* V = W + SPI_PINV_MAX_M * SPI_PINV_MAX_M;
@@ -105,114 +204,30 @@ __global__ __launch_bounds__(PT) void k_pinv(spi_domain_t dom, spi_systems_t sys
       V[e] = (i == j) ? 1.0 : 0.0;
       fm += x * x;
     }
-    fm = cta_sum(fm, red);
-    const int mm = m + (m & 1);
-    bool conv = false;
-    double prev = __longlong_as_double(0x7ff0000000000000LL);
-    for (int sweep = 0; sweep < kSweeps; ++sweep) {
-      double off2 = 0.0;
-      for (int e = tid; e < m * m; e += PT) {
-        const int i = e / m, j = e - i * m;
-        if (i != j) off2 += W[e] * W[e];
-      }
-      off2 = cta_sum(off2, red);
-      // converged: each off-diagonal entry at the rounding level of its
-      // rotations (~eps times its row's diagonal), or stalled there
-      if (off2 <= 8.0 * m * kEps * kEps * fm || (off2 <= 1e-24 * fm && off2 > 0.25 * prev)) {
-        conv = true;
-        break;
-      }
-      prev = off2;
-      for (int r = 0; r < mm - 1; ++r) {
-        // the round's rotations
-        if (tid < mm / 2) {
-          int p, q;
-          round_pair(r, tid, mm, p, q);
-          if (p > q) {
-            const int t = p;
-            p = q;
-            q = t;
-          }
-          double c = 1.0, sn = 0.0;
-          if (q < m) {
-            const double apq = W[p * m + q];
-            if (apq != 0.0) {
-              const double app = W[p * m + p], aqq = W[q * m + q];
-              const double th = (aqq - app) / (2.0 * apq);
-              double t;
-              if (fabs(th) > 1e150)
-                t = 0.5 / th;
-              else
-                t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-              c = 1.0 / sqrt(t * t + 1.0);
-              sn = t * c;
-            }
-          }
-          rp[tid] = p;
-          rq[tid] = q;
-          rc[tid] = c;
-          rs[tid] = sn;
-        }
-        __syncthreads();
-        // rows p, q of W (W <- J' W)
-        for (int e = tid; e < (mm / 2) * m; e += PT) {
-          const int k = e / m, j = e - k * m;
-          const int p = rp[k], q = rq[k];
-          if (q >= m || rs[k] == 0.0) continue;
-          const double c = rc[k], sn = rs[k];
-          const double wp = W[p * m + j], wq = W[q * m + j];
-          W[p * m + j] = c * wp - sn * wq;
-          W[q * m + j] = sn * wp + c * wq;
-        }
-        __syncthreads();
-        // columns p, q of W and V (W <- W J, V <- V J)
-        for (int e = tid; e < m * (mm / 2); e += PT) {
-          const int i = e / (mm / 2), k = e - i * (mm / 2);
-          const int p = rp[k], q = rq[k];
-          if (q >= m || rs[k] == 0.0) continue;
-          const double c = rc[k], sn = rs[k];
-          const double wp = W[i * m + p], wq = W[i * m + q];
-          W[i * m + p] = c * wp - sn * wq;
-          W[i * m + q] = sn * wp + c * wq;
-          const double vp = V[i * m + p], vq = V[i * m + q];
-          V[i * m + p] = c * vp - sn * vq;
-          V[i * m + q] = sn * vp + c * vq;
-        }
-        __syncthreads();
-      }
-    }
+    fm = cta_sum(fm, sm.red);
+    const bool conv = jacobi_sweeps(W, V, m, fm, sm);
     // the eigenvalues, pinv's cut-off and the band around it
     double mx = 0.0;
     for (int i = tid; i < m; i += PT) mx = fmax(mx, fabs(W[i * m + i]));
-    mx = cta_max(mx, red);
+    mx = cta_max(mx, sm.red);
     const double cut = kRcond * mx;
     double dropped = 0.0, near = 0.0, kept_min = 1e308;
     for (int i = tid; i < m; i += PT) {
       const double l = W[i * m + i], al = fabs(l);
-      lam_inv[i] = (al > cut) ? 1.0 / l : 0.0;
+      sm.lam_inv[i] = (al > cut) ? 1.0 / l : 0.0;
       dropped += (al <= cut) ? 1.0 : 0.0;
       near += (al > cut / GAP && al < cut * GAP) ? 1.0 : 0.0;
       if (al > cut) kept_min = fmin(kept_min, al);
     }
-    dropped = cta_sum(dropped, red);
-    near = cta_sum(near, red);
-    kept_min = -cta_max(-kept_min, red);
+    dropped = cta_sum(dropped, sm.red);
+    near = cta_sum(near, sm.red);
+    kept_min = -cta_max(-kept_min, sm.red);
     const bool gj_ok = rt == 3;
     const bool gapped = dropped > 0.0 && near == 0.0;
     const bool take = conv && (gapped || !gj_ok);
-    if (take) {
-      // P = V diag(lam_inv) V' into the arena (row-major m x m, as the
-      // Gauss-Jordan inverse)
-      double* P = ws.l_arena + sys.mat_off[s];
-      for (int e = tid; e < m * m; e += PT) {
-        const int i = e / m, j = e - i * m;
-        const double* vi = V + i * m;
-        const double* vj = V + j * m;
-        double t = 0.0;
-        for (int k = 0; k < m; ++k) t = fma(vi[k] * lam_inv[k], vj[k], t);
-        P[e] = t;
-      }
-    }
+    // P = V diag(lam_inv) V' into the arena (row-major m x m, as the
+    // Gauss-Jordan inverse)
+    if (take) pinv_assemble(V, sm.lam_inv, m, ws.l_arena + sys.mat_off[s]);
     __syncthreads();
     if (tid == 0) {
       ws.route[s] = (take || gj_ok) ? 1 : 2;
@@ -221,6 +236,42 @@ __global__ __launch_bounds__(PT) void k_pinv(spi_domain_t dom, spi_systems_t sys
     }
     __syncthreads();
   }
+}
+
+// The pseudo-inverse of one explicit symmetric matrix (spi_sym_pinv):
+// eigenvalues with |lambda| <= rtol max |lambda| are dropped.
+__global__ __launch_bounds__(PT) void k_sym_pinv(const double* __restrict__ M, int m,
+                                                 double rtol, double* __restrict__ P,
+                                                 double* __restrict__ scratch,
+                                                 int32_t* __restrict__ status) {
+  __shared__ JacobiSmem sm;
+  const int tid = threadIdx.x;
+  double* W = scratch;
+  double* V = scratch + (size_t)m * m;
+  double fm = 0.0;
+  for (int e = tid; e < m * m; e += PT) {
+    const int i = e / m, j = e - i * m;
+    // the symmetric part (the matrices passed are symmetric up to rounding)
+    const double x = 0.5 * (M[e] + M[(int64_t)j * m + i]);
+    W[e] = x;
+    V[e] = (i == j) ? 1.0 : 0.0;
+    fm += x * x;
+  }
+  fm = cta_sum(fm, sm.red);
+  const bool conv = jacobi_sweeps(W, V, m, fm, sm);
+  double mx = 0.0;
+  for (int i = tid; i < m; i += PT) mx = fmax(mx, fabs(W[i * m + i]));
+  mx = cta_max(mx, sm.red);
+  const double cut = rtol * mx;
+  double dropped = 0.0;
+  for (int i = tid; i < m; i += PT) {
+    const double l = W[i * m + i];
+    sm.lam_inv[i] = (fabs(l) > cut) ? 1.0 / l : 0.0;
+    dropped += (fabs(l) > cut) ? 0.0 : 1.0;
+  }
+  dropped = cta_sum(dropped, sm.red);
+  pinv_assemble(V, sm.lam_inv, m, P);
+  if (tid == 0) *status = conv ? (int32_t)dropped : -1;
 }
 
 }  // namespace
@@ -236,3 +287,15 @@ int launch_pinv(const spi_domain_t& dom, const spi_systems_t& sys, const spi_kri
 }
 
 }  // namespace spi
+
+using namespace spi;
+
+extern "C" int spi_sym_pinv(const double* M, int32_t m, double rtol, double* P, double* scratch,
+                            int32_t* status, spi_stream_t stream) {
+  if (!M || !P || !scratch || !status || m < 1) return SPI_ERR_ARG;
+  if (m > SPI_PINV_MAX_M) return SPI_ERR_TOO_LARGE;
+  if (!(rtol >= 0.0)) return SPI_ERR_ARG;
+  k_sym_pinv<<<1, PT, 0, (cudaStream_t)stream>>>(M, m, rtol, P, scratch, status);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}

@@ -28,8 +28,9 @@ Differences, by design:
   are dropped) removes nothing, which is certain while
   ||A||_F ||A^-1||_F <= 1e15.
 - Above that bound, for example with duplicated stations, the matrix takes
-  ``torch.linalg.pinv``: an SVD pseudo-inverse on the GPU with torch's
-  default cut-off, m * eps times the largest singular value. An exactly
+  a pseudo-inverse from this package's Jacobi eigen-decomposition on the
+  GPU (``spi_sym_pinv``, up to 256 rows; above that ``torch.linalg.pinv``),
+  dropping the eigenvalues up to m * eps times the largest. An exactly
   singular matrix's null singular values come out of an SVD as rounding
   noise of about eps to 16 eps times the largest, on either side of
   numpy's 1e-15 depending on the LAPACK build; the wider cut-off drops
@@ -97,6 +98,24 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _pinv(lhs, st):
+    """The pseudo-inverse of the (symmetric) kriging matrix, eigenvalues up
+    to m eps times the largest dropped: spi_sym_pinv's Jacobi
+    eigen-decomposition up to SPI_PINV_MAX_M rows, torch.linalg.pinv (an
+    SVD with the same cut-off) above that or where the sweeps do not
+    converge."""
+    m = int(lhs.shape[0])
+    if m <= nat.SPI_PINV_MAX_M:
+        out = torch.empty_like(lhs)
+        scratch = torch.empty(2 * m * m, dtype=torch.float64, device=lhs.device)
+        status = torch.zeros(1, dtype=torch.int32, device=lhs.device)
+        nat.call("spi_sym_pinv", _ptr(lhs), m, m * float(np.finfo(np.float64).eps), _ptr(out),
+                 _ptr(scratch), _ptr(status), st)
+        if int(status.item()) >= 0:
+            return out
+    return torch.linalg.pinv(lhs).contiguous()
+
+
 def krige_points(kind, xi, yi, zi, xk, yk, model, si=None, sk=None, ixi=None, want_est=True):
     """One legacy kriging run on CUDA tensors (float64, contiguous).
 
@@ -105,8 +124,8 @@ def krige_points(kind, xi, yi, zi, xk, yk, model, si=None, sk=None, ixi=None, wa
     dict of device tensors: in_dists, lhs, lhs_inv, rhss, lambdas, mus
     [m - n, n_out] (None for SK), zk, est (None when want_est is false or for
     EDK), ik (None without ixi), and ``route``: "gj" (the Gauss-Jordan
-    inverse) or "pinv" (the SVD pseudo-inverse, taken where pinv's cut-off
-    may drop a singular value). Runs on the current stream."""
+    inverse) or "pinv" (the pseudo-inverse, taken where pinv's cut-off may
+    drop a singular value). Runs on the current stream."""
     comps = parse_model(model) if not isinstance(model, list) else model
     vg = _vg_struct(comps)
     code = nat.KIND[kind]
@@ -127,7 +146,7 @@ def krige_points(kind, xi, yi, zi, xk, yk, model, si=None, sk=None, ixi=None, wa
              st)
     route = "gj"
     if int(status.item()) or not float(cond.item()) <= PINV_COND:
-        inv = torch.linalg.pinv(lhs).contiguous()
+        inv = _pinv(lhs, st)
         route = "pinv"
     rhss = torch.empty((n_out, m), **f64)
     lambdas = torch.empty((n_out, n), **f64)

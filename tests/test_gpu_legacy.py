@@ -130,3 +130,32 @@ def test_legacy_device_entry_and_errors():
     e = legacy.OrdinaryKriging(xi, yi, zi, xk[:0], yk[:0], model=model)
     e.krige()
     assert e.zk.shape == (0,) and e.lambdas.shape == (0, 30)
+
+
+@pytest.mark.parametrize("m, rank", [(40, 40), (64, 61), (201, 197), (256, 250)])
+def test_sym_pinv_matches_numpy(m, rank):
+    """spi_sym_pinv (the legacy classes' pseudo-inverse) against numpy's
+    pinv with the same cut-off (m eps of the largest singular value) on
+    symmetric indefinite matrices of the given rank, saddle-like scales."""
+    import ctypes
+    import torch
+    from spinterps_gb300 import _native as nat
+    rng = np.random.default_rng(m + rank)
+    q, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    lam = rng.uniform(0.1, 10.0, m) * rng.choice([-1.0, 1.0], m)
+    lam[rank:] = 0.0
+    a = (q * lam) @ q.T
+    a = 0.5 * (a + a.T)
+    ref = np.linalg.pinv(a, rcond=m * np.finfo(np.float64).eps)
+    dev = torch.device("cuda")
+    t = torch.as_tensor(a, device=dev)
+    out = torch.empty_like(t)
+    scratch = torch.empty(2 * m * m, dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    ptr = lambda x: ctypes.c_void_p(x.data_ptr())
+    nat.call("spi_sym_pinv", ptr(t), m, m * float(np.finfo(np.float64).eps), ptr(out),
+             ptr(scratch), ptr(status), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert int(status.item()) == m - rank
+    err = np.abs(out.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err <= 1e-10, err
