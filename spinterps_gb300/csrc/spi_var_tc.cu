@@ -144,8 +144,8 @@ __device__ __forceinline__ void vt_load(uint32_t dst, const float* src, uint32_t
 // One FP32 right-hand side of a single-structure variogram (CODE: Exp, Gau
 // or Sph; kd.single indexes it) for the tensor-core variance. A keeps 22
 // bits (two TF32 terms), so an FP32 entry (the distance from the split
-// coordinates, the model in FP32 with the hardware exp: a few 1e-7
-// relative) costs the variance little beside the split and the FP32
+// coordinates, the model in FP32 with CUDA's expf: a few 1e-7 relative)
+// costs the variance little beside the split and the FP32
 // accumulation in TMEM, at under half the instructions of the double-float
 // entry. The min_vg_val cut as rhs_df_cut, with a band wide enough for
 // FP32 (1e-6 of the cut and of the total sill): entries within it take
@@ -160,9 +160,9 @@ __device__ __forceinline__ float vt_rhs_f32(const spi_domain_t& dom, const spi_v
   const int q = kd.single;
   float rho;
   if constexpr (CODE == SPI_VG_GAU) {
-    rho = __expf(d2 * kd.k2[q].h);
+    rho = expf(d2 * kd.k2[q].h);
   } else if constexpr (CODE == SPI_VG_EXP) {
-    rho = __expf(sqrtf(d2) * kd.k1[q].h);
+    rho = expf(sqrtf(d2) * kd.k1[q].h);
   } else {
     const float t = sqrtf(d2) * kd.inv_r[q].h;  // h / r
     const float u = 1.0f - t;
