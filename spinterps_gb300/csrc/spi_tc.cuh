@@ -1,0 +1,107 @@
+// tcgen05 / TMA building blocks shared by the tensor-core kernels
+// (spi_var_tc.cu, spi_idw_tc.cu): shared-memory matrix descriptors and the
+// no-swizzle K-major tile layout, the TF32 split, the kind::tf32 MMA, and
+// bounded mbarrier waits with bulk copies counted on them.
+#pragma once
+#include <cstdint>
+
+namespace spi {
+
+constexpr long TC_SPIN = 1L << 26;   // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major; lbo = byte stride
+// between core matrices along K, sbo = between 8-row groups.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of sm_100-class tensor cores
+  return d;
+}
+
+// Byte offset of (row, k) in an R x 8 TF32 tile (K-major, no swizzle):
+// core matrix (row / 8, k / 4) at (k / 4) * R * 16 + (row / 8) * 128.
+__device__ __forceinline__ int tile_off(int R, int row, int k) {
+  return (k >> 2) * (R * 16) + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+// TF32 keeps the top 19 bits of an FP32 value: x rounded to those bits
+// (half away from zero on the magnitude); the remainder x - tf32_rn(x) is
+// exact in FP32 and at most 2^-11 |x|.
+__device__ __forceinline__ float tf32_rn(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// x = hi + lo with hi = tf32_rn(x) and lo the exact remainder, itself
+// truncated by the tensor core. Rounding the head rather than truncating
+// it halves lo and the split's error.
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = tf32_rn(x);
+  lo = x - hi;
+}
+
+// D (TMEM) = A B (+ D when acc), A and B from shared-memory descriptors.
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// Instruction descriptor of kind::tf32 with FP32 D, K-major A and B.
+__device__ __forceinline__ uint32_t tf32_idesc(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+// polls the mbarrier until the phase of the given parity has completed, at
+// most TC_SPIN times; false if it never did
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+  uint32_t done = 0;
+  for (long it = 0; it < TC_SPIN && !done; ++it)
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity));
+  return done != 0;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
+}
+
+// One thread: bytes (a multiple of 16, both addresses 16-byte aligned) from
+// global memory into shared memory by one bulk copy, counted on the
+// mbarrier (its expected transaction bytes raised by the same amount).
+__device__ __forceinline__ void tc_bulk_load(uint32_t dst, const float* src, uint32_t bytes,
+                                             uint32_t mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
+               "r"(bytes));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
+// The TMEM load of 32 lanes x 32 columns (one per register) at addr.
+__device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+      "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+}
+
+}  // namespace spi

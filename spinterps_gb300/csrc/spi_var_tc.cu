@@ -40,6 +40,7 @@
 // kernel.
 #include "spi_cells.cuh"
 #include "spi_rhs.cuh"
+#include "spi_tc.cuh"
 
 namespace spi {
 
@@ -48,7 +49,6 @@ constexpr int VT_N = 256;   // Linv rows per block (MMA N, TMEM columns)
 constexpr int VT_KC = SPI_VAR_TC_KC;  // stations per chunk (one MMA K-step)
 constexpr int VT_T = 256;   // threads
 constexpr int VT_NST = 3;   // ring stages
-constexpr long VT_SPIN = 1L << 26;   // mbarrier polls before giving up
 
 constexpr size_t VT_A_BYTES = (size_t)VT_M * VT_KC * 4;       // one TF32 term of A
 constexpr size_t VT_B_BYTES = (size_t)VT_N * VT_KC * 4;       // one TF32 term of B
@@ -69,76 +69,13 @@ struct VarTcArgs {
   int32_t* err;
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// Shared-memory matrix descriptor: no swizzle, K-major; lbo = byte stride
-// between core matrices along K, sbo = between 8-row groups.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version of sm_100-class tensor cores
-  return d;
-}
-
-// Byte offset of (row, k) in an R x KC TF32 tile (K-major, no swizzle):
-// core matrix (row / 8, k / 4) at (k / 4) * R * 16 + (row / 8) * 128.
-__device__ __forceinline__ int tile_off(int R, int row, int k) {
-  return (k >> 2) * (R * 16) + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4;
-}
-
-__device__ __forceinline__ float tf32_rn(float x) {
-  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
-
-// TF32 keeps the top 19 bits of an FP32 value: hi = x rounded to those
-// bits (half away from zero on the magnitude), lo = the exact remainder
-// (|lo| <= 2^-11 |x|), itself truncated by the tensor core. Rounding the
-// head rather than truncating it halves lo and the split's error.
-__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
-  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-  lo = x - hi;
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-
-// polls the mbarrier until the phase of the given parity has completed, at
-// most VT_SPIN times; false if it never did
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
-  uint32_t done = 0;
-  for (long it = 0; it < VT_SPIN && !done; ++it)
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        "selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(parity));
-  return done != 0;
-}
-
-// Chunks of 16 columns of B in the 256-row block starting at row rb.
+// Chunks of VT_KC columns of B in the 256-row block starting at row rb.
 __device__ __forceinline__ int vt_chunks(int n, int rb) { return (min(n, rb + VT_N) + VT_KC - 1) / VT_KC; }
 
-__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
-}
-
 // One thread: packed chunk (B and its stations) by one bulk copy into the
-// stage, counted on the stage's mbarrier (expect_tx of the copy's bytes).
+// stage, counted on the stage's mbarrier.
 __device__ __forceinline__ void vt_load(uint32_t dst, const float* src, uint32_t mbar) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
-               "r"((uint32_t)VT_CHUNK_BYTES));
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"((uint32_t)VT_CHUNK_BYTES), "r"(mbar)
-      : "memory");
+  tc_bulk_load(dst, src, (uint32_t)VT_CHUNK_BYTES, mbar);
 }
 
 // One FP32 right-hand side of a single-structure variogram (CODE: Exp, Gau
@@ -250,8 +187,7 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tbase;
   // kind::tf32, D FP32, A/B TF32 K-major, N = 256, M = 128
-  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(VT_N >> 3) << 17) |
-                         ((uint32_t)(VT_M >> 4) << 24);
+  const uint32_t idesc = tf32_idesc(VT_M, VT_N);
   // the single structure's model, uniform over the CTA (-1: general form)
   const int scode = (kd.exact && kd.single >= 0) ? kd.code[kd.single] : -1;
 
@@ -355,17 +291,7 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
       uint32_t r[32];
       const uint32_t addr =
           tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(e_half * 128 + cc * 32);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-          "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-            "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-            "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-            "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-            "=r"(r[31])
-          : "r"(addr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      tmem_ld32(addr, r);
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
         const float y = __uint_as_float(r[i]);

@@ -641,10 +641,18 @@ class InterpPlan:
                 a = 1 + self.dom.st.n_drift if kind == "EDK" else 1
                 self.krig.append((kind, out, var is not None, batches, fills, a))
         self.idw = []
+        self.idw_pack = self.idw_err = None
         if any(t in ("IDW", "NNB") for t in types):
             self.data_d = torch.as_tensor(data, device=dev)
             self.data_hi = self.data_lo = None
-            if prec == 1:
+            if prec == 1 and tensor_cores and "IDW" in types:
+                # IDW as the masked GEMM pair on the tensor cores
+                # (spi_idw_cells_tc): its packed B per 64 steps
+                self.idw_pack_floats = nat.idw_tc_pack_floats(self.dom.N, len(multi))
+                self.idw_pack = torch.empty(max(self.idw_pack_floats, 4), dtype=torch.float32,
+                                            device=dev)
+                self.idw_err = torch.zeros(1, dtype=torch.int32, device=dev)
+            elif prec == 1:
                 self.data_hi = torch.empty(data.size, dtype=torch.float32, device=dev)
                 self.data_lo = torch.empty(data.size, dtype=torch.float32, device=dev)
             self.steps_t = torch.as_tensor(multi.astype(np.int32), device=dev)
@@ -689,7 +697,12 @@ class InterpPlan:
             if timing:
                 ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                 ev[0].record()
-            if t == "IDW":
+            if t == "IDW" and self.idw_pack is not None:
+                nat.call("spi_idw_cells_tc", ctypes.byref(self.dom.st), len(self.multi),
+                         _ptr(self.steps_t), _ptr(self.steps_t), _ptr(self.data_d),
+                         _ptr(self.flag_t), _ptr(self.mean_t), p, _ptr(self.idw_pack),
+                         self.idw_pack_floats, ctypes.byref(out), _ptr(self.idw_err), s)
+            elif t == "IDW":
                 if self.data_hi is not None:
                     nat.call("spi_split_f64", _ptr(self.data_d), _ptr(self.data_hi),
                              _ptr(self.data_lo), self.data_d.numel(), s)
@@ -775,11 +788,14 @@ class InterpPlan:
         self._graph.replay()
 
     def collect_info(self):
+        if self.idw_err is not None and int(self.idw_err.item()):
+            raise RuntimeError("spi_idw_cells_tc: a tensor-core wait timed out (its cells hold "
+                               "NaN)")
         for kind, out, want_var, batches, fills, a in self.krig:
             failed, routed, cond, pinv = [], [], {}, []
             for b in batches:
                 if b.tc_err is not None and int(b.tc_err.item()):
-                    raise nat.SpiError("spi_krige_var_tc: a tensor-core wait timed out")
+                    raise RuntimeError("spi_krige_var_tc: a tensor-core wait timed out")
                 rt = b.route.cpu().numpy()
                 cn = b.cond.cpu().numpy()
                 pu = b.pinv_used.cpu().numpy()
@@ -869,7 +885,7 @@ class InterpPlan:
                 n += 2 if b.precision == 1 else 1
         for t, out, fill, p in self.idw:
             n += (fill is not None) + (len(self.multi) > 0) * (
-                1 + (t == "IDW" and self.data_hi is not None))
+                1 + (t == "IDW" and (self.data_hi is not None or self.idw_pack is not None)))
         return int(n)
 
     def kernel_times(self, evs):

@@ -415,3 +415,31 @@ def test_fp32_factor_with_fp64_refinement():
     for lab in ref64:
         assert _err(got[lab], ref64[lab]) <= FP64_TOL, lab
         assert _err(got[lab], ora[lab]) <= MIXED_TOL, lab
+
+
+@pytest.mark.parametrize("p", [1.0, 2.0, 3.5])
+def test_idw_on_tensor_cores(p):
+    """IDW as the masked GEMM pair on the tensor cores (spi_idw_cells_tc,
+    the mixed path) against the FP64 path: 150 steps (three groups of 64),
+    missing stations, steps under min_var_thr (the step mean), a cell on a
+    station (NaN where that station is present), float64 fields, within
+    the mixed bar of the field's largest magnitude."""
+    spi = _spi()
+    rng = np.random.default_rng(int(p * 10))
+    N, T, C = 500, 150, 6000
+    sx, sy = rng.uniform(0, 2e5, N), rng.uniform(0, 2e5, N)
+    z = rng.gamma(0.6, 4.0, (T, N))
+    z[rng.uniform(size=(T, N)) < 0.3] = np.nan
+    z[5] = np.where(np.isnan(z[5]), np.nan, 0.01)        # under the threshold
+    cx, cy = rng.uniform(0, 2e5, C), rng.uniform(0, 2e5, C)
+    cx[17], cy[17] = sx[3], sy[3]                         # a cell on station 3
+    z[7, 3] = np.nan                                      # missing at step 7
+    z[8, 3] = 2.5                                         # present at step 8
+    args = port.interp_args_for([("IDW", p)], est_vars=False)
+    kw = dict(min_var_thr=0.1, intrp_dtype=np.float64)
+    f64, _ = spi.interp_steps(sx, sy, z, cx, cy, [None] * T, args, **kw)
+    mixed, _ = spi.interp_steps(sx, sy, z, cx, cy, [None] * T, args, precision="mixed", **kw)
+    lab = "IDW_000"
+    assert np.isnan(mixed[lab][8, 17]) and np.isfinite(mixed[lab][7, 17])
+    assert np.all(mixed[lab][5] == f64[lab][5])
+    assert _err(mixed[lab], f64[lab]) <= MIXED_TOL

@@ -153,6 +153,8 @@ def test_plan_dry_run(monkeypatch, precision):
         if name == "spi_krige_duals":
             ws = a[3]._obj
             return 1 if ws.linv_arena else (3 + (5 if ws.l32 else 0))
+        if name == "spi_idw_cells_tc":
+            return 2  # the pack of B, the contraction
         return 1
 
     for timing in (False, True):
@@ -160,10 +162,14 @@ def test_plan_dry_run(monkeypatch, precision):
         evs = plan.execute(timing=timing)
         assert plan.launches_per_execute() == sum(kernels(n, a) for n, a in calls)
     names = {n for n, _ in calls}
-    assert {"spi_krige_factor", "spi_krige_duals", "spi_krige_cells_tiled", "spi_idw_cells",
+    assert {"spi_krige_factor", "spi_krige_duals", "spi_krige_cells_tiled",
             "spi_nnb_cells", "spi_fill_rows"} <= names
     if precision == "mixed":
-        assert {"spi_krige_tier", "spi_krige_var_tc", "spi_krige_var_df"} <= names
+        assert {"spi_krige_tier", "spi_krige_var_tc", "spi_krige_var_df",
+                "spi_idw_cells_tc"} <= names
+        assert "spi_idw_cells" not in names
+    else:
+        assert "spi_idw_cells" in names
     times = plan.kernel_times(evs)
     assert {"idw", "nnb"} <= set(times)
     assert times["nnb"][2] == 0.0 and times["idw"][2] > 0.0
