@@ -354,7 +354,8 @@ KERNEL_BOUND = {
     "cells_fp32": ("fp32", "spi::k_krige_cells<float> (FP32 tier: estimates, sum check)"),
     "cells_fp64": ("fp64", "spi::k_krige_cells<double> (FP64 tier: ill-conditioned and "
                            "routed systems, the plain path's kernel)"),
-    "idw": ("fp32", "spi::k_idw"),
+    "idw": ("fp32", "spi::k_idw (FP64 path) / spi::k_idw_tc (mixed path: tcgen05 masked GEMM "
+                    "pair)"),
 }
 
 
