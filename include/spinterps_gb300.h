@@ -187,12 +187,12 @@ typedef struct {
  * coordinates (float4 each) */
 #define SPI_VAR_TC_KC 8
 #define SPI_VAR_TC_CHUNK_FLOATS (3 * 256 * SPI_VAR_TC_KC + 4 * SPI_VAR_TC_KC)
-/* spi_idw_cells_tc's packed chunks: 8 stations of 128 columns (64 steps x
+/* spi_idw_cells_tc's packed chunks: 8 stations of 64 columns (32 steps x
  * value, mask) as 3 TF32 tiles, then the stations' split coordinates; one
- * chunk per 8 stations and group of 64 steps */
-#define SPI_IDW_TC_CHUNK_FLOATS (3 * 128 * 8 + 4 * 8)
+ * chunk per 8 stations and group of 32 steps */
+#define SPI_IDW_TC_CHUNK_FLOATS (3 * 64 * 8 + 4 * 8)
 #define SPI_IDW_TC_PACK_FLOATS(n_stns, n_steps) \
-    ((((int64_t)(n_steps) + 63) / 64) * (((int64_t)(n_stns) + 7) / 8) * SPI_IDW_TC_CHUNK_FLOATS)
+    ((((int64_t)(n_steps) + 31) / 32) * (((int64_t)(n_stns) + 7) / 8) * SPI_IDW_TC_CHUNK_FLOATS)
 #define SPI_PINV_SLOTS 16
 #define SPI_PINV_SCRATCH_DOUBLES (SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M)
 
@@ -462,12 +462,13 @@ int spi_idw_cells(const spi_domain_t *dom, int32_t n_steps, const int32_t *steps
                   spi_stream_t stream);
 
 /* The same IDW on the tensor cores (tcgen05), for the mixed path: per group
- * of 64 listed steps one GEMM D [cells x 128] = W [cells x n_stns] B
- * [n_stns x 128], B's columns (2t, 2t + 1) = (the step's values with 0
+ * of 32 listed steps one GEMM D [cells x 64] = W [cells x n_stns] B
+ * [n_stns x 64], B's columns (2t, 2t + 1) = (the step's values with 0
  * where missing, its mask), the weights as in precision 1 (FP32 distances
  * from dom->stn_split / cell_split) split into two TF32 terms, B into
- * three; FP32 accumulation in tensor memory (the large products and the
- * corrections in separate accumulators). pack: a 16-byte aligned device
+ * three; FP32 accumulation in tensor memory (the large products in three
+ * accumulators taking every third 8-station chunk, the corrections in a
+ * fourth, added in FP64). pack: a 16-byte aligned device
  * buffer of at least SPI_IDW_TC_PACK_FLOATS(n_stns, n_steps) floats that the
  * call fills with B (two launches: the pack, the contraction). A timed-out
  * wait sets *err_flag (device) and leaves NaN in the CTA's fields. Other

@@ -21,12 +21,12 @@ SPI_MAX_DRIFT = 7
 SPI_PINV_MAX_M = 256
 SPI_VAR_TC_KC = 8
 SPI_VAR_TC_CHUNK_FLOATS = 3 * 256 * SPI_VAR_TC_KC + 4 * SPI_VAR_TC_KC
-SPI_IDW_TC_CHUNK_FLOATS = 3 * 128 * 8 + 4 * 8
+SPI_IDW_TC_CHUNK_FLOATS = 3 * 64 * 8 + 4 * 8
 
 
 def idw_tc_pack_floats(n_stns, n_steps):
     """SPI_IDW_TC_PACK_FLOATS of the header."""
-    return ((n_steps + 63) // 64) * ((n_stns + 7) // 8) * SPI_IDW_TC_CHUNK_FLOATS
+    return ((n_steps + 31) // 32) * ((n_stns + 7) // 8) * SPI_IDW_TC_CHUNK_FLOATS
 SPI_IR_MAX_ITERS = 12
 SPI_PINV_SLOTS = 16
 SPI_PINV_SCRATCH_DOUBLES = SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M

@@ -8,19 +8,22 @@
 // masked contraction pair over all stations:
 //   num_t = sum_i W[i] m_ti z_ti,  den_t = sum_i W[i] m_ti,  est = num/den,
 // m_ti = 1 where station i has a value at step t. Here both are one GEMM
-// per group of 64 steps: D [128 cells x 128 columns] = W [128 x N] B [N x 128]
+// per group of 32 steps: D [128 cells x 64 columns] = W [128 x N] B [N x 64]
 // with B's columns (2t, 2t + 1) = (m_t z_t, m_t) for the group's steps t.
 //
 // One CTA = 128 cells x 256 threads, two CTAs per SM. Stations go in chunks
 // of 8 (one MMA K-step) through a three-stage ring: B's three TF32 terms
 // (values to ~33 bits; the masks are exact) and the chunk's stations'
 // split coordinates, packed once per launch (k_idw_tc_pack), arrive by one
-// 12 KB bulk copy per chunk issued one chunk ahead; all threads compute the
+// 6 KB bulk copy per chunk issued one chunk ahead; all threads compute the
 // chunk's weights in FP32 and store them as two TF32 terms (w = a0 + a1).
-// One thread issues per chunk a0 b0 into the accumulator D0 (TMEM columns
-// 0..127) and a0 b1 + a1 b0 + a0 b2 + a1 b1 into D1 (columns 128..255):
-// the large products keep one FP32 accumulation per chunk, the corrections
-// accumulate at their own scale. Every wait is bounded: on expiry the
+// One thread issues per chunk g the large products a0 b0 into one of three
+// accumulators D0[g % 3] (TMEM columns 0..191) and the corrections a0 b1 +
+// a1 b0 + a0 b2 + a1 b1 into D1 (columns 192..255): each large-product
+// accumulator takes every third chunk, so the FP32 roundings of these
+// positive sums are a third of one running sum's, the corrections
+// accumulate at their own scale, and the four are added in FP64 at the
+// end. Every wait is bounded: on expiry the
 // kernel raises err_flag, writes NaN over its cells, drains on a
 // best-effort basis, frees its TMEM and returns.
 #include "spi_common.cuh"
@@ -29,7 +32,8 @@
 namespace spi {
 
 constexpr int IT_M = 128;   // cells per CTA (MMA M)
-constexpr int IT_N = 128;   // B columns: 64 steps x (value, mask)
+constexpr int IT_N = 64;    // B columns: 32 steps x (value, mask)
+constexpr int IT_SEG = 3;   // large-product accumulators
 constexpr int IT_G = IT_N / 2;   // steps per group
 constexpr int IT_KC = 8;    // stations per chunk
 constexpr int IT_T = 256;
@@ -92,7 +96,7 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tbase)),
-                 "r"(2 * IT_N));
+                 "r"((IT_SEG + 1) * IT_N));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
@@ -189,12 +193,12 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
         const uint64_t b0 = umma_desc(b, IT_N * 16, 128);
         const uint64_t b1 = umma_desc(b + (uint32_t)IT_B_BYTES, IT_N * 16, 128);
         const uint64_t b2 = umma_desc(b + 2 * (uint32_t)IT_B_BYTES, IT_N * 16, 128);
-        const uint32_t acc = g > 0 ? 1u : 0u;
-        mma_tf32(tmem, ah, b0, idesc, acc);
-        mma_tf32(tmem + IT_N, ah, b1, idesc, acc);
-        mma_tf32(tmem + IT_N, al, b0, idesc, 1u);
-        mma_tf32(tmem + IT_N, ah, b2, idesc, 1u);
-        mma_tf32(tmem + IT_N, al, b1, idesc, 1u);
+        const uint32_t d1 = tmem + IT_SEG * IT_N;
+        mma_tf32(tmem + (uint32_t)((g % IT_SEG) * IT_N), ah, b0, idesc, g >= IT_SEG ? 1u : 0u);
+        mma_tf32(d1, ah, b1, idesc, g > 0 ? 1u : 0u);
+        mma_tf32(d1, al, b0, idesc, 1u);
+        mma_tf32(d1, ah, b2, idesc, 1u);
+        mma_tf32(d1, al, b1, idesc, 1u);
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -217,25 +221,40 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
     __syncthreads();
   }
 
-  // ---- 3. per cell and step: num / den, the mean for unflagged steps, NaN
-  // on a present co-located station; TMEM lanes of warp % 4, steps of the
-  // column half warp / 4 (32 steps, 64 columns) ----
+  // ---- 3. per cell and step: num / den (the four accumulators added in
+  // FP64), the mean for unflagged steps, NaN on a present co-located
+  // station; TMEM lanes of warp % 4, steps of the column half warp / 4 (16
+  // steps, 32 columns of each accumulator) ----
   const int e_cell = (warp & 3) * 32 + lane, e_half = warp >> 2;
   const int64_t ge = c0 + e_cell;
   const int on = min(s_on[0][e_cell], s_on[1][e_cell]);
   float* est_f = reinterpret_cast<float*>(A.out.est);
   double* est_d = reinterpret_cast<double*>(A.out.est);
   const int64_t N64 = N;
-#pragma unroll
+  const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+  // accumulators a chunk never reached (fewer than IT_SEG chunks) hold
+  // whatever TMEM held: only the ones written count
+  const int used = total < IT_SEG ? total : IT_SEG;
+#pragma unroll 1
   for (int cc = 0; cc < 2; ++cc) {
-    uint32_t r0[32], r1[32];
-    const uint32_t col = (uint32_t)(e_half * 64 + cc * 32);
-    const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
-    tmem_ld32(tmem + lanes + col, r0);
-    tmem_ld32(tmem + lanes + IT_N + col, r1);
+    const uint32_t col = (uint32_t)(e_half * 32 + cc * 16);
+    double num[8], den[8];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int k = grp * IT_G + e_half * 32 + cc * 16 + i;
+    for (int i = 0; i < 8; ++i) num[i] = den[i] = 0.0;
+#pragma unroll 1
+    for (int a = 0; a <= IT_SEG; ++a) {
+      uint32_t r[16];
+      tmem_ld16(tmem + lanes + (uint32_t)(a * IT_N) + col, r);
+      if (a < IT_SEG && a >= used) continue;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        num[i] += (double)__uint_as_float(r[2 * i]);
+        den[i] += (double)__uint_as_float(r[2 * i + 1]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int k = grp * IT_G + e_half * 16 + cc * 8 + i;
       if (k >= A.n_steps || ge >= C) continue;
       const int j = A.steps[k];
       double e;
@@ -246,9 +265,7 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
       } else if (on != 0x7fffffff && !isnan(A.data[(int64_t)j * N64 + on])) {
         e = __longlong_as_double(0x7ff8000000000000LL);
       } else {
-        const float num = __uint_as_float(r0[2 * i]) + __uint_as_float(r1[2 * i]);
-        const float den = __uint_as_float(r0[2 * i + 1]) + __uint_as_float(r1[2 * i + 1]);
-        e = (double)num / (double)den;
+        e = num[i] / den[i];
       }
       e = clip_est(e, A.out);
       const int64_t o = (int64_t)A.out_row[k] * C + ge;
@@ -260,7 +277,7 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(2 * IT_N));
+                 "r"((IT_SEG + 1) * IT_N));
 }
 
 // B of chunk blockIdx.x (stations 8 chunk .. + 7) of step group blockIdx.y:

@@ -647,7 +647,7 @@ class InterpPlan:
             self.data_hi = self.data_lo = None
             if prec == 1 and tensor_cores and "IDW" in types:
                 # IDW as the masked GEMM pair on the tensor cores
-                # (spi_idw_cells_tc): its packed B per 64 steps
+                # (spi_idw_cells_tc): its packed B per 32 steps
                 self.idw_pack_floats = nat.idw_tc_pack_floats(self.dom.N, len(multi))
                 self.idw_pack = torch.empty(max(self.idw_pack_floats, 4), dtype=torch.float32,
                                             device=dev)

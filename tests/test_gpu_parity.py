@@ -420,7 +420,7 @@ def test_fp32_factor_with_fp64_refinement():
 @pytest.mark.parametrize("p", [1.0, 2.0, 3.5])
 def test_idw_on_tensor_cores(p):
     """IDW as the masked GEMM pair on the tensor cores (spi_idw_cells_tc,
-    the mixed path) against the FP64 path: 150 steps (three groups of 64),
+    the mixed path) against the FP64 path: 150 steps (five groups of 32),
     missing stations, steps under min_var_thr (the step mean), a cell on a
     station (NaN where that station is present), float64 fields, within
     the mixed bar of the field's largest magnitude."""
