@@ -32,6 +32,8 @@ SPI_PINV_SLOTS = 16
 SPI_PINV_SCRATCH_DOUBLES = SPI_PINV_SLOTS * 2 * SPI_PINV_MAX_M * SPI_PINV_MAX_M
 GA = SPI_MAX_DRIFT + 1
 KIND = {"OK": 0, "SK": 1, "EDK": 2}
+# spi_vg_t codes (SPI_VG_*)
+VG_CODE = {"Rng": 0, "Nug": 1, "Sph": 2, "Exp": 3, "Lin": 4, "Gau": 5, "Pow": 6, "Hol": 7}
 SPI_NOALLOC_MAX_STNS = 512
 SPI_NOALLOC_MAX_STEPS = 64
 

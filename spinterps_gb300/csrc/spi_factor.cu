@@ -64,6 +64,24 @@ __device__ double block_sum(double t, double* red) {
 // station matrix from dists[lo, hi] and mirrors it (cyth/interpmthds.pyx:
 // 196-226); with ascending station lists the entry (i, j), i > j, is the
 // mirror of (j, i), whose distance is dist(stn[j], stn[i]).
+// A variogram of nuggets alone. The reference's semivariogram is then the
+// total sill at every distance, h = 0 included (cyth/interpmthds.pyx:38-84),
+// so its saddle matrix [[c J, F], [F', 0]] has rank 2 a and numpy's pinv
+// gives its minimum-norm solution: lambda = F (F'F)^-1 f with zero
+// multipliers (OK: the mean of the values; EDK: the drifts' least-squares
+// fit), and for SK (a zero covariance matrix) lambda = 0.
+__device__ __forceinline__ bool nug_only(const spi_vg_t& vg) {
+  for (int c = 0; c < vg.n_comp; ++c)
+    if (vg.code[c] != SPI_VG_NUG) return false;
+  return vg.n_comp > 0;
+}
+
+// The system matrix of the Cholesky path: the covariance form sh - Gamma
+// (SK: the covariances). For a nugget-only variogram the covariance form
+// is the zero matrix; the identity takes its place: the dual form then
+// gives lambda = c - F nu with F'lambda = f, and with the covariances c = 0
+// that is the minimum-norm solution above (SK: lambda = c = 0), whatever
+// the matrix's size.
 __global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restrict__ l_arena,
                             double* __restrict__ shift_out, int full) {
   const int s = blockIdx.y;
@@ -71,6 +89,7 @@ __global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restr
   const spi_vg_t vg = sys.vg[s];
   const int sk = sys.kind == SPI_KIND_SK;
   const double sh = sk ? 0.0 : total_sill(vg);
+  const bool nug = nug_only(vg);
   if (blockIdx.x == 0 && threadIdx.x == 0) shift_out[s] = sh;
   double* A = l_arena + v.moff;
   const int64_t nn = (int64_t)v.n * v.n;
@@ -79,6 +98,10 @@ __global__ void k_build_sys(spi_domain_t dom, spi_systems_t sys, double* __restr
     int i = (int)(e / v.n), j = (int)(e - (int64_t)i * v.n);
     if (j > i && !full) {
       A[e] = 0.0;
+      continue;
+    }
+    if (nug) {
+      A[e] = (i == j) ? 1.0 : 0.0;
       continue;
     }
     // (i, j) and its mirror from the same distance: dists[lo, hi]

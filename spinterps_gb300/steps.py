@@ -606,6 +606,9 @@ class InterpPlan:
         # scratch of the pinv check of exact-inverse systems (spi_krige_factor)
         self.pinv = (torch.empty(nat.SPI_PINV_SCRATCH_DOUBLES, dtype=torch.float64, device=dev)
                      if krig else None)
+        # rows written after the kriging kernels: the OK variance of
+        # nugget-only variograms (below)
+        self.post_fills = []
         if krig:
             vgs = np.asarray(vgs, dtype=object)
             assert np.all(vgs != "nan"), "NaN VGs not allowed!"
@@ -627,6 +630,21 @@ class InterpPlan:
                         systems[key] = (np.where(avail[j])[0], vgs[j], [])
                     systems[key][2].append(int(j))
                 systems = list(systems.values())
+                if var is not None:
+                    # nugget-only variograms (the cell kernels take the
+                    # minimum-norm weights there, spi_krige_factor): the
+                    # reference's variance lambda'gamma + mu is the total
+                    # sill on every cell (lambda sums to 1, gamma is the
+                    # sill everywhere, mu = 0)
+                    rows, vv = [], []
+                    for _, v, sl in systems:
+                        pv = parse_vg(v)
+                        if all(pv.code[c] == nat.VG_CODE["Nug"] for c in range(pv.n_comp)):
+                            rows.extend(sl)
+                            vv.extend([float(sum(pv.sill[c] for c in range(pv.n_comp)))] * len(sl))
+                    if rows:
+                        self.post_fills.append((_out_struct(var, None, None, None),
+                                                _fill_args(dev, rows, vv, None)))
                 val_off = np.zeros(T, dtype=np.int64)
                 beta = torch.zeros((T, nat.GA), dtype=torch.float64, device=dev)
                 batches = [_KrigeBatch(dev, self.dom, kind, systems, ch, data, T, val_off, beta,
@@ -689,6 +707,8 @@ class InterpPlan:
                       self.probe_args if self.pdom is not None else None, self.cond_df)
                 if timing:
                     evs["krige"].append((b, want_var, a, ev))
+        for out, fill in self.post_fills:
+            _fill_run(fill, C, out, s)
         for t, out, fill, p in self.idw:
             _fill_run(fill, C, out, s)
             if not len(self.multi):
@@ -883,6 +903,7 @@ class InterpPlan:
                 n += 1 if (b.yy is not None and want_var) else 0
                 n += 1 if (b.yy is not None and want_var and b.tier is not None) else 0
                 n += 2 if b.precision == 1 else 1
+        n += len(self.post_fills)
         for t, out, fill, p in self.idw:
             n += (fill is not None) + (len(self.multi) > 0) * (
                 1 + (t == "IDW" and (self.data_hi is not None or self.idw_pack is not None)))

@@ -39,7 +39,9 @@ def test_reference_arm_line():
     # the CPU model and the seed; the step's system solves are spread over
     # the workload's cells (a fixed cost per step and a cost per cell)
     assert cb["cpu_model"] and cb["seed"] == bench.SEED
-    assert cb["fixed_s_per_step"] > 0 and cb["ms_per_cell"] > 0
+    # (the fixed cost is fitted from two timings and clipped at 0: on a
+    # loaded host it can come out as 0)
+    assert cb["fixed_s_per_step"] >= 0 and cb["ms_per_cell"] > 0
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
 

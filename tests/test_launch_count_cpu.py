@@ -77,7 +77,7 @@ def test_launch_count_follows_run(monkeypatch, kind, prec, want_var, n_probe, tc
     b.run(dom, out, want_var, 1e13, 1e10, None, probe)
     launched = sum(entry_kernels(c, b) for c in calls)
     plan = types.SimpleNamespace(krig=[(kind, out, want_var, [b], [None], 1)], idw=[],
-                                 multi=[], pdom=pdom, data_hi=None)
+                                 multi=[], pdom=pdom, data_hi=None, post_fills=[])
     assert steps.InterpPlan.launches_per_execute(plan) == launched, calls
 
 
