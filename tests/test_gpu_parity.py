@@ -443,3 +443,41 @@ def test_idw_on_tensor_cores(p):
     assert np.isnan(mixed[lab][8, 17]) and np.isfinite(mixed[lab][7, 17])
     assert np.all(mixed[lab][5] == f64[lab][5])
     assert _err(mixed[lab], f64[lab]) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nugget_only_variogram_any_size(precision):
+    """A nugget-only variogram with a range (as fits can return): the
+    reference's saddle matrix is then rank 2a and its pinv gives the
+    minimum-norm weights: OK the mean of the values (variance: the sill),
+    EDK the drifts' least-squares fit, SK zero weights (every cell falls
+    back to its nearest station). 300 stations, above the pinv check's 256
+    rows; no problem steps."""
+    spi = _spi()
+    rng = np.random.default_rng(77)
+    N, T, C = 300, 3, 900
+    sx, sy = rng.uniform(0, 1e5, N), rng.uniform(0, 1e5, N)
+    z = rng.gamma(1.5, 2.0, (T, N))
+    z[1, rng.choice(N, 40, replace=False)] = np.nan
+    cx, cy = rng.uniform(0, 1e5, C), rng.uniform(0, 1e5, C)
+    sd = rng.uniform(0, 500, (N, 1))
+    cd = rng.uniform(0, 500, (1, C))
+    vgs = ["0.9 Nug(2000.0)"] * T
+    args = port.interp_args_for(["OK", "SK", "EDK"], est_vars=True)
+    got, prblm = spi.interp_steps(sx, sy, z, cx, cy, vgs, args, stn_drifts=sd, cell_drifts=cd,
+                                  est_vars=True, min_vg_val=1e-4, intrp_dtype=np.float64,
+                                  precision=precision)
+    assert prblm == []
+    d = np.hypot(cx[:, None] - sx[None], cy[:, None] - sy[None])
+    for t in range(T):
+        idx = np.where(np.isfinite(z[t]))[0]
+        zt = z[t, idx]
+        ok = np.full(C, zt.mean())
+        F = np.column_stack([np.ones(idx.size), sd[idx, 0]])
+        beta = np.linalg.lstsq(F, zt, rcond=None)[0]
+        edk = beta[0] + beta[1] * cd[0]
+        sk = zt[np.argmin(d[:, idx], 1)]
+        assert _err(got["OK"][t], ok) <= FP64_TOL
+        assert _err(got["EST_VARS_OK"][t], np.full(C, 0.9)) <= FP64_TOL
+        assert _err(got["EDK"][t], edk) <= FP64_TOL
+        assert np.array_equal(got["SK"][t], sk)
