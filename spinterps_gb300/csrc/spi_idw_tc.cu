@@ -152,12 +152,10 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
   };
   for (; g < total; ++g) {
     const int st = g % IT_NST;
-    // chunk g + 1 refills the stage of chunk g - 2 and chunk g's weights
-    // overwrite those of chunk g - 3: each thread waits for their MMAs
-    // itself (every thread read chunk g - 2's stations before the previous
-    // iteration's barrier), so one barrier per chunk suffices, the one
-    // before the MMAs are issued
+    // chunk g + 1 refills the stage of chunk g - 2: its MMAs must be done
     wait_mma(g - 1);
+    __syncthreads();
+    if (fail) break;
     if (tid == 0 && g + 1 < total) {
       tc_bulk_load(smem_u32(stage((g + 1) % IT_NST) + 2 * IT_A_BYTES),
                    pk + (int64_t)(g + 1) * IT_CHUNK_FLOATS, (uint32_t)IT_CHUNK_BYTES,
@@ -186,9 +184,8 @@ __global__ __launch_bounds__(IT_T, 2) void k_idw_tc(IdwTcArgs A) {
     }
     asm volatile("fence.proxy.async.shared::cta;");
     __syncthreads();
-    if (fail) break;  // set before the barrier: the same for every thread
     if (tid == 0) {
-      {
+      if (!fail) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint64_t ah = umma_desc(smem_u32(sAh), IT_M * 16, 128);
         const uint64_t al = umma_desc(smem_u32(sAl), IT_M * 16, 128);

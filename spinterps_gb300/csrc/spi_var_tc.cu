@@ -223,12 +223,10 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
     const int nc = vt_chunks(n, rb);
     for (int kc = 0; kc < nc; ++kc, ++g) {
       const int st = g % VT_NST;
-      // chunk g + 1 refills the stage of chunk g - 2 and chunk g's right-
-      // hand sides overwrite those of chunk g - 3: each thread waits for
-      // their MMAs itself (every thread read chunk g - 2's stations before
-      // the previous iteration's barrier), so one barrier per chunk
-      // suffices, the one before the MMAs are issued
+      // chunk g + 1 refills the stage of chunk g - 2: its MMAs must be done
       wait_mma(g - 1);
+      __syncthreads();
+      if (fail) break;
       if (tid == 0 && g + 1 < total) {
         vt_load(smem_u32(stage((g + 1) % VT_NST) + 2 * VT_A_BYTES),
                 pk + (int64_t)(g + 1) * VT_CHUNK_FLOATS, smem_u32(&bbar[(g + 1) % VT_NST]));
@@ -262,9 +260,8 @@ __global__ __launch_bounds__(VT_T, 2) void k_var_tc(VarTcArgs A) {
       }
       asm volatile("fence.proxy.async.shared::cta;");
       __syncthreads();
-      if (fail) break;  // set before the barrier: the same for every thread
       if (tid == 0) {
-        {
+        if (!fail) {
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t ah = umma_desc(smem_u32(sAh), VT_M * 16, 128);
           const uint64_t al = umma_desc(smem_u32(sAl), VT_M * 16, 128);
