@@ -1100,8 +1100,10 @@ def run_nebs(args):
     """The neighbour methods (interp/steps.py:584-833): the batched
     workload's stations and first steps, OK+var / IDW from each cell's 16
     nearest present stations ('nrst') on a nebs_nx^2 grid. value: through
-    interp_steps (spi_neb_select + spi_local_cells): wall time of the whole
-    call, numpy in and out, its host work per step group included;
+    interp_steps (spi_neb_select, spi_local_groups for kriging,
+    spi_local_cells for IDW): wall time of the whole call, numpy in and
+    out, its host work per step group included; entries_ms: device time per
+    entry point in a second run;
     cpu_baseline: the oracle's restatement (the reference's per-group loop)
     on a sample."""
     import torch
@@ -1125,6 +1127,28 @@ def run_nebs(args):
         out, _ = spi.interp_steps(w["sx"], w["sy"], z, cx, cy, vgs, iargs, **kw)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+    # a second run with each native call bracketed by CUDA events on its
+    # stream: device time per entry point
+    from spinterps_gb300 import _native as nat
+    spans, plain_call = {}, nat.call
+
+    def timed_call(name, *a):
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        rc = plain_call(name, *a)
+        e1.record(s)
+        spans.setdefault(name, []).append((e0, e1))
+        return rc
+
+    nat.call = timed_call
+    try:
+        spi.interp_steps(w["sx"], w["sy"], z, cx, cy, vgs, iargs, **kw)
+        torch.cuda.synchronize()
+    finally:
+        nat.call = plain_call
+    entries = {k: {"ms": sum(a.elapsed_time(b) for a, b in v), "calls": len(v)}
+               for k, v in spans.items()}
     C = cx.size
     # the oracle on a small block of cells and steps
     rng = np.random.default_rng(5)
@@ -1147,7 +1171,7 @@ def run_nebs(args):
                              "cores": 1, "kind": "port",
                              "sample": f"{sel.size} random cells x {ts} steps, the oracle's "
                                        "per-group loop"},
-            "err_vs_oracle_on_sample": err, "clocks": clk.summary()}
+            "err_vs_oracle_on_sample": err, "entries_ms": entries, "clocks": clk.summary()}
     print(json.dumps(line))
 
 

@@ -666,12 +666,61 @@ int spi_krige_ok_noalloc(const spi_domain_t *dom, const int32_t *stn_idx, int32_
  * variogram vg[q]), the sum check's nearest-neighbour fallback, and
  * prblm[q] = 1 where a system is exactly singular (nearest neighbour). The
  * OK variance (want_var, out->var) is lambda'r + lambda_n. data [.., ld]:
- * station values by row. FP64. k <= 64. Device arrays. */
+ * station values by row. FP64. k <= 64. Device arrays. Kriging here solves
+ * one system per (cell, step); spi_local_groups solves one per neighbour
+ * group and step, as the reference does, and follows its pinv on singular
+ * groups. */
 int spi_local_cells(const spi_domain_t *dom, int32_t kind, int32_t k, const int32_t *nebs,
                     int32_t n_steps, const int32_t *steps, const int32_t *out_row,
                     const double *data, int64_t ld, const spi_vg_t *vg, const int32_t *nug,
                     double min_var_thr, double idw_exp, int32_t want_var,
                     const spi_out_t *out, int32_t *prblm, spi_stream_t stream);
+
+/* Neighbour slots of spi_local_cells and spi_local_groups. */
+#define SPI_LOCAL_MAX_NEBS 64
+/* CTAs of spi_local_groups' pinv check, and its scratch for systems of up
+ * to mm rows (bytes, a multiple of 16). */
+#define SPI_LOCAL_GRP_PINV_SLOTS 152
+#define SPI_LOCAL_GRP_PINV_BYTES(mm) \
+  ((((int64_t)SPI_LOCAL_GRP_PINV_SLOTS * 2 * (mm) * (mm) * 8) + 15) / 16 * 16)
+/* Scratch of spi_local_groups per (group, step): the inverse, its status. */
+#define SPI_LOCAL_GRP_BYTES(mm) ((int64_t)(mm) * (mm) * 8 + 4)
+
+/* Kriging from each cell's own neighbours with one system per neighbour
+ * group, as the reference's neighbour methods solve it (interp/steps.py:
+ * 673-833: _get_interp once per group of cells with identical neighbour
+ * lists, its pinv once per step, interp/steps.py:351-352, and lambda =
+ * inv @ rhs per cell, interp/steps.py:403-435). Group g's stations are
+ * grp_nebs[g * k .. g * k + k) (indices into dom's stations, -1 = empty
+ * slot, the valid ones first, all present at the steps); cell c belongs to
+ * group cell_grp[c]. cell_order (optional): a permutation of the cells
+ * listing each group's cells together, so that neighbouring threads read
+ * the same inverse. For every listed step q (data row steps[q], output row
+ * out_row[q]) and kind OK / SK / EDK: the group's saddle matrix is
+ * inverted once (FP64 Gauss-Jordan with partial pivoting; where
+ * ||M||_F ||inv||_F > 1e15 or a pivot is zero, numpy.linalg.pinv's
+ * truncated inverse by the rule of spi_krige_factor's pinv check, and the
+ * nearest neighbour with prblm[q] = 1 where that check finds no valid
+ * inverse); then per cell the estimate, the sum check's nearest-neighbour
+ * fallback and the OK variance sum(lambda * rhs) + lambda_n (want_var,
+ * out->var); the mean (variance 0) where no value reaches min_var_thr or
+ * nug[q]; a single neighbour's value (variance NaN). scratch: 16-byte
+ * aligned, at least spi_local_groups_scratch_bytes(kind, k, dom->n_drift,
+ * n_grps, 1) bytes; steps are processed in chunks that fit it (all at once
+ * with spi_local_groups_scratch_bytes(..., n_steps)). k <=
+ * SPI_LOCAL_MAX_NEBS. Device arrays. */
+int spi_local_groups(const spi_domain_t *dom, int32_t kind, int32_t k,
+                     const int32_t *grp_nebs, int32_t n_grps, const int32_t *cell_grp,
+                     const int32_t *cell_order, int32_t n_steps, const int32_t *steps,
+                     const int32_t *out_row, const double *data, int64_t ld,
+                     const spi_vg_t *vg, const int32_t *nug, double min_var_thr,
+                     int32_t want_var, const spi_out_t *out, void *scratch,
+                     int64_t scratch_bytes, int32_t *prblm, spi_stream_t stream);
+
+/* Scratch bytes of spi_local_groups for n_steps steps at once (-1 for
+ * invalid arguments). Host only. */
+int64_t spi_local_groups_scratch_bytes(int32_t kind, int32_t k, int32_t n_drift,
+                                       int32_t n_grps, int32_t n_steps);
 
 /* ---- the driver flow around the step engine ------------------------------ */
 

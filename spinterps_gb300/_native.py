@@ -160,12 +160,16 @@ _SIGS = {
                           c_i32, ctypes.POINTER(VgT), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                           c_ptr, c_ptr],
     "spi_sym_pinv": [c_ptr, c_i32, c_dbl, c_ptr, c_ptr, c_ptr, c_ptr],
+    "spi_local_groups": [ctypes.POINTER(DomainT), c_i32, c_i32, c_ptr, c_i32, c_ptr, c_ptr,
+                         c_i32, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_dbl, c_i32,
+                         ctypes.POINTER(OutT), c_ptr, c_i64, c_ptr, c_ptr],
     "spi_idw_cells_tc": [ctypes.POINTER(DomainT), c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                          c_dbl, c_ptr, c_i64, ctypes.POINTER(OutT), c_ptr, c_ptr],
 }
 
 # every entry point the header declares (checked by the CPU tests)
-EXPORTS = sorted(list(_SIGS) + ["spi_version", "spi_cuda_error", "spi_mlp_n_params"])
+EXPORTS = sorted(list(_SIGS) + ["spi_version", "spi_cuda_error", "spi_mlp_n_params",
+                                 "spi_local_groups_scratch_bytes"])
 
 _lib = None
 _lock = threading.Lock()
@@ -192,6 +196,8 @@ def load(path=LIB_PATH):
         lib.spi_cuda_error.argtypes = []
         lib.spi_mlp_n_params.restype = c_i64
         lib.spi_mlp_n_params.argtypes = [c_i32, c_i32, c_i32, c_i32]
+        lib.spi_local_groups_scratch_bytes.restype = c_i64
+        lib.spi_local_groups_scratch_bytes.argtypes = [c_i32, c_i32, c_i32, c_i32, c_i32]
         _lib = lib
         return lib
 

@@ -25,7 +25,7 @@
 
 namespace spi {
 
-constexpr int LOC_KMAX = 64;  // neighbours per cell
+constexpr int LOC_KMAX = SPI_LOCAL_MAX_NEBS;  // neighbours per cell
 
 struct LocalArgs {
   spi_domain_t dom;

@@ -167,15 +167,16 @@ __device__ bool jacobi_sweeps(double* W, double* V, int m, double fm, JacobiSmem
   return false;
 }
 
-// P = V diag(lam_inv) V' (row-major m x m).
-__device__ void pinv_assemble(const double* V, const double* lam_inv, int m, double* P) {
+// P = V diag(lam_inv) V' (row-major m x m, row stride ld).
+__device__ void pinv_assemble(const double* V, const double* lam_inv, int m, double* P,
+                              int ld) {
   for (int e = threadIdx.x; e < m * m; e += PT) {
     const int i = e / m, j = e - i * m;
     const double* vi = V + i * m;
     const double* vj = V + j * m;
     double t = 0.0;
     for (int k = 0; k < m; ++k) t = fma(vi[k] * lam_inv[k], vj[k], t);
-    P[e] = t;
+    P[(int64_t)i * ld + j] = t;
   }
 }
 
@@ -227,7 +228,7 @@ __global__ __launch_bounds__(PT) void k_pinv(spi_domain_t dom, spi_systems_t sys
     const bool take = conv && (gapped || !gj_ok);
     // P = V diag(lam_inv) V' into the arena (row-major m x m, as the
     // Gauss-Jordan inverse)
-    if (take) pinv_assemble(V, sm.lam_inv, m, ws.l_arena + sys.mat_off[s]);
+    if (take) pinv_assemble(V, sm.lam_inv, m, ws.l_arena + sys.mat_off[s], m);
     __syncthreads();
     if (tid == 0) {
       ws.route[s] = (take || gj_ok) ? 1 : 2;
@@ -270,11 +271,118 @@ __global__ __launch_bounds__(PT) void k_sym_pinv(const double* __restrict__ M, i
     dropped += (fabs(l) > cut) ? 0.0 : 1.0;
   }
   dropped = cta_sum(dropped, sm.red);
-  pinv_assemble(V, sm.lam_inv, m, P);
+  pinv_assemble(V, sm.lam_inv, m, P, m);
   if (tid == 0) *status = conv ? (int32_t)dropped : -1;
 }
 
+// The neighbour groups' suspects (csrc/spi_local_grp.cu): status 3 (a
+// Gauss-Jordan inverse with ||M||_F ||P||_F > 1e15) or 4 (a zero pivot) of
+// the (group, step) tasks t = ql * n_grps + g of steps q0 .. q0 + nq - 1.
+// Each is diagonalised; eigenvalues up to GAP times pinv's cut-off
+// (1e-15 max |lambda|) are taken for rounding noise, and the truncated
+// pseudo-inverse without them replaces the inverse (row stride ld) where
+// the Jacobi sweeps converged and either the smallest kept eigenvalue lies
+// a further factor GAP above or Gauss-Jordan met a zero pivot; else the
+// Gauss-Jordan inverse stays where it is valid, and otherwise the task is
+// singular (status 1: the cells take their nearest neighbour and prblm[q]
+// is set). In a neighbour group the dropped eigenvalues are mostly the
+// rounding noise of co-located stations, whose rows are identical. Every CTA scans PT statuses at a time and works
+// through the candidates among them.
+__global__ __launch_bounds__(PT) void k_grp_pinv(spi_domain_t dom, int kind, int k,
+                                                 const int32_t* __restrict__ grp_nebs,
+                                                 int32_t n_grps, int32_t q0, int32_t nq,
+                                                 const spi_vg_t* __restrict__ vg, double* inv,
+                                                 int ld, int32_t* status, double* scratch,
+                                                 int32_t* prblm) {
+  __shared__ JacobiSmem sm;
+  __shared__ int cand[PT];
+  __shared__ int n_cand;
+  const int tid = threadIdx.x;
+  double* W = scratch + (size_t)blockIdx.x * 2 * ld * ld;
+  double* V = W + (size_t)ld * ld;
+  const int sk = kind == SPI_KIND_SK;
+  const int a = extra_rows(kind, dom.n_drift);
+  const int64_t G = n_grps;
+  const int64_t ntask = G * nq;
+  for (int64_t base = (int64_t)blockIdx.x * PT; base < ntask; base += (int64_t)gridDim.x * PT) {
+    if (tid == 0) n_cand = 0;
+    __syncthreads();
+    {
+      const int64_t t = base + tid;
+      const int32_t s = t < ntask ? status[t] : 0;
+      if (s == 3 || s == 4) cand[atomicAdd(&n_cand, 1)] = tid;
+    }
+    __syncthreads();
+    const int nc = n_cand;
+    for (int c = 0; c < nc; ++c) {
+      const int64_t t = base + cand[c];
+      const int gj_ok = status[t] == 3;
+      const int ql = (int)(t / G);
+      const int64_t g = t - (int64_t)ql * G;
+      const int q = q0 + ql;
+      const int32_t* nb = grp_nebs + g * k;
+      int n = 0;
+      while (n < k && nb[n] >= 0) ++n;
+      const int m = n + a;
+      const spi_vg_t v = vg[q];
+      double fm = 0.0;
+      for (int e = tid; e < m * m; e += PT) {
+        const int i = e / m, j = e - i * m;
+        const double x = saddle_entry(dom, v, nb, n, sk, i, j);
+        W[e] = x;
+        V[e] = (i == j) ? 1.0 : 0.0;
+        fm += x * x;
+      }
+      fm = cta_sum(fm, sm.red);
+      const bool conv = jacobi_sweeps(W, V, m, fm, sm);
+      double mx = 0.0;
+      for (int i = tid; i < m; i += PT) mx = fmax(mx, fabs(W[i * m + i]));
+      mx = cta_max(mx, sm.red);
+      // An exact rank deficiency (co-located stations) leaves eigenvalues
+      // at the sweeps' rounding level, a few eps ||M|| and so up to about
+      // pinv's cut-off itself, where numpy's SVD puts them far below it:
+      // eigenvalues up to GAP times the cut-off count as that noise and
+      // are dropped, and the truncation is clear when the smallest kept
+      // eigenvalue lies a further factor GAP above.
+      const double cut = kRcond * mx * GAP;
+      double kept_min = 1e308;
+      for (int i = tid; i < m; i += PT) {
+        const double l = W[i * m + i], al = fabs(l);
+        sm.lam_inv[i] = (al > cut) ? 1.0 / l : 0.0;
+        if (al > cut) kept_min = fmin(kept_min, al);
+      }
+      kept_min = -cta_max(-kept_min, sm.red);
+      const bool clear = kept_min > cut * GAP;
+      const bool take = conv && (clear || !gj_ok);
+      if (take) pinv_assemble(V, sm.lam_inv, m, inv + t * (int64_t)ld * ld, ld);
+      __syncthreads();
+      if (tid == 0) {
+        const bool ok = take || gj_ok;
+        status[t] = ok ? 0 : 1;
+        if (!ok) atomicOr(prblm + q, 1);
+      }
+      __syncthreads();
+    }
+    __syncthreads();  // every thread has read n_cand before it is reset
+  }
+}
+
 }  // namespace
+
+int local_grp_pinv(const spi_domain_t& dom, int kind, int k, const int32_t* grp_nebs,
+                   int32_t n_grps, int32_t q0, int32_t nq, const spi_vg_t* vg, double* inv,
+                   int32_t ld, int32_t* status, double* pinv_scratch, int32_t* prblm,
+                   cudaStream_t st) {
+  const int64_t ntask = (int64_t)n_grps * nq;
+  if (ntask <= 0) return SPI_OK;
+  if (dom.n_drift < 0 || dom.n_drift > SPI_MAX_DRIFT) return SPI_ERR_TOO_LARGE;
+  const int64_t blocks = (ntask + PT - 1) / PT;
+  const int grid = blocks < SPI_LOCAL_GRP_PINV_SLOTS ? (int)blocks : SPI_LOCAL_GRP_PINV_SLOTS;
+  k_grp_pinv<<<grid, PT, 0, st>>>(dom, kind, k, grp_nebs, n_grps, q0, nq, vg, inv, ld, status,
+                                  pinv_scratch, prblm);
+  SPI_LAUNCH_CHECK();
+  return SPI_OK;
+}
 
 int launch_pinv(const spi_domain_t& dom, const spi_systems_t& sys, const spi_krige_ws_t& ws,
                 cudaStream_t st) {

@@ -35,13 +35,14 @@ class SpInterpNeighborGrouping:
         self._d = (torch.as_tensor(self._dst_xs, device=self.dev),
                    torch.as_tensor(self._dst_ys, device=self.dev))
 
-    def neb_idxs(self, ref_xs, ref_ys):
-        """[n_dst, k] neighbour indices into ref_xs (ascending per row)."""
+    def neb_idxs_device(self, ref_xs, ref_ys):
+        """[n_dst, k] int32 device tensor of neighbour indices into ref_xs
+        (ascending per row, -1 in unused slots at the end)."""
         ref_xs = np.ascontiguousarray(ref_xs, dtype=np.float64)
         ref_ys = np.ascontiguousarray(ref_ys, dtype=np.float64)
         n, C = ref_xs.size, self._dst_xs.size
         if self._neb_sel_mthd == "all":
-            return np.tile(np.arange(n), (C, 1))
+            return torch.arange(n, dtype=torch.int32, device=self.dev).expand(C, n).contiguous()
         k = min(self._n_nebs, n) if self._neb_sel_mthd == "nrst" else self._n_nebs
         rx = torch.as_tensor(ref_xs, device=self.dev)
         ry = torch.as_tensor(ref_ys, device=self.dev)
@@ -49,7 +50,11 @@ class SpInterpNeighborGrouping:
         nat.call("spi_neb_select", METHODS[self._neb_sel_mthd], _ptr(self._d[0]),
                  _ptr(self._d[1]), C, _ptr(rx), _ptr(ry), n, int(self._n_nebs),
                  int(self._n_pies or 0), _ptr(out), _stream())
-        return out.cpu().numpy().astype(np.int64)
+        return out
+
+    def neb_idxs(self, ref_xs, ref_ys):
+        """[n_dst, k] neighbour indices into ref_xs (ascending per row)."""
+        return self.neb_idxs_device(ref_xs, ref_ys).cpu().numpy().astype(np.int64)
 
     @staticmethod
     def groups(all_neb_idxs):
@@ -73,6 +78,21 @@ class SpInterpNeighborGrouping:
 LOCAL_KIND = {"OK": 0, "SK": 1, "EDK": 2, "IDW": 3, "NNB": 4}
 
 
+# Scratch for the per-group inverses of one call of spi_local_groups; steps
+# beyond it are processed in chunks.
+GRP_SCRATCH_BYTES = 2 << 30
+
+
+def device_groups(nb):
+    """Cells with identical neighbour lists, on the device: (grp_nebs [G, k],
+    cell_grp [C], cell_order [C]) as int32, cell_order listing each group's
+    cells together in ascending cell order."""
+    grp_nebs, cell_grp = torch.unique(nb, dim=0, return_inverse=True)
+    cell_order = torch.argsort(cell_grp, stable=True)
+    return (grp_nebs.to(torch.int32).contiguous(), cell_grp.to(torch.int32).contiguous(),
+            cell_order.to(torch.int32).contiguous())
+
+
 def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_sel_mthd,
                       n_nebs, n_pies, *, stn_drifts=None, cell_drifts=None,
                       intrp_dtype=np.float32, time_steps=None, device="cuda", est_vars=False,
@@ -81,12 +101,14 @@ def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_
     """The step engine with 'nrst' / 'pie' neighbours (interp/steps.py:584-606,
     673-833). Stations that are nobody's neighbour with every station
     present are dropped. Then, per group of steps with the same stations,
-    every cell is interpolated from its own neighbours among them: the
-    reference's _get_interp per group of cells with identical neighbour
-    lists, done by spi_local_cells with one warp per (cell, step) and a
-    system of at most 64 + 8 rows (FP64 in either precision; the other
-    keywords of steps.interp_steps do not apply). Returns (fields, problem
-    steps) like steps.interp_steps."""
+    the neighbour lists are selected and grouped on the device, and
+    - kriging (OK / SK / EDK) runs as the reference's _get_interp per group
+      of cells with identical neighbour lists: spi_local_groups inverts
+      each group's system once per step and applies it to the group's
+      cells;
+    - IDW and NNB run per cell (spi_local_cells, one warp per (cell, step)).
+    FP64 in either precision; the other keywords of steps.interp_steps do
+    not apply. Returns (fields, problem steps) like steps.interp_steps."""
     import torch
     from . import _native as nat
     from .steps import (_Domain, _out_struct, _ptr, _require_cuda, _stream, _vg_tensor,
@@ -118,6 +140,7 @@ def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_
         vgt = _vg_tensor([parse_vg(v) for v in vgl], dev).view(T, -1)
         nug = torch.as_tensor(np.array([check_full_nuggetness(v, min_vg_val) for v in vgl],
                                        dtype=np.int32), device=dev)
+    n_drift = int(dom.st.n_drift)
     prblm = []
     flags = torch.zeros(T, dtype=torch.int32, device=dev)
     avail = np.isfinite(data)
@@ -132,15 +155,16 @@ def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_
         if not stn_idxs.size:
             prblm.extend(t for t in time_steps[rows] if t not in prblm)
             continue
-        nidx = g.neb_idxs(sx[stn_idxs], sy[stn_idxs])
+        nidx = g.neb_idxs_device(sx[stn_idxs], sy[stn_idxs])
         k = nidx.shape[1]
-        nb = np.where(nidx >= 0, stn_idxs[np.maximum(nidx, 0)], -1).astype(np.int32)
-        d_nb = torch.as_tensor(np.ascontiguousarray(nb), device=dev)
+        d_stn = torch.as_tensor(stn_idxs.astype(np.int32), device=dev)
+        d_nb = torch.where(nidx >= 0, d_stn[nidx.clamp(min=0).long()], nidx).contiguous()
         d_rows = torch.as_tensor(rows.astype(np.int32), device=dev)
         d_vg = vgt[d_rows.long()].contiguous() if krig else None
         d_nug = nug[d_rows.long()].contiguous() if krig else None
         d_pr = torch.zeros(rows.size, dtype=torch.int32, device=dev)
-        held.append((d_nb, d_rows, d_vg, d_nug, d_pr))
+        grp = scratch = None
+        held.append((d_stn, d_nb, d_rows, d_vg, d_nug, d_pr))
         for a in interp_args:
             if a[0] == "EST_VARS_OK":  # written by the OK launch
                 continue
@@ -148,11 +172,28 @@ def interp_steps_nebs(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, neb_
             want_var = bool(est_vars and a[0] == "OK" and "EST_VARS_OK" in flds)
             out = _out_struct(flds[a[2]], flds["EST_VARS_OK"] if want_var else None,
                               min_var_cut, max_var_cut)
-            nat.call("spi_local_cells", ctypes.byref(dom.st), kind, k, _ptr(d_nb), rows.size,
-                     _ptr(d_rows), _ptr(d_rows), _ptr(d_data), data.shape[1],
-                     _ptr(d_vg), _ptr(d_nug), float(min_var_thr),
-                     float(a[3]) if a[0] == "IDW" else 0.0, int(want_var), ctypes.byref(out),
-                     _ptr(d_pr), s)
+            if kind <= 2:
+                if grp is None:
+                    grp = device_groups(d_nb)
+                    G = grp[0].shape[0]
+                    held.append(grp)
+                need = nat.lib().spi_local_groups_scratch_bytes(kind, k, n_drift, G, rows.size)
+                one = nat.lib().spi_local_groups_scratch_bytes(kind, k, n_drift, G, 1)
+                nbytes = max(one, min(need, GRP_SCRATCH_BYTES))
+                if scratch is None or scratch.numel() < nbytes:
+                    scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+                    held.append(scratch)
+                nat.call("spi_local_groups", ctypes.byref(dom.st), kind, k, _ptr(grp[0]), G,
+                         _ptr(grp[1]), _ptr(grp[2]), rows.size, _ptr(d_rows), _ptr(d_rows),
+                         _ptr(d_data), data.shape[1], _ptr(d_vg), _ptr(d_nug),
+                         float(min_var_thr), int(want_var), ctypes.byref(out), _ptr(scratch),
+                         scratch.numel(), _ptr(d_pr), s)
+            else:
+                nat.call("spi_local_cells", ctypes.byref(dom.st), kind, k, _ptr(d_nb),
+                         rows.size, _ptr(d_rows), _ptr(d_rows), _ptr(d_data), data.shape[1],
+                         _ptr(d_vg), _ptr(d_nug), float(min_var_thr),
+                         float(a[3]) if a[0] == "IDW" else 0.0, int(want_var),
+                         ctypes.byref(out), _ptr(d_pr), s)
         flags.index_add_(0, d_rows.long(), d_pr)
     bad = np.where(flags.cpu().numpy() != 0)[0]
     prblm.extend(t for t in time_steps[bad] if t not in prblm)

@@ -194,6 +194,34 @@ def test_entry_points_check_arguments_before_any_gpu_work():
                                None) == TOO_LARGE
     assert lib.spi_local_cells(ctypes.byref(dom), 7, 8, dummy, 1, dummy, dummy, dummy, 1, dummy,
                                dummy, 0.0, 2.0, 0, ctypes.byref(out), dummy, None) == ARG
+    # spi_local_groups: argument checks that return before any CUDA call
+    grp_args = lambda kind, k, scratch, nbytes: (  # noqa: E731
+        ctypes.byref(dom), kind, k, dummy, 4, dummy, None, 1, dummy, dummy, dummy, 1, dummy,
+        dummy, 0.0, 0, ctypes.byref(out), scratch, nbytes, dummy, None)
+    dom.n_cells = 10
+    out.est = dummy
+    for f in ("cell_x", "cell_y", "stn_x", "stn_y"):
+        setattr(dom, f, dummy)
+    assert lib.spi_local_groups(None, *grp_args(0, 8, dummy, 1 << 30)[1:]) == ARG
+    assert lib.spi_local_groups(*grp_args(3, 8, dummy, 1 << 30)) == ARG  # IDW: per cell
+    assert lib.spi_local_groups(*grp_args(0, 65, dummy, 1 << 30)) == TOO_LARGE
+    aligned = ctypes.c_void_p(64)
+    assert lib.spi_local_groups(*grp_args(0, 8, ctypes.c_void_p(72), 1 << 30)) == ARG
+    need = lib.spi_local_groups_scratch_bytes(0, 8, 0, 4, 1)
+    assert lib.spi_local_groups(*grp_args(0, 8, aligned, need - 1)) == TOO_LARGE
+    # scratch: the pinv check's slots, then per (group, step) the inverse and its status
+    mm = 9
+    pinv = (152 * 2 * mm * mm * 8 + 15) // 16 * 16
+    assert need == pinv + 4 * (mm * mm * 8 + 4)
+    assert lib.spi_local_groups_scratch_bytes(2, 16, 3, 100, 7) == (
+        (152 * 2 * 20 * 20 * 8 + 15) // 16 * 16 + 700 * (20 * 20 * 8 + 4))
+    assert lib.spi_local_groups_scratch_bytes(1, 16, 3, 100, 7) == (
+        (152 * 2 * 16 * 16 * 8 + 15) // 16 * 16 + 700 * (16 * 16 * 8 + 4))
+    assert lib.spi_local_groups_scratch_bytes(4, 16, 0, 1, 1) == -1
+    dom.n_cells = 0
+    out.est = None
+    for f in ("cell_x", "cell_y", "stn_x", "stn_y"):
+        setattr(dom, f, None)
     assert lib.spi_legacy_system(9, dummy, dummy, 5, None, 0, ctypes.byref(vg), dummy, dummy,
                                  dummy, dummy, None, None) == ARG
     vg0 = nat.VgT()
