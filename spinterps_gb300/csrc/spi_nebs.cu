@@ -4,7 +4,8 @@
 // destination, results as each destination's sorted station indices.
 //
 // nrst: the n_nebs nearest (FP64 distances, the correctly rounded root as
-// numpy's ** 0.5), kept in an insertion-sorted list by (distance, index).
+// numpy's ** 0.5), kept in an insertion-sorted list by (distance, index);
+// an FP32 bound skips the stations that cannot enter it (k_neb_nrst).
 // pie: every station's angle from the destination by the reference's rules
 // (atan(dy / dx), pushed into [0, 2 pi) for dx < 0 or dy < 0 -- dx == 0
 // gives 0, and dx < 0 with dy == 0 stays 0), its pie
@@ -54,18 +55,60 @@ __device__ __forceinline__ void sort_ints(int* a, int n) {
   }
 }
 
-__global__ void k_neb_nrst(const double* __restrict__ dx_, const double* __restrict__ dy_,
-                           int64_t n_dst, const double* __restrict__ rx,
-                           const double* __restrict__ ry, int n_ref, int k,
-                           int32_t* __restrict__ out) {
+// nrst: every destination's k nearest by (FP64 distance, index). The
+// stations pass through shared memory in tiles as FP32 coordinates relative
+// to station 0, with |x| + |y| beside them. Once a destination holds k
+// stations, a station whose FP32 squared distance exceeds lim^2,
+//   lim = thr (1 + 1e-5) + 2^-20 (|x_s| + |y_s| + |x_c| + |y_c|),
+// thr the current k-th FP64 distance, is skipped: the rounding of the FP32
+// coordinates and arithmetic moves a distance by at most 2^-23 (|x_s| + |y_s|
+// + |x_c| + |y_c|) plus a few 1e-7 of it, so such a station's FP64 distance
+// is above thr and neb_insert would reject it whatever its index. thr only
+// falls during the scan, so the skipped stations stay out and the selection
+// equals the FP64 scan of every station. The others take dist_f64 and
+// neb_insert as before.
+constexpr int NRST_T = 128;      // threads per CTA
+constexpr int NRST_TILE = 1024;  // stations per shared-memory tile
+constexpr float kNrstRel = 1.00001f;
+constexpr float kNrstAbs = 9.5367431640625e-07f;  // 2^-20
+
+__global__ __launch_bounds__(NRST_T) void k_neb_nrst(const double* __restrict__ dx_,
+                                                     const double* __restrict__ dy_,
+                                                     int64_t n_dst,
+                                                     const double* __restrict__ rx,
+                                                     const double* __restrict__ ry, int n_ref,
+                                                     int k, int32_t* __restrict__ out) {
+  __shared__ float4 tile[NRST_TILE];
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n_dst) return;
+  const bool act = i < n_dst;
   double ld[NEB_MAX];
   int li[NEB_MAX];
   int len = 0;
-  const double x = dx_[i], y = dy_[i];
-  for (int j = 0; j < n_ref; ++j)
-    neb_insert(ld, li, &len, k, dist_f64(x, y, rx[j], ry[j]), j);
+  const double ox = rx[0], oy = ry[0];
+  const double x = act ? dx_[i] : ox, y = act ? dy_[i] : oy;
+  const float xc = (float)(x - ox), yc = (float)(y - oy);
+  const float sc = fabsf(xc) + fabsf(yc);
+  float lim0 = INFINITY;  // thr (1 + 1e-5) once k stations are held
+  for (int t0 = 0; t0 < n_ref; t0 += NRST_TILE) {
+    const int tn = min(NRST_TILE, n_ref - t0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < tn; j += NRST_T) {
+      const float xs = (float)(rx[t0 + j] - ox), ys = (float)(ry[t0 + j] - oy);
+      tile[j] = make_float4(xs, ys, fabsf(xs) + fabsf(ys), 0.0f);
+    }
+    __syncthreads();
+    if (!act) continue;
+    for (int j = 0; j < tn; ++j) {
+      const float4 s = tile[j];
+      const float ex = s.x - xc, ey = s.y - yc;
+      const float lim = fmaf(kNrstAbs, s.z + sc, lim0);
+      if (ex * ex + ey * ey > lim * lim) continue;
+      const int js = t0 + j;
+      neb_insert(ld, li, &len, k, dist_f64(x, y, rx[js], ry[js]), js);
+      if (len == k) lim0 = (float)ld[k - 1] * kNrstRel;
+    }
+  }
+  if (!act) return;
   sort_ints(li, len);
   for (int q = 0; q < k; ++q) out[i * k + q] = li[q];
 }
@@ -140,8 +183,8 @@ extern "C" int spi_neb_select(int32_t method, const double* dst_x, const double*
   if (method == 1) {
     const int k = n_nebs < n_ref ? n_nebs : n_ref;
     if (k > spi::NEB_MAX) return SPI_ERR_TOO_LARGE;
-    spi::k_neb_nrst<<<(unsigned)blocks, 128, 0, st>>>(dst_x, dst_y, n_dst, ref_x, ref_y, n_ref,
-                                                      k, idxs);
+    spi::k_neb_nrst<<<(unsigned)blocks, spi::NRST_T, 0, st>>>(dst_x, dst_y, n_dst, ref_x,
+                                                               ref_y, n_ref, k, idxs);
   } else if (method == 2) {
     if (n_pies < 1 || n_nebs < n_pies || n_ref < n_nebs) return SPI_ERR_ARG;
     if (n_nebs > spi::NEB_MAX || n_pies > 16 || n_pies * n_nebs > spi::NEB_PIE_SLOTS)
