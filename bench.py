@@ -1245,7 +1245,7 @@ def main():
     ap.add_argument("--legacy-nx", type=int, default=500)
     ap.add_argument("--legacy-cpu-points", type=int, default=4000)
     ap.add_argument("--nebs", action="store_true",
-                    help="the neighbour method 'nrst' (per-cell systems) instead")
+                    help="the neighbour method 'nrst' (one kriging system per neighbour group) instead")
     ap.add_argument("--nebs-nx", type=int, default=500)
     ap.add_argument("--nebs-steps", type=int, default=73)
     ap.add_argument("--nebs-cpu-cells", type=int, default=2000)
