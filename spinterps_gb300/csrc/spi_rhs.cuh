@@ -99,8 +99,9 @@ __device__ __forceinline__ float pow2i(int m) {
   return __int_as_float((m1 + 127) << 23) * __int_as_float((m2 + 127) << 23);
 }
 
-// 2^(j/16), j = 0..15, as double-floats (one 128-byte line: the lanes of a
-// warp read it with one L1 wavefront).
+// 2^(j/16), j = 0..15, as double-floats (head = the float nearest to
+// 2^(j/16), tail = the float nearest to the rest; one 128-byte line: the
+// lanes of a warp read it with one L1 wavefront).
 __device__ const float2 kExp2Sixteenths[16] = {
     {1.0f, 0.0f},
     {1.0442737340927124f, 4.8334701574503924e-08f},
@@ -120,7 +121,9 @@ __device__ const float2 kExp2Sixteenths[16] = {
     {1.9152065515518188f, 9.845328108326612e-09f},
 };
 
-// exp of a double-float argument (t <= 0 here), relative error ~1e-12:
+// exp of a double-float argument (t <= 0 here), relative error ~1e-12, by
+// the table-driven method of P. T. P. Tang (ACM TOMS 15(2), 1989) with a
+// 16-entry table:
 // t = m ln2/16 + r (ln2/16 as a 12-bit head, so m * head is exact for
 // |m| < 2^12, plus a two-float tail), |r| <= ln2/32; exp(r) = 1 + r + r^2/2
 // (double-float) + r^3 (1/6 + r/24 + r^2/120) (FP32, <= 1.7e-6, truncation
