@@ -20,6 +20,13 @@ copies the finished wave's fields to the host and calls
 ``sink(first_step, fields)`` with numpy arrays [wave steps, cells].
 ``nc_sink`` returns a sink that writes those rows into a netCDF file laid
 out as the reference's (``ncout.write_interp_nc`` with deferred fields).
+
+With the neighbour methods (``neb_sel_mthd`` 'nrst' / 'pie') a wave is a
+call of ``nebs.interp_steps_nebs`` on its steps: a step then costs only its
+fields, and every wave also holds one step group's neighbour lists, their
+grouping and the kriging scratch (``nebs_fixed_bytes``). The stations kept
+and every cell's neighbours depend on the coordinates alone, so a wave's
+fields again equal the same rows of a one-shot run.
 """
 import numpy as np
 import torch
@@ -49,19 +56,33 @@ def step_bytes(n_present, n_cells, n_labels, out_itemsize, krige_kinds, ok_var, 
     return int(b)
 
 
+def nebs_fixed_bytes(n_cells, k):
+    """Device bytes a wave of the neighbour methods holds besides its
+    fields: one step group's neighbour lists ([n_cells, k] int32, selected
+    and mapped), their grouping (int64 inverse and order, int32 copies)
+    and the kriging scratch of spi_local_groups (at most
+    nebs.GRP_SCRATCH_BYTES)."""
+    from .nebs import GRP_SCRATCH_BYTES
+    return int(GRP_SCRATCH_BYTES + n_cells * (3 * 4 * max(int(k), 1) + 4 * 8))
+
+
 def plan_waves(data, n_cells, interp_args, *, budget, out_itemsize=4, est_vars=False,
-               precision="fp64"):
+               precision="fp64", neighbours=False):
     """Cut the steps of ``data`` [T, N] (NaN = missing) into consecutive
     waves whose step_bytes add up to at most ``budget``; a step that alone
-    exceeds it is a wave of its own. Returns [(first, end), ...]."""
+    exceeds it is a wave of its own. With ``neighbours`` (the neighbour
+    methods) a step costs its fields only. Returns [(first, end), ...]."""
     types = [a[0] for a in interp_args]
     kinds = [t for t in ("OK", "SK", "EDK") if t in types]
     n_labels = len(interp_args)
     n_av = np.isfinite(np.asarray(data)).sum(1)
     waves, t0, acc = [], 0, 0
     for t in range(n_av.size):
-        b = step_bytes(int(n_av[t]), n_cells, n_labels, out_itemsize, kinds, est_vars,
-                       precision == "mixed")
+        if neighbours:
+            b = n_cells * n_labels * out_itemsize
+        else:
+            b = step_bytes(int(n_av[t]), n_cells, n_labels, out_itemsize, kinds, est_vars,
+                           precision == "mixed")
         if t > t0 and acc + b > budget:
             waves.append((t0, t))
             t0, acc = t, 0
@@ -80,8 +101,10 @@ def interp_steps_waves(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, 
     fields {label: [wave steps, cells]}. ``budget``: device bytes per wave
     (default: a third of the free device memory; two waves' plans are alive
     at once while the next is built). The other arguments are
-    ``interp_steps``'s. Returns (problem time steps, info per wave: steps,
-    seconds of host planning, and the plan's collect_info())."""
+    ``interp_steps``'s, ``neb_sel_mthd`` / ``n_nebs`` / ``n_pies`` included.
+    Returns (problem time steps, info per wave: steps, seconds of host
+    planning, and the plan's collect_info(); with the neighbour methods the
+    seconds of the wave's call)."""
     import time
     dev = _require_cuda(device)
     data = np.ascontiguousarray(data, dtype=np.float64)
@@ -93,9 +116,29 @@ def interp_steps_waves(stn_x, stn_y, data, cell_x, cell_y, vgs, interp_args, *, 
     if budget is None:
         budget = torch.cuda.mem_get_info(dev)[0] // 3
     itemsize = np.dtype(intrp_dtype).itemsize
+    neb = plan_kw.pop("neb_sel_mthd", "all")
+    n_nebs, n_pies = plan_kw.pop("n_nebs", None), plan_kw.pop("n_pies", None)
+    prblm, info = [], []
+    if neb != "all":
+        from .nebs import interp_steps_nebs
+        k = n_nebs if n_nebs else int(np.asarray(stn_x).size)
+        waves = plan_waves(data, C, interp_args, out_itemsize=itemsize, neighbours=True,
+                           budget=max(budget - nebs_fixed_bytes(C, k), 1))
+        for a, b in waves:
+            t0 = time.perf_counter()
+            flds, pr = interp_steps_nebs(
+                stn_x, stn_y, data[a:b], cell_x, cell_y, vgs[a:b], interp_args, neb, n_nebs,
+                n_pies, stn_drifts=stn_drifts, cell_drifts=cell_drifts,
+                intrp_dtype=intrp_dtype, time_steps=np.asarray(time_steps)[a:b],
+                device=device, est_vars=est_vars, precision=precision, **plan_kw)
+            sink(a, flds)
+            for t in pr:
+                if t not in prblm:
+                    prblm.append(t)
+            info.append({"steps": [int(a), int(b)], "call_s": time.perf_counter() - t0})
+        return prblm, info
     waves = plan_waves(data, C, interp_args, budget=budget, out_itemsize=itemsize,
                        est_vars=est_vars, precision=precision)
-    prblm, info = [], []
 
     def build(w):
         a, b = w
